@@ -1,0 +1,82 @@
+// fs_internal.h -- shared between the host model (fs_model.cu) and the
+// kernels (fs_kernels.cu). Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fs {
+
+// Per-model device control block. `err` holds the first error status of the
+// current fs_step call; the remaining words are reset before every timestep.
+struct Ctl {
+  int err;                 // FS_OK or first FS_ERR_* seen by any kernel
+  int err_detail;          // phase code where err was raised
+  int nlevels;             // levels found by the last walk
+  int total;               // cells placed in the ordering by the last walk
+  unsigned long long walk_ns[3];  // accumulated walk time: ordering,
+                                  // accumulation, erosion (block 0's clock)
+  // --- reset before every timestep (from `top` on) ---
+  int top;                 // level-0 fill pointer (absolute stack index)
+  unsigned int bar;        // grid-barrier arrival counter
+  int lvlcnt[3];           // rotating per-level append counters (relative)
+  int pad[3];
+};
+constexpr size_t kCtlResetOffset = offsetof(Ctl, top);
+constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
+
+// Where an error was detected (Ctl::err_detail).
+enum ErrPhase : int {
+  kPhaseNone = 0,
+  kPhaseBarrier = 1,
+  kPhaseOrder = 2,
+  kPhaseErode = 3,
+  kPhaseTest = 4,
+};
+
+// How pow(x, n) and pow(x, n-1) are evaluated inside the Newton loop.
+enum NMode : int {
+  kNGeneral = 0,  // CUDA pow (not bit-identical to glibc)
+  kNOne = 1,      // pow(x,1) = x, pow(x,0) = 1: exact
+  kNTwo = 2,      // pow(x,2) = x*x, pow(x,1) = x
+};
+
+struct StepGeom {
+  int W, H;
+  int size;  // W*H (< 2^31)
+};
+
+struct WalkArgs {
+  double *h;
+  const int8_t *rec;
+  const uint8_t *mask;
+  int32_t *stack;
+  int32_t *lvl_off;        // size+2 entries
+  uint32_t *cnt;           // drainage cell counts
+  const double *fact;      // fact[2*k + cls], k in [1, size]
+  Ctl *ctl;
+  int W, size;
+  double u_dt, neq, tol;
+  int nmode;
+  int do_erode;            // 0: ordering + accumulation only
+  int stamp;               // 1: accumulate phase times into ctl->walk_ns
+  unsigned long long timeout_ns;
+};
+
+// Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
+cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
+                             double dr_orth, double dr_diag, cudaStream_t s);
+cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
+                                 int32_t *stack, double *h, Ctl *ctl,
+                                 StepGeom g, double u_dt, cudaStream_t s);
+cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s);
+int walk_threads();
+const void *walk_kernel_ptr();
+cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
+                                cudaStream_t s);
+cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,
+                                cudaStream_t s);
+cudaError_t launch_test_wait(Ctl *ctl, int blocks,
+                             unsigned long long timeout_ns, cudaStream_t s);
+
+}  // namespace fs

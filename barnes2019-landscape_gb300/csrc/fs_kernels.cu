@@ -1,0 +1,468 @@
+// fs_kernels.cu -- sm_103a kernels of the FastScape timestep.
+//
+// One timestep = three launches on the model's stream:
+//   1. k_receivers       D8 steepest descent over the interior
+//                        (fastscape_RB.cpp:160-182)
+//   2. k_donors_level0   donor masks (pull form of fastscape_RB.cpp:188-203),
+//                        level-0 frontier (fastscape_RB.cpp:221-227) and the
+//                        uplift of interior level-0 cells (:285-296)
+//   3. k_walk            persistent cooperative kernel: level-by-level
+//                        ordering (:229-251), flow accumulation back down the
+//                        levels (:262-279) and the implicit erosion solved
+//                        upward from base level (:306-328, level order of
+//                        fastscape_RB+P.cpp:319-350), with uplift of the
+//                        eroded cells folded into their first read.
+//
+// Floating point follows the reference's operation order exactly; the whole
+// file is compiled with -fmad=false so no multiply-add is contracted, and
+// double division is IEEE round-to-nearest.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "fastscape_gb300.h"
+#include "fs_internal.h"
+
+namespace fs {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWalkThreads = 512;
+constexpr int kNewtonMaxIt = 1000;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int *p) {
+  return *reinterpret_cast<const volatile int *>(p);
+}
+
+__device__ __forceinline__ void raise_err(Ctl *ctl, int code, int phase) {
+  if (atomicCAS(&ctl->err, 0, code) == 0) ctl->err_detail = phase;
+}
+
+// Grid-wide barrier for a cooperative launch. Arrival counter only grows
+// during a launch (reset by the host before it), so barrier number `epoch`
+// completes when bar reaches epoch*gridDim.x. Every wait is bounded by
+// `timeout_ns` of wall time; on timeout, or when another block has already
+// raised an error, it returns false and the caller leaves the kernel.
+__device__ bool grid_barrier(Ctl *ctl, unsigned &epoch,
+                             unsigned long long timeout_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ++epoch;
+    const unsigned target = epoch * gridDim.x;
+    __threadfence();
+    atomicAdd(&ctl->bar, 1u);
+    int ok = 1;
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (ld_acquire_u32(&ctl->bar) < target) {
+      if (ld_volatile_i32(&ctl->err) != 0) { ok = 0; break; }
+      if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+        raise_err(ctl, FS_ERR_TIMEOUT, kPhaseBarrier);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ void nshift8(int W, int o[8]) {
+  o[0] = -1; o[1] = -W - 1; o[2] = -W; o[3] = -W + 1;
+  o[4] = 1;  o[5] = W + 1;  o[6] = W;  o[7] = W - 1;
+}
+
+// nshift[k] (fastscape_RB.cpp:137) for a run-time k without a local array:
+// dx+1 and dy+1 of the 8 directions packed two bits per direction.
+__device__ __forceinline__ int nbr_off(int k, int W) {
+  const int dx = ((0x1A90 >> (2 * k)) & 3) - 1;
+  const int dy = ((0xA901 >> (2 * k)) & 3) - 1;
+  return dy * W + dx;
+}
+
+// ---------------------------------------------------------------------------
+// 1. Receivers: fastscape_RB.cpp:160-182. slope = (h[c]-h[n])/dr[n], strict
+// '>' against a running maximum that starts at 0, so the first maximum in
+// neighbour order wins and a cell with no strictly lower neighbour keeps
+// NO_FLOW.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
+            int H, double dr_orth, double dr_diag) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x + 2;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 2;
+  if (x >= W - 2 || y >= H - 2) return;
+  const long long c = (long long)y * W + x;
+  int o[8];
+  nshift8(W, o);
+  const double hc = h[c];
+  double max_slope = 0;
+  int max_n = FS_NO_FLOW;
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const double slope = (hc - h[c + o[n]]) / ((n & 1) ? dr_diag : dr_orth);
+    if (slope > max_slope) {
+      max_slope = slope;
+      max_n = n;
+    }
+  }
+  rec[c] = (int8_t)max_n;
+}
+
+// ---------------------------------------------------------------------------
+// 2. Donor masks + level 0 + uplift of interior level-0 cells.
+// Bit k of mask[c] is set when neighbour c+nshift[k] has receiver code
+// (k+4)%8, i.e. drains into c (the pull form of fastscape_RB+GPU.cpp:155-182).
+// Level 0 = every NO_FLOW cell (fastscape_RB.cpp:221-227), appended with one
+// atomic per warp. Interior NO_FLOW cells are never eroded, so their uplift
+// (fastscape_RB.cpp:285-296) is applied here, before any erosion reads them.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
+                int32_t *__restrict__ stack, double *__restrict__ h, Ctl *ctl,
+                int W, int H, int size, double u_dt) {
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int o[8];
+  nshift8(W, o);
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+       base < size; base += stride) {
+    const long long c = base + lane;
+    bool level0 = false;
+    if (c < size) {
+      const int y = (int)c / W;
+      const int x = (int)c - y * W;
+      const int r = rec[c];
+      unsigned m = 0;
+      if (x >= 1 && x <= W - 2 && y >= 1 && y <= H - 2) {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+          if (rec[c + o[k]] == ((k + 4) & 7)) m |= 1u << k;
+      }
+      mask[c] = (uint8_t)m;
+      level0 = (r == FS_NO_FLOW);
+      if (level0 && x >= 2 && x < W - 2 && y >= 2 && y < H - 2) h[c] += u_dt;
+    }
+    const unsigned b = __ballot_sync(kFull, level0);
+    if (b) {
+      int base_pos = 0;
+      if (lane == 0) base_pos = atomicAdd(&ctl->top, __popc(b));
+      base_pos = __shfl_sync(kFull, base_pos, 0);
+      if (level0) stack[base_pos + __popc(b & ((1u << lane) - 1u))] = (int32_t)c;
+    }
+  }
+}
+
+// pow(x, n) and pow(x, n-1) for the Newton update of fastscape_RB.cpp:322.
+__device__ __forceinline__ void powers(double x, double neq, int nmode,
+                                       double &pn, double &pn1) {
+  if (nmode == kNOne) {
+    pn = x;
+    pn1 = 1.0;
+  } else if (nmode == kNTwo) {
+    pn = x * x;
+    pn1 = x;
+  } else {
+    pn = pow(x, neq);
+    pn1 = pow(x, neq - 1.0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. Persistent level walker (cooperative launch, one grid barrier per level
+// per sweep).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWalkThreads)
+k_walk(WalkArgs a) {
+  unsigned epoch = 0;
+  Ctl *ctl = a.ctl;
+  if (ld_volatile_i32(&ctl->err) != 0) return;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthreads = gridDim.x * blockDim.x;
+  const bool stamp = a.stamp && tid == 0;
+  unsigned long long t_prev = stamp ? globaltimer_ns() : 0;
+  auto lap = [&](int slot) {
+    if (stamp) {
+      const unsigned long long t = globaltimer_ns();
+      atomicAdd(&ctl->walk_ns[slot], t - t_prev);
+      t_prev = t;
+    }
+  };
+
+  // ---- ordering: fastscape_RB.cpp:229-251 -------------------------------
+  int lo = 0;
+  int hi = ld_volatile_i32(&ctl->top);
+  if (tid == 0) {
+    a.lvl_off[0] = 0;
+    a.lvl_off[1] = hi;
+  }
+  int nlev = 1;
+  for (;;) {
+    const int j = (nlev - 1) % 3;  // counter of this expansion
+    if (tid == 0) ctl->lvlcnt[nlev % 3] = 0;  // counter of the next one
+    for (int i0 = lo + warp_global * 32; i0 < hi; i0 += nwarps * 32) {
+      const int i = i0 + lane;
+      unsigned m = 0;
+      int c = 0;
+      if (i < hi) {
+        c = __ldcg(&a.stack[i]);
+        m = a.mask[c];
+      }
+      const int nd = __popc(m);
+      int incl = nd;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += t;
+      }
+      const int total = __shfl_sync(kFull, incl, 31);
+      int base = 0;
+      if (lane == 31 && total) base = atomicAdd(&ctl->lvlcnt[j], total);
+      base = __shfl_sync(kFull, base, 31);
+      int pos = hi + base + incl - nd;
+      while (m) {
+        const int k = __ffs(m) - 1;
+        m &= m - 1;
+        if (pos < a.size)
+          a.stack[pos] = c + nbr_off(k, a.W);
+        else
+          raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+        ++pos;
+      }
+    }
+    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    const int added = ld_volatile_i32(&ctl->lvlcnt[j]);
+    if (added == 0) break;
+    lo = hi;
+    hi = hi + added;
+    ++nlev;
+    if (hi > a.size) {
+      if (tid == 0) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+      return;
+    }
+    if (tid == 0) a.lvl_off[nlev] = hi;
+  }
+  if (tid == 0) {
+    ctl->nlevels = nlev;
+    ctl->total = hi;
+  }
+  if (hi != a.size) {
+    // Some cells never reached base level: the receivers contain a cycle.
+    if (tid == 0) raise_err(ctl, FS_ERR_ORDER, kPhaseOrder);
+    return;
+  }
+  lap(0);
+
+  // ---- accumulation: fastscape_RB.cpp:262-279, pulled level by level ----
+  // cnt[c] = 1 + sum of the donors' counts; the reference's accum[c] is
+  // cnt[c]*cell_area (exact: integer multiples of cell_area).
+  for (int L = nlev - 1; L >= 0; --L) {
+    const int b = __ldcg(&a.lvl_off[L]);
+    const int e = __ldcg(&a.lvl_off[L + 1]);
+    for (int i = b + tid; i < e; i += nthreads) {
+      const int c = __ldcg(&a.stack[i]);
+      unsigned m = a.mask[c];
+      uint32_t s = 1;
+      while (m) {
+        const int k = __ffs(m) - 1;
+        m &= m - 1;
+        s += __ldcg(&a.cnt[c + nbr_off(k, a.W)]);
+      }
+      a.cnt[c] = s;
+    }
+    if (L > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+  }
+  lap(1);
+  if (!a.do_erode) return;
+  // No barrier here: level-1 erosion needs only the counts of level-1 cells
+  // (complete since the barrier after accumulation level 1) and the final h
+  // of level-0 cells (written by k_donors_level0). Accumulation of level 0,
+  // possibly still running in other blocks, reads counts and never h.
+
+  // ---- erosion: fastscape_RB.cpp:306-328 in the level order of
+  // fastscape_RB+P.cpp:319-350. Level 0 never erodes; its interior cells
+  // were uplifted by k_donors_level0. Each eroded cell's uplift
+  // (fastscape_RB.cpp:294) is applied to its first read.
+  for (int L = 1; L < nlev; ++L) {
+    const int b = __ldcg(&a.lvl_off[L]);
+    const int e = __ldcg(&a.lvl_off[L + 1]);
+    for (int i = b + tid; i < e; i += nthreads) {
+      const int c = __ldcg(&a.stack[i]);
+      const int r = a.rec[c];
+      const int n = c + nbr_off(r, a.W);
+      const uint32_t k = __ldcg(&a.cnt[c]);
+      const double fact = a.fact[2 * (size_t)k + (r & 1)];
+      const double h0 = __ldcg(&a.h[c]) + a.u_dt;
+      const double hn = __ldcg(&a.h[n]);
+      double hnew = h0;
+      double hp = h0;
+      double diff = 2 * a.tol;
+      int it = 0;
+      while (fabs(diff) > a.tol) {
+        double pn, pn1;
+        powers(hnew - hn, a.neq, a.nmode, pn, pn1);
+        hnew -= (hnew - h0 + fact * pn) / (1. + fact * a.neq * pn1);
+        diff = hnew - hp;
+        hp = hnew;
+        if (++it >= kNewtonMaxIt) {
+          raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
+          break;
+        }
+      }
+      if (!isfinite(hnew)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+      a.h[c] = hnew;
+    }
+    if (L + 1 < nlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+  }
+  lap(2);
+}
+
+__global__ void k_check_finite(const double *__restrict__ h, int size, Ctl *ctl) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  bool bad = false;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < size; i += stride)
+    bad |= !isfinite(h[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0)
+    raise_err(ctl, FS_ERR_NONFINITE, kPhaseNone);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11), counter = cell index,
+// key = seed. Two 32-bit outputs give one U[0,1) double with 53 random bits.
+__device__ __forceinline__ void philox4x32_10(uint32_t ctr[4], uint32_t key[2]) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  uint32_t k0 = key[0], k1 = key[1];
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(M0, ctr[0]), lo0 = M0 * ctr[0];
+    const uint32_t hi1 = __umulhi(M1, ctr[2]), lo1 = M1 * ctr[2];
+    const uint32_t n0 = hi1 ^ ctr[1] ^ k0;
+    const uint32_t n1 = lo1;
+    const uint32_t n2 = hi0 ^ ctr[3] ^ k1;
+    const uint32_t n3 = lo0;
+    ctr[0] = n0; ctr[1] = n1; ctr[2] = n2; ctr[3] = n3;
+    k0 += W0;
+    k1 += W1;
+  }
+}
+
+__global__ void k_philox_field(double *__restrict__ h, int W, int H, int size,
+                               uint32_t key0, uint32_t key1) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < size; c += stride) {
+    uint32_t ctr[4] = {(uint32_t)c, (uint32_t)((unsigned long long)c >> 32), 0u, 0u};
+    uint32_t key[2] = {key0, key1};
+    philox4x32_10(ctr, key);
+    const unsigned long long bits =
+        ((unsigned long long)(ctr[0] >> 5) << 26) | (unsigned long long)(ctr[1] >> 6);
+    double v = (double)bits * (1.0 / 9007199254740992.0);
+    const int y = (int)(c / W);
+    const int x = (int)(c - (long long)y * W);
+    if (x <= 1 || y <= 1 || x >= W - 2 || y >= H - 2) v = 0.0;
+    h[c] = v;
+  }
+}
+
+// A wait on a count that no block ever completes; the bounded barrier must
+// give up after timeout_ns and report FS_ERR_TIMEOUT. Used by the tests of
+// the failure path only.
+__global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
+  if (threadIdx.x == 0) {
+    const unsigned target = gridDim.x + 1;  // never reached
+    atomicAdd(&ctl->bar, 1u);
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (ld_acquire_u32(&ctl->bar) < target) {
+      if (ld_volatile_i32(&ctl->err) != 0) break;
+      if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+        raise_err(ctl, FS_ERR_TIMEOUT, kPhaseTest);
+        break;
+      }
+      __nanosleep(64);
+    }
+  }
+}
+
+}  // namespace
+
+int walk_threads() { return kWalkThreads; }
+const void *walk_kernel_ptr() { return reinterpret_cast<const void *>(&k_walk); }
+
+cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
+                             double dr_orth, double dr_diag, cudaStream_t s) {
+  const int iw = g.W - 4, ih = g.H - 4;
+  if (iw <= 0 || ih <= 0) return cudaSuccess;
+  dim3 block(32, 8);
+  dim3 grid((iw + 31) / 32, (ih + 7) / 8);
+  k_receivers<<<grid, block, 0, s>>>(h, rec, g.W, g.H, dr_orth, dr_diag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
+                                 int32_t *stack, double *h, Ctl *ctl,
+                                 StepGeom g, double u_dt, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long want = ((long long)g.size + 255) / 256;
+  int blocks = (int)(want < (long long)sms * 16 ? want : (long long)sms * 16);
+  if (blocks < 1) blocks = 1;
+  k_donors_level0<<<blocks, 256, 0, s>>>(rec, mask, stack, h, ctl, g.W, g.H,
+                                        g.size, u_dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s) {
+  WalkArgs args = a;
+  void *params[] = {&args};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(&k_walk),
+                                     dim3(blocks), dim3(kWalkThreads), params,
+                                     0, s);
+}
+
+cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
+                                cudaStream_t s) {
+  int blocks = (size + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  if (blocks < 1) blocks = 1;
+  k_check_finite<<<blocks, 256, 0, s>>>(h, size, ctl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,
+                                cudaStream_t s) {
+  int blocks = (g.size + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  if (blocks < 1) blocks = 1;
+  k_philox_field<<<blocks, 256, 0, s>>>(h, g.W, g.H, g.size, (uint32_t)seed,
+                                       (uint32_t)(seed >> 32));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_test_wait(Ctl *ctl, int blocks,
+                             unsigned long long timeout_ns, cudaStream_t s) {
+  k_test_wait<<<blocks, 32, 0, s>>>(ctl, timeout_ns);
+  return cudaGetLastError();
+}
+
+}  // namespace fs

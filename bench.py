@@ -1,0 +1,414 @@
+"""Benchmark: FastScape timestep on a 10000x10000 FP64 grid, one GB300.
+
+Workload (the reference's 10000^2 configuration): the reference's initial
+field (uniform [0,1) m, rings 0 and 1 at 0 m), K 2e-6, m 0.4, n 1,
+U 2e-3 m/yr, dt 1000 yr, dx = dy = 100 m. A bench "step" is one FastScape
+timestep over the whole grid (1e8 cell-steps): receivers, donors, level
+ordering, accumulation, uplift, erosion.
+
+  value      cell-steps/s with the field resident in HBM, timed with CUDA
+             events on the model's stream (K timesteps after W warm-up
+             timesteps). h (800 MB) is larger than L2, so no flush is needed.
+  e2e        the same metric through the reference-facing call sequence with
+             host buffers: fs_set_elevation (pinned host -> device), fs_run(20)
+             (21 timesteps, the reference's run semantics) and
+             fs_get_elevation (device -> pinned host), all inside the timed
+             region.
+  roofline   the dominant kernel's algorithmic bytes per launch / its mean
+             launch time (CUDA events), against the measured HBM copy peak.
+  cpu_baseline  the oracle's fastscape_RB+P restatement (OpenMP on every host
+             core) on a bounded sample of the same workload, rank 0 only.
+
+--impl reference times the reference's CPU implementation of the timestep:
+the reference's own FastScape_RBP compiled from its sources (oracle/_ref)
+where that build exists, else the oracle's restatement of it.
+
+Multi-GPU (torchrun): one independent replica per rank ("replicas only": a
+single grid does not shard); value = all ranks' cell-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-steps/s at 10000^2 FP64"
+UNIT = "cell-steps/s"
+SIDE = 10000
+RUN_NSTEP = 20            # run(20) executes 21 timesteps
+# Algorithmic bytes per cell for each kernel in this layout (h f64, rec i8,
+# mask u8, stack i32, cnt u32): each array the kernel must touch, once.
+ALG_BYTES = {
+    "receivers": 8 + 1,                     # h read, rec write
+    "donors_level0": 1 + 1,                 # rec read, mask write (+ level-0 list)
+    "walk": (4 + 1 + 4) + (4 + 1 + 4 + 4) + (4 + 1 + 4 + 8 + 8),
+    # ordering: stack read, mask read, stack write; accumulation: stack,
+    # mask, donor counts read once, count write; erosion: stack, rec, count,
+    # h read, h write.
+}
+STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [x for x in sm if x > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return dist, rank, ws, local
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def pinned_buffer(n: int):
+    """n float64 in page-locked host memory (torch is used only to pin)."""
+    import torch
+    t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    return t, t.numpy()
+
+
+def cpu_sample(side: int, nsteps: int, prefer_reference: bool):
+    """Times the CPU implementation of the timestep on a side^2 grid.
+    Returns (cell-steps/s, kind, threads, description)."""
+    import ctypes
+
+    from oracle.pyoracle import Oracle, workload_params
+    p = workload_params()
+    if prefer_reference:
+        path = ROOT / "oracle" / "_ref" / "libfsref_param_shipped.so"
+        if path.exists():
+            try:
+                from oracle.pyoracle import RefHarness
+                hr = RefHarness("param", "shipped")
+                m = hr.model(side, side, p, 1)
+                m.prepare()
+                m.step()                       # warm-up timestep
+                t0 = time.perf_counter()
+                for _ in range(nsteps):
+                    m.step()
+                dt = time.perf_counter() - t0
+                thr = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+                return (side * side * nsteps / dt, "reference", thr,
+                        f"reference FastScape_RBP (oracle/_ref, -O3 -march=native), "
+                        f"{side}^2, {nsteps} timesteps after 1 warm-up")
+            except OSError:
+                pass
+    o = Oracle()
+    h = o.terrain(side, side, 0)
+    lib = o.lib
+    from oracle.pyoracle import FsoParams
+
+    class Work(ctypes.Structure):
+        _fields_ = [("W", ctypes.c_int), ("H", ctypes.c_int)] + \
+                   [(n, ctypes.c_void_p) for n in ("rec", "ndon", "donor", "stack", "levels", "accum")] + \
+                   [("nlevel", ctypes.c_int)]
+    lib.fso_work_init.argtypes = [ctypes.POINTER(Work), ctypes.c_int, ctypes.c_int]
+    lib.fso_work_free.argtypes = [ctypes.POINTER(Work)]
+    lib.fso_step.argtypes = [ctypes.POINTER(Work), ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(FsoParams), ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_double)]
+    w = Work()
+    if lib.fso_work_init(ctypes.byref(w), side, side) != 0:
+        raise MemoryError("oracle work arrays")
+    pc = p.c()
+    hp = h.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    lib.fso_step(ctypes.byref(w), hp, ctypes.byref(pc), 1, None)   # warm-up
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        lib.fso_step(ctypes.byref(w), hp, ctypes.byref(pc), 1, None)
+    dt = time.perf_counter() - t0
+    lib.fso_work_free(ctypes.byref(w))
+    return (side * side * nsteps / dt, "port", o.threads(),
+            f"oracle restatement of fastscape_RB+P (level-parallel erosion, OpenMP), "
+            f"{side}^2, {nsteps} timesteps after 1 warm-up")
+
+
+def run_reference_arm(args, dist, rank, ws):
+    if rank != 0:
+        return
+    side = args.side
+    t_all = []
+    # one bounded CPU timestep per bench step
+    import ctypes
+    from oracle.pyoracle import workload_params
+    p = workload_params()
+    kind, desc, thr = None, None, None
+    path = ROOT / "oracle" / "_ref" / "libfsref_param_shipped.so"
+    stepper = None
+    if path.exists():
+        try:
+            from oracle.pyoracle import RefHarness
+            hr = RefHarness("param", "shipped")
+            m = hr.model(side, side, p, 1)
+            m.prepare()
+            stepper = m.step
+            kind = "reference"
+            thr = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+            desc = f"reference FastScape_RBP compiled from its sources (-O3 -march=native), {side}^2"
+        except OSError:
+            stepper = None
+    if stepper is None:
+        from oracle.pyoracle import FsoParams, Oracle
+        o = Oracle()
+        h = o.terrain(side, side, 0)
+
+        class Work(ctypes.Structure):
+            _fields_ = [("W", ctypes.c_int), ("H", ctypes.c_int)] + \
+                       [(n, ctypes.c_void_p) for n in ("rec", "ndon", "donor", "stack", "levels", "accum")] + \
+                       [("nlevel", ctypes.c_int)]
+        lib = o.lib
+        lib.fso_work_init.argtypes = [ctypes.POINTER(Work), ctypes.c_int, ctypes.c_int]
+        lib.fso_step.argtypes = [ctypes.POINTER(Work), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(FsoParams), ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_double)]
+        w = Work()
+        lib.fso_work_init(ctypes.byref(w), side, side)
+        pc = p.c()
+        hp = h.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        stepper = lambda: lib.fso_step(ctypes.byref(w), hp, ctypes.byref(pc), 1, None)  # noqa: E731
+        kind = "port"
+        thr = o.threads()
+        desc = f"oracle restatement of fastscape_RB+P (OpenMP), {side}^2"
+    for _ in range(args.warmup):
+        stepper()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        stepper()
+        t_all.append(time.perf_counter() - t0)
+    tot = sum(t_all)
+    value = side * side * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"FastScape timestep, {side}x{side} FP64, K 2e-6 m 0.4 n 1 "
+                               f"U 2e-3 dt 1000 dx 100", "grid": [side, side],
+                   "step": "one timestep over the whole grid", "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": kind,
+                         "sample": f"{desc}, {args.steps} timesteps after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--side", type=int, default=SIDE)
+    ap.add_argument("--e2e-calls", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+
+    dist, rank, ws, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, dist, rank, ws)
+        return
+
+    import __graft_entry__ as ge
+    pkg = ge.load()
+    lib = pkg.library()
+    import torch  # noqa: F401  (pinned host buffers)
+    if ws > 1:
+        torch.cuda.set_device(local)
+    side = args.side
+    p = pkg.workload_params()
+    m = pkg.FastScape_RBP(side, side, params=p, init=pkg.INIT_REFERENCE, seed=123)
+    h0 = m.getH()
+
+    # ---- device-resident throughput -------------------------------------
+    m.step(args.warmup)
+    m.set_timing(True)
+    m.phase_times(reset=True)
+    barrier(dist)
+    m.synchronize()
+    with Clocks(local) as clk:
+        m.step(args.steps)
+    barrier(dist)
+    t = m.phase_times(reset=True)
+    m.set_timing(False)
+    total_ms = max_over_ranks(dist, float(t[3]))
+    cells = side * side
+    value = ws * cells * args.steps / (total_ms * 1e-3)
+    launches = 3 * args.steps
+
+    # ---- roofline of the dominant kernel ----------------------------------
+    peak, peak_kind = load_peaks()
+    kern = {"receivers": t[0], "donors_level0": t[1], "walk": t[2]}
+    dom = max(kern, key=kern.get)
+    per_launch_ms = kern[dom] / args.steps
+    achieved = ALG_BYTES[dom] * cells / (per_launch_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "alg_bytes_per_cell": ALG_BYTES[dom], "peak_source": f"{peak_kind} hbm_gbs",
+                "kernel_ms": {k: v / args.steps for k, v in kern.items()},
+                "walk_split_ms": {"ordering": t[4] / args.steps,
+                                  "accumulation": t[5] / args.steps,
+                                  "erosion": t[6] / args.steps}}
+    step_rf = cells * args.steps / (total_ms * 1e-3) * STEP_ALG_BYTES / 1e9
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            tr = json.loads(prof.read_text())
+            if dom in tr:
+                roofline["traffic"] = tr[dom]["bytes_per_launch_at_10000"]
+        except (ValueError, KeyError):
+            pass
+
+    # ---- end to end through the reference-facing calls ------------------
+    hbuf_t, hbuf = pinned_buffer(cells)
+    obuf_t, obuf = pinned_buffer(cells)
+    hbuf[:] = h0
+    dp = C.POINTER(C.c_double)
+    hptr = hbuf.ctypes.data_as(dp)
+    optr = obuf.ctypes.data_as(dp)
+    pkg.check(lib.fs_set_elevation(m.handle, hptr))
+    pkg.check(lib.fs_run(m.handle, RUN_NSTEP))   # warm-up of the e2e path
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_calls):
+        pkg.check(lib.fs_set_elevation(m.handle, hptr))
+        pkg.check(lib.fs_run(m.handle, RUN_NSTEP))
+        pkg.check(lib.fs_get_elevation(m.handle, optr))
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = ws * cells * (RUN_NSTEP + 1) * args.e2e_calls / e2e_s
+    checksum = float(np.sum(obuf))
+    m.close()
+
+    # ---- CPU baseline (rank 0, N = 1 only) --------------------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        v, kind, thr, desc = cpu_sample(side, args.cpu_steps, prefer_reference=False)
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": kind, "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"FastScape timestep, {side}x{side} FP64, reference initial "
+                                   f"field, K 2e-6 m 0.4 n 1 U 2e-3 dt 1000 dx 100",
+                       "grid": [side, side], "step": "one timestep over the whole grid",
+                       "e2e_step": f"fs_set_elevation + fs_run({RUN_NSTEP}) "
+                                   f"({RUN_NSTEP + 1} timesteps) + fs_get_elevation",
+                       "l2": "inputs larger than L2 (h is 800 MB)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roofline,
+            "step_roofline": {"alg_bytes_per_cell_step": STEP_ALG_BYTES,
+                              "achieved_gbs": step_rf, "frac": step_rf / peak},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": 8 * cells, "d2h_bytes_per_step": 8 * cells,
+                    "calls": args.e2e_calls, "checksum": checksum},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,171 @@
+/*
+ * fastscape_gb300.h -- C ABI of the GB300 FastScape timestep.
+ *
+ * The reference exposes one C++ model object per variant, e.g.
+ *   class FastScape_RBP                      fastscape_RB+P.cpp:46
+ *     FastScape_RBP(int width, int height)   fastscape_RB+P.cpp:138-154
+ *     void run(int nstep)                    fastscape_RB+P.cpp:363-424
+ *     std::vector<double>& getH()            fastscape_RB+P.cpp:429-431
+ * with its physical constants hard-coded at fastscape_RB.cpp:58-65. This ABI
+ * keeps that object model (create from width/height, run N timesteps, read
+ * back elevation) behind plain C types, adds the parameters as a struct, and
+ * adds read-backs of the intermediate fields the reference keeps private
+ * (accumulation, receivers, levels, donors).
+ *
+ * Conventions (identical to the reference, fastscape_RB.cpp:69-97):
+ *   - grids are row-major, cell c = y*width + x, width*height cells;
+ *   - ring 0 (outermost) is a halo and ring 1 is fixed base level; only
+ *     cells with 2 <= x < width-2 and 2 <= y < height-2 are computed;
+ *   - receiver direction codes: 0..7 = W, NW, N, NE, E, SE, S, SW
+ *     (neighbour offsets -1, -W-1, -W, -W+1, +1, +W+1, +W, +W-1), and
+ *     FS_NO_FLOW (-1) for a cell with no strictly lower neighbour.
+ *
+ * Every function returns FS_OK (0) or a negative FS_ERR_* status; the text of
+ * the last error on the calling thread is available from fs_last_error().
+ * No C++ exception crosses this boundary. A model is not thread-safe: use one
+ * model per host thread or lock around calls. Each model owns one CUDA stream
+ * on the device that was current when it was created.
+ */
+#ifndef FASTSCAPE_GB300_H
+#define FASTSCAPE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_NO_FLOW (-1)
+
+/* Status codes. */
+#define FS_OK 0
+#define FS_ERR_ARG (-1)            /* invalid argument                         */
+#define FS_ERR_CUDA (-2)           /* CUDA runtime error (see fs_last_error)   */
+#define FS_ERR_TIMEOUT (-3)        /* a grid-wide barrier wait ran out         */
+#define FS_ERR_LEVEL_OVERFLOW (-4) /* level walk exceeded width*height levels  */
+#define FS_ERR_NONFINITE (-5)      /* NaN/Inf elevation produced or supplied   */
+#define FS_ERR_ORDER (-6)          /* receivers do not form a forest (cycle)   */
+#define FS_ERR_NEWTON (-7)         /* Newton iteration did not converge        */
+#define FS_ERR_NOMEM (-8)          /* device allocation failed                 */
+#define FS_ERR_STATE (-9)          /* no timestep has been executed yet        */
+
+/* Initial-field generators for fs_create. */
+#define FS_INIT_ZERO 0        /* all zeros; set the field with fs_set_elevation */
+#define FS_INIT_REFERENCE 1   /* the reference's field: std::mt19937 seeded with
+                                 seed*0 (random.cpp:31 seeds thread t with
+                                 seed*t; the field is built on thread 0), so it
+                                 is the same for every nonzero seed, drawn with
+                                 uniform_real_distribution<double>(0,1) over
+                                 all cells row-major, rings 0 and 1 set to 0
+                                 (fastscape_RB.cpp:111-130)                     */
+#define FS_INIT_MT19937 2     /* same generator seeded with `seed` itself       */
+#define FS_INIT_PHILOX 3      /* device Philox4x32-10 keyed by `seed`, U[0,1)
+                                 with 53-bit resolution; rings set to 0        */
+
+/* Physical constants of one realization; the reference hard-codes them at
+ * fastscape_RB.cpp:58-65 (keq, neq, meq, ueq, dt, dr[8], tol, cell_area). */
+typedef struct fs_params {
+  double keq;       /* stream-power coefficient K                          */
+  double neq;       /* slope exponent n                                    */
+  double meq;       /* drainage-area exponent m                            */
+  double ueq;       /* uplift rate U (applied to interior cells)           */
+  double dt;        /* timestep                                            */
+  double dr_orth;   /* distance to the W/N/E/S neighbours (dr[0,2,4,6])    */
+  double dr_diag;   /* distance to the diagonal neighbours (dr[1,3,5,7])   */
+  double tol;       /* Newton convergence tolerance                        */
+  double cell_area; /* area of one cell (accumulation unit)                */
+} fs_params;
+
+typedef struct fs_model fs_model;
+
+/* The reference's own constants (fastscape_RB.cpp:58-65): K 2e-6, n 2, m 0.8,
+ * U 2e-3, dt 1000, dr {1, SQRT2}, tol 1e-3, cell_area 40000. */
+void fs_params_reference(fs_params *out);
+
+/* The 1000^2 / 10000^2 workload: K 2e-6, n 1, m 0.4, U 2e-3, dt 1000,
+ * dr {dx, dx*SQRT2}, tol 1e-3, cell_area dx*dx, with dx = 100 m. */
+void fs_params_workload(fs_params *out, double dx);
+
+/* Replaces the constructor FastScape_RBP(width, height)
+ * (fastscape_RB+P.cpp:138-154; terrain fastscape_RB.cpp:111-130).
+ * width, height >= 3. Returns NULL on failure with *status set. */
+fs_model *fs_create(int width, int height, const fs_params *params,
+                    int init_mode, uint64_t seed, int *status);
+
+/* Frees every device buffer. Safe on NULL. */
+void fs_destroy(fs_model *m);
+
+/* Replaces FastScape_RBP::run(nstep) (fastscape_RB+P.cpp:363-424): executes
+ * nstep+1 timesteps, exactly as the reference's `step<=nstep` loop does
+ * (fastscape_RB.cpp:366). nstep >= -1. */
+int fs_run(fs_model *m, int nstep);
+
+/* Executes exactly k timesteps (k >= 0). */
+int fs_step(fs_model *m, int k);
+
+/* Replaces getH() (fastscape_RB+P.cpp:429-431): copies width*height
+ * elevations into caller-owned host memory. */
+int fs_get_elevation(const fs_model *m, double *out);
+
+/* Replaces the field (the reference lets callers alter h between runs,
+ * fastscape_RB.cpp:334-340). Rejects NaN/Inf with FS_ERR_NONFINITE. */
+int fs_set_elevation(fs_model *m, const double *in);
+
+/* Flow accumulation of the last executed timestep (fastscape_RB.cpp:262-279;
+ * private and freed in the reference): width*height doubles. */
+int fs_get_accumulation(const fs_model *m, double *out);
+
+/* Receiver direction codes of the last executed timestep
+ * (fastscape_RB.cpp:160-182): width*height int32 in {-1, 0..7}. */
+int fs_get_receivers(const fs_model *m, int32_t *dir);
+
+/* Receiver cell indices: rec index, or the cell itself for FS_NO_FLOW (the
+ * self-receiver convention of FastScapeMin.f90:63). */
+int fs_get_receiver_index(const fs_model *m, int64_t *idx);
+
+/* Level of every cell in the last timestep's ordering (fastscape_RB.cpp:
+ * 213-254): level 0 = FS_NO_FLOW cells, level k+1 = donors of level k.
+ * *nlevels = number of levels (the reference's `nlevel` is *nlevels + 1). */
+int fs_get_levels(const fs_model *m, int32_t *level_id, int32_t *nlevels);
+
+/* Donor mask of the last timestep: bit k set when the neighbour in
+ * direction k drains into the cell. The reference's donor list of a cell
+ * (fastscape_RB.cpp:188-203, ascending cell index) is the set bits taken in
+ * the order NW(1), N(2), NE(3), W(0), E(4), SW(7), S(6), SE(5). */
+int fs_get_donor_mask(const fs_model *m, uint8_t *mask);
+
+/* Grid geometry and counters. */
+int fs_get_shape(const fs_model *m, int *width, int *height);
+int fs_get_params(const fs_model *m, fs_params *out);
+int64_t fs_steps_executed(const fs_model *m);
+
+/* Device time in milliseconds accumulated over timed fs_step/fs_run calls
+ * since the last reset, measured with CUDA events on the model's stream
+ * (enabled by fs_set_timing(m, 1)). ms[] holds FS_NUM_TIMERS values:
+ *   0 receiver kernel, 1 donor/level-0 kernel, 2 level-walk kernel,
+ *   3 whole timed calls (first event to last),
+ *   4..6 split of the level walk measured inside it (ordering,
+ *        accumulation, uplift+erosion). */
+#define FS_NUM_TIMERS 7
+int fs_set_timing(fs_model *m, int enable);
+int fs_get_phase_times(const fs_model *m, double *ms, int reset);
+
+/* Limit (milliseconds) on every grid-wide barrier wait; default 2000. */
+int fs_set_barrier_timeout(fs_model *m, double ms);
+
+/* Waits for the model's stream. */
+int fs_synchronize(const fs_model *m);
+
+/* Copies the last error message of this thread into buf (NUL-terminated);
+ * returns the message length. */
+size_t fs_last_error(char *buf, size_t n);
+
+/* Library version string. */
+const char *fs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTSCAPE_GB300_H */

@@ -1,0 +1,29 @@
+/*
+ * fastscape_gb300_testing.h -- testing hooks of the GB300 FastScape library.
+ * They exercise the failure paths on the host side of the boundary; they
+ * have no counterpart in the reference (which has no error reporting,
+ * fastscape_RB+P.cpp:229-260 uses assert).
+ */
+#ifndef FASTSCAPE_GB300_TESTING_H
+#define FASTSCAPE_GB300_TESTING_H
+
+#include "fastscape_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Installs caller-supplied receiver codes (rings must be FS_NO_FLOW) and runs
+ * donors, ordering and accumulation without uplift or erosion. Receivers
+ * that contain a cycle make it return FS_ERR_ORDER. */
+int fs_test_order_from_receivers(fs_model *m, const int32_t *dir);
+
+/* Runs a device wait on a count that never completes, bounded by `ms`
+ * milliseconds; returns FS_ERR_TIMEOUT when the bound works. */
+int fs_test_barrier_timeout(fs_model *m, double ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,156 @@
+"""GPU parity: the CUDA timestep through the C ABI against the golden fixtures
+(produced by the reference's own code) and against the oracle, bit-for-bit.
+
+Receivers, donor masks, level ids, accumulation and elevation must be
+identical (tolerance 0 ulp) for n = 1 (the workload) and n = 2 (the
+reference's own constants): the device follows the reference's operation
+order with no multiply-add contraction, and pow(k*cell_area, m) comes from a
+table evaluated with the C library's pow.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Params, donor_mask_from_rec, level_ids
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+STEP_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz")
+                    if not p.stem.startswith(("run_", "terrain_")))
+RUN_CASES = sorted(p.stem for p in GOLDEN.glob("run_*.npz"))
+
+
+def load(name):
+    return dict(np.load(GOLDEN / f"{name}.npz"))
+
+
+def gpu_params(pkg, arr):
+    return pkg.Params(*[float(x) for x in arr])
+
+
+def assert_step_equal(m, W, H, ref, tag=""):
+    rec = m.receivers()
+    assert np.array_equal(rec, ref["rec"].astype(np.int32)), f"receivers {tag}"
+    assert np.array_equal(m.donor_mask(), donor_mask_from_rec(rec, W, H)), f"donor mask {tag}"
+    lid, nl = m.levels()
+    want_lid = level_ids(ref["stack"], ref["levels"], W * H)
+    assert nl == len(ref["levels"]) - 1, f"nlevels {tag}"
+    assert np.array_equal(lid, want_lid), f"level ids {tag}"
+    assert np.array_equal(m.accumulation(), ref["accum"]), f"accumulation {tag}"
+    assert np.array_equal(m.getH(), ref["h"]), f"elevation {tag}"
+
+
+@pytest.mark.parametrize("name", STEP_CASES)
+def test_golden_per_timestep(pkg, name):
+    g = load(name)
+    W, H, ns = int(g["W"]), int(g["H"]), int(g["nsteps"])
+    with pkg.FastScape_RBP(W, H, params=gpu_params(pkg, g["params"]), init=pkg.INIT_ZERO) as m:
+        m.setH(g["h0"])
+        for s in range(ns):
+            m.step(1)
+            ref = {"rec": g[f"rec_{s}"], "stack": g[f"stack_{s}"], "levels": g[f"levels_{s}"],
+                   "accum": g[f"accum_{s}"], "h": g[f"h_{s}"]}
+            assert_step_equal(m, W, H, ref, f"{name} step {s}")
+
+
+@pytest.mark.parametrize("name", RUN_CASES)
+def test_golden_run(pkg, name):
+    g = load(name)
+    W = int(g["W"])
+    with pkg.FastScape_RBP(W, W, params=gpu_params(pkg, g["params"]),
+                           init=pkg.INIT_REFERENCE) as m:
+        assert np.array_equal(m.getH(), g["h0"])
+        m.run(int(g["nstep"]))
+        assert m.steps_executed() == int(g["nstep"]) + 1
+        assert np.array_equal(m.getH(), g["h_final"])
+
+
+@pytest.mark.parametrize("W,H,steps,seed,n", [
+    (5, 5, 4, 1, 1), (7, 5, 4, 2, 1), (64, 64, 10, 3, 1), (129, 67, 10, 4, 2),
+    (333, 250, 6, 5, 1), (512, 512, 12, 6, 2),
+])
+def test_oracle_trajectory(pkg, oracle, W, H, steps, seed, n):
+    rng = np.random.default_rng(seed)
+    p = pkg.workload_params() if n == 1 else pkg.reference_params()
+    op = Params(*p.as_tuple())
+    h = rng.uniform(0, 3, W * H)
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+        m.setH(h)
+        for s in range(steps):
+            m.step(1)
+            ref = oracle.phases(h, W, H, op)
+            assert_step_equal(m, W, H, ref, f"step {s}")
+
+
+def test_reference_field_generator(pkg, oracle):
+    for W, H in [(16, 16), (101, 37)]:
+        with pkg.FastScape_RBP(W, H, init=pkg.INIT_REFERENCE, seed=123) as m:
+            assert np.array_equal(m.getH(), oracle.terrain(W, H, 0))
+        with pkg.FastScape_RBP(W, H, init=pkg.INIT_MT19937, seed=77) as m:
+            assert np.array_equal(m.getH(), oracle.terrain(W, H, 77))
+
+
+def test_philox_field(pkg):
+    W, H = 300, 200
+    with pkg.FastScape_RBP(W, H, init=pkg.INIT_PHILOX, seed=42) as a, \
+            pkg.FastScape_RBP(W, H, init=pkg.INIT_PHILOX, seed=42) as b, \
+            pkg.FastScape_RBP(W, H, init=pkg.INIT_PHILOX, seed=43) as c:
+        ha, hb, hc = a.getH(), b.getH(), c.getH()
+    assert np.array_equal(ha, hb) and not np.array_equal(ha, hc)
+    g = ha.reshape(H, W)
+    assert np.all(g[:2, :] == 0) and np.all(g[-2:, :] == 0)
+    assert np.all(g[:, :2] == 0) and np.all(g[:, -2:] == 0)
+    inner = g[2:-2, 2:-2]
+    assert inner.min() >= 0 and inner.max() < 1 and abs(inner.mean() - 0.5) < 0.01
+
+
+def test_workload_1000_full_run(pkg, oracle):
+    """The 1000x1000 workload: run(120) = 121 timesteps, final elevation
+    bit-identical to the oracle (fastscape_RB+P semantics)."""
+    W = 1000
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(W, W, params=p, init=pkg.INIT_REFERENCE) as m:
+        m.run(120)
+        got = m.getH()
+        lid, nl = m.levels()
+        acc = m.accumulation()
+    h = oracle.terrain(W, W, 0)
+    oracle.run(h, W, W, Params(*p.as_tuple()), 120, parallel=True)
+    assert np.array_equal(got, h)
+    assert nl >= 2 and acc.min() == p.cell_area
+
+
+def test_run_then_run_equals_one_run(pkg):
+    """State carried between run() calls is only h (fastscape_RB.cpp:334-340)."""
+    W = 200
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(W, W, params=p) as a, pkg.FastScape_RBP(W, W, params=p) as b:
+        a.run(4); a.run(9)          # 5 + 10 timesteps
+        b.step(15)
+        assert np.array_equal(a.getH(), b.getH())
+
+
+def test_deterministic_repeat(pkg):
+    W = 700
+    p = pkg.workload_params()
+    outs = []
+    for _ in range(2):
+        with pkg.FastScape_RBP(W, W, params=p, init=pkg.INIT_PHILOX, seed=9) as m:
+            m.step(6)
+            outs.append((m.getH(), m.receivers(), m.levels()[0], m.accumulation()))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_timing_counters(pkg):
+    with pkg.FastScape_RBP(256, 256, params=pkg.workload_params()) as m:
+        m.set_timing(True)
+        m.step(3)
+        t = m.phase_times(reset=True)
+        assert np.all(t > 0)
+        assert t[3] >= t[0] + t[1] + t[2] * 0.99
+        assert np.all(m.phase_times() == 0)
