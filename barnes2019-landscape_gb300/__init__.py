@@ -43,6 +43,7 @@ ABI_SYMBOLS = [
     "fs_steps_executed", "fs_set_timing", "fs_get_phase_times",
     "fs_set_barrier_timeout", "fs_synchronize", "fs_last_error", "fs_version",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
+    "fs_test_set_receiver_path", "fs_test_receiver_fixups",
 ]
 
 
@@ -120,6 +121,8 @@ def library() -> C.CDLL:
     L.fs_version.restype = C.c_char_p
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
     L.fs_test_barrier_timeout.argtypes = [vp, C.c_double]
+    L.fs_test_set_receiver_path.argtypes = [vp, C.c_int]
+    L.fs_test_receiver_fixups.argtypes = [vp, i32p]
     _lib = L
     return L
 

@@ -20,7 +20,8 @@ struct Ctl {
   int top;                 // level-0 fill pointer (absolute stack index)
   unsigned int bar;        // grid-barrier arrival counter
   int lvlcnt[3];           // rotating per-level append counters (relative)
-  int pad[3];
+  int amb;                 // cells queued by the receiver filter
+  int pad[2];
 };
 constexpr size_t kCtlResetOffset = offsetof(Ctl, top);
 constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
@@ -66,6 +67,9 @@ struct WalkArgs {
 // Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
 cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
                              double dr_orth, double dr_diag, cudaStream_t s);
+cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
+                                  Ctl *ctl, StepGeom g, double dr_orth,
+                                  double dr_diag, cudaStream_t s);
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
                                  int32_t *stack, double *h, Ctl *ctl,
                                  StepGeom g, double u_dt, cudaStream_t s);

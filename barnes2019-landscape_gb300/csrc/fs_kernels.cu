@@ -127,6 +127,135 @@ k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
 }
 
 // ---------------------------------------------------------------------------
+// 1b. Receivers, fast path. GB300 runs FP64 at ~1.6 lanes/clock/SM against
+// ~113 for FP32, so the eight FP64 divides per cell of the reference formula
+// would dominate the timestep. This kernel decides the receiver from FP32
+// approximations with a rigorous error bound and hands the rare cells it
+// cannot prove to k_receivers_fixup, which evaluates the reference formula in
+// FP64. The result is identical to k_receivers for every input.
+//
+// Bound: f = h truncated to FP32 (|f-h| <= 2^-23|h| + 2^-126),
+// a_n = fl(fl(f_c - f_n) * g_n) with g_n = fl(1/dr_n); then for the exact
+// reference slope q_n = RN(RN(h_c-h_n)/dr_n):
+//   |a_n - q_n| <= 2^-20 * gmax * (M + 2^-100) =: E/2,
+// M = max |f| over the 3x3 window, gmax = max g_n. So
+//   best - second > 2E  and best > E  => q_best is the unique maximum > 0;
+//   best < -E                         => every q_n < 0 (NO_FLOW);
+// otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
+// ---------------------------------------------------------------------------
+constexpr int kRxTile = 32;  // interior cells per tile in x
+constexpr int kRyTile = 32;  // interior cells per tile in y
+
+// Truncation of a double to FP32 with integer operations only (no FP64
+// pipe): rebias the exponent, keep the top 23 fraction bits. Values below
+// 2^-126 flush to signed zero; |x| >= 2^128, Inf and NaN give NaN, which
+// sends the cell to the exact path.
+__device__ __forceinline__ float trunc_to_float(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  const unsigned frac = (unsigned)(b >> 29) & 0x7FFFFFu;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(0x7FC00000u);
+  return __uint_as_float(sign | ((unsigned)e << 23) | frac);
+}
+
+__global__ void __launch_bounds__(256)
+k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
+                   int32_t *__restrict__ amb, Ctl *ctl, int W, int H,
+                   float g_orth, float g_diag, float gmax) {
+  __shared__ float s[kRyTile + 2][kRxTile + 3];
+  const int x0 = blockIdx.x * kRxTile + 1;  // grid x of s[.][0]
+  const int y0 = blockIdx.y * kRyTile + 1;  // grid y of s[0][.]
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int idx = t; idx < (kRyTile + 2) * (kRxTile + 2); idx += 256) {
+    const int ly = idx / (kRxTile + 2);
+    const int lx = idx - ly * (kRxTile + 2);
+    const int gx = x0 + lx, gy = y0 + ly;
+    float v = 0.f;
+    if (gx < W && gy < H) v = trunc_to_float(h[(size_t)gy * W + gx]);
+    s[ly][lx] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x;
+  const int lx = threadIdx.x + 1;
+  const int gx = x0 + lx;
+#pragma unroll 1
+  for (int r = 0; r < kRyTile / 8; r++) {
+    const int ly = threadIdx.y + 8 * r + 1;
+    const int gy = y0 + ly;
+    const bool valid = gx < W - 2 && gy < H - 2;
+    bool queue = false;
+    if (valid) {
+      const float fc = s[ly][lx];
+      const float f[8] = {s[ly][lx - 1], s[ly - 1][lx - 1], s[ly - 1][lx],
+                          s[ly - 1][lx + 1], s[ly][lx + 1], s[ly + 1][lx + 1],
+                          s[ly + 1][lx], s[ly + 1][lx - 1]};
+      float best = -INFINITY, second = -INFINITY;
+      int bn = 0;
+      float M = fabsf(fc);
+      bool bad = !(fc == fc);
+#pragma unroll
+      for (int n = 0; n < 8; n++) {
+        const float a = (fc - f[n]) * ((n & 1) ? g_diag : g_orth);
+        M = fmaxf(M, fabsf(f[n]));
+        bad |= !(a == a);
+        if (a > best) {
+          second = best;
+          best = a;
+          bn = n;
+        } else if (a > second) {
+          second = a;
+        }
+      }
+      const float E = 0x1p-19f * gmax * (M + 0x1p-100f);
+      int code = -2;  // undecided
+      if (!bad) {
+        if (best - second > 2.f * E && best > E)
+          code = bn;
+        else if (best < -E)
+          code = FS_NO_FLOW;
+      }
+      if (code == -2)
+        queue = true;
+      else
+        rec[(size_t)gy * W + gx] = (int8_t)code;
+    }
+    const unsigned bq = __ballot_sync(kFull, queue);
+    if (bq) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&ctl->amb, __popc(bq));
+      base = __shfl_sync(kFull, base, 0);
+      if (queue) amb[base + __popc(bq & ((1u << lane) - 1u))] = gy * W + gx;
+    }
+  }
+}
+
+// The queued cells of k_receivers_filter, with the reference formula in FP64.
+__global__ void __launch_bounds__(256)
+k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
+                  const int32_t *__restrict__ amb, const Ctl *ctl, int W,
+                  double dr_orth, double dr_diag) {
+  const int n_amb = ld_volatile_i32(&ctl->amb);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_amb; i += gridDim.x * blockDim.x) {
+    const int c = amb[i];
+    const double hc = h[c];
+    double max_slope = 0;
+    int max_n = FS_NO_FLOW;
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      const double slope = (hc - h[c + nbr_off(n, W)]) / ((n & 1) ? dr_diag : dr_orth);
+      if (slope > max_slope) {
+        max_slope = slope;
+        max_n = n;
+      }
+    }
+    rec[c] = (int8_t)max_n;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // 2. Donor masks + level 0 + uplift of interior level-0 cells.
 // Bit k of mask[c] is set when neighbour c+nshift[k] has receiver code
 // (k+4)%8, i.e. drains into c (the pull form of fastscape_RB+GPU.cpp:155-182).
@@ -415,6 +544,25 @@ cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
   dim3 block(32, 8);
   dim3 grid((iw + 31) / 32, (ih + 7) / 8);
   k_receivers<<<grid, block, 0, s>>>(h, rec, g.W, g.H, dr_orth, dr_diag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
+                                  Ctl *ctl, StepGeom g, double dr_orth,
+                                  double dr_diag, cudaStream_t s) {
+  const int iw = g.W - 4, ih = g.H - 4;
+  if (iw <= 0 || ih <= 0) return cudaSuccess;
+  const float g_orth = (float)(1.0 / dr_orth), g_diag = (float)(1.0 / dr_diag);
+  const float gmax = g_orth > g_diag ? g_orth : g_diag;
+  dim3 block(32, 8);
+  dim3 grid((iw + kRxTile - 1) / kRxTile, (ih + kRyTile - 1) / kRyTile);
+  k_receivers_filter<<<grid, block, 0, s>>>(h, rec, amb, ctl, g.W, g.H, g_orth, g_diag, gmax);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_receivers_fixup<<<sms, 256, 0, s>>>(h, rec, amb, ctl, g.W, dr_orth, dr_diag);
   return cudaGetLastError();
 }
 

@@ -90,6 +90,7 @@ struct fs_model {
   int8_t *d_rec = nullptr;
   uint8_t *d_mask = nullptr;
   int32_t *d_stack = nullptr;
+  int32_t *d_amb = nullptr;   // cells the receiver filter could not decide
   int32_t *d_lvl = nullptr;
   uint32_t *d_cnt = nullptr;
   double *d_fact = nullptr;
@@ -102,6 +103,7 @@ struct fs_model {
   long long steps = 0;
   bool have_step = false;
   bool timing = false;
+  bool exact_receivers = false;  // testing: FP64 reference formula for every cell
   std::vector<cudaEvent_t> ev;  // timing mode: 3 per timestep + 1
   double phase_ms[4] = {0, 0, 0, 0};
 };
@@ -118,6 +120,7 @@ void free_model(fs_model *m) {
   cudaFree(m->d_rec);
   cudaFree(m->d_mask);
   cudaFree(m->d_stack);
+  cudaFree(m->d_amb);
   cudaFree(m->d_lvl);
   cudaFree(m->d_cnt);
   cudaFree(m->d_fact);
@@ -230,7 +233,11 @@ int one_step(fs_model *m, int i) {
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i], m->stream));
   FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(m->d_ctl) + fs::kCtlResetOffset, 0,
                           fs::kCtlResetBytes, m->stream));
-  FS_CUDA(fs::launch_receivers(m->d_h, m->d_rec, g, m->p.dr_orth, m->p.dr_diag, m->stream));
+  if (m->exact_receivers)
+    FS_CUDA(fs::launch_receivers(m->d_h, m->d_rec, g, m->p.dr_orth, m->p.dr_diag, m->stream));
+  else
+    FS_CUDA(fs::launch_receivers_fast(m->d_h, m->d_rec, m->d_amb, m->d_ctl, g, m->p.dr_orth,
+                                      m->p.dr_diag, m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 1], m->stream));
   FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_h, m->d_ctl, g,
                                    m->u_dt, m->stream));
@@ -347,6 +354,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
       !cu(cudaMalloc(&m->d_rec, n), "cudaMalloc(rec)") ||
       !cu(cudaMalloc(&m->d_mask, n), "cudaMalloc(mask)") ||
       !cu(cudaMalloc(&m->d_stack, n * sizeof(int32_t)), "cudaMalloc(stack)") ||
+      !cu(cudaMalloc(&m->d_amb, n * sizeof(int32_t)), "cudaMalloc(amb)") ||
       !cu(cudaMalloc(&m->d_lvl, (n + 2) * sizeof(int32_t)), "cudaMalloc(lvl)") ||
       !cu(cudaMalloc(&m->d_cnt, n * sizeof(uint32_t)), "cudaMalloc(cnt)") ||
       !cu(cudaMalloc(&m->d_fact, 2 * (n + 1) * sizeof(double)), "cudaMalloc(fact)") ||
@@ -608,6 +616,27 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
   FS_CUDA(fs::launch_walk(walk_args(m, 0), m->walk_blocks, m->stream));
   m->have_step = true;
   return collect_status(m);
+}
+
+// Selects the receiver kernel: 1 = the FP64 reference formula for every
+// cell, 0 = the FP32 filter with FP64 fix-up (default). Both give identical
+// receivers; the switch exists to test that.
+int fs_test_set_receiver_path(fs_model *m, int exact) {
+  if (int st = check_model(m)) return st;
+  m->exact_receivers = exact != 0;
+  return FS_OK;
+}
+
+// Number of cells the receiver filter queued for the FP64 fix-up in the last
+// timestep.
+int fs_test_receiver_fixups(const fs_model *m, int32_t *count) {
+  if (int st = check_model(m)) return st;
+  if (!count) return set_error(FS_ERR_ARG, "count is NULL");
+  DeviceGuard dg(m->device);
+  FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
+  FS_CUDA(cudaStreamSynchronize(m->stream));
+  *count = m->h_ctl->amb;
+  return FS_OK;
 }
 
 // Runs a bounded wait on a count that is never reached and returns its

@@ -22,6 +22,15 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir);
  * milliseconds; returns FS_ERR_TIMEOUT when the bound works. */
 int fs_test_barrier_timeout(fs_model *m, double ms);
 
+/* Selects the receiver kernel: 1 = FP64 reference formula for every cell,
+ * 0 (default) = FP32 filter with FP64 fix-up of the cells it cannot decide.
+ * Both produce identical receivers. */
+int fs_test_set_receiver_path(fs_model *m, int exact);
+
+/* Cells queued for the FP64 fix-up by the receiver filter in the last
+ * timestep. */
+int fs_test_receiver_fixups(const fs_model *m, int32_t *count);
+
 #ifdef __cplusplus
 }
 #endif
