@@ -126,7 +126,9 @@ int fs_get_receiver_index(const fs_model *m, int64_t *idx);
 
 /* Level of every cell in the last timestep's ordering (fastscape_RB.cpp:
  * 213-254): level 0 = FS_NO_FLOW cells, level k+1 = donors of level k.
- * *nlevels = number of levels (the reference's `nlevel` is *nlevels + 1). */
+ * *nlevels = number of non-empty levels. The reference's `nlevel` is
+ * *nlevels + 2: its level table ends with the offset of one empty level
+ * plus the duplicate end entry (fastscape_RB.cpp:246-251). */
 int fs_get_levels(const fs_model *m, int32_t *level_id, int32_t *nlevels);
 
 /* Donor mask of the last timestep: bit k set when the neighbour in

@@ -36,7 +36,9 @@ def assert_step_equal(m, W, H, ref, tag=""):
     assert np.array_equal(m.donor_mask(), donor_mask_from_rec(rec, W, H)), f"donor mask {tag}"
     lid, nl = m.levels()
     want_lid = level_ids(ref["stack"], ref["levels"], W * H)
-    assert nl == len(ref["levels"]) - 1, f"nlevels {tag}"
+    # the reference's level table has nlevel = levels + 2 entries
+    # (fastscape_RB.cpp:246-251 leaves an empty last level plus a duplicate)
+    assert nl == len(ref["levels"]) - 2, f"nlevels {tag}"
     assert np.array_equal(lid, want_lid), f"level ids {tag}"
     assert np.array_equal(m.accumulation(), ref["accum"]), f"accumulation {tag}"
     assert np.array_equal(m.getH(), ref["h"]), f"elevation {tag}"
@@ -154,3 +156,23 @@ def test_timing_counters(pkg):
         assert np.all(t > 0)
         assert t[3] >= t[0] + t[1] + t[2] * 0.99
         assert np.all(m.phase_times() == 0)
+
+
+def test_receiver_filter_equals_fp64_formula(pkg):
+    """The FP32 filter + FP64 fix-up path gives the receivers of the FP64
+    reference formula on every cell, over an evolving landscape."""
+    import ctypes as C
+    W, H = 1500, 1100
+    p = pkg.workload_params()
+    L = pkg.library()
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_PHILOX, seed=5) as a, \
+            pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_PHILOX, seed=5) as b:
+        L.fs_test_set_receiver_path(b.handle, 1)
+        for s in range(8):
+            a.step(1)
+            b.step(1)
+            assert np.array_equal(a.receivers(), b.receivers()), f"step {s}"
+            assert np.array_equal(a.getH(), b.getH()), f"step {s}"
+        n = C.c_int32(0)
+        pkg.check(L.fs_test_receiver_fixups(a.handle, C.byref(n)))
+        assert 0 < n.value < W * H // 100

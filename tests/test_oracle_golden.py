@@ -77,3 +77,13 @@ def test_donor_mask_encodes_reference_donor_order(name):
     for c in range(W * H):
         lst = [c + nshift[k] for k in order if mask[c] >> k & 1]
         assert lst == list(g["donor_0"][c, :nd[c]])
+
+
+@pytest.mark.parametrize("name", STEP_CASES)
+def test_reference_level_table_shape(name):
+    # fastscape_RB.cpp:246-251: the table closes with an empty level and a
+    # duplicate end offset, so nlevel = non-empty levels + 2.
+    g = load(name)
+    lv = g["levels_0"]
+    assert lv[0] == 0 and lv[-1] == lv[-2] == int(g["W"]) * int(g["H"])
+    assert np.all(np.diff(lv[:-1]) > 0)
