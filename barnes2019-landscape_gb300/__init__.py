@@ -44,6 +44,7 @@ ABI_SYMBOLS = [
     "fs_set_barrier_timeout", "fs_synchronize", "fs_last_error", "fs_version",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_receiver_fixups",
+    "fs_test_table_capacity",
 ]
 
 
@@ -123,6 +124,7 @@ def library() -> C.CDLL:
     L.fs_test_barrier_timeout.argtypes = [vp, C.c_double]
     L.fs_test_set_receiver_path.argtypes = [vp, C.c_int]
     L.fs_test_receiver_fixups.argtypes = [vp, i32p]
+    L.fs_test_table_capacity.argtypes = [vp, i32p]
     _lib = L
     return L
 

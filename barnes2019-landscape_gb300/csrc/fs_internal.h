@@ -12,6 +12,9 @@ namespace fs {
 struct Ctl {
   int err;                 // FS_OK or first FS_ERR_* seen by any kernel
   int err_detail;          // phase code where err was raised
+  int abort_k;             // > 0: a drainage count >= the table capacity was
+                           // met; the timestep stopped before touching h
+  int steps_done;          // timesteps completed in the current fs_step call
   int nlevels;             // levels found by the last walk
   int total;               // cells placed in the ordering by the last walk
   unsigned long long walk_ns[3];  // accumulated walk time: ordering,
@@ -23,6 +26,19 @@ struct Ctl {
   int amb;                 // cells queued by the receiver filter
   int pad[2];
 };
+constexpr size_t kCtlCallResetBytes = 4 * sizeof(int);  // err .. steps_done
+
+// Receiver code of an interior cell without a lower neighbour. The ABI
+// reports it as FS_NO_FLOW (-1), like the rings; internally it marks the
+// level-0 cells that are uplifted (fastscape_RB.cpp:291-295).
+constexpr int kPit = -2;
+
+// Erosion table: one 64-byte record per drainage count k (cells), holding
+// for each direction class (0 orthogonal, 1 diagonal) at doubles 4*cls+0..2:
+//   F = keq*dt*pow(k*cell_area, meq)/pow(dr_cls, neq)  (fastscape_RB.cpp:315)
+//   D = 1 + F          (the n = 1 Newton denominator, fastscape_RB.cpp:322)
+//   R = RN(1/D)        (reciprocal for the correctly rounded division)
+constexpr int kTabStride = 8;
 constexpr size_t kCtlResetOffset = offsetof(Ctl, top);
 constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
 
@@ -54,10 +70,13 @@ struct WalkArgs {
   int32_t *stack;
   int32_t *lvl_off;        // size+2 entries
   uint32_t *cnt;           // drainage cell counts
-  const double *fact;      // fact[2*k + cls], k in [1, size]
+  const double *tab;       // erosion table, kTabStride doubles per count
+  int tab_cap;             // counts k < tab_cap are in the table
   Ctl *ctl;
   int W, size;
   double u_dt, neq, tol;
+  long long half_tol_bits; // bits of tol/2 (one-iteration test, n = 1)
+  long long h0_lim_bits;   // bits of tol*2^48
   int nmode;
   int do_erode;            // 0: ordering + accumulation only
   int stamp;               // 1: accumulate phase times into ctl->walk_ns
@@ -65,17 +84,17 @@ struct WalkArgs {
 };
 
 // Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
-cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
+cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
                              double dr_orth, double dr_diag, cudaStream_t s);
 cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
                                   Ctl *ctl, StepGeom g, double dr_orth,
                                   double dr_diag, cudaStream_t s);
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, double *h, Ctl *ctl,
-                                 StepGeom g, double u_dt, cudaStream_t s);
+                                 int32_t *stack, Ctl *ctl, StepGeom g,
+                                 cudaStream_t s);
 cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s);
 int walk_threads();
-const void *walk_kernel_ptr();
+const void *walk_kernel_ptr(int nmode);
 cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
                                 cudaStream_t s);
 cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,

@@ -1,21 +1,22 @@
 // fs_kernels.cu -- sm_103a kernels of the FastScape timestep.
 //
-// One timestep = three launches on the model's stream:
-//   1. k_receivers       D8 steepest descent over the interior
-//                        (fastscape_RB.cpp:160-182)
-//   2. k_donors_level0   donor masks (pull form of fastscape_RB.cpp:188-203),
-//                        level-0 frontier (fastscape_RB.cpp:221-227) and the
-//                        uplift of interior level-0 cells (:285-296)
-//   3. k_walk            persistent cooperative kernel: level-by-level
-//                        ordering (:229-251), flow accumulation back down the
-//                        levels (:262-279) and the implicit erosion solved
-//                        upward from base level (:306-328, level order of
-//                        fastscape_RB+P.cpp:319-350), with uplift of the
-//                        eroded cells folded into their first read.
+// One timestep = four launches on the model's stream:
+//   1. k_receivers_filter  D8 steepest descent over the interior
+//      + k_receivers_fixup (fastscape_RB.cpp:160-182): FP32 proof of the
+//                          receiver, FP64 reference formula for the cells
+//                          the proof cannot settle
+//   2. k_donors_level0     donor masks (pull form of fastscape_RB.cpp:188-203)
+//                          and the level-0 frontier (fastscape_RB.cpp:221-227)
+//   3. k_walk              persistent cooperative kernel: level-by-level
+//                          ordering (:229-251), flow accumulation back down
+//                          the levels (:262-279), uplift (:285-296) and the
+//                          implicit erosion solved upward from base level
+//                          (:306-328, in the level order of
+//                          fastscape_RB+P.cpp:319-350).
 //
 // Floating point follows the reference's operation order exactly; the whole
 // file is compiled with -fmad=false so no multiply-add is contracted, and
-// double division is IEEE round-to-nearest.
+// every FP64 division is correctly rounded.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -105,7 +106,8 @@ __device__ __forceinline__ int nbr_off(int k, int W) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
-            int H, double dr_orth, double dr_diag) {
+            int H, double dr_orth, double dr_diag, const Ctl *ctl) {
+  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   const int x = blockIdx.x * blockDim.x + threadIdx.x + 2;
   const int y = blockIdx.y * blockDim.y + threadIdx.y + 2;
   if (x >= W - 2 || y >= H - 2) return;
@@ -123,7 +125,7 @@ k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
       max_n = n;
     }
   }
-  rec[c] = (int8_t)max_n;
+  rec[c] = (int8_t)(max_n == FS_NO_FLOW ? kPit : max_n);
 }
 
 // ---------------------------------------------------------------------------
@@ -165,6 +167,7 @@ __global__ void __launch_bounds__(256)
 k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
                    int32_t *__restrict__ amb, Ctl *ctl, int W, int H,
                    float g_orth, float g_diag, float gmax) {
+  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   __shared__ float s[kRyTile + 2][kRxTile + 3];
   const int x0 = blockIdx.x * kRxTile + 1;  // grid x of s[.][0]
   const int y0 = blockIdx.y * kRyTile + 1;  // grid y of s[0][.]
@@ -215,7 +218,7 @@ k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
         if (best - second > 2.f * E && best > E)
           code = bn;
         else if (best < -E)
-          code = FS_NO_FLOW;
+          code = kPit;
       }
       if (code == -2)
         queue = true;
@@ -237,6 +240,7 @@ __global__ void __launch_bounds__(256)
 k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
                   const int32_t *__restrict__ amb, const Ctl *ctl, int W,
                   double dr_orth, double dr_diag) {
+  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   const int n_amb = ld_volatile_i32(&ctl->amb);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_amb; i += gridDim.x * blockDim.x) {
     const int c = amb[i];
@@ -251,34 +255,31 @@ k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
         max_n = n;
       }
     }
-    rec[c] = (int8_t)max_n;
+    rec[c] = (int8_t)(max_n == FS_NO_FLOW ? kPit : max_n);
   }
 }
 
 // ---------------------------------------------------------------------------
-// 2. Donor masks + level 0 + uplift of interior level-0 cells.
+// 2. Donor masks + level 0.
 // Bit k of mask[c] is set when neighbour c+nshift[k] has receiver code
 // (k+4)%8, i.e. drains into c (the pull form of fastscape_RB+GPU.cpp:155-182).
-// Level 0 = every NO_FLOW cell (fastscape_RB.cpp:221-227), appended with one
-// atomic per warp. Interior NO_FLOW cells are never eroded, so their uplift
-// (fastscape_RB.cpp:285-296) is applied here, before any erosion reads them.
+// Level 0 = every cell without a receiver (rings and pits,
+// fastscape_RB.cpp:221-227), appended with one atomic per warp.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
-                int32_t *__restrict__ stack, double *__restrict__ h, Ctl *ctl,
-                int W, int H, int size, double u_dt) {
+                int32_t *__restrict__ stack, Ctl *ctl, int W, int H, int size) {
+  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   const int lane = threadIdx.x & 31;
-  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int stride = gridDim.x * blockDim.x;
   int o[8];
   nshift8(W, o);
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
-       base < size; base += stride) {
-    const long long c = base + lane;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < size; base += stride) {
+    const int c = base + lane;
     bool level0 = false;
     if (c < size) {
-      const int y = (int)c / W;
-      const int x = (int)c - y * W;
-      const int r = rec[c];
+      const int y = c / W;
+      const int x = c - y * W;
       unsigned m = 0;
       if (x >= 1 && x <= W - 2 && y >= 1 && y <= H - 2) {
 #pragma unroll
@@ -286,26 +287,52 @@ k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
           if (rec[c + o[k]] == ((k + 4) & 7)) m |= 1u << k;
       }
       mask[c] = (uint8_t)m;
-      level0 = (r == FS_NO_FLOW);
-      if (level0 && x >= 2 && x < W - 2 && y >= 2 && y < H - 2) h[c] += u_dt;
+      level0 = rec[c] < 0;
     }
     const unsigned b = __ballot_sync(kFull, level0);
     if (b) {
       int base_pos = 0;
       if (lane == 0) base_pos = atomicAdd(&ctl->top, __popc(b));
       base_pos = __shfl_sync(kFull, base_pos, 0);
-      if (level0) stack[base_pos + __popc(b & ((1u << lane) - 1u))] = (int32_t)c;
+      if (level0) stack[base_pos + __popc(b & ((1u << lane) - 1u))] = c;
     }
   }
 }
 
+__device__ __forceinline__ long long abs_bits(double x) {
+  return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
+}
+
+// Correctly rounded num/D for D > 0 given R = RN(1/D), without the FP64
+// divide routine: Markstein's correction q1 = q0 + (num - q0*D)*R with
+// fused multiply-adds (P. Markstein, IBM J. Res. Dev. 34(1), 1990), then an
+// exact check of the remainder r1 = num - q1*D: q1 is accepted only if
+// |r1| < D*ulp(q1)/2 (then |num/D - q1| < ulp(q1)/2, so q1 = RN(num/D)),
+// q1 is not a power of two (where the spacing below halves) and its
+// exponent is far from the subnormal/overflow range. Anything else -- zero
+// numerators included -- takes the IEEE division. 4 FP64 operations against
+// ~7.5 for the divide routine on this part.
+__device__ __forceinline__ double div_rn(double num, double D, double R) {
+  const double q0 = num * R;
+  const double r0 = fma(-q0, D, num);
+  const double q1 = fma(r0, R, q0);
+  const double r1 = fma(-q1, D, num);
+  const long long qb = abs_bits(q1);
+  const int e = (int)(qb >> 52);
+  if (e >= 64 && e <= 1980 && (qb & 0x000FFFFFFFFFFFFFll) != 0) {
+    const long long thr = __double_as_longlong(D) + ((long long)(e - 1076) << 52);
+    if (abs_bits(r1) < thr) return q1;
+  }
+  return num / D;
+}
+
 // pow(x, n) and pow(x, n-1) for the Newton update of fastscape_RB.cpp:322.
-__device__ __forceinline__ void powers(double x, double neq, int nmode,
-                                       double &pn, double &pn1) {
-  if (nmode == kNOne) {
+template <int NMODE>
+__device__ __forceinline__ void powers(double x, double neq, double &pn, double &pn1) {
+  if (NMODE == kNOne) {
     pn = x;
     pn1 = 1.0;
-  } else if (nmode == kNTwo) {
+  } else if (NMODE == kNTwo) {
     pn = x * x;
     pn1 = x;
   } else {
@@ -314,15 +341,78 @@ __device__ __forceinline__ void powers(double x, double neq, int nmode,
   }
 }
 
+// Erosion of one cell: fastscape_RB.cpp:315-326 with h0 the uplifted
+// elevation, hn the receiver's final elevation and T the table record of the
+// cell's drainage count and direction class (T[0] = fact).
+template <int NMODE>
+__device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
+                                             double h0, double hn) {
+  const double fact = T[0];
+  double hnew, hp, diff;
+  int it;
+  if (NMODE == kNOne) {
+    // First iterate: hnew - h0 = +0, pow(x,1) = x and pow(x,0) = 1, so
+    // hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)) with D = RN(1+fact).
+    const double D = T[1], R = T[2];
+    const double num = fact * (h0 - hn);
+    const double q = div_rn(num, D, R);
+    hnew = h0 - q;
+    // |q| <= tol/2 and |h0| <= tol*2^48 give |RN(hnew-h0)| <= 9tol/16 < tol:
+    // the reference loop stops after this iterate.
+    if (abs_bits(q) <= a.half_tol_bits && abs_bits(h0) <= a.h0_lim_bits) return hnew;
+    hp = h0;
+    diff = hnew - hp;
+    hp = hnew;
+    it = 1;
+    while (fabs(diff) > a.tol) {
+      const double num2 = (hnew - h0) + fact * (hnew - hn);
+      hnew -= div_rn(num2, D, R);
+      diff = hnew - hp;
+      hp = hnew;
+      if (++it >= kNewtonMaxIt) {
+        raise_err(a.ctl, FS_ERR_NEWTON, kPhaseErode);
+        break;
+      }
+    }
+    return hnew;
+  }
+  hnew = h0;
+  hp = h0;
+  diff = 2 * a.tol;
+  it = 0;
+  while (fabs(diff) > a.tol) {
+    double pn, pn1;
+    powers<NMODE>(hnew - hn, a.neq, pn, pn1);
+    hnew -= (hnew - h0 + fact * pn) / (1. + fact * a.neq * pn1);
+    diff = hnew - hp;
+    hp = hnew;
+    if (++it >= kNewtonMaxIt) {
+      raise_err(a.ctl, FS_ERR_NEWTON, kPhaseErode);
+      break;
+    }
+  }
+  return hnew;
+}
+
+// Uplift of the interior level-0 cells (pits), fastscape_RB.cpp:291-295.
+__device__ __forceinline__ void uplift_pits(const WalkArgs &a, int lvl0_end, int tid,
+                                            int nthreads) {
+  for (int i = tid; i < lvl0_end; i += nthreads) {
+    const int c = __ldcg(&a.stack[i]);
+    if (a.rec[c] == kPit) a.h[c] = __ldcg(&a.h[c]) + a.u_dt;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 3. Persistent level walker (cooperative launch, one grid barrier per level
 // per sweep).
 // ---------------------------------------------------------------------------
+template <int NMODE>
 __global__ void __launch_bounds__(kWalkThreads)
 k_walk(WalkArgs a) {
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
-  if (ld_volatile_i32(&ctl->err) != 0) return;
+  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   const int lane = threadIdx.x & 31;
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -339,8 +429,13 @@ k_walk(WalkArgs a) {
   };
 
   // ---- ordering: fastscape_RB.cpp:229-251 -------------------------------
+  // Level k+1 = the donors of level k. Each warp expands 32 frontier cells:
+  // a warp scan of the donor counts and one atomic reserve their slots. The
+  // append counter rotates over three words so a block that reads the size
+  // of level k after the barrier never races with the reset for level k+2.
   int lo = 0;
   int hi = ld_volatile_i32(&ctl->top);
+  const int lvl0_end = hi;
   if (tid == 0) {
     a.lvl_off[0] = 0;
     a.lvl_off[1] = hi;
@@ -404,8 +499,11 @@ k_walk(WalkArgs a) {
 
   // ---- accumulation: fastscape_RB.cpp:262-279, pulled level by level ----
   // cnt[c] = 1 + sum of the donors' counts; the reference's accum[c] is
-  // cnt[c]*cell_area (exact: integer multiples of cell_area).
+  // cnt[c]*cell_area (exact: integer multiples of cell_area). A count at
+  // level >= 1 beyond the erosion table stops the timestep before any
+  // elevation changes; the host grows the table and repeats it.
   for (int L = nlev - 1; L >= 0; --L) {
+    if (L == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
     const int b = __ldcg(&a.lvl_off[L]);
     const int e = __ldcg(&a.lvl_off[L + 1]);
     for (int i = b + tid; i < e; i += nthreads) {
@@ -418,20 +516,20 @@ k_walk(WalkArgs a) {
         s += __ldcg(&a.cnt[c + nbr_off(k, a.W)]);
       }
       a.cnt[c] = s;
+      if (a.do_erode && L > 0 && s >= (uint32_t)a.tab_cap) atomicMax(&ctl->abort_k, (int)s);
     }
     if (L > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
   }
   lap(1);
   if (!a.do_erode) return;
-  // No barrier here: level-1 erosion needs only the counts of level-1 cells
-  // (complete since the barrier after accumulation level 1) and the final h
-  // of level-0 cells (written by k_donors_level0). Accumulation of level 0,
-  // possibly still running in other blocks, reads counts and never h.
 
-  // ---- erosion: fastscape_RB.cpp:306-328 in the level order of
-  // fastscape_RB+P.cpp:319-350. Level 0 never erodes; its interior cells
-  // were uplifted by k_donors_level0. Each eroded cell's uplift
-  // (fastscape_RB.cpp:294) is applied to its first read.
+  // ---- uplift + erosion: fastscape_RB.cpp:285-296 and :306-328 in the
+  // level order of fastscape_RB+P.cpp:319-350. Eroded cells are uplifted on
+  // their first read; level-1 cells see their pit receiver's uplift added on
+  // read, and the pits themselves are uplifted once no level-1 cell can read
+  // them any more (during level 2, or after a barrier when level 1 is the
+  // last). No barrier is needed before level 1: it reads counts complete
+  // since the barrier after accumulation level 1 and never-written h.
   for (int L = 1; L < nlev; ++L) {
     const int b = __ldcg(&a.lvl_off[L]);
     const int e = __ldcg(&a.lvl_off[L + 1]);
@@ -440,30 +538,23 @@ k_walk(WalkArgs a) {
       const int r = a.rec[c];
       const int n = c + nbr_off(r, a.W);
       const uint32_t k = __ldcg(&a.cnt[c]);
-      const double fact = a.fact[2 * (size_t)k + (r & 1)];
+      const double *T = a.tab + (size_t)k * kTabStride + 4 * (r & 1);
       const double h0 = __ldcg(&a.h[c]) + a.u_dt;
-      const double hn = __ldcg(&a.h[n]);
-      double hnew = h0;
-      double hp = h0;
-      double diff = 2 * a.tol;
-      int it = 0;
-      while (fabs(diff) > a.tol) {
-        double pn, pn1;
-        powers(hnew - hn, a.neq, a.nmode, pn, pn1);
-        hnew -= (hnew - h0 + fact * pn) / (1. + fact * a.neq * pn1);
-        diff = hnew - hp;
-        hp = hnew;
-        if (++it >= kNewtonMaxIt) {
-          raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
-          break;
-        }
-      }
+      double hn = __ldcg(&a.h[n]);
+      if (L == 1 && a.rec[n] == kPit) hn = hn + a.u_dt;
+      const double hnew = erode_cell<NMODE>(a, T, h0, hn);
       if (!isfinite(hnew)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
       a.h[c] = hnew;
     }
+    if (L == 2) uplift_pits(a, lvl0_end, tid, nthreads);
     if (L + 1 < nlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
   }
+  if (nlev <= 2) {
+    if (nlev == 2 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    uplift_pits(a, lvl0_end, tid, nthreads);
+  }
   lap(2);
+  if (tid == 0) atomicAdd(&ctl->steps_done, 1);
 }
 
 __global__ void k_check_finite(const double *__restrict__ h, int size, Ctl *ctl) {
@@ -535,15 +626,14 @@ __global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
 }  // namespace
 
 int walk_threads() { return kWalkThreads; }
-const void *walk_kernel_ptr() { return reinterpret_cast<const void *>(&k_walk); }
 
-cudaError_t launch_receivers(const double *h, int8_t *rec, StepGeom g,
+cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
                              double dr_orth, double dr_diag, cudaStream_t s) {
   const int iw = g.W - 4, ih = g.H - 4;
   if (iw <= 0 || ih <= 0) return cudaSuccess;
   dim3 block(32, 8);
   dim3 grid((iw + 31) / 32, (ih + 7) / 8);
-  k_receivers<<<grid, block, 0, s>>>(h, rec, g.W, g.H, dr_orth, dr_diag);
+  k_receivers<<<grid, block, 0, s>>>(h, rec, g.W, g.H, dr_orth, dr_diag, ctl);
   return cudaGetLastError();
 }
 
@@ -567,25 +657,29 @@ cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
 }
 
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, double *h, Ctl *ctl,
-                                 StepGeom g, double u_dt, cudaStream_t s) {
+                                 int32_t *stack, Ctl *ctl, StepGeom g,
+                                 cudaStream_t s) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long want = ((long long)g.size + 255) / 256;
   int blocks = (int)(want < (long long)sms * 16 ? want : (long long)sms * 16);
   if (blocks < 1) blocks = 1;
-  k_donors_level0<<<blocks, 256, 0, s>>>(rec, mask, stack, h, ctl, g.W, g.H,
-                                        g.size, u_dt);
+  k_donors_level0<<<blocks, 256, 0, s>>>(rec, mask, stack, ctl, g.W, g.H, g.size);
   return cudaGetLastError();
+}
+
+const void *walk_kernel_ptr(int nmode) {
+  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne>);
+  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo>);
+  return reinterpret_cast<const void *>(&k_walk<kNGeneral>);
 }
 
 cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s) {
   WalkArgs args = a;
   void *params[] = {&args};
-  return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(&k_walk),
-                                     dim3(blocks), dim3(kWalkThreads), params,
-                                     0, s);
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode), dim3(blocks),
+                                     dim3(kWalkThreads), params, 0, s);
 }
 
 cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,

@@ -10,8 +10,9 @@
 //   stack   int32[size]         cells grouped by level
 //   lvl_off int32[size+2]       level offsets into stack
 //   cnt     uint32[size]        drainage cell counts (accum = cnt*cell_area)
-//   fact    double[2*(size+1)]  keq*dt*pow(k*cell_area,m)/pow(dr,n) per
-//                               count k and direction class (orth, diag)
+//   amb     int32[size]         cells queued for the FP64 receiver fix-up
+//   tab     double[8*tab_cap]   erosion table per drainage count k < tab_cap
+//                               (see fs_internal.h); grows on demand
 //   ctl     fs::Ctl             status word, counters, barrier
 #include <cuda_runtime.h>
 
@@ -93,7 +94,8 @@ struct fs_model {
   int32_t *d_amb = nullptr;   // cells the receiver filter could not decide
   int32_t *d_lvl = nullptr;
   uint32_t *d_cnt = nullptr;
-  double *d_fact = nullptr;
+  double *d_tab = nullptr;
+  int tab_cap = 0;
   fs::Ctl *d_ctl = nullptr;
   fs::Ctl *h_ctl = nullptr;  // pinned mirror for status reads
   int walk_blocks = 0;
@@ -123,7 +125,7 @@ void free_model(fs_model *m) {
   cudaFree(m->d_amb);
   cudaFree(m->d_lvl);
   cudaFree(m->d_cnt);
-  cudaFree(m->d_fact);
+  cudaFree(m->d_tab);
   cudaFree(m->d_ctl);
   if (m->h_ctl) cudaFreeHost(m->h_ctl);
   for (auto &e : m->ev) cudaEventDestroy(e);
@@ -132,27 +134,33 @@ void free_model(fs_model *m) {
   delete m;
 }
 
-// fact[2k+cls] = keq*dt*pow(k*cell_area, meq)/pow(dr_cls, neq), evaluated on
-// the host in exactly the order of fastscape_RB.cpp:315 with the C library's
-// pow, so the device erosion sees the same bits as the reference (the
-// reference's accum[c] is k*cell_area exactly: integer multiples summed
-// below 2^53).
-void build_fact_table(const fs_params &p, int size, std::vector<double> &fact) {
-  fact.assign(2 * (static_cast<size_t>(size) + 1), 0.0);
+// Erosion table records for counts k in [k0, k1): for each direction class
+// F = keq*dt*pow(k*cell_area, meq)/pow(dr_cls, neq) evaluated in exactly the
+// order of fastscape_RB.cpp:315 with the C library's pow (the reference's
+// accum[c] is k*cell_area exactly: integer multiples summed below 2^53), then
+// D = 1 + F and R = 1/D, both correctly rounded. Host arithmetic is IEEE
+// double without contraction, so the device sees the reference's bits.
+void fill_table(const fs_params &p, long long k0, long long k1, double *rec) {
   const double kd = p.keq * p.dt;
-  const double pl0 = std::pow(p.dr_orth, p.neq);
-  const double pl1 = std::pow(p.dr_diag, p.neq);
+  const double pl[2] = {std::pow(p.dr_orth, p.neq), std::pow(p.dr_diag, p.neq)};
   unsigned nt = std::max(1u, std::thread::hardware_concurrency());
   nt = std::min<unsigned>(nt, 64);
-  if (size < 100000) nt = 1;
+  if (k1 - k0 < 65536) nt = 1;
   auto work = [&](unsigned t) {
-    const long long lo = 1 + (long long)size * t / nt;
-    const long long hi = 1 + (long long)size * (t + 1) / nt;
+    const long long lo = k0 + (k1 - k0) * t / nt;
+    const long long hi = k0 + (k1 - k0) * (t + 1) / nt;
     for (long long k = lo; k < hi; k++) {
       const double A = static_cast<double>(k) * p.cell_area;
       const double pa = std::pow(A, p.meq);
-      fact[2 * k + 0] = kd * pa / pl0;
-      fact[2 * k + 1] = kd * pa / pl1;
+      double *r = rec + (k - k0) * fs::kTabStride;
+      for (int cls = 0; cls < 2; cls++) {
+        const double F = kd * pa / pl[cls];
+        const double D = 1. + F;
+        r[4 * cls + 0] = F;
+        r[4 * cls + 1] = D;
+        r[4 * cls + 2] = 1. / D;
+        r[4 * cls + 3] = 0.;
+      }
     }
   };
   if (nt == 1) {
@@ -212,13 +220,19 @@ fs::WalkArgs walk_args(const fs_model *m, int do_erode) {
   a.stack = m->d_stack;
   a.lvl_off = m->d_lvl;
   a.cnt = m->d_cnt;
-  a.fact = m->d_fact;
+  a.tab = m->d_tab;
+  a.tab_cap = m->tab_cap;
   a.ctl = m->d_ctl;
   a.W = m->W;
   a.size = m->size;
   a.u_dt = do_erode ? m->u_dt : 0.0;
   a.neq = m->p.neq;
   a.tol = m->p.tol;
+  {
+    const double ht = m->p.tol * 0.5, hl = std::ldexp(m->p.tol, 48);
+    std::memcpy(&a.half_tol_bits, &ht, 8);
+    std::memcpy(&a.h0_lim_bits, &hl, 8);
+  }
   a.nmode = m->nmode;
   a.do_erode = do_erode;
   a.stamp = m->timing ? 1 : 0;
@@ -234,13 +248,13 @@ int one_step(fs_model *m, int i) {
   FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(m->d_ctl) + fs::kCtlResetOffset, 0,
                           fs::kCtlResetBytes, m->stream));
   if (m->exact_receivers)
-    FS_CUDA(fs::launch_receivers(m->d_h, m->d_rec, g, m->p.dr_orth, m->p.dr_diag, m->stream));
+    FS_CUDA(fs::launch_receivers(m->d_h, m->d_rec, m->d_ctl, g, m->p.dr_orth, m->p.dr_diag,
+                                 m->stream));
   else
     FS_CUDA(fs::launch_receivers_fast(m->d_h, m->d_rec, m->d_amb, m->d_ctl, g, m->p.dr_orth,
                                       m->p.dr_diag, m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 1], m->stream));
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_h, m->d_ctl, g,
-                                   m->u_dt, m->stream));
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 2], m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 1), m->walk_blocks, m->stream));
   return FS_OK;
@@ -267,6 +281,30 @@ int harvest_events(fs_model *m, int k) {
   float tot = 0;
   FS_CUDA(cudaEventElapsedTime(&tot, m->ev[0], m->ev[3 * k]));
   m->phase_ms[3] += tot;
+  return FS_OK;
+}
+
+// Makes the erosion table cover every drainage count below `need`+1
+// (doubling, capped at the grid size + 1).
+int grow_table(fs_model *m, long long need) {
+  long long cap = std::max<long long>(m->tab_cap, 1);
+  while (cap <= need) cap *= 2;
+  cap = std::min<long long>(cap, static_cast<long long>(m->size) + 1);
+  if (cap <= m->tab_cap) return set_error(FS_ERR_CUDA, "erosion table cannot grow past %d", m->tab_cap);
+  std::vector<double> host(static_cast<size_t>(cap) * fs::kTabStride);
+  fill_table(m->p, 0, cap, host.data());
+  double *d = nullptr;
+  FS_CUDA(cudaMalloc(&d, host.size() * sizeof(double)));
+  cudaError_t e = cudaMemcpyAsync(d, host.data(), host.size() * sizeof(double),
+                                  cudaMemcpyHostToDevice, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_error(e, "upload(erosion table)");
+  }
+  cudaFree(m->d_tab);
+  m->d_tab = d;
+  m->tab_cap = static_cast<int>(cap);
   return FS_OK;
 }
 
@@ -357,7 +395,6 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
       !cu(cudaMalloc(&m->d_amb, n * sizeof(int32_t)), "cudaMalloc(amb)") ||
       !cu(cudaMalloc(&m->d_lvl, (n + 2) * sizeof(int32_t)), "cudaMalloc(lvl)") ||
       !cu(cudaMalloc(&m->d_cnt, n * sizeof(uint32_t)), "cudaMalloc(cnt)") ||
-      !cu(cudaMalloc(&m->d_fact, 2 * (n + 1) * sizeof(double)), "cudaMalloc(fact)") ||
       !cu(cudaMalloc(&m->d_ctl, sizeof(fs::Ctl)), "cudaMalloc(ctl)") ||
       !cu(cudaMallocHost(&m->h_ctl, sizeof(fs::Ctl)), "cudaMallocHost(ctl)"))
     return fail(*status);
@@ -370,14 +407,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
       !cu(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream), "memset(ctl)"))
     return fail(*status);
 
-  {
-    std::vector<double> fact;
-    build_fact_table(p, m->size, fact);
-    if (!cu(cudaMemcpyAsync(m->d_fact, fact.data(), fact.size() * sizeof(double),
-                            cudaMemcpyHostToDevice, m->stream), "upload(fact)") ||
-        !cu(cudaStreamSynchronize(m->stream), "sync"))
-      return fail(*status);
-  }
+  if (int st = grow_table(m, std::min<long long>(m->size, 65535))) return fail(st);
 
   const fs::StepGeom g{m->W, m->H, m->size};
   if (init_mode == FS_INIT_REFERENCE || init_mode == FS_INIT_MT19937) {
@@ -399,7 +429,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
 
   int occ = 0, sms = 0;
   if (!cu(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device), "attr") ||
-      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(),
+      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(m->nmode),
                                                         fs::walk_threads(), 0),
           "occupancy"))
     return fail(*status);
@@ -416,19 +446,34 @@ int fs_step(fs_model *m, int k) {
   if (k < 0) return set_error(FS_ERR_ARG, "step count must be >= 0 (got %d)", k);
   if (k == 0) return FS_OK;
   DeviceGuard dg(m->device);
-  if (m->timing)
-    if (int st = ensure_events(m, 3 * static_cast<size_t>(k) + 1)) return st;
-  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, 2 * sizeof(int), m->stream));  // err, err_detail
-  for (int i = 0; i < k; i++) {
-    if (int st = one_step(m, i)) return st;
+  int done = 0;
+  while (done < k) {
+    const int batch = k - done;
+    if (m->timing)
+      if (int st = ensure_events(m, 3 * static_cast<size_t>(batch) + 1)) return st;
+    FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, fs::kCtlCallResetBytes, m->stream));
+    for (int i = 0; i < batch; i++) {
+      if (int st = one_step(m, i)) return st;
+    }
+    if (m->timing) {
+      FS_CUDA(cudaEventRecord(m->ev[3 * batch], m->stream));
+      if (int st = harvest_events(m, batch)) return st;
+    }
+    if (int st = collect_status(m)) return st;
+    const int completed = m->h_ctl->steps_done;
+    done += completed;
+    m->steps += completed;
+    if (completed > 0) m->have_step = true;
+    if (m->h_ctl->abort_k > 0) {
+      // A drainage count outgrew the erosion table; that timestep stopped
+      // before changing h and the remaining ones did nothing. Grow and redo.
+      if (int st = grow_table(m, m->h_ctl->abort_k)) return st;
+    } else if (completed != batch) {
+      return set_error(FS_ERR_CUDA, "%d of %d timesteps completed without a status", completed,
+                       batch);
+    }
   }
-  if (m->timing) {
-    FS_CUDA(cudaEventRecord(m->ev[3 * k], m->stream));
-    if (int st = harvest_events(m, k)) return st;
-  }
-  m->steps += k;
-  m->have_step = true;
-  return collect_status(m);
+  return FS_OK;
 }
 
 int fs_run(fs_model *m, int nstep) {
@@ -451,7 +496,7 @@ int fs_set_elevation(fs_model *m, const double *in) {
   if (!in) return set_error(FS_ERR_ARG, "in is NULL");
   DeviceGuard dg(m->device);
   FS_CUDA(cudaMemcpyAsync(m->d_h, in, sizeof(double) * m->size, cudaMemcpyHostToDevice, m->stream));
-  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, 2 * sizeof(int), m->stream));  // err, err_detail
+  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, fs::kCtlCallResetBytes, m->stream));
   FS_CUDA(fs::launch_check_finite(m->d_h, m->size, m->d_ctl, m->stream));
   const int st = collect_status(m);
   if (st == FS_ERR_NONFINITE)
@@ -480,7 +525,7 @@ int fs_get_receivers(const fs_model *m, int32_t *dir) {
   std::vector<int8_t> r(m->size);
   FS_CUDA(cudaMemcpyAsync(r.data(), m->d_rec, m->size, cudaMemcpyDeviceToHost, m->stream));
   FS_CUDA(cudaStreamSynchronize(m->stream));
-  for (int i = 0; i < m->size; i++) dir[i] = r[i];
+  for (int i = 0; i < m->size; i++) dir[i] = r[i] < 0 ? FS_NO_FLOW : r[i];
   return FS_OK;
 }
 
@@ -605,14 +650,13 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
     const bool interior = x >= 2 && x < m->W - 2 && y >= 2 && y < m->H - 2;
     if (dir[i] < -1 || dir[i] > 7 || (!interior && dir[i] != -1))
       return set_error(FS_ERR_ARG, "invalid receiver code %d at cell %d", dir[i], i);
-    r[i] = static_cast<int8_t>(dir[i]);
+    r[i] = static_cast<int8_t>(interior && dir[i] == FS_NO_FLOW ? fs::kPit : dir[i]);
   }
   DeviceGuard dg(m->device);
   FS_CUDA(cudaMemcpyAsync(m->d_rec, r.data(), m->size, cudaMemcpyHostToDevice, m->stream));
   FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream));
   const fs::StepGeom g{m->W, m->H, m->size};
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_h, m->d_ctl, g, 0.0,
-                                   m->stream));
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 0), m->walk_blocks, m->stream));
   m->have_step = true;
   return collect_status(m);
@@ -636,6 +680,15 @@ int fs_test_receiver_fixups(const fs_model *m, int32_t *count) {
   FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
   FS_CUDA(cudaStreamSynchronize(m->stream));
   *count = m->h_ctl->amb;
+  return FS_OK;
+}
+
+// Current capacity of the erosion table (drainage counts below it are
+// covered).
+int fs_test_table_capacity(const fs_model *m, int32_t *cap) {
+  if (int st = check_model(m)) return st;
+  if (!cap) return set_error(FS_ERR_ARG, "cap is NULL");
+  *cap = m->tab_cap;
   return FS_OK;
 }
 

@@ -31,6 +31,11 @@ int fs_test_set_receiver_path(fs_model *m, int exact);
  * timestep. */
 int fs_test_receiver_fixups(const fs_model *m, int32_t *count);
 
+/* Capacity of the erosion table: drainage counts (cells) below it are
+ * covered. The table starts at min(65536, cells+1) records and doubles when
+ * a timestep meets a larger count (that timestep is redone, bit-exactly). */
+int fs_test_table_capacity(const fs_model *m, int32_t *cap);
+
 #ifdef __cplusplus
 }
 #endif
