@@ -213,17 +213,18 @@ k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
         }
       }
       const float E = 0x1p-19f * gmax * (M + 0x1p-100f);
-      int code = -2;  // undecided
+      int code = 0;
+      queue = true;
       if (!bad) {
-        if (best - second > 2.f * E && best > E)
+        if (best - second > 2.f * E && best > E) {
           code = bn;
-        else if (best < -E)
+          queue = false;
+        } else if (best < -E) {
           code = kPit;
+          queue = false;
+        }
       }
-      if (code == -2)
-        queue = true;
-      else
-        rec[(size_t)gy * W + gx] = (int8_t)code;
+      if (!queue) rec[(size_t)gy * W + gx] = (int8_t)code;
     }
     const unsigned bq = __ballot_sync(kFull, queue);
     if (bq) {

@@ -202,11 +202,12 @@ def test_receiver_filter_equals_fp64_formula(pkg):
         assert 0 < n.value < W * H // 100
 
 
-def cone(W, H, c0=5.0):
-    """Cone with its apex down at the centre: one basin drains nearly every
-    cell into the central pit, so drainage counts reach ~W*H."""
+def valley(W, H):
+    """V-shaped valley whose axis runs down to the base-level ring at y = 1:
+    nearly every cell drains into the axis, so the axis cell next to base
+    level (a level-1 cell) carries a drainage count of ~W*H."""
     yy, xx = np.divmod(np.arange(W * H), W)
-    h = c0 + np.hypot(xx - W // 2 + 0.3, yy - H // 2 + 0.1) * 0.7
+    h = 1.0 + 0.5 * np.abs(xx - W // 2) + 0.05 * yy
     h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
     return h
 
@@ -219,7 +220,7 @@ def test_table_growth_large_basin(pkg, oracle, n):
     W, H = 420, 400
     p = pkg.workload_params() if n == 1 else pkg.reference_params()
     op = Params(*p.as_tuple())
-    h = cone(W, H)
+    h = valley(W, H)
     with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
         m.setH(h)
         cap = C.c_int32(0)
