@@ -20,7 +20,7 @@ struct Ctl {
   unsigned long long walk_ns[3];  // accumulated walk time: ordering,
                                   // accumulation, erosion (block 0's clock)
   // --- reset before every timestep (from `top` on) ---
-  int top;                 // level-0 fill pointer (absolute stack index)
+  int top;                 // pits appended to level 0 (after the rings)
   unsigned int bar;        // grid-barrier arrival counter
   int lvlcnt[3];           // rotating per-level append counters (relative)
   int amb;                 // cells queued by the receiver filter
@@ -74,9 +74,9 @@ struct WalkArgs {
   int tab_cap;             // counts k < tab_cap are in the table
   Ctl *ctl;
   int W, size;
+  int nring;               // ring cells, pre-placed at stack[0, nring)
   double u_dt, neq, tol;
-  long long half_tol_bits; // bits of tol/2 (one-iteration test, n = 1)
-  long long h0_lim_bits;   // bits of tol*2^48
+  long long tol_bits;      // bits of tol (magnitude compares as integers)
   int nmode;
   int do_erode;            // 0: ordering + accumulation only
   int stamp;               // 1: accumulate phase times into ctl->walk_ns
@@ -90,7 +90,7 @@ cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
                                   Ctl *ctl, StepGeom g, double dr_orth,
                                   double dr_diag, cudaStream_t s);
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, Ctl *ctl, StepGeom g,
+                                 int32_t *stack, Ctl *ctl, StepGeom g, int nring,
                                  cudaStream_t s);
 cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s);
 int walk_threads();

@@ -30,6 +30,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
+constexpr int kPer = 8;  // frontier cells per thread per expansion chunk
 constexpr int kNewtonMaxIt = 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -264,40 +265,91 @@ k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
 // 2. Donor masks + level 0.
 // Bit k of mask[c] is set when neighbour c+nshift[k] has receiver code
 // (k+4)%8, i.e. drains into c (the pull form of fastscape_RB+GPU.cpp:155-182).
-// Level 0 = every cell without a receiver (rings and pits,
-// fastscape_RB.cpp:221-227), appended with one atomic per warp.
+// Level 0 = every cell without a receiver (fastscape_RB.cpp:221-227): the
+// two outer rings, which never change and sit at stack[0, nring) from model
+// creation on, and the interior pits, appended here with one atomic per
+// 32x64 tile (block scan of the per-thread pit counts).
 // ---------------------------------------------------------------------------
+constexpr int kDxTile = 32;  // tile of cells over [1, W-2] x [1, H-2]
+constexpr int kDyTile = 64;
+constexpr int kDRows = kDyTile / 8;
+
+// Exclusive block scan of one int per thread (blockDim.x multiple of 32,
+// at most 1024 threads); returns the prefix and the block total.
+__device__ __forceinline__ int block_excl_scan(int v, int &total) {
+  __shared__ int s_w[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int t = __shfl_up_sync(kFull, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) s_w[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < nw ? s_w[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(kFull, w, d);
+      if (lane >= d) w += t;
+    }
+    if (lane < nw) s_w[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  total = s_w[nw - 1];
+  const int before = wid ? s_w[wid - 1] : 0;
+  __syncthreads();  // s_w may be reused by the caller's next scan
+  return before + incl - v;
+}
+
 __global__ void __launch_bounds__(256)
 k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
-                int32_t *__restrict__ stack, Ctl *ctl, int W, int H, int size) {
+                int32_t *__restrict__ stack, Ctl *ctl, int W, int H, int nring) {
   if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
-  const int lane = threadIdx.x & 31;
-  const int stride = gridDim.x * blockDim.x;
-  int o[8];
-  nshift8(W, o);
-  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < size; base += stride) {
-    const int c = base + lane;
-    bool level0 = false;
-    if (c < size) {
-      const int y = c / W;
-      const int x = c - y * W;
-      unsigned m = 0;
-      if (x >= 1 && x <= W - 2 && y >= 1 && y <= H - 2) {
+  __shared__ int8_t sr[kDyTile + 2][kDxTile + 4];
+  __shared__ int s_base;
+  const int x0 = blockIdx.x * kDxTile;  // grid x of sr[.][0]
+  const int y0 = blockIdx.y * kDyTile;  // grid y of sr[0][.]
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  for (int idx = t; idx < (kDyTile + 2) * (kDxTile + 2); idx += 256) {
+    const int ly = idx / (kDxTile + 2);
+    const int lx = idx - ly * (kDxTile + 2);
+    const int gx = x0 + lx, gy = y0 + ly;
+    sr[ly][lx] = (gx < W && gy < H) ? rec[(size_t)gy * W + gx] : (int8_t)FS_NO_FLOW;
+  }
+  __syncthreads();
+  const int lx = threadIdx.x + 1;
+  const int gx = x0 + lx;
+  unsigned pit_bits = 0;
 #pragma unroll
-        for (int k = 0; k < 8; k++)
-          if (rec[c + o[k]] == ((k + 4) & 7)) m |= 1u << k;
-      }
-      mask[c] = (uint8_t)m;
-      level0 = rec[c] < 0;
-    }
-    const unsigned b = __ballot_sync(kFull, level0);
-    if (b) {
-      int base_pos = 0;
-      if (lane == 0) base_pos = atomicAdd(&ctl->top, __popc(b));
-      base_pos = __shfl_sync(kFull, base_pos, 0);
-      if (level0) stack[base_pos + __popc(b & ((1u << lane) - 1u))] = c;
+  for (int r = 0; r < kDRows; r++) {
+    const int ly = threadIdx.y + 8 * r + 1;
+    const int gy = y0 + ly;
+    if (gx <= W - 2 && gy <= H - 2) {
+      unsigned m = 0;
+      m |= (sr[ly][lx - 1] == 4) ? 1u : 0u;         // W  neighbour drains E
+      m |= (sr[ly - 1][lx - 1] == 5) ? 2u : 0u;     // NW drains SE
+      m |= (sr[ly - 1][lx] == 6) ? 4u : 0u;         // N  drains S
+      m |= (sr[ly - 1][lx + 1] == 7) ? 8u : 0u;     // NE drains SW
+      m |= (sr[ly][lx + 1] == 0) ? 16u : 0u;        // E  drains W
+      m |= (sr[ly + 1][lx + 1] == 1) ? 32u : 0u;    // SE drains NW
+      m |= (sr[ly + 1][lx] == 2) ? 64u : 0u;        // S  drains N
+      m |= (sr[ly + 1][lx - 1] == 3) ? 128u : 0u;   // SW drains NE
+      mask[(size_t)gy * W + gx] = (uint8_t)m;
+      if (sr[ly][lx] == kPit) pit_bits |= 1u << r;
     }
   }
+  int total;
+  const int excl = block_excl_scan(__popc(pit_bits), total);
+  if (total == 0) return;
+  if (t == 0) s_base = nring + atomicAdd(&ctl->top, total);
+  __syncthreads();
+  int pos = s_base + excl;
+#pragma unroll
+  for (int r = 0; r < kDRows; r++)
+    if (pit_bits >> r & 1u) stack[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
 }
 
 __device__ __forceinline__ long long abs_bits(double x) {
@@ -356,16 +408,13 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
     // hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)) with D = RN(1+fact).
     const double D = T[1], R = T[2];
     const double num = fact * (h0 - hn);
-    const double q = div_rn(num, D, R);
-    hnew = h0 - q;
-    // |q| <= tol/2 and |h0| <= tol*2^48 give |RN(hnew-h0)| <= 9tol/16 < tol:
-    // the reference loop stops after this iterate.
-    if (abs_bits(q) <= a.half_tol_bits && abs_bits(h0) <= a.h0_lim_bits) return hnew;
-    hp = h0;
-    diff = hnew - hp;
+    hnew = h0 - div_rn(num, D, R);
+    diff = hnew - h0;
     hp = hnew;
     it = 1;
-    while (fabs(diff) > a.tol) {
+    // fabs(diff) > tol as an integer compare of the magnitudes' bits (both
+    // non-negative; a NaN diff stops the loop, as fabs(NaN) > tol is false)
+    while (abs_bits(diff) > a.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
       const double num2 = (hnew - h0) + fact * (hnew - hn);
       hnew -= div_rn(num2, D, R);
       diff = hnew - hp;
@@ -398,9 +447,9 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
 // Uplift of the interior level-0 cells (pits), fastscape_RB.cpp:291-295.
 __device__ __forceinline__ void uplift_pits(const WalkArgs &a, int lvl0_end, int tid,
                                             int nthreads) {
-  for (int i = tid; i < lvl0_end; i += nthreads) {
+  for (int i = a.nring + tid; i < lvl0_end; i += nthreads) {
     const int c = __ldcg(&a.stack[i]);
-    if (a.rec[c] == kPit) a.h[c] = __ldcg(&a.h[c]) + a.u_dt;
+    a.h[c] = __ldcg(&a.h[c]) + a.u_dt;
   }
 }
 
@@ -414,9 +463,6 @@ k_walk(WalkArgs a) {
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
   if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
-  const int lane = threadIdx.x & 31;
-  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthreads = gridDim.x * blockDim.x;
   const bool stamp = a.stamp && tid == 0;
@@ -435,44 +481,54 @@ k_walk(WalkArgs a) {
   // append counter rotates over three words so a block that reads the size
   // of level k after the barrier never races with the reset for level k+2.
   int lo = 0;
-  int hi = ld_volatile_i32(&ctl->top);
+  int hi = a.nring + ld_volatile_i32(&ctl->top);
   const int lvl0_end = hi;
   if (tid == 0) {
     a.lvl_off[0] = 0;
     a.lvl_off[1] = hi;
   }
   int nlev = 1;
+  __shared__ int s_base;
   for (;;) {
     const int j = (nlev - 1) % 3;  // counter of this expansion
     if (tid == 0) ctl->lvlcnt[nlev % 3] = 0;  // counter of the next one
-    for (int i0 = lo + warp_global * 32; i0 < hi; i0 += nwarps * 32) {
-      const int i = i0 + lane;
-      unsigned m = 0;
-      int c = 0;
-      if (i < hi) {
-        c = __ldcg(&a.stack[i]);
-        m = a.mask[c];
-      }
-      const int nd = __popc(m);
-      int incl = nd;
+    // Each block expands chunks of kPer*blockDim.x consecutive frontier
+    // cells (kPer consecutive per thread, so the next level keeps the
+    // frontier's spatial order) with one block scan and one atomic.
+    const int chunk = kPer * kWalkThreads;
+    for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
+      const int i0 = base + threadIdx.x * kPer;
+      int cs[kPer];
+      unsigned ms[kPer];
+      int nd = 0;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int t = __shfl_up_sync(kFull, incl, d);
-        if (lane >= d) incl += t;
+      for (int q = 0; q < kPer; q++) {
+        ms[q] = 0;
+        cs[q] = 0;
+        if (i0 + q < hi) {
+          cs[q] = __ldcg(&a.stack[i0 + q]);
+          ms[q] = a.mask[cs[q]];
+        }
+        nd += __popc(ms[q]);
       }
-      const int total = __shfl_sync(kFull, incl, 31);
-      int base = 0;
-      if (lane == 31 && total) base = atomicAdd(&ctl->lvlcnt[j], total);
-      base = __shfl_sync(kFull, base, 31);
-      int pos = hi + base + incl - nd;
-      while (m) {
-        const int k = __ffs(m) - 1;
-        m &= m - 1;
-        if (pos < a.size)
-          a.stack[pos] = c + nbr_off(k, a.W);
-        else
-          raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
-        ++pos;
+      int total;
+      const int excl = block_excl_scan(nd, total);
+      if (threadIdx.x == 0) s_base = total ? atomicAdd(&ctl->lvlcnt[j], total) : 0;
+      __syncthreads();
+      int pos = hi + s_base + excl;
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < kPer; q++) {
+        unsigned m = ms[q];
+        while (m) {
+          const int k = __ffs(m) - 1;
+          m &= m - 1;
+          if (pos < a.size)
+            a.stack[pos] = cs[q] + nbr_off(k, a.W);
+          else
+            raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+          ++pos;
+        }
       }
     }
     if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
@@ -658,15 +714,13 @@ cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
 }
 
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, Ctl *ctl, StepGeom g,
+                                 int32_t *stack, Ctl *ctl, StepGeom g, int nring,
                                  cudaStream_t s) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  long long want = ((long long)g.size + 255) / 256;
-  int blocks = (int)(want < (long long)sms * 16 ? want : (long long)sms * 16);
-  if (blocks < 1) blocks = 1;
-  k_donors_level0<<<blocks, 256, 0, s>>>(rec, mask, stack, ctl, g.W, g.H, g.size);
+  const int iw = g.W - 2, ih = g.H - 2;
+  if (iw <= 0 || ih <= 0) return cudaSuccess;
+  dim3 block(32, 8);
+  dim3 grid((iw + kDxTile - 1) / kDxTile, (ih + kDyTile - 1) / kDyTile);
+  k_donors_level0<<<grid, block, 0, s>>>(rec, mask, stack, ctl, g.W, g.H, nring);
   return cudaGetLastError();
 }
 

@@ -99,6 +99,7 @@ struct fs_model {
   fs::Ctl *d_ctl = nullptr;
   fs::Ctl *h_ctl = nullptr;  // pinned mirror for status reads
   int walk_blocks = 0;
+  int nring = 0;             // cells of rings 0 and 1 (always level 0)
   int nmode = fs::kNGeneral;
   double u_dt = 0;
   unsigned long long timeout_ns = 2000000000ull;
@@ -228,11 +229,8 @@ fs::WalkArgs walk_args(const fs_model *m, int do_erode) {
   a.u_dt = do_erode ? m->u_dt : 0.0;
   a.neq = m->p.neq;
   a.tol = m->p.tol;
-  {
-    const double ht = m->p.tol * 0.5, hl = std::ldexp(m->p.tol, 48);
-    std::memcpy(&a.half_tol_bits, &ht, 8);
-    std::memcpy(&a.h0_lim_bits, &hl, 8);
-  }
+  std::memcpy(&a.tol_bits, &m->p.tol, 8);
+  a.nring = m->nring;
   a.nmode = m->nmode;
   a.do_erode = do_erode;
   a.stamp = m->timing ? 1 : 0;
@@ -254,7 +252,8 @@ int one_step(fs_model *m, int i) {
     FS_CUDA(fs::launch_receivers_fast(m->d_h, m->d_rec, m->d_amb, m->d_ctl, g, m->p.dr_orth,
                                       m->p.dr_diag, m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 1], m->stream));
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->stream));
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->nring,
+                                   m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 2], m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 1), m->walk_blocks, m->stream));
   return FS_OK;
@@ -408,6 +407,19 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
     return fail(*status);
 
   if (int st = grow_table(m, std::min<long long>(m->size, 65535))) return fail(st);
+  {
+    // Rings 0 and 1 never get a receiver: they are the head of level 0 in
+    // every timestep, in ascending order, written once here.
+    std::vector<int32_t> ring;
+    for (int y = 0; y < m->H; y++)
+      for (int x = 0; x < m->W; x++)
+        if (x <= 1 || y <= 1 || x >= m->W - 2 || y >= m->H - 2) ring.push_back(y * m->W + x);
+    m->nring = static_cast<int>(ring.size());
+    if (!cu(cudaMemcpyAsync(m->d_stack, ring.data(), ring.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, m->stream), "upload(ring)") ||
+        !cu(cudaStreamSynchronize(m->stream), "sync"))
+      return fail(*status);
+  }
 
   const fs::StepGeom g{m->W, m->H, m->size};
   if (init_mode == FS_INIT_REFERENCE || init_mode == FS_INIT_MT19937) {
@@ -656,7 +668,8 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
   FS_CUDA(cudaMemcpyAsync(m->d_rec, r.data(), m->size, cudaMemcpyHostToDevice, m->stream));
   FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream));
   const fs::StepGeom g{m->W, m->H, m->size};
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->stream));
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->nring,
+                                   m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 0), m->walk_blocks, m->stream));
   m->have_step = true;
   return collect_status(m);
