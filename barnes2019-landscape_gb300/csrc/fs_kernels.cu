@@ -274,12 +274,13 @@ constexpr int kDxTile = 32;  // tile of cells over [1, W-2] x [1, H-2]
 constexpr int kDyTile = 64;
 constexpr int kDRows = kDyTile / 8;
 
-// Exclusive block scan of one int per thread (blockDim.x multiple of 32,
-// at most 1024 threads); returns the prefix and the block total.
-__device__ __forceinline__ int block_excl_scan(int v, int &total) {
+// Exclusive block scan of one int per thread; t is the thread's linear index
+// in the block and nthreads the block size (a multiple of 32, at most 1024).
+// Returns the prefix and the block total.
+__device__ __forceinline__ int block_excl_scan(int v, int &total, int t, int nthreads) {
   __shared__ int s_w[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
+  const int lane = t & 31, wid = t >> 5;
+  const int nw = nthreads >> 5;
   int incl = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -342,7 +343,7 @@ k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
     }
   }
   int total;
-  const int excl = block_excl_scan(__popc(pit_bits), total);
+  const int excl = block_excl_scan(__popc(pit_bits), total, t, 256);
   if (total == 0) return;
   if (t == 0) s_base = nring + atomicAdd(&ctl->top, total);
   __syncthreads();
@@ -512,7 +513,7 @@ k_walk(WalkArgs a) {
         nd += __popc(ms[q]);
       }
       int total;
-      const int excl = block_excl_scan(nd, total);
+      const int excl = block_excl_scan(nd, total, threadIdx.x, kWalkThreads);
       if (threadIdx.x == 0) s_base = total ? atomicAdd(&ctl->lvlcnt[j], total) : 0;
       __syncthreads();
       int pos = hi + s_base + excl;
