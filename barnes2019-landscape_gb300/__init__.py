@@ -42,6 +42,7 @@ ABI_SYMBOLS = [
     "fs_get_levels", "fs_get_donor_mask", "fs_get_shape", "fs_get_params",
     "fs_steps_executed", "fs_set_timing", "fs_get_phase_times",
     "fs_set_barrier_timeout", "fs_synchronize", "fs_last_error", "fs_version",
+    "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_receiver_fixups",
     "fs_test_table_capacity",

@@ -99,6 +99,9 @@ cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
                                 cudaStream_t s);
 cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,
                                 cudaStream_t s);
+// Stores `msg` as this thread's fs_last_error() text; returns status.
+int record_error(int status, const char *msg);
+
 cudaError_t launch_test_wait(Ctl *ctl, int blocks,
                              unsigned long long timeout_ns, cudaStream_t s);
 

@@ -82,6 +82,8 @@ bool finite_params(const fs_params &p) {
 
 }  // namespace
 
+int fs::record_error(int status, const char *msg) { return set_error(status, "%s", msg); }
+
 struct fs_model {
   int W = 0, H = 0, size = 0;
   fs_params p{};

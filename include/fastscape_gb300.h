@@ -166,6 +166,26 @@ size_t fs_last_error(char *buf, size_t n);
 /* Library version string. */
 const char *fs_version(void);
 
+/* Largest grid (width*height cells) fs_step_noalloc accepts. */
+#define FS_NOALLOC_MAX_CELLS 262144
+
+/* Advances a caller-owned device elevation buffer d_h (width*height doubles,
+ * row-major, the layout of fs_get_elevation) by exactly nsteps timesteps on
+ * `stream` (a cudaStream_t; NULL for the default stream), with results
+ * identical to fs_create + fs_set_elevation + fs_step, and waits for them.
+ * No counterpart in the reference. It allocates nothing: for callers that
+ * may not allocate device memory while running (a host application that
+ * owns all device memory through its own pool, a latency-critical loop where
+ * cudaMalloc/cudaFree would synchronize the device, a plugin with a fixed
+ * footprint). All scratch (~21 MB) is one static device array in the
+ * library, held on every GPU that loads it until the process exits, shared
+ * by all calls and keeping the last call's contents: calls that overlap on
+ * the GPU race and must be serialized by the caller. Grids larger than
+ * FS_NOALLOC_MAX_CELLS return FS_ERR_ARG. The first call on a device looks
+ * up the array's device address; make it before any stream capture. */
+int fs_step_noalloc(double *d_h, int width, int height, const fs_params *params,
+                    int nsteps, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
