@@ -63,25 +63,39 @@ struct StepGeom {
   int size;  // W*H (< 2^31)
 };
 
+// Arrays indexed by position i in the level order (the reference's stack):
+//   ent[i]   cell index; level 0 starts with the two rings (fixed) followed
+//            by the pits of this timestep
+//   pdir[i]  receiver direction of ent[i] (0..7), bit 3 set when that
+//            receiver is a pit (levels >= 1 only)
+//   nd[i]    number of donors of ent[i]
+//   kid[i]   position of its first donor; its donors are contiguous
+//   acc[i]   drainage cell count of ent[i]
 struct WalkArgs {
   double *h;
-  const int8_t *rec;
   const uint8_t *mask;
-  int32_t *stack;
+  int32_t *ent;
+  uint8_t *pdir;
+  uint8_t *nd;
+  int32_t *kid;
+  uint32_t *acc;
   int32_t *lvl_off;        // size+2 entries
-  uint32_t *cnt;           // drainage cell counts
   const double *tab;       // erosion table, kTabStride doubles per count
   int tab_cap;             // counts k < tab_cap are in the table
   Ctl *ctl;
   int W, size;
-  int nring;               // ring cells, pre-placed at stack[0, nring)
+  int nring;               // ring cells, pre-placed at ent[0, nring)
   double u_dt, neq, tol;
   long long tol_bits;      // bits of tol (magnitude compares as integers)
+  float tol_lo_f;          // an FP32 value <= tol*(1-2^-20)
   int nmode;
   int do_erode;            // 0: ordering + accumulation only
   int stamp;               // 1: accumulate phase times into ctl->walk_ns
   unsigned long long timeout_ns;
 };
+
+// An FP32 number not above tol*(1 - 2^-20), for the one-iterate test.
+float tol_lower_float(double tol);
 
 // Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
 cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
@@ -90,7 +104,7 @@ cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
                                   Ctl *ctl, StepGeom g, double dr_orth,
                                   double dr_diag, cudaStream_t s);
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, Ctl *ctl, StepGeom g, int nring,
+                                 int32_t *ent, Ctl *ctl, StepGeom g, int nring,
                                  cudaStream_t s);
 cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s);
 int walk_threads();

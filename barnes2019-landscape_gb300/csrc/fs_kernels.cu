@@ -307,7 +307,7 @@ __device__ __forceinline__ int block_excl_scan(int v, int &total, int t, int nth
 
 __global__ void __launch_bounds__(256)
 k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
-                int32_t *__restrict__ stack, Ctl *ctl, int W, int H, int nring) {
+                int32_t *__restrict__ ent, Ctl *ctl, int W, int H, int nring) {
   if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   __shared__ int8_t sr[kDyTile + 2][kDxTile + 4];
   __shared__ int s_base;
@@ -350,7 +350,7 @@ k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
   int pos = s_base + excl;
 #pragma unroll
   for (int r = 0; r < kDRows; r++)
-    if (pit_bits >> r & 1u) stack[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
+    if (pit_bits >> r & 1u) ent[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
 }
 
 __device__ __forceinline__ long long abs_bits(double x) {
@@ -409,7 +409,16 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
     // hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)) with D = RN(1+fact).
     const double D = T[1], R = T[2];
     const double num = fact * (h0 - hn);
-    hnew = h0 - div_rn(num, D, R);
+    const double q = div_rn(num, D, R);
+    hnew = h0 - q;
+    // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
+    // |RN(hnew-h0)| <= |q| + 2^-51(|h0|+|q|), an FP32 test on truncated
+    // magnitudes with 2^-21 of slack proves it for almost every cell without
+    // spending the FP64 subtraction (see the bound in fs_kernels.cu's
+    // header); the rest evaluate diff exactly and follow the reference loop.
+    const float qf = fabsf(trunc_to_float(q));
+    const float hf = fabsf(trunc_to_float(h0));
+    if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= a.tol_lo_f) return hnew;
     diff = hnew - h0;
     hp = hnew;
     it = 1;
@@ -449,7 +458,7 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
 __device__ __forceinline__ void uplift_pits(const WalkArgs &a, int lvl0_end, int tid,
                                             int nthreads) {
   for (int i = a.nring + tid; i < lvl0_end; i += nthreads) {
-    const int c = __ldcg(&a.stack[i]);
+    const int c = __ldcg(&a.ent[i]);
     a.h[c] = __ldcg(&a.h[c]) + a.u_dt;
   }
 }
@@ -457,6 +466,14 @@ __device__ __forceinline__ void uplift_pits(const WalkArgs &a, int lvl0_end, int
 // ---------------------------------------------------------------------------
 // 3. Persistent level walker (cooperative launch, one grid barrier per level
 // per sweep).
+//
+// The ordering is kept as arrays indexed by position in the level order
+// ("stack" in the reference): ent[i] the cell, pdir[i] its receiver
+// direction (bit 3: the receiver is a pit), nd[i] and kid[i] the number of
+// donors and the position of the first one in the next level (the donors of
+// one entry are contiguous), acc[i] the drainage count. Accumulation and
+// erosion then read these by position -- coalesced -- instead of gathering
+// receivers, masks and counts by cell index.
 // ---------------------------------------------------------------------------
 template <int NMODE>
 __global__ void __launch_bounds__(kWalkThreads)
@@ -477,10 +494,12 @@ k_walk(WalkArgs a) {
   };
 
   // ---- ordering: fastscape_RB.cpp:229-251 -------------------------------
-  // Level k+1 = the donors of level k. Each warp expands 32 frontier cells:
-  // a warp scan of the donor counts and one atomic reserve their slots. The
-  // append counter rotates over three words so a block that reads the size
-  // of level k after the barrier never races with the reset for level k+2.
+  // Level k+1 = the donors of level k. Each block expands chunks of
+  // kPer*blockDim.x consecutive frontier entries (kPer consecutive per
+  // thread, so the next level keeps the frontier's spatial order) with one
+  // block scan and one atomic per chunk. The append counter rotates over
+  // three words so a block that reads the size of level k after the barrier
+  // never races with the reset for level k+2.
   int lo = 0;
   int hi = a.nring + ld_volatile_i32(&ctl->top);
   const int lvl0_end = hi;
@@ -493,9 +512,6 @@ k_walk(WalkArgs a) {
   for (;;) {
     const int j = (nlev - 1) % 3;  // counter of this expansion
     if (tid == 0) ctl->lvlcnt[nlev % 3] = 0;  // counter of the next one
-    // Each block expands chunks of kPer*blockDim.x consecutive frontier
-    // cells (kPer consecutive per thread, so the next level keeps the
-    // frontier's spatial order) with one block scan and one atomic.
     const int chunk = kPer * kWalkThreads;
     for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
       const int i0 = base + threadIdx.x * kPer;
@@ -507,7 +523,7 @@ k_walk(WalkArgs a) {
         ms[q] = 0;
         cs[q] = 0;
         if (i0 + q < hi) {
-          cs[q] = __ldcg(&a.stack[i0 + q]);
+          cs[q] = __ldcg(&a.ent[i0 + q]);
           ms[q] = a.mask[cs[q]];
         }
         nd += __popc(ms[q]);
@@ -520,14 +536,22 @@ k_walk(WalkArgs a) {
       __syncthreads();
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
+        if (i0 + q >= hi) break;
         unsigned m = ms[q];
+        a.kid[i0 + q] = pos;
+        a.nd[i0 + q] = (uint8_t)__popc(m);
+        // level-1 entries remember whether their receiver is a pit
+        // (level-0 entries past the rings)
+        const unsigned pit = (nlev == 1 && i0 + q >= a.nring) ? 8u : 0u;
         while (m) {
           const int k = __ffs(m) - 1;
           m &= m - 1;
-          if (pos < a.size)
-            a.stack[pos] = cs[q] + nbr_off(k, a.W);
-          else
+          if (pos < a.size) {
+            a.ent[pos] = cs[q] + nbr_off(k, a.W);
+            a.pdir[pos] = (uint8_t)(((k + 4) & 7) | pit);
+          } else {
             raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+          }
           ++pos;
         }
       }
@@ -556,24 +580,23 @@ k_walk(WalkArgs a) {
   lap(0);
 
   // ---- accumulation: fastscape_RB.cpp:262-279, pulled level by level ----
-  // cnt[c] = 1 + sum of the donors' counts; the reference's accum[c] is
-  // cnt[c]*cell_area (exact: integer multiples of cell_area). A count at
-  // level >= 1 beyond the erosion table stops the timestep before any
-  // elevation changes; the host grows the table and repeats it.
+  // acc[i] = 1 + sum of the donors' counts, read from the contiguous run
+  // [kid[i], kid[i] + nd[i]) of the next level; the reference's accum is
+  // acc*cell_area (exact: integer multiples of cell_area). A count at level
+  // >= 1 beyond the erosion table stops the timestep before any elevation
+  // changes; the host grows the table and repeats it.
   for (int L = nlev - 1; L >= 0; --L) {
     if (L == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
     const int b = __ldcg(&a.lvl_off[L]);
     const int e = __ldcg(&a.lvl_off[L + 1]);
     for (int i = b + tid; i < e; i += nthreads) {
-      const int c = __ldcg(&a.stack[i]);
-      unsigned m = a.mask[c];
+      const int n = __ldcg(&a.nd[i]);
       uint32_t s = 1;
-      while (m) {
-        const int k = __ffs(m) - 1;
-        m &= m - 1;
-        s += __ldcg(&a.cnt[c + nbr_off(k, a.W)]);
+      if (n) {
+        const int k0 = __ldcg(&a.kid[i]);
+        for (int q = 0; q < n; q++) s += __ldcg(&a.acc[k0 + q]);
       }
-      a.cnt[c] = s;
+      a.acc[i] = s;
       if (a.do_erode && L > 0 && s >= (uint32_t)a.tab_cap) atomicMax(&ctl->abort_k, (int)s);
     }
     if (L > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
@@ -583,26 +606,46 @@ k_walk(WalkArgs a) {
 
   // ---- uplift + erosion: fastscape_RB.cpp:285-296 and :306-328 in the
   // level order of fastscape_RB+P.cpp:319-350. Eroded cells are uplifted on
-  // their first read; level-1 cells see their pit receiver's uplift added on
+  // their first read; level-1 cells add the uplift of a pit receiver on
   // read, and the pits themselves are uplifted once no level-1 cell can read
   // them any more (during level 2, or after a barrier when level 1 is the
   // last). No barrier is needed before level 1: it reads counts complete
   // since the barrier after accumulation level 1 and never-written h.
+  // Two entries per thread per pass, their loads issued together.
   for (int L = 1; L < nlev; ++L) {
     const int b = __ldcg(&a.lvl_off[L]);
     const int e = __ldcg(&a.lvl_off[L + 1]);
-    for (int i = b + tid; i < e; i += nthreads) {
-      const int c = __ldcg(&a.stack[i]);
-      const int r = a.rec[c];
-      const int n = c + nbr_off(r, a.W);
-      const uint32_t k = __ldcg(&a.cnt[c]);
-      const double *T = a.tab + (size_t)k * kTabStride + 4 * (r & 1);
-      const double h0 = __ldcg(&a.h[c]) + a.u_dt;
-      double hn = __ldcg(&a.h[n]);
-      if (L == 1 && a.rec[n] == kPit) hn = hn + a.u_dt;
-      const double hnew = erode_cell<NMODE>(a, T, h0, hn);
-      if (!isfinite(hnew)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-      a.h[c] = hnew;
+    for (int i = b + tid; i < e; i += 2 * nthreads) {
+      const int i2 = i + nthreads;
+      const bool two = i2 < e;
+      const int c1 = __ldcg(&a.ent[i]);
+      const int d1 = __ldcg(&a.pdir[i]);
+      const uint32_t k1 = __ldcg(&a.acc[i]);
+      int c2 = c1, d2 = d1;
+      uint32_t k2 = k1;
+      if (two) {
+        c2 = __ldcg(&a.ent[i2]);
+        d2 = __ldcg(&a.pdir[i2]);
+        k2 = __ldcg(&a.acc[i2]);
+      }
+      const int n1 = c1 + nbr_off(d1 & 7, a.W);
+      const int n2 = c2 + nbr_off(d2 & 7, a.W);
+      const double *T1 = a.tab + (size_t)k1 * kTabStride + 4 * (d1 & 1);
+      const double *T2 = a.tab + (size_t)k2 * kTabStride + 4 * (d2 & 1);
+      const double hc1 = __ldcg(&a.h[c1]);
+      double hn1 = __ldcg(&a.h[n1]);
+      const double hc2 = __ldcg(&a.h[c2]);
+      double hn2 = __ldcg(&a.h[n2]);
+      if (d1 & 8) hn1 = hn1 + a.u_dt;
+      if (d2 & 8) hn2 = hn2 + a.u_dt;
+      const double r1 = erode_cell<NMODE>(a, T1, hc1 + a.u_dt, hn1);
+      if (!isfinite(r1)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+      a.h[c1] = r1;
+      if (two) {
+        const double r2 = erode_cell<NMODE>(a, T2, hc2 + a.u_dt, hn2);
+        if (!isfinite(r2)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+        a.h[c2] = r2;
+      }
     }
     if (L == 2) uplift_pits(a, lvl0_end, tid, nthreads);
     if (L + 1 < nlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
@@ -685,6 +728,13 @@ __global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
 
 int walk_threads() { return kWalkThreads; }
 
+float tol_lower_float(double tol) {
+  const double t = tol * (1.0 - 0x1p-20);
+  float f = (float)t;
+  while ((double)f > t) f = nextafterf(f, 0.f);
+  return f;
+}
+
 cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
                              double dr_orth, double dr_diag, cudaStream_t s) {
   const int iw = g.W - 4, ih = g.H - 4;
@@ -715,13 +765,13 @@ cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
 }
 
 cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *stack, Ctl *ctl, StepGeom g, int nring,
+                                 int32_t *ent, Ctl *ctl, StepGeom g, int nring,
                                  cudaStream_t s) {
   const int iw = g.W - 2, ih = g.H - 2;
   if (iw <= 0 || ih <= 0) return cudaSuccess;
   dim3 block(32, 8);
   dim3 grid((iw + kDxTile - 1) / kDxTile, (ih + kDyTile - 1) / kDyTile);
-  k_donors_level0<<<grid, block, 0, s>>>(rec, mask, stack, ctl, g.W, g.H, nring);
+  k_donors_level0<<<grid, block, 0, s>>>(rec, mask, ent, ctl, g.W, g.H, nring);
   return cudaGetLastError();
 }
 

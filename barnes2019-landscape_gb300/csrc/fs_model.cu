@@ -7,9 +7,13 @@
 //                               timesteps, as in the reference)
 //   rec     int8[size]          receiver direction code, -1 = NO_FLOW
 //   mask    uint8[size]         donor mask (bit k: neighbour k drains here)
-//   stack   int32[size]         cells grouped by level
+//   ent     int32[size]         cells grouped by level (the reference's stack)
+//   pdir    uint8[size]         receiver direction by level position
+//   nd      uint8[size]         donor count by level position
+//   kid     int32[size]         first donor's position by level position
 //   lvl_off int32[size+2]       level offsets into stack
-//   cnt     uint32[size]        drainage cell counts (accum = cnt*cell_area)
+//   acc     uint32[size]        drainage cell counts by level position
+//                               (accum = acc*cell_area)
 //   amb     int32[size]         cells queued for the FP64 receiver fix-up
 //   tab     double[8*tab_cap]   erosion table per drainage count k < tab_cap
 //                               (see fs_internal.h); grows on demand
@@ -92,10 +96,13 @@ struct fs_model {
   double *d_h = nullptr;
   int8_t *d_rec = nullptr;
   uint8_t *d_mask = nullptr;
-  int32_t *d_stack = nullptr;
+  int32_t *d_ent = nullptr;
+  uint8_t *d_pdir = nullptr;
+  uint8_t *d_nd = nullptr;
+  int32_t *d_kid = nullptr;
   int32_t *d_amb = nullptr;   // cells the receiver filter could not decide
   int32_t *d_lvl = nullptr;
-  uint32_t *d_cnt = nullptr;
+  uint32_t *d_acc = nullptr;
   double *d_tab = nullptr;
   int tab_cap = 0;
   fs::Ctl *d_ctl = nullptr;
@@ -124,10 +131,13 @@ void free_model(fs_model *m) {
   cudaFree(m->d_h);
   cudaFree(m->d_rec);
   cudaFree(m->d_mask);
-  cudaFree(m->d_stack);
+  cudaFree(m->d_ent);
+  cudaFree(m->d_pdir);
+  cudaFree(m->d_nd);
+  cudaFree(m->d_kid);
   cudaFree(m->d_amb);
   cudaFree(m->d_lvl);
-  cudaFree(m->d_cnt);
+  cudaFree(m->d_acc);
   cudaFree(m->d_tab);
   cudaFree(m->d_ctl);
   if (m->h_ctl) cudaFreeHost(m->h_ctl);
@@ -218,11 +228,13 @@ int collect_status(fs_model *m) {
 fs::WalkArgs walk_args(const fs_model *m, int do_erode) {
   fs::WalkArgs a{};
   a.h = m->d_h;
-  a.rec = m->d_rec;
   a.mask = m->d_mask;
-  a.stack = m->d_stack;
+  a.ent = m->d_ent;
+  a.pdir = m->d_pdir;
+  a.nd = m->d_nd;
+  a.kid = m->d_kid;
+  a.acc = m->d_acc;
   a.lvl_off = m->d_lvl;
-  a.cnt = m->d_cnt;
   a.tab = m->d_tab;
   a.tab_cap = m->tab_cap;
   a.ctl = m->d_ctl;
@@ -232,6 +244,7 @@ fs::WalkArgs walk_args(const fs_model *m, int do_erode) {
   a.neq = m->p.neq;
   a.tol = m->p.tol;
   std::memcpy(&a.tol_bits, &m->p.tol, 8);
+  a.tol_lo_f = fs::tol_lower_float(m->p.tol);
   a.nring = m->nring;
   a.nmode = m->nmode;
   a.do_erode = do_erode;
@@ -254,7 +267,7 @@ int one_step(fs_model *m, int i) {
     FS_CUDA(fs::launch_receivers_fast(m->d_h, m->d_rec, m->d_amb, m->d_ctl, g, m->p.dr_orth,
                                       m->p.dr_diag, m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 1], m->stream));
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->nring,
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_ent, m->d_ctl, g, m->nring,
                                    m->stream));
   if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 2], m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 1), m->walk_blocks, m->stream));
@@ -392,10 +405,13 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
       !cu(cudaMalloc(&m->d_h, n * sizeof(double)), "cudaMalloc(h)") ||
       !cu(cudaMalloc(&m->d_rec, n), "cudaMalloc(rec)") ||
       !cu(cudaMalloc(&m->d_mask, n), "cudaMalloc(mask)") ||
-      !cu(cudaMalloc(&m->d_stack, n * sizeof(int32_t)), "cudaMalloc(stack)") ||
+      !cu(cudaMalloc(&m->d_ent, n * sizeof(int32_t)), "cudaMalloc(ent)") ||
+      !cu(cudaMalloc(&m->d_pdir, n), "cudaMalloc(pdir)") ||
+      !cu(cudaMalloc(&m->d_nd, n), "cudaMalloc(nd)") ||
+      !cu(cudaMalloc(&m->d_kid, n * sizeof(int32_t)), "cudaMalloc(kid)") ||
       !cu(cudaMalloc(&m->d_amb, n * sizeof(int32_t)), "cudaMalloc(amb)") ||
       !cu(cudaMalloc(&m->d_lvl, (n + 2) * sizeof(int32_t)), "cudaMalloc(lvl)") ||
-      !cu(cudaMalloc(&m->d_cnt, n * sizeof(uint32_t)), "cudaMalloc(cnt)") ||
+      !cu(cudaMalloc(&m->d_acc, n * sizeof(uint32_t)), "cudaMalloc(acc)") ||
       !cu(cudaMalloc(&m->d_ctl, sizeof(fs::Ctl)), "cudaMalloc(ctl)") ||
       !cu(cudaMallocHost(&m->h_ctl, sizeof(fs::Ctl)), "cudaMallocHost(ctl)"))
     return fail(*status);
@@ -403,7 +419,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
   // only ever written for interior cells.
   if (!cu(cudaMemsetAsync(m->d_rec, 0xff, n, m->stream), "memset(rec)") ||
       !cu(cudaMemsetAsync(m->d_mask, 0, n, m->stream), "memset(mask)") ||
-      !cu(cudaMemsetAsync(m->d_cnt, 0, n * sizeof(uint32_t), m->stream), "memset(cnt)") ||
+      !cu(cudaMemsetAsync(m->d_acc, 0, n * sizeof(uint32_t), m->stream), "memset(acc)") ||
       !cu(cudaMemsetAsync(m->d_lvl, 0, (n + 2) * sizeof(int32_t), m->stream), "memset(lvl)") ||
       !cu(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream), "memset(ctl)"))
     return fail(*status);
@@ -417,7 +433,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
       for (int x = 0; x < m->W; x++)
         if (x <= 1 || y <= 1 || x >= m->W - 2 || y >= m->H - 2) ring.push_back(y * m->W + x);
     m->nring = static_cast<int>(ring.size());
-    if (!cu(cudaMemcpyAsync(m->d_stack, ring.data(), ring.size() * sizeof(int32_t),
+    if (!cu(cudaMemcpyAsync(m->d_ent, ring.data(), ring.size() * sizeof(int32_t),
                             cudaMemcpyHostToDevice, m->stream), "upload(ring)") ||
         !cu(cudaStreamSynchronize(m->stream), "sync"))
       return fail(*status);
@@ -523,11 +539,14 @@ int fs_get_accumulation(const fs_model *m, double *out) {
   if (!out) return set_error(FS_ERR_ARG, "out is NULL");
   if (!m->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
   DeviceGuard dg(m->device);
-  std::vector<uint32_t> cnt(m->size);
-  FS_CUDA(cudaMemcpyAsync(cnt.data(), m->d_cnt, sizeof(uint32_t) * m->size, cudaMemcpyDeviceToHost,
+  std::vector<uint32_t> acc(m->size);
+  std::vector<int32_t> ent(m->size);
+  FS_CUDA(cudaMemcpyAsync(acc.data(), m->d_acc, sizeof(uint32_t) * m->size, cudaMemcpyDeviceToHost,
+                          m->stream));
+  FS_CUDA(cudaMemcpyAsync(ent.data(), m->d_ent, sizeof(int32_t) * m->size, cudaMemcpyDeviceToHost,
                           m->stream));
   FS_CUDA(cudaStreamSynchronize(m->stream));
-  for (int i = 0; i < m->size; i++) out[i] = static_cast<double>(cnt[i]) * m->p.cell_area;
+  for (int i = 0; i < m->size; i++) out[ent[i]] = static_cast<double>(acc[i]) * m->p.cell_area;
   return FS_OK;
 }
 
@@ -564,7 +583,7 @@ int fs_get_levels(const fs_model *m, int32_t *level_id, int32_t *nlevels) {
   if (nlevels) *nlevels = nl;
   if (!level_id) return FS_OK;
   std::vector<int32_t> stack(m->size), off(nl + 1);
-  FS_CUDA(cudaMemcpyAsync(stack.data(), m->d_stack, sizeof(int32_t) * m->size,
+  FS_CUDA(cudaMemcpyAsync(stack.data(), m->d_ent, sizeof(int32_t) * m->size,
                           cudaMemcpyDeviceToHost, m->stream));
   FS_CUDA(cudaMemcpyAsync(off.data(), m->d_lvl, sizeof(int32_t) * (nl + 1), cudaMemcpyDeviceToHost,
                           m->stream));
@@ -670,7 +689,7 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
   FS_CUDA(cudaMemcpyAsync(m->d_rec, r.data(), m->size, cudaMemcpyHostToDevice, m->stream));
   FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream));
   const fs::StepGeom g{m->W, m->H, m->size};
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_stack, m->d_ctl, g, m->nring,
+  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_ent, m->d_ctl, g, m->nring,
                                    m->stream));
   FS_CUDA(fs::launch_walk(walk_args(m, 0), m->walk_blocks, m->stream));
   m->have_step = true;

@@ -14,7 +14,7 @@
 // Limits and sharing:
 //   * grids of at most FS_NOALLOC_MAX_CELLS cells (width*height); larger
 //     grids are rejected with FS_ERR_ARG;
-//   * the scratch array (~21 MB: receivers, donor masks, level lists and
+//   * the scratch array (~23 MB: receivers, donor masks, level lists and
 //     offsets, drainage counts, the erosion table for every possible count,
 //     the control block) lives in the library image, so every GPU that loads
 //     the library holds it until the process exits;
@@ -45,13 +45,16 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(25
 // Regions of the scratch array, each 256-byte aligned.
 constexpr size_t kOffCtl = 0;
 constexpr size_t kOffTab = align256(kOffCtl + sizeof(fs::Ctl));
-constexpr size_t kOffStack = align256(kOffTab + kTabRecords * fs::kTabStride * sizeof(double));
-constexpr size_t kOffAmb = align256(kOffStack + kMaxCells * sizeof(int32_t));
+constexpr size_t kOffEnt = align256(kOffTab + kTabRecords * fs::kTabStride * sizeof(double));
+constexpr size_t kOffKid = align256(kOffEnt + kMaxCells * sizeof(int32_t));
+constexpr size_t kOffAmb = align256(kOffKid + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffLvl = align256(kOffAmb + kMaxCells * sizeof(int32_t));
-constexpr size_t kOffCnt = align256(kOffLvl + (kMaxCells + 2) * sizeof(int32_t));
-constexpr size_t kOffRec = align256(kOffCnt + kMaxCells * sizeof(uint32_t));
+constexpr size_t kOffAcc = align256(kOffLvl + (kMaxCells + 2) * sizeof(int32_t));
+constexpr size_t kOffRec = align256(kOffAcc + kMaxCells * sizeof(uint32_t));
 constexpr size_t kOffMask = align256(kOffRec + kMaxCells);
-constexpr size_t kScratchBytes = align256(kOffMask + kMaxCells);
+constexpr size_t kOffPdir = align256(kOffMask + kMaxCells);
+constexpr size_t kOffNd = align256(kOffPdir + kMaxCells);
+constexpr size_t kScratchBytes = align256(kOffNd + kMaxCells);
 
 // The scratch. Host code must not use this name as a device address (on the
 // host it is only a stand-in); the address comes from cudaGetSymbolAddress.
@@ -183,12 +186,15 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
 
   fs::Ctl *ctl = reinterpret_cast<fs::Ctl *>(d.base + kOffCtl);
   double *tab = reinterpret_cast<double *>(d.base + kOffTab);
-  int32_t *stack = reinterpret_cast<int32_t *>(d.base + kOffStack);
+  int32_t *ent = reinterpret_cast<int32_t *>(d.base + kOffEnt);
+  int32_t *kid = reinterpret_cast<int32_t *>(d.base + kOffKid);
   int32_t *amb = reinterpret_cast<int32_t *>(d.base + kOffAmb);
   int32_t *lvl = reinterpret_cast<int32_t *>(d.base + kOffLvl);
-  uint32_t *cnt = reinterpret_cast<uint32_t *>(d.base + kOffCnt);
+  uint32_t *acc = reinterpret_cast<uint32_t *>(d.base + kOffAcc);
   int8_t *rec = reinterpret_cast<int8_t *>(d.base + kOffRec);
   uint8_t *mask = reinterpret_cast<uint8_t *>(d.base + kOffMask);
+  uint8_t *pdir = reinterpret_cast<uint8_t *>(d.base + kOffPdir);
+  uint8_t *nd = reinterpret_cast<uint8_t *>(d.base + kOffNd);
 
   if (!d.tab_valid || !same_params(d.tab_params, p)) {
     fill_host_table(p);
@@ -211,17 +217,19 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   if (e == cudaSuccess) e = cudaMemsetAsync(rec, 0xff, size, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(mask, 0, size, s);
   if (e != cudaSuccess) return cuda_fail(e, "scratch reset");
-  k_place_rings<<<64, 256, 0, s>>>(stack, width, height);
+  k_place_rings<<<64, 256, 0, s>>>(ent, width, height);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "ring placement");
 
   const int nmode = (p.neq == 1.0) ? fs::kNOne : (p.neq == 2.0) ? fs::kNTwo : fs::kNGeneral;
   fs::WalkArgs a{};
   a.h = d_h;
-  a.rec = rec;
   a.mask = mask;
-  a.stack = stack;
+  a.ent = ent;
+  a.pdir = pdir;
+  a.nd = nd;
+  a.kid = kid;
+  a.acc = acc;
   a.lvl_off = lvl;
-  a.cnt = cnt;
   a.tab = tab;
   a.tab_cap = static_cast<int>(kTabRecords);
   a.ctl = ctl;
@@ -232,6 +240,7 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   a.neq = p.neq;
   a.tol = p.tol;
   std::memcpy(&a.tol_bits, &p.tol, sizeof(double));
+  a.tol_lo_f = fs::tol_lower_float(p.tol);
   a.nmode = nmode;
   a.do_erode = 1;
   a.stamp = 0;
@@ -241,7 +250,7 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
                         fs::kCtlResetBytes, s);
     if (e == cudaSuccess)
       e = fs::launch_receivers_fast(d_h, rec, amb, ctl, g, p.dr_orth, p.dr_diag, s);
-    if (e == cudaSuccess) e = fs::launch_donors_level0(rec, mask, stack, ctl, g, nring, s);
+    if (e == cudaSuccess) e = fs::launch_donors_level0(rec, mask, ent, ctl, g, nring, s);
     if (e == cudaSuccess) e = fs::launch_walk(a, d.walk_blocks[nmode], s);
     if (e != cudaSuccess) return cuda_fail(e, "timestep launch");
   }
