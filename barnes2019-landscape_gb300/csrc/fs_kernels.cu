@@ -512,47 +512,85 @@ k_walk(WalkArgs a) {
   for (;;) {
     const int j = (nlev - 1) % 3;  // counter of this expansion
     if (tid == 0) ctl->lvlcnt[nlev % 3] = 0;  // counter of the next one
+    // A block expands a chunk of kPer*blockDim.x consecutive entries; warp w
+    // covers 32*kPer of them in kPer coalesced passes (entry wbase+32q+lane).
+    // Warp scans give each entry's first-donor offset in entry order, one
+    // block scan over the warps and one atomic place the chunk, and the
+    // donors are written cooperatively (lane r writes the r-th donor of the
+    // pass), so every store of the expansion is coalesced and the next level
+    // keeps this level's order.
     const int chunk = kPer * kWalkThreads;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
-      const int i0 = base + threadIdx.x * kPer;
+      const int wbase = base + wid * (32 * kPer);
       int cs[kPer];
       unsigned ms[kPer];
-      int nd = 0;
+      int incl[kPer];
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
-        ms[q] = 0;
+        const int i = wbase + 32 * q + lane;
         cs[q] = 0;
-        if (i0 + q < hi) {
-          cs[q] = __ldcg(&a.ent[i0 + q]);
+        ms[q] = 0;
+        if (i < hi) {
+          cs[q] = __ldcg(&a.ent[i]);
           ms[q] = a.mask[cs[q]];
         }
-        nd += __popc(ms[q]);
+      }
+      int wtot = 0;
+#pragma unroll
+      for (int q = 0; q < kPer; q++) {
+        int v = __popc(ms[q]);
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int t = __shfl_up_sync(kFull, v, d);
+          if (lane >= d) v += t;
+        }
+        incl[q] = wtot + v;  // inclusive, relative to the warp's first donor
+        wtot += __shfl_sync(kFull, v, 31);
       }
       int total;
-      const int excl = block_excl_scan(nd, total, threadIdx.x, kWalkThreads);
+      const int wexcl = block_excl_scan(lane == 0 ? wtot : 0, total, threadIdx.x, kWalkThreads);
+      const int wstart = __shfl_sync(kFull, wexcl, 0);
       if (threadIdx.x == 0) s_base = total ? atomicAdd(&ctl->lvlcnt[j], total) : 0;
       __syncthreads();
-      int pos = hi + s_base + excl;
+      const int cbase = hi + s_base + wstart;  // position of the warp's first donor
       __syncthreads();
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
-        if (i0 + q >= hi) break;
-        unsigned m = ms[q];
-        a.kid[i0 + q] = pos;
-        a.nd[i0 + q] = (uint8_t)__popc(m);
-        // level-1 entries remember whether their receiver is a pit
-        // (level-0 entries past the rings)
-        const unsigned pit = (nlev == 1 && i0 + q >= a.nring) ? 8u : 0u;
-        while (m) {
-          const int k = __ffs(m) - 1;
-          m &= m - 1;
-          if (pos < a.size) {
-            a.ent[pos] = cs[q] + nbr_off(k, a.W);
-            a.pdir[pos] = (uint8_t)(((k + 4) & 7) | pit);
-          } else {
-            raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+        const int i = wbase + 32 * q + lane;
+        const int nd = __popc(ms[q]);
+        if (i < hi) {
+          a.kid[i] = cbase + incl[q] - nd;
+          a.nd[i] = (uint8_t)nd;
+        }
+        const int q_lo = __shfl_sync(kFull, incl[q] - nd, 0);
+        const int q_hi = __shfl_sync(kFull, incl[q], 31);
+        for (int r0 = q_lo; r0 < q_hi; r0 += 32) {
+          const int r = r0 + lane;
+          // owner = number of lanes whose inclusive count is <= r
+          int o = 0;
+#pragma unroll
+          for (int step = 16; step >= 1; step >>= 1) {
+            const int v = __shfl_sync(kFull, incl[q], o + step - 1);
+            if (v <= r) o += step;
           }
-          ++pos;
+          const int oc = __shfl_sync(kFull, cs[q], o);
+          unsigned om = __shfl_sync(kFull, ms[q], o);
+          const int ofirst = __shfl_sync(kFull, incl[q] - __popc(ms[q]), o);
+          if (r < q_hi) {
+            for (int skip = r - ofirst; skip > 0; --skip) om &= om - 1;
+            const int k = __ffs(om) - 1;
+            // level-1 entries remember whether their receiver is a pit
+            // (a level-0 entry past the rings)
+            const unsigned pit = (nlev == 1 && wbase + 32 * q + o >= a.nring) ? 8u : 0u;
+            const int pos = cbase + r;
+            if (pos < a.size) {
+              a.ent[pos] = oc + nbr_off(k, a.W);
+              a.pdir[pos] = (uint8_t)(((k + 4) & 7) | pit);
+            } else {
+              raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+            }
+          }
         }
       }
     }

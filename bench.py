@@ -51,11 +51,12 @@ RUN_NSTEP = 20            # run(20) executes 21 timesteps
 # mask u8, stack i32, cnt u32): each array the kernel must touch, once.
 ALG_BYTES = {
     "receivers": 8 + 1,                     # h read, rec write
-    "donors_level0": 1 + 1,                 # rec read, mask write (+ level-0 list)
-    "walk": (4 + 1 + 4) + (4 + 1 + 4 + 4) + (4 + 1 + 4 + 8 + 8),
-    # ordering: stack read, mask read, stack write; accumulation: stack,
-    # mask, donor counts read once, count write; erosion: stack, rec, count,
-    # h read, h write.
+    "donors_level0": 1 + 1,                 # rec read, mask write (+ pit list)
+    "walk": (4 + 1 + 4 + 1 + 4 + 1) + (1 + 4 + 4 + 4) + (4 + 1 + 4 + 8 + 8),
+    # ordering: entry read, mask read, entry + direction write, first-donor
+    # position + donor count write; accumulation: donor count, first-donor
+    # position, donors' counts read once, count write; erosion: entry,
+    # direction, count, h read, h write.
 }
 STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
 
