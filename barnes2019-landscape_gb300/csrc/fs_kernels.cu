@@ -31,6 +31,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
 constexpr int kPer = 8;  // frontier cells per thread per expansion chunk
+constexpr int kAccU = 4;  // 32-entry groups per warp per accumulation pass
 constexpr int kNewtonMaxIt = 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -314,11 +315,12 @@ k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
   const int x0 = blockIdx.x * kDxTile;  // grid x of sr[.][0]
   const int y0 = blockIdx.y * kDyTile;  // grid y of sr[0][.]
   const int t = threadIdx.y * 32 + threadIdx.x;
-  for (int idx = t; idx < (kDyTile + 2) * (kDxTile + 2); idx += 256) {
-    const int ly = idx / (kDxTile + 2);
-    const int lx = idx - ly * (kDxTile + 2);
-    const int gx = x0 + lx, gy = y0 + ly;
-    sr[ly][lx] = (gx < W && gy < H) ? rec[(size_t)gy * W + gx] : (int8_t)FS_NO_FLOW;
+  for (int ly = threadIdx.y; ly < kDyTile + 2; ly += 8) {
+    const int gy = y0 + ly;
+    for (int lx = threadIdx.x; lx < kDxTile + 2; lx += 32) {
+      const int gx = x0 + lx;
+      sr[ly][lx] = (gx < W && gy < H) ? rec[(size_t)gy * W + gx] : (int8_t)FS_NO_FLOW;
+    }
   }
   __syncthreads();
   const int lx = threadIdx.x + 1;
@@ -483,6 +485,7 @@ k_walk(WalkArgs a) {
   if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthreads = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
   const bool stamp = a.stamp && tid == 0;
   unsigned long long t_prev = stamp ? globaltimer_ns() : 0;
   auto lap = [&](int slot) {
@@ -520,7 +523,7 @@ k_walk(WalkArgs a) {
     // pass), so every store of the expansion is coalesced and the next level
     // keeps this level's order.
     const int chunk = kPer * kWalkThreads;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int wid = threadIdx.x >> 5;
     for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
       const int wbase = base + wid * (32 * kPer);
       int cs[kPer];
@@ -627,15 +630,56 @@ k_walk(WalkArgs a) {
     if (L == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
     const int b = __ldcg(&a.lvl_off[L]);
     const int e = __ldcg(&a.lvl_off[L + 1]);
-    for (int i = b + tid; i < e; i += nthreads) {
-      const int n = __ldcg(&a.nd[i]);
-      uint32_t s = 1;
-      if (n) {
-        const int k0 = __ldcg(&a.kid[i]);
-        for (int q = 0; q < n; q++) s += __ldcg(&a.acc[k0 + q]);
+    // Warp-cooperative: a warp takes kAccU groups of 32 consecutive entries
+    // (each group lies inside one expansion chunk, so its donors form one
+    // contiguous run starting at kid of its first entry), loads the runs
+    // coalesced -- all groups' first 32 donors in flight together -- and
+    // each lane sums its own donors out of the run with shuffles.
+    for (int g0 = b + (tid & ~31); g0 < e; g0 += kAccU * nthreads) {
+      int n[kAccU], incl[kAccU], run[kAccU], tot[kAccU];
+      uint32_t v0[kAccU];
+#pragma unroll
+      for (int u = 0; u < kAccU; u++) {
+        const int i = g0 + u * nthreads + lane;
+        int k = 0;
+        n[u] = 0;
+        if (i < e) {
+          n[u] = __ldcg(&a.nd[i]);
+          k = __ldcg(&a.kid[i]);
+        }
+        int v = n[u];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int t = __shfl_up_sync(kFull, v, d);
+          if (lane >= d) v += t;
+        }
+        incl[u] = v;
+        tot[u] = __shfl_sync(kFull, v, 31);
+        run[u] = __shfl_sync(kFull, k, 0);
       }
-      a.acc[i] = s;
-      if (a.do_erode && L > 0 && s >= (uint32_t)a.tab_cap) atomicMax(&ctl->abort_k, (int)s);
+#pragma unroll
+      for (int u = 0; u < kAccU; u++)
+        v0[u] = lane < tot[u] ? __ldcg(&a.acc[run[u] + lane]) : 0u;
+#pragma unroll
+      for (int u = 0; u < kAccU; u++) {
+        const int first = incl[u] - n[u];
+        uint32_t s = 1;
+        for (int r0 = 0; r0 < tot[u]; r0 += 32) {
+          uint32_t v = v0[u];
+          if (r0 > 0) v = r0 + lane < tot[u] ? __ldcg(&a.acc[run[u] + r0 + lane]) : 0u;
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const int r = first + q - r0;
+            const uint32_t x = __shfl_sync(kFull, v, r & 31);
+            if (q < n[u] && r >= 0 && r < 32) s += x;
+          }
+        }
+        const int i = g0 + u * nthreads + lane;
+        if (i < e) {
+          a.acc[i] = s;
+          if (a.do_erode && L > 0 && s >= (uint32_t)a.tab_cap) atomicMax(&ctl->abort_k, (int)s);
+        }
+      }
     }
     if (L > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
   }
