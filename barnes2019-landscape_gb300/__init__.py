@@ -42,6 +42,11 @@ ABI_SYMBOLS = [
     "fs_get_levels", "fs_get_donor_mask", "fs_get_shape", "fs_get_params",
     "fs_steps_executed", "fs_set_timing", "fs_get_phase_times",
     "fs_set_barrier_timeout", "fs_synchronize", "fs_last_error", "fs_version",
+    "fs_batch_create", "fs_batch_destroy", "fs_batch_step", "fs_batch_run",
+    "fs_batch_get_elevation", "fs_batch_set_elevation", "fs_batch_get_accumulation",
+    "fs_batch_get_receivers", "fs_batch_get_levels", "fs_batch_info",
+    "fs_batch_set_timing", "fs_batch_get_phase_times", "fs_batch_use_graph",
+    "fs_batch_autotune", "fs_batch_synchronize",
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_receiver_fixups",
@@ -121,6 +126,24 @@ def library() -> C.CDLL:
     L.fs_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.fs_last_error.restype = C.c_size_t
     L.fs_version.restype = C.c_char_p
+    ip = C.POINTER(C.c_int)
+    L.fs_batch_create.argtypes = [C.c_int, ip, ip, pp, C.c_int, C.POINTER(C.c_uint64), ip]
+    L.fs_batch_create.restype = vp
+    L.fs_batch_destroy.argtypes = [vp]
+    L.fs_batch_step.argtypes = [vp, C.c_int]
+    L.fs_batch_run.argtypes = [vp, C.c_int]
+    L.fs_batch_get_elevation.argtypes = [vp, C.c_int, dp]
+    L.fs_batch_set_elevation.argtypes = [vp, C.c_int, dp]
+    L.fs_batch_get_accumulation.argtypes = [vp, C.c_int, dp]
+    L.fs_batch_get_receivers.argtypes = [vp, C.c_int, i32p]
+    L.fs_batch_get_levels.argtypes = [vp, C.c_int, i32p, i32p]
+    L.fs_batch_info.argtypes = [vp, ip, C.POINTER(C.c_int64)]
+    L.fs_batch_set_timing.argtypes = [vp, C.c_int]
+    L.fs_batch_get_phase_times.argtypes = [vp, dp, C.c_int]
+    L.fs_batch_use_graph.argtypes = [vp, C.c_int]
+    L.fs_batch_autotune.argtypes = [vp, C.c_int, ip]
+    L.fs_batch_synchronize.argtypes = [vp]
+    L.fs_step_noalloc.argtypes = [vp, C.c_int, C.c_int, pp, C.c_int, vp]
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
     L.fs_test_barrier_timeout.argtypes = [vp, C.c_double]
     L.fs_test_set_receiver_path.argtypes = [vp, C.c_int]
@@ -260,6 +283,114 @@ class FastScape_RBP:
 
 # The serial reference class has the same interface.
 FastScape_RB = FastScape_RBP
+
+
+class FastScapeBatch:
+    """A ragged batch of independent realizations stepped together
+    (fs_batch_* in the C ABI). Each realization r has its own grid
+    ``widths[r] x heights[r]`` and constants ``params[r]`` (one n for all)
+    and evolves exactly as a FastScape_RBP of its own would."""
+
+    def __init__(self, widths, heights, params, init: int = INIT_PHILOX, seeds=None):
+        L = library()
+        n = len(widths)
+        if not (len(heights) == n and len(params) == n):
+            raise ValueError("widths, heights and params must have the same length")
+        self.n = n
+        self.widths = [int(w) for w in widths]
+        self.heights = [int(h) for h in heights]
+        self.params = list(params)
+        w = (C.c_int * n)(*self.widths)
+        h = (C.c_int * n)(*self.heights)
+        pa = (Params * n)(*self.params)
+        sd = None
+        if seeds is not None:
+            sd = (C.c_uint64 * n)(*[int(s) & 0xFFFFFFFFFFFFFFFF for s in seeds])
+        st = C.c_int(0)
+        self._b = L.fs_batch_create(n, w, h, pa, int(init), sd, C.byref(st))
+        if not self._b:
+            raise FastScapeError(st.value, last_error())
+
+    def close(self):
+        if getattr(self, "_b", None):
+            library().fs_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def size(self, r: int) -> int:
+        return self.widths[r] * self.heights[r]
+
+    def cells(self) -> int:
+        n, c = C.c_int(0), C.c_int64(0)
+        check(library().fs_batch_info(self._b, C.byref(n), C.byref(c)))
+        return c.value
+
+    def step(self, k: int = 1) -> None:
+        check(library().fs_batch_step(self._b, int(k)))
+
+    def run(self, nstep: int) -> None:
+        check(library().fs_batch_run(self._b, int(nstep)))
+
+    def getH(self, r: int) -> np.ndarray:
+        out = np.empty(self.size(r), np.float64)
+        check(library().fs_batch_get_elevation(self._b, int(r), _p(out, C.c_double)))
+        return out
+
+    def setH(self, r: int, h) -> None:
+        h = np.ascontiguousarray(h, np.float64).reshape(-1)
+        if h.size != self.size(r):
+            raise ValueError(f"expected {self.size(r)} elevations, got {h.size}")
+        check(library().fs_batch_set_elevation(self._b, int(r), _p(h, C.c_double)))
+
+    def accumulation(self, r: int) -> np.ndarray:
+        out = np.empty(self.size(r), np.float64)
+        check(library().fs_batch_get_accumulation(self._b, int(r), _p(out, C.c_double)))
+        return out
+
+    def receivers(self, r: int) -> np.ndarray:
+        out = np.empty(self.size(r), np.int32)
+        check(library().fs_batch_get_receivers(self._b, int(r), _p(out, C.c_int32)))
+        return out
+
+    def levels(self, r: int):
+        out = np.empty(self.size(r), np.int32)
+        n = C.c_int32(0)
+        check(library().fs_batch_get_levels(self._b, int(r), _p(out, C.c_int32), C.byref(n)))
+        return out, n.value
+
+    def set_timing(self, on: bool = True) -> None:
+        check(library().fs_batch_set_timing(self._b, int(bool(on))))
+
+    def phase_times(self, reset: bool = False):
+        out = np.zeros(len(FastScape_RBP.TIMERS), np.float64)
+        check(library().fs_batch_get_phase_times(self._b, _p(out, C.c_double), int(reset)))
+        return out
+
+    def use_graph(self, on: bool = True) -> None:
+        check(library().fs_batch_use_graph(self._b, int(bool(on))))
+
+    def autotune(self, probe_steps: int = 2):
+        out = (C.c_int * 2)()
+        check(library().fs_batch_autotune(self._b, int(probe_steps), out))
+        return {"walk_blocks_per_sm": out[0], "graph": bool(out[1])}
+
+    def synchronize(self) -> None:
+        check(library().fs_batch_synchronize(self._b))
+
+    @property
+    def handle(self):
+        return self._b
 
 
 def version() -> str:

@@ -1,32 +1,76 @@
-// fs_internal.h -- shared between the host model (fs_model.cu) and the
-// kernels (fs_kernels.cu). Not part of the public ABI.
+// fs_internal.h -- shared between the host side (fs_model.cu, fs_noalloc.cu)
+// and the kernels (fs_kernels.cu). Not part of the public ABI.
+//
+// Every timestep runs over a batch of realizations (a single model is a
+// batch of one). Realization r owns the cells [off_r, off_r + size_r) of
+// every per-cell and per-position array and the level-table entries
+// [lvl_base_r, lvl_base_r + size_r + 2); cell indices stored in `ent` are
+// local to the realization (c = y*W_r + x).
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace fs {
 
-// Per-model device control block. `err` holds the first error status of the
-// current fs_step call; the remaining words are reset before every timestep.
+// Batch-wide control block. `err` holds the first error status of the
+// current fs_step call; the words from `bar` on are reset before every
+// timestep.
 struct Ctl {
   int err;                 // FS_OK or first FS_ERR_* seen by any kernel
   int err_detail;          // phase code where err was raised
-  int abort_k;             // > 0: a drainage count >= the table capacity was
-                           // met; the timestep stopped before touching h
+  int abort_k;             // > 0: a drainage count >= its realization's table
+                           // capacity was met; the timestep stopped before
+                           // touching h
   int steps_done;          // timesteps completed in the current fs_step call
-  int nlevels;             // levels found by the last walk
-  int total;               // cells placed in the ordering by the last walk
+  int abort_r;             // realization that raised abort_k
+  int pad0[3];
   unsigned long long walk_ns[3];  // accumulated walk time: ordering,
                                   // accumulation, erosion (block 0's clock)
-  // --- reset before every timestep (from `top` on) ---
-  int top;                 // pits appended to level 0 (after the rings)
+  // --- reset before every timestep (from `bar` on) ---
   unsigned int bar;        // grid-barrier arrival counter
-  int lvlcnt[3];           // rotating per-level append counters (relative)
   int amb;                 // cells queued by the receiver filter
+  int pad1[2];
+};
+constexpr size_t kCtlResetOffset = offsetof(Ctl, bar);
+constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
+constexpr size_t kCtlCallResetBytes = 5 * sizeof(int);  // err .. abort_r
+
+// Per-realization counters written by the kernels; `top` and `lvlcnt` are
+// reset before every timestep.
+struct RealCtl {
+  int top;                 // pits appended to level 0 (after the rings)
+  int lvlcnt[3];           // rotating per-level append counters
+  int nlevels;             // levels found by the last walk
+  int total;               // cells placed in the ordering by the last walk
   int pad[2];
 };
-constexpr size_t kCtlCallResetBytes = 4 * sizeof(int);  // err .. steps_done
+constexpr size_t kRealCtlResetBytes = 4 * sizeof(int);  // top, lvlcnt
+
+// Read-only description of one realization.
+struct RealDesc {
+  int W, H, size;
+  int off;                 // first cell / position of the realization
+  int lvl_base;            // first entry of its level table
+  int nring;               // ring cells, pre-placed at ent[off, off+nring)
+  double u_dt;             // ueq*dt
+  double tol;
+  long long tol_bits;      // bits of tol (magnitude compares as integers)
+  float tol_lo_f;          // an FP32 value <= tol*(1-2^-20)
+  float g_orth, g_diag, gmax;  // FP32 1/dr for the receiver filter
+  double dr_orth, dr_diag;
+  const double *tab;       // erosion table, kTabStride doubles per count
+  int tab_cap;             // counts k < tab_cap are in the table
+  int pad;
+};
+
+// A 2-D tile of one realization for the stencil kernels.
+struct Tile {
+  int r;                   // realization
+  int x0, y0;              // grid coordinates of the tile's first cell
+  int pad;
+};
 
 // Receiver code of an interior cell without a lower neighbour. The ABI
 // reports it as FS_NO_FLOW (-1), like the rings; internally it marks the
@@ -39,8 +83,10 @@ constexpr int kPit = -2;
 //   D = 1 + F          (the n = 1 Newton denominator, fastscape_RB.cpp:322)
 //   R = RN(1/D)        (reciprocal for the correctly rounded division)
 constexpr int kTabStride = 8;
-constexpr size_t kCtlResetOffset = offsetof(Ctl, top);
-constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
+
+// Tiles: receivers over the interior [2, W-3]^2, donors over [1, W-2]^2.
+constexpr int kRxTile = 32, kRyTile = 32;
+constexpr int kDxTile = 32, kDyTile = 64;
 
 // Where an error was detected (Ctl::err_detail).
 enum ErrPhase : int {
@@ -58,65 +104,73 @@ enum NMode : int {
   kNTwo = 2,      // pow(x,2) = x*x, pow(x,1) = x
 };
 
-struct StepGeom {
-  int W, H;
-  int size;  // W*H (< 2^31)
-};
-
 // Arrays indexed by position i in the level order (the reference's stack):
-//   ent[i]   cell index; level 0 starts with the two rings (fixed) followed
-//            by the pits of this timestep
+//   ent[i]   cell index (local); level 0 starts with the two rings (fixed)
+//            followed by the pits of this timestep
 //   pdir[i]  receiver direction of ent[i] (0..7), bit 3 set when that
 //            receiver is a pit (levels >= 1 only)
 //   nd[i]    number of donors of ent[i]
-//   kid[i]   position of its first donor; its donors are contiguous
+//   kid[i]   position of its first donor (local); its donors are contiguous
 //   acc[i]   drainage cell count of ent[i]
-struct WalkArgs {
+struct StepArgs {
   double *h;
-  const uint8_t *mask;
+  int8_t *rec;
+  uint8_t *mask;
   int32_t *ent;
   uint8_t *pdir;
   uint8_t *nd;
   int32_t *kid;
   uint32_t *acc;
-  int32_t *lvl_off;        // size+2 entries
-  const double *tab;       // erosion table, kTabStride doubles per count
-  int tab_cap;             // counts k < tab_cap are in the table
+  int32_t *amb;            // queued cells (global index) of the filter
+  int32_t *amb_r;          // and their realization
+  int32_t *lvl_off;        // per realization: size+2 local level offsets
+  const RealDesc *desc;
+  RealCtl *rctl;
   Ctl *ctl;
-  int W, size;
-  int nring;               // ring cells, pre-placed at ent[0, nring)
-  double u_dt, neq, tol;
-  long long tol_bits;      // bits of tol (magnitude compares as integers)
-  float tol_lo_f;          // an FP32 value <= tol*(1-2^-20)
+  int nreal;
+  const Tile *rtiles;
+  int nrtiles;
+  const Tile *dtiles;
+  int ndtiles;
   int nmode;
+  double neq;
   int do_erode;            // 0: ordering + accumulation only
   int stamp;               // 1: accumulate phase times into ctl->walk_ns
   unsigned long long timeout_ns;
 };
 
-// An FP32 number not above tol*(1 - 2^-20), for the one-iterate test.
-float tol_lower_float(double tol);
+// Largest batch one walk launch handles.
+constexpr int kMaxReal = 4096;
+// Shared memory the walk kernel needs for `nreal` realizations.
+size_t walk_smem_bytes(int nreal);
 
 // Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
-cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
-                             double dr_orth, double dr_diag, cudaStream_t s);
-cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
-                                  Ctl *ctl, StepGeom g, double dr_orth,
-                                  double dr_diag, cudaStream_t s);
-cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *ent, Ctl *ctl, StepGeom g, int nring,
-                                 cudaStream_t s);
-cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s);
+cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s);
+cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
+cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s);
 int walk_threads();
 const void *walk_kernel_ptr(int nmode);
-cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
-                                cudaStream_t s);
-cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,
-                                cudaStream_t s);
+cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
+cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s);
+cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s);
+cudaError_t launch_place_rings(int32_t *ent, int W, int H, cudaStream_t s);
+cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns,
+                             cudaStream_t s);
+
+// Host helpers shared by the entry points.
+float tol_lower_float(double tol);
+int ring_cells(int W, int H);
+// Appends the receiver (kind 0) or donor (kind 1) tiles of realization r to
+// out (capacity cap); returns the number appended, or -1 if out is full.
+int append_tiles(int kind, int r, int W, int H, Tile *out, int cap);
+// Erosion-table records for counts [k0, k1) into rec (kTabStride doubles
+// each), single-threaded.
+void fill_table_range(double keq, double neq, double meq, double dt, double dr_orth,
+                      double dr_diag, double cell_area, long long k0, long long k1,
+                      double *rec);
+
 // Stores `msg` as this thread's fs_last_error() text; returns status.
 int record_error(int status, const char *msg);
-
-cudaError_t launch_test_wait(Ctl *ctl, int blocks,
-                             unsigned long long timeout_ns, cudaStream_t s);
 
 }  // namespace fs

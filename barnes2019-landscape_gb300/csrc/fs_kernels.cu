@@ -1,6 +1,7 @@
-// fs_kernels.cu -- sm_103a kernels of the FastScape timestep.
+// fs_kernels.cu -- sm_103a kernels of the FastScape timestep, over a batch
+// of realizations (a single model is a batch of one).
 //
-// One timestep = four launches on the model's stream:
+// One timestep = four launches on the stream:
 //   1. k_receivers_filter  D8 steepest descent over the interior
 //      + k_receivers_fixup (fastscape_RB.cpp:160-182): FP32 proof of the
 //                          receiver, FP64 reference formula for the cells
@@ -12,13 +13,16 @@
 //                          the levels (:262-279), uplift (:285-296) and the
 //                          implicit erosion solved upward from base level
 //                          (:306-328, in the level order of
-//                          fastscape_RB+P.cpp:319-350).
+//                          fastscape_RB+P.cpp:319-350). All realizations
+//                          walk their levels in lock step, so one grid
+//                          barrier per level serves the whole batch.
 //
 // Floating point follows the reference's operation order exactly; the whole
 // file is compiled with -fmad=false so no multiply-add is contracted, and
 // every FP64 division is correctly rounded.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "fastscape_gb300.h"
@@ -30,8 +34,10 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
-constexpr int kPer = 8;  // frontier cells per thread per expansion chunk
+constexpr int kPer = 8;   // entries per thread per expansion chunk
+constexpr int kChunk = kPer * kWalkThreads;
 constexpr int kAccU = 4;  // 32-entry groups per warp per accumulation pass
+constexpr int kEroU = 2;  // 32-entry groups per warp per erosion pass
 constexpr int kNewtonMaxIt = 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -54,13 +60,16 @@ __device__ __forceinline__ void raise_err(Ctl *ctl, int code, int phase) {
   if (atomicCAS(&ctl->err, 0, code) == 0) ctl->err_detail = phase;
 }
 
+__device__ __forceinline__ bool stopped(const Ctl *ctl) {
+  return (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) != 0;
+}
+
 // Grid-wide barrier for a cooperative launch. Arrival counter only grows
 // during a launch (reset by the host before it), so barrier number `epoch`
 // completes when bar reaches epoch*gridDim.x. Every wait is bounded by
 // `timeout_ns` of wall time; on timeout, or when another block has already
 // raised an error, it returns false and the caller leaves the kernel.
-__device__ bool grid_barrier(Ctl *ctl, unsigned &epoch,
-                             unsigned long long timeout_ns) {
+__device__ bool grid_barrier(Ctl *ctl, unsigned &epoch, unsigned long long timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -87,56 +96,126 @@ __device__ bool grid_barrier(Ctl *ctl, unsigned &epoch,
   return s_ok != 0;
 }
 
-__device__ __forceinline__ void nshift8(int W, int o[8]) {
-  o[0] = -1; o[1] = -W - 1; o[2] = -W; o[3] = -W + 1;
-  o[4] = 1;  o[5] = W + 1;  o[6] = W;  o[7] = W - 1;
-}
-
 // nshift[k] (fastscape_RB.cpp:137) for a run-time k without a local array:
-// dx+1 and dy+1 of the 8 directions packed two bits per direction.
+// dx+1 and dy+1 of the 8 directions packed two bits per direction
+// (W, NW, N, NE, E, SE, S, SW).
 __device__ __forceinline__ int nbr_off(int k, int W) {
   const int dx = ((0x1A90 >> (2 * k)) & 3) - 1;
   const int dy = ((0xA901 >> (2 * k)) & 3) - 1;
   return dy * W + dx;
 }
 
+// Exclusive block scan of one int per thread; t is the thread's linear index
+// in the block and nthreads the block size (a multiple of 32, at most 1024).
+// Returns the prefix and the block total.
+__device__ __forceinline__ int block_excl_scan(int v, int &total, int t, int nthreads) {
+  __shared__ int s_w[32];
+  const int lane = t & 31, wid = t >> 5;
+  const int nw = nthreads >> 5;
+  int incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int x = __shfl_up_sync(kFull, incl, d);
+    if (lane >= d) incl += x;
+  }
+  if (lane == 31) s_w[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < nw ? s_w[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int x = __shfl_up_sync(kFull, w, d);
+      if (lane >= d) w += x;
+    }
+    if (lane < nw) s_w[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  total = s_w[nw - 1];
+  const int before = wid ? s_w[wid - 1] : 0;
+  __syncthreads();  // s_w may be reused by the caller's next scan
+  return before + incl - v;
+}
+
+// Exclusive prefix over realizations of count(r) into s_pre[0..n]; the walk
+// kernel's block-wide view of how a level's work splits across the batch.
+template <class F>
+__device__ __forceinline__ int block_prefix(int n, F count, int *s_pre) {
+  const int per = (n + kWalkThreads - 1) / kWalkThreads;
+  const int r0 = threadIdx.x * per;
+  int sum = 0;
+  for (int r = r0; r < r0 + per && r < n; r++) sum += count(r);
+  int total;
+  int run = block_excl_scan(sum, total, threadIdx.x, kWalkThreads);
+  for (int r = r0; r < r0 + per && r < n; r++) {
+    s_pre[r] = run;
+    run += count(r);
+  }
+  if (threadIdx.x == 0) s_pre[n] = total;
+  __syncthreads();
+  return total;
+}
+
+// Realization of global work item g: the r with s_pre[r] <= g < s_pre[r+1]
+// (g < s_pre[n]); empty realizations are skipped because the largest such
+// r is taken.
+__device__ __forceinline__ int find_real(const int *s_pre, int n, int g) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (s_pre[mid] <= g) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ long long abs_bits(double x) {
+  return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
+}
+
 // ---------------------------------------------------------------------------
 // 1. Receivers: fastscape_RB.cpp:160-182. slope = (h[c]-h[n])/dr[n], strict
 // '>' against a running maximum that starts at 0, so the first maximum in
 // neighbour order wins and a cell with no strictly lower neighbour keeps
-// NO_FLOW.
+// NO_FLOW. k_receivers_exact is that formula verbatim in FP64 (kept to test
+// the fast path against); k_receivers_filter + k_receivers_fixup is the fast
+// path.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
-            int H, double dr_orth, double dr_diag, const Ctl *ctl) {
-  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x + 2;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y + 2;
-  if (x >= W - 2 || y >= H - 2) return;
-  const long long c = (long long)y * W + x;
-  int o[8];
-  nshift8(W, o);
+__device__ __forceinline__ int receiver_fp64(const double *h, int c, int W, double dr_orth,
+                                             double dr_diag) {
   const double hc = h[c];
   double max_slope = 0;
   int max_n = FS_NO_FLOW;
 #pragma unroll
   for (int n = 0; n < 8; n++) {
-    const double slope = (hc - h[c + o[n]]) / ((n & 1) ? dr_diag : dr_orth);
+    const double slope = (hc - h[c + nbr_off(n, W)]) / ((n & 1) ? dr_diag : dr_orth);
     if (slope > max_slope) {
       max_slope = slope;
       max_n = n;
     }
   }
-  rec[c] = (int8_t)(max_n == FS_NO_FLOW ? kPit : max_n);
+  return max_n == FS_NO_FLOW ? kPit : max_n;
 }
 
-// ---------------------------------------------------------------------------
-// 1b. Receivers, fast path. GB300 runs FP64 at ~1.6 lanes/clock/SM against
-// ~113 for FP32, so the eight FP64 divides per cell of the reference formula
-// would dominate the timestep. This kernel decides the receiver from FP32
-// approximations with a rigorous error bound and hands the rare cells it
-// cannot prove to k_receivers_fixup, which evaluates the reference formula in
-// FP64. The result is identical to k_receivers for every input.
+__global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
+  if (stopped(a.ctl)) return;
+  const Tile t = a.rtiles[blockIdx.x];
+  const RealDesc &d = a.desc[t.r];
+  const double *h = a.h + d.off;
+  int8_t *rec = a.rec + d.off;
+  const int x = t.x0 + threadIdx.x;
+#pragma unroll 1
+  for (int y = t.y0 + threadIdx.y; y < t.y0 + kRyTile; y += 8) {
+    if (x < d.W - 2 && y < d.H - 2) {
+      const int c = y * d.W + x;
+      rec[c] = (int8_t)receiver_fp64(h, c, d.W, d.dr_orth, d.dr_diag);
+    }
+  }
+}
+
+// GB300 runs FP64 at ~1.6 lanes/clock/SM against ~113 for FP32, so the eight
+// FP64 divides per cell of the reference formula would dominate the
+// timestep. The filter decides the receiver from FP32 approximations with a
+// rigorous error bound and queues the rare cells it cannot prove for the
+// FP64 formula. The result is identical to k_receivers_exact for every input.
 //
 // Bound: f = h truncated to FP32 (|f-h| <= 2^-23|h| + 2^-126),
 // a_n = fl(fl(f_c - f_n) * g_n) with g_n = fl(1/dr_n); then for the exact
@@ -146,14 +225,10 @@ k_receivers(const double *__restrict__ h, int8_t *__restrict__ rec, int W,
 //   best - second > 2E  and best > E  => q_best is the unique maximum > 0;
 //   best < -E                         => every q_n < 0 (NO_FLOW);
 // otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
-// ---------------------------------------------------------------------------
-constexpr int kRxTile = 32;  // interior cells per tile in x
-constexpr int kRyTile = 32;  // interior cells per tile in y
 
 // Truncation of a double to FP32 with integer operations only (no FP64
 // pipe): rebias the exponent, keep the top 23 fraction bits. Values below
-// 2^-126 flush to signed zero; |x| >= 2^128, Inf and NaN give NaN, which
-// sends the cell to the exact path.
+// 2^-126 flush to signed zero; |x| >= 2^128, Inf and NaN give NaN.
 __device__ __forceinline__ float trunc_to_float(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32);
@@ -165,24 +240,24 @@ __device__ __forceinline__ float trunc_to_float(double x) {
   return __uint_as_float(sign | ((unsigned)e << 23) | frac);
 }
 
-__global__ void __launch_bounds__(256)
-k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
-                   int32_t *__restrict__ amb, Ctl *ctl, int W, int H,
-                   float g_orth, float g_diag, float gmax) {
-  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
+__global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
+  if (stopped(a.ctl)) return;
   __shared__ float s[kRyTile + 2][kRxTile + 3];
-  const int x0 = blockIdx.x * kRxTile + 1;  // grid x of s[.][0]
-  const int y0 = blockIdx.y * kRyTile + 1;  // grid y of s[0][.]
-  const int t = threadIdx.y * 32 + threadIdx.x;
-  for (int idx = t; idx < (kRyTile + 2) * (kRxTile + 2); idx += 256) {
-    const int ly = idx / (kRxTile + 2);
-    const int lx = idx - ly * (kRxTile + 2);
-    const int gx = x0 + lx, gy = y0 + ly;
-    float v = 0.f;
-    if (gx < W && gy < H) v = trunc_to_float(h[(size_t)gy * W + gx]);
-    s[ly][lx] = v;
+  const Tile t = a.rtiles[blockIdx.x];
+  const RealDesc &d = a.desc[t.r];
+  const int W = d.W, H = d.H;
+  const double *h = a.h + d.off;
+  int8_t *rec = a.rec + d.off;
+  const int x0 = t.x0 - 1, y0 = t.y0 - 1;  // grid coordinates of s[0][0]
+  for (int ly = threadIdx.y; ly < kRyTile + 2; ly += 8) {
+    const int gy = y0 + ly;
+    for (int lx = threadIdx.x; lx < kRxTile + 2; lx += 32) {
+      const int gx = x0 + lx;
+      s[ly][lx] = (gx < W && gy < H) ? trunc_to_float(h[gy * W + gx]) : 0.f;
+    }
   }
   __syncthreads();
+  const float g_orth = d.g_orth, g_diag = d.g_diag, gmax = d.gmax;
   const int lane = threadIdx.x;
   const int lx = threadIdx.x + 1;
   const int gx = x0 + lx;
@@ -203,15 +278,15 @@ k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
       bool bad = !(fc == fc);
 #pragma unroll
       for (int n = 0; n < 8; n++) {
-        const float a = (fc - f[n]) * ((n & 1) ? g_diag : g_orth);
+        const float av = (fc - f[n]) * ((n & 1) ? g_diag : g_orth);
         M = fmaxf(M, fabsf(f[n]));
-        bad |= !(a == a);
-        if (a > best) {
+        bad |= !(av == av);
+        if (av > best) {
           second = best;
-          best = a;
+          best = av;
           bn = n;
-        } else if (a > second) {
-          second = a;
+        } else if (av > second) {
+          second = av;
         }
       }
       const float E = 0x1p-19f * gmax * (M + 0x1p-100f);
@@ -226,39 +301,30 @@ k_receivers_filter(const double *__restrict__ h, int8_t *__restrict__ rec,
           queue = false;
         }
       }
-      if (!queue) rec[(size_t)gy * W + gx] = (int8_t)code;
+      if (!queue) rec[gy * W + gx] = (int8_t)code;
     }
     const unsigned bq = __ballot_sync(kFull, queue);
     if (bq) {
       int base = 0;
-      if (lane == 0) base = atomicAdd(&ctl->amb, __popc(bq));
+      if (lane == 0) base = atomicAdd(&a.ctl->amb, __popc(bq));
       base = __shfl_sync(kFull, base, 0);
-      if (queue) amb[base + __popc(bq & ((1u << lane) - 1u))] = gy * W + gx;
+      if (queue) {
+        const int q = base + __popc(bq & ((1u << lane) - 1u));
+        a.amb[q] = d.off + gy * W + gx;
+        a.amb_r[q] = t.r;
+      }
     }
   }
 }
 
 // The queued cells of k_receivers_filter, with the reference formula in FP64.
-__global__ void __launch_bounds__(256)
-k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
-                  const int32_t *__restrict__ amb, const Ctl *ctl, int W,
-                  double dr_orth, double dr_diag) {
-  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
-  const int n_amb = ld_volatile_i32(&ctl->amb);
+__global__ void __launch_bounds__(256) k_receivers_fixup(StepArgs a) {
+  if (stopped(a.ctl)) return;
+  const int n_amb = ld_volatile_i32(&a.ctl->amb);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_amb; i += gridDim.x * blockDim.x) {
-    const int c = amb[i];
-    const double hc = h[c];
-    double max_slope = 0;
-    int max_n = FS_NO_FLOW;
-#pragma unroll
-    for (int n = 0; n < 8; n++) {
-      const double slope = (hc - h[c + nbr_off(n, W)]) / ((n & 1) ? dr_diag : dr_orth);
-      if (slope > max_slope) {
-        max_slope = slope;
-        max_n = n;
-      }
-    }
-    rec[c] = (int8_t)(max_n == FS_NO_FLOW ? kPit : max_n);
+    const RealDesc &d = a.desc[a.amb_r[i]];
+    const int c = a.amb[i] - d.off;
+    a.rec[d.off + c] = (int8_t)receiver_fp64(a.h + d.off, c, d.W, d.dr_orth, d.dr_diag);
   }
 }
 
@@ -267,67 +333,34 @@ k_receivers_fixup(const double *__restrict__ h, int8_t *__restrict__ rec,
 // Bit k of mask[c] is set when neighbour c+nshift[k] has receiver code
 // (k+4)%8, i.e. drains into c (the pull form of fastscape_RB+GPU.cpp:155-182).
 // Level 0 = every cell without a receiver (fastscape_RB.cpp:221-227): the
-// two outer rings, which never change and sit at stack[0, nring) from model
-// creation on, and the interior pits, appended here with one atomic per
-// 32x64 tile (block scan of the per-thread pit counts).
+// two outer rings, which never change and sit at ent[0, nring) of their
+// realization from creation on, and the interior pits, appended here with
+// one atomic per 32x64 tile.
 // ---------------------------------------------------------------------------
-constexpr int kDxTile = 32;  // tile of cells over [1, W-2] x [1, H-2]
-constexpr int kDyTile = 64;
-constexpr int kDRows = kDyTile / 8;
-
-// Exclusive block scan of one int per thread; t is the thread's linear index
-// in the block and nthreads the block size (a multiple of 32, at most 1024).
-// Returns the prefix and the block total.
-__device__ __forceinline__ int block_excl_scan(int v, int &total, int t, int nthreads) {
-  __shared__ int s_w[32];
-  const int lane = t & 31, wid = t >> 5;
-  const int nw = nthreads >> 5;
-  int incl = v;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int t = __shfl_up_sync(kFull, incl, d);
-    if (lane >= d) incl += t;
-  }
-  if (lane == 31) s_w[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    int w = lane < nw ? s_w[lane] : 0;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int t = __shfl_up_sync(kFull, w, d);
-      if (lane >= d) w += t;
-    }
-    if (lane < nw) s_w[lane] = w;  // inclusive warp prefix
-  }
-  __syncthreads();
-  total = s_w[nw - 1];
-  const int before = wid ? s_w[wid - 1] : 0;
-  __syncthreads();  // s_w may be reused by the caller's next scan
-  return before + incl - v;
-}
-
-__global__ void __launch_bounds__(256)
-k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
-                int32_t *__restrict__ ent, Ctl *ctl, int W, int H, int nring) {
-  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
+__global__ void __launch_bounds__(256) k_donors_level0(StepArgs a) {
+  if (stopped(a.ctl)) return;
   __shared__ int8_t sr[kDyTile + 2][kDxTile + 4];
   __shared__ int s_base;
-  const int x0 = blockIdx.x * kDxTile;  // grid x of sr[.][0]
-  const int y0 = blockIdx.y * kDyTile;  // grid y of sr[0][.]
-  const int t = threadIdx.y * 32 + threadIdx.x;
+  const Tile t = a.dtiles[blockIdx.x];
+  const RealDesc &d = a.desc[t.r];
+  const int W = d.W, H = d.H;
+  const int8_t *rec = a.rec + d.off;
+  const int x0 = t.x0 - 1, y0 = t.y0 - 1;  // grid coordinates of sr[0][0]
+  const int tt = threadIdx.y * 32 + threadIdx.x;
   for (int ly = threadIdx.y; ly < kDyTile + 2; ly += 8) {
     const int gy = y0 + ly;
     for (int lx = threadIdx.x; lx < kDxTile + 2; lx += 32) {
       const int gx = x0 + lx;
-      sr[ly][lx] = (gx < W && gy < H) ? rec[(size_t)gy * W + gx] : (int8_t)FS_NO_FLOW;
+      sr[ly][lx] = (gx < W && gy < H) ? rec[gy * W + gx] : (int8_t)FS_NO_FLOW;
     }
   }
   __syncthreads();
   const int lx = threadIdx.x + 1;
   const int gx = x0 + lx;
+  constexpr int kRows = kDyTile / 8;
   unsigned pit_bits = 0;
 #pragma unroll
-  for (int r = 0; r < kDRows; r++) {
+  for (int r = 0; r < kRows; r++) {
     const int ly = threadIdx.y + 8 * r + 1;
     const int gy = y0 + ly;
     if (gx <= W - 2 && gy <= H - 2) {
@@ -340,24 +373,24 @@ k_donors_level0(const int8_t *__restrict__ rec, uint8_t *__restrict__ mask,
       m |= (sr[ly + 1][lx + 1] == 1) ? 32u : 0u;    // SE drains NW
       m |= (sr[ly + 1][lx] == 2) ? 64u : 0u;        // S  drains N
       m |= (sr[ly + 1][lx - 1] == 3) ? 128u : 0u;   // SW drains NE
-      mask[(size_t)gy * W + gx] = (uint8_t)m;
+      a.mask[d.off + gy * W + gx] = (uint8_t)m;
       if (sr[ly][lx] == kPit) pit_bits |= 1u << r;
     }
   }
   int total;
-  const int excl = block_excl_scan(__popc(pit_bits), total, t, 256);
+  const int excl = block_excl_scan(__popc(pit_bits), total, tt, 256);
   if (total == 0) return;
-  if (t == 0) s_base = nring + atomicAdd(&ctl->top, total);
+  if (tt == 0) s_base = d.off + d.nring + atomicAdd(&a.rctl[t.r].top, total);
   __syncthreads();
   int pos = s_base + excl;
 #pragma unroll
-  for (int r = 0; r < kDRows; r++)
-    if (pit_bits >> r & 1u) ent[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
+  for (int r = 0; r < kRows; r++)
+    if (pit_bits >> r & 1u) a.ent[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
 }
 
-__device__ __forceinline__ long long abs_bits(double x) {
-  return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
-}
+// ---------------------------------------------------------------------------
+// 3. Erosion of one cell and the division it needs.
+// ---------------------------------------------------------------------------
 
 // Correctly rounded num/D for D > 0 given R = RN(1/D), without the FP64
 // divide routine: Markstein's correction q1 = q0 + (num - q0*D)*R with
@@ -401,8 +434,8 @@ __device__ __forceinline__ void powers(double x, double neq, double &pn, double 
 // elevation, hn the receiver's final elevation and T the table record of the
 // cell's drainage count and direction class (T[0] = fact).
 template <int NMODE>
-__device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
-                                             double h0, double hn) {
+__device__ __forceinline__ double erode_cell(const RealDesc &d, double neq, Ctl *ctl,
+                                             const double *T, double h0, double hn) {
   const double fact = T[0];
   double hnew, hp, diff;
   int it;
@@ -414,25 +447,25 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
     const double q = div_rn(num, D, R);
     hnew = h0 - q;
     // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
-    // |RN(hnew-h0)| <= |q| + 2^-51(|h0|+|q|), an FP32 test on truncated
-    // magnitudes with 2^-21 of slack proves it for almost every cell without
-    // spending the FP64 subtraction (see the bound in fs_kernels.cu's
-    // header); the rest evaluate diff exactly and follow the reference loop.
+    // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
+    // truncated magnitudes (each within 2^-23 relative, flushed below
+    // 2^-126) with 2^-21 of slack proves it for almost every cell without
+    // the FP64 subtraction; the rest evaluate diff and follow the loop.
     const float qf = fabsf(trunc_to_float(q));
     const float hf = fabsf(trunc_to_float(h0));
-    if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= a.tol_lo_f) return hnew;
+    if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= d.tol_lo_f) return hnew;
     diff = hnew - h0;
     hp = hnew;
     it = 1;
     // fabs(diff) > tol as an integer compare of the magnitudes' bits (both
     // non-negative; a NaN diff stops the loop, as fabs(NaN) > tol is false)
-    while (abs_bits(diff) > a.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
+    while (abs_bits(diff) > d.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
       const double num2 = (hnew - h0) + fact * (hnew - hn);
       hnew -= div_rn(num2, D, R);
       diff = hnew - hp;
       hp = hnew;
       if (++it >= kNewtonMaxIt) {
-        raise_err(a.ctl, FS_ERR_NEWTON, kPhaseErode);
+        raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
         break;
       }
     }
@@ -440,52 +473,48 @@ __device__ __forceinline__ double erode_cell(const WalkArgs &a, const double *T,
   }
   hnew = h0;
   hp = h0;
-  diff = 2 * a.tol;
+  diff = 2 * d.tol;
   it = 0;
-  while (fabs(diff) > a.tol) {
+  while (fabs(diff) > d.tol) {
     double pn, pn1;
-    powers<NMODE>(hnew - hn, a.neq, pn, pn1);
-    hnew -= (hnew - h0 + fact * pn) / (1. + fact * a.neq * pn1);
+    powers<NMODE>(hnew - hn, neq, pn, pn1);
+    hnew -= (hnew - h0 + fact * pn) / (1. + fact * neq * pn1);
     diff = hnew - hp;
     hp = hnew;
     if (++it >= kNewtonMaxIt) {
-      raise_err(a.ctl, FS_ERR_NEWTON, kPhaseErode);
+      raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
       break;
     }
   }
   return hnew;
 }
 
-// Uplift of the interior level-0 cells (pits), fastscape_RB.cpp:291-295.
-__device__ __forceinline__ void uplift_pits(const WalkArgs &a, int lvl0_end, int tid,
-                                            int nthreads) {
-  for (int i = a.nring + tid; i < lvl0_end; i += nthreads) {
-    const int c = __ldcg(&a.ent[i]);
-    a.h[c] = __ldcg(&a.h[c]) + a.u_dt;
-  }
-}
-
 // ---------------------------------------------------------------------------
-// 3. Persistent level walker (cooperative launch, one grid barrier per level
-// per sweep).
+// 4. Persistent level walker (cooperative launch).
 //
 // The ordering is kept as arrays indexed by position in the level order
-// ("stack" in the reference): ent[i] the cell, pdir[i] its receiver
-// direction (bit 3: the receiver is a pit), nd[i] and kid[i] the number of
-// donors and the position of the first one in the next level (the donors of
-// one entry are contiguous), acc[i] the drainage count. Accumulation and
-// erosion then read these by position -- coalesced -- instead of gathering
-// receivers, masks and counts by cell index.
+// (fs_internal.h): accumulation and erosion read them by position --
+// coalesced -- instead of gathering receivers, masks and counts by cell.
+// Per level, every block keeps each realization's range [lo, hi) in shared
+// memory and maps global work items (expansion chunks, 32-entry groups) to
+// realizations through a prefix over the batch.
 // ---------------------------------------------------------------------------
 template <int NMODE>
-__global__ void __launch_bounds__(kWalkThreads)
-k_walk(WalkArgs a) {
+__global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
+  extern __shared__ int smem[];
+  const int nreal = a.nreal;
+  int *s_lo = smem;               // per realization: current range start
+  int *s_hi = s_lo + nreal;       // and end (local positions)
+  int *s_nlev = s_hi + nreal;     // levels found so far
+  int *s_pre = s_nlev + nreal;    // prefix over the batch, nreal+1
+  __shared__ int s_base;
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
-  if (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) return;
+  if (stopped(ctl)) return;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthreads = gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warp_global = tid >> 5, nwarps = nthreads >> 5;
   const bool stamp = a.stamp && tid == 0;
   unsigned long long t_prev = stamp ? globaltimer_ns() : 0;
   auto lap = [&](int slot) {
@@ -497,35 +526,41 @@ k_walk(WalkArgs a) {
   };
 
   // ---- ordering: fastscape_RB.cpp:229-251 -------------------------------
-  // Level k+1 = the donors of level k. Each block expands chunks of
-  // kPer*blockDim.x consecutive frontier entries (kPer consecutive per
-  // thread, so the next level keeps the frontier's spatial order) with one
-  // block scan and one atomic per chunk. The append counter rotates over
-  // three words so a block that reads the size of level k after the barrier
-  // never races with the reset for level k+2.
-  int lo = 0;
-  int hi = a.nring + ld_volatile_i32(&ctl->top);
-  const int lvl0_end = hi;
-  if (tid == 0) {
-    a.lvl_off[0] = 0;
-    a.lvl_off[1] = hi;
+  // Level k+1 = the donors of level k. A block expands a chunk of kChunk
+  // consecutive entries of one realization; warp w covers 32*kPer of them
+  // in kPer coalesced passes (entry wbase+32q+lane). Warp scans give each
+  // entry's first-donor offset in entry order, one block scan over the
+  // warps and one atomic place the chunk, and the donors are written
+  // cooperatively (lane r writes the r-th donor of the pass), so the next
+  // level keeps this level's order. Each realization's append counter
+  // rotates over three words so a block that reads the size of level k after
+  // the barrier never races with the reset for level k+2.
+  for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+    const RealDesc &d = a.desc[r];
+    s_lo[r] = 0;
+    s_hi[r] = d.nring + ld_volatile_i32(&a.rctl[r].top);
+    s_nlev[r] = 1;
+    if (blockIdx.x == 0) {
+      a.lvl_off[d.lvl_base + 0] = 0;
+      a.lvl_off[d.lvl_base + 1] = s_hi[r];
+    }
   }
-  int nlev = 1;
-  __shared__ int s_base;
+  __syncthreads();
+  int L = 0;  // level being expanded
   for (;;) {
-    const int j = (nlev - 1) % 3;  // counter of this expansion
-    if (tid == 0) ctl->lvlcnt[nlev % 3] = 0;  // counter of the next one
-    // A block expands a chunk of kPer*blockDim.x consecutive entries; warp w
-    // covers 32*kPer of them in kPer coalesced passes (entry wbase+32q+lane).
-    // Warp scans give each entry's first-donor offset in entry order, one
-    // block scan over the warps and one atomic place the chunk, and the
-    // donors are written cooperatively (lane r writes the r-th donor of the
-    // pass), so every store of the expansion is coalesced and the next level
-    // keeps this level's order.
-    const int chunk = kPer * kWalkThreads;
-    const int wid = threadIdx.x >> 5;
-    for (int base = lo + blockIdx.x * chunk; base < hi; base += gridDim.x * chunk) {
+    const int j = L % 3;
+    if (blockIdx.x == 0)
+      for (int r = threadIdx.x; r < nreal; r += kWalkThreads) a.rctl[r].lvlcnt[(L + 1) % 3] = 0;
+    const int nchunks = block_prefix(
+        nreal, [&](int r) { return (s_hi[r] - s_lo[r] + kChunk - 1) / kChunk; }, s_pre);
+    for (int g = blockIdx.x; g < nchunks; g += gridDim.x) {
+      const int r = find_real(s_pre, nreal, g);
+      const RealDesc &d = a.desc[r];
+      const int hi = s_hi[r];
+      const int base = s_lo[r] + (g - s_pre[r]) * kChunk;
       const int wbase = base + wid * (32 * kPer);
+      int32_t *ent = a.ent + d.off;
+      const uint8_t *mask = a.mask + d.off;
       int cs[kPer];
       unsigned ms[kPer];
       int incl[kPer];
@@ -535,8 +570,8 @@ k_walk(WalkArgs a) {
         cs[q] = 0;
         ms[q] = 0;
         if (i < hi) {
-          cs[q] = __ldcg(&a.ent[i]);
-          ms[q] = a.mask[cs[q]];
+          cs[q] = __ldcg(&ent[i]);
+          ms[q] = mask[cs[q]];
         }
       }
       int wtot = 0;
@@ -544,9 +579,9 @@ k_walk(WalkArgs a) {
       for (int q = 0; q < kPer; q++) {
         int v = __popc(ms[q]);
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const int t = __shfl_up_sync(kFull, v, d);
-          if (lane >= d) v += t;
+        for (int dd = 1; dd < 32; dd <<= 1) {
+          const int x = __shfl_up_sync(kFull, v, dd);
+          if (lane >= dd) v += x;
         }
         incl[q] = wtot + v;  // inclusive, relative to the warp's first donor
         wtot += __shfl_sync(kFull, v, 31);
@@ -554,42 +589,42 @@ k_walk(WalkArgs a) {
       int total;
       const int wexcl = block_excl_scan(lane == 0 ? wtot : 0, total, threadIdx.x, kWalkThreads);
       const int wstart = __shfl_sync(kFull, wexcl, 0);
-      if (threadIdx.x == 0) s_base = total ? atomicAdd(&ctl->lvlcnt[j], total) : 0;
+      if (threadIdx.x == 0) s_base = total ? atomicAdd(&a.rctl[r].lvlcnt[j], total) : 0;
       __syncthreads();
       const int cbase = hi + s_base + wstart;  // position of the warp's first donor
       __syncthreads();
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
         const int i = wbase + 32 * q + lane;
-        const int nd = __popc(ms[q]);
+        const int n_d = __popc(ms[q]);
         if (i < hi) {
-          a.kid[i] = cbase + incl[q] - nd;
-          a.nd[i] = (uint8_t)nd;
+          a.kid[d.off + i] = cbase + incl[q] - n_d;
+          a.nd[d.off + i] = (uint8_t)n_d;
         }
-        const int q_lo = __shfl_sync(kFull, incl[q] - nd, 0);
+        const int q_lo = __shfl_sync(kFull, incl[q] - n_d, 0);
         const int q_hi = __shfl_sync(kFull, incl[q], 31);
         for (int r0 = q_lo; r0 < q_hi; r0 += 32) {
-          const int r = r0 + lane;
-          // owner = number of lanes whose inclusive count is <= r
+          const int rr = r0 + lane;
+          // owner = number of lanes whose inclusive count is <= rr
           int o = 0;
 #pragma unroll
           for (int step = 16; step >= 1; step >>= 1) {
             const int v = __shfl_sync(kFull, incl[q], o + step - 1);
-            if (v <= r) o += step;
+            if (v <= rr) o += step;
           }
           const int oc = __shfl_sync(kFull, cs[q], o);
           unsigned om = __shfl_sync(kFull, ms[q], o);
           const int ofirst = __shfl_sync(kFull, incl[q] - __popc(ms[q]), o);
-          if (r < q_hi) {
-            for (int skip = r - ofirst; skip > 0; --skip) om &= om - 1;
+          if (rr < q_hi) {
+            for (int skip = rr - ofirst; skip > 0; --skip) om &= om - 1;
             const int k = __ffs(om) - 1;
             // level-1 entries remember whether their receiver is a pit
             // (a level-0 entry past the rings)
-            const unsigned pit = (nlev == 1 && wbase + 32 * q + o >= a.nring) ? 8u : 0u;
-            const int pos = cbase + r;
-            if (pos < a.size) {
-              a.ent[pos] = oc + nbr_off(k, a.W);
-              a.pdir[pos] = (uint8_t)(((k + 4) & 7) | pit);
+            const unsigned pit = (L == 0 && wbase + 32 * q + o >= d.nring) ? 8u : 0u;
+            const int pos = cbase + rr;
+            if (pos < d.size) {
+              ent[pos] = oc + nbr_off(k, d.W);
+              a.pdir[d.off + pos] = (uint8_t)(((k + 4) & 7) | pit);
             } else {
               raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
             }
@@ -598,64 +633,102 @@ k_walk(WalkArgs a) {
       }
     }
     if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
-    const int added = ld_volatile_i32(&ctl->lvlcnt[j]);
-    if (added == 0) break;
-    lo = hi;
-    hi = hi + added;
-    ++nlev;
-    if (hi > a.size) {
-      if (tid == 0) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+    int any = 0;
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      const int added = ld_volatile_i32(&a.rctl[r].lvlcnt[j]);
+      s_lo[r] = s_hi[r];
+      if (added) {
+        s_hi[r] += added;
+        s_nlev[r] = L + 2;
+        any = 1;
+        if (s_hi[r] > a.desc[r].size) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+        if (blockIdx.x == 0 && s_hi[r] <= a.desc[r].size)
+          a.lvl_off[a.desc[r].lvl_base + L + 2] = s_hi[r];
+      }
+    }
+    if (!__syncthreads_or(any)) break;
+    if (ld_volatile_i32(&ctl->err) != 0) return;
+    ++L;
+  }
+  const int maxlev = L + 1;  // levels of the deepest realization
+  // s_hi[r] is the realization's total; anything short of its size means
+  // cells that never reached base level: the receivers contain a cycle.
+  {
+    int bad = 0;
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      if (blockIdx.x == 0) {
+        a.rctl[r].nlevels = s_nlev[r];
+        a.rctl[r].total = s_hi[r];
+      }
+      bad |= s_hi[r] != a.desc[r].size;
+    }
+    if (__syncthreads_or(bad)) {
+      if (tid == 0) raise_err(ctl, FS_ERR_ORDER, kPhaseOrder);
       return;
     }
-    if (tid == 0) a.lvl_off[nlev] = hi;
-  }
-  if (tid == 0) {
-    ctl->nlevels = nlev;
-    ctl->total = hi;
-  }
-  if (hi != a.size) {
-    // Some cells never reached base level: the receivers contain a cycle.
-    if (tid == 0) raise_err(ctl, FS_ERR_ORDER, kPhaseOrder);
-    return;
   }
   lap(0);
+
+  // Level Lv of every realization as [s_lo[r], s_hi[r]) (empty past its
+  // depth), and the prefix of its 32-entry groups over the batch.
+  auto level_groups = [&](int Lv) -> int {
+    __syncthreads();  // every warp is done with the previous ranges
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      if (Lv < s_nlev[r]) {
+        const int b = a.desc[r].lvl_base;
+        s_lo[r] = __ldcg(&a.lvl_off[b + Lv]);
+        s_hi[r] = __ldcg(&a.lvl_off[b + Lv + 1]);
+      } else {
+        s_lo[r] = s_hi[r] = 0;
+      }
+    }
+    __syncthreads();
+    return block_prefix(nreal, [&](int r) { return (s_hi[r] - s_lo[r] + 31) >> 5; }, s_pre);
+  };
 
   // ---- accumulation: fastscape_RB.cpp:262-279, pulled level by level ----
   // acc[i] = 1 + sum of the donors' counts, read from the contiguous run
   // [kid[i], kid[i] + nd[i]) of the next level; the reference's accum is
-  // acc*cell_area (exact: integer multiples of cell_area). A count at level
-  // >= 1 beyond the erosion table stops the timestep before any elevation
-  // changes; the host grows the table and repeats it.
-  for (int L = nlev - 1; L >= 0; --L) {
-    if (L == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
-    const int b = __ldcg(&a.lvl_off[L]);
-    const int e = __ldcg(&a.lvl_off[L + 1]);
-    // Warp-cooperative: a warp takes kAccU groups of 32 consecutive entries
-    // (each group lies inside one expansion chunk, so its donors form one
-    // contiguous run starting at kid of its first entry), loads the runs
-    // coalesced -- all groups' first 32 donors in flight together -- and
-    // each lane sums its own donors out of the run with shuffles.
-    for (int g0 = b + (tid & ~31); g0 < e; g0 += kAccU * nthreads) {
-      int n[kAccU], incl[kAccU], run[kAccU], tot[kAccU];
+  // acc*cell_area (exact: integer multiples of cell_area). A warp takes
+  // kAccU 32-entry groups (a group lies inside one expansion chunk, so its
+  // donors form one contiguous run starting at kid of its first entry),
+  // loads the runs coalesced -- all groups' first 32 donors in flight
+  // together -- and each lane sums its own donors with shuffles. A count at
+  // level >= 1 beyond its realization's erosion table stops the timestep
+  // before any elevation changes; the host grows the table and repeats it.
+  for (int Lv = maxlev - 1; Lv >= 0; --Lv) {
+    if (Lv == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
+    const int ngroups = level_groups(Lv);
+    for (int g0 = warp_global * kAccU; g0 < ngroups; g0 += nwarps * kAccU) {
+      int n[kAccU], incl[kAccU], run[kAccU], tot[kAccU], ii[kAccU], rr[kAccU];
       uint32_t v0[kAccU];
 #pragma unroll
       for (int u = 0; u < kAccU; u++) {
-        const int i = g0 + u * nthreads + lane;
+        const int g = g0 + u;
         int k = 0;
         n[u] = 0;
-        if (i < e) {
-          n[u] = __ldcg(&a.nd[i]);
-          k = __ldcg(&a.kid[i]);
+        rr[u] = 0;
+        ii[u] = -1;
+        if (g < ngroups) {
+          const int r = find_real(s_pre, nreal, g);
+          const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
+          rr[u] = r;
+          if (i < s_hi[r]) {
+            const int off = a.desc[r].off;
+            ii[u] = i;
+            n[u] = __ldcg(&a.nd[off + i]);
+            k = __ldcg(&a.kid[off + i]);
+          }
         }
         int v = n[u];
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const int t = __shfl_up_sync(kFull, v, d);
-          if (lane >= d) v += t;
+        for (int dd = 1; dd < 32; dd <<= 1) {
+          const int x = __shfl_up_sync(kFull, v, dd);
+          if (lane >= dd) v += x;
         }
         incl[u] = v;
         tot[u] = __shfl_sync(kFull, v, 31);
-        run[u] = __shfl_sync(kFull, k, 0);
+        run[u] = a.desc[rr[u]].off + __shfl_sync(kFull, k, 0);
       }
 #pragma unroll
       for (int u = 0; u < kAccU; u++)
@@ -669,19 +742,21 @@ k_walk(WalkArgs a) {
           if (r0 > 0) v = r0 + lane < tot[u] ? __ldcg(&a.acc[run[u] + r0 + lane]) : 0u;
 #pragma unroll
           for (int q = 0; q < 8; q++) {
-            const int r = first + q - r0;
-            const uint32_t x = __shfl_sync(kFull, v, r & 31);
-            if (q < n[u] && r >= 0 && r < 32) s += x;
+            const int rq = first + q - r0;
+            const uint32_t x = __shfl_sync(kFull, v, rq & 31);
+            if (q < n[u] && rq >= 0 && rq < 32) s += x;
           }
         }
-        const int i = g0 + u * nthreads + lane;
-        if (i < e) {
-          a.acc[i] = s;
-          if (a.do_erode && L > 0 && s >= (uint32_t)a.tab_cap) atomicMax(&ctl->abort_k, (int)s);
+        if (ii[u] >= 0) {
+          const RealDesc &d = a.desc[rr[u]];
+          a.acc[d.off + ii[u]] = s;
+          if (a.do_erode && Lv > 0 && s >= (uint32_t)d.tab_cap) {
+            if (atomicMax(&ctl->abort_k, (int)s) < (int)s) ctl->abort_r = rr[u];
+          }
         }
       }
     }
-    if (L > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (Lv > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
   }
   lap(1);
   if (!a.do_erode) return;
@@ -691,62 +766,95 @@ k_walk(WalkArgs a) {
   // their first read; level-1 cells add the uplift of a pit receiver on
   // read, and the pits themselves are uplifted once no level-1 cell can read
   // them any more (during level 2, or after a barrier when level 1 is the
-  // last). No barrier is needed before level 1: it reads counts complete
+  // deepest). No barrier is needed before level 1: it reads counts complete
   // since the barrier after accumulation level 1 and never-written h.
-  // Two entries per thread per pass, their loads issued together.
-  for (int L = 1; L < nlev; ++L) {
-    const int b = __ldcg(&a.lvl_off[L]);
-    const int e = __ldcg(&a.lvl_off[L + 1]);
-    for (int i = b + tid; i < e; i += 2 * nthreads) {
-      const int i2 = i + nthreads;
-      const bool two = i2 < e;
-      const int c1 = __ldcg(&a.ent[i]);
-      const int d1 = __ldcg(&a.pdir[i]);
-      const uint32_t k1 = __ldcg(&a.acc[i]);
-      int c2 = c1, d2 = d1;
-      uint32_t k2 = k1;
-      if (two) {
-        c2 = __ldcg(&a.ent[i2]);
-        d2 = __ldcg(&a.pdir[i2]);
-        k2 = __ldcg(&a.acc[i2]);
+  auto uplift_pits = [&]() {
+    // pits of realization r: level-0 positions [nring, lvl_off[1])
+    __syncthreads();  // every warp is done with the level's ranges
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      const RealDesc &d = a.desc[r];
+      s_lo[r] = d.nring;
+      s_hi[r] = __ldcg(&a.lvl_off[d.lvl_base + 1]);
+    }
+    __syncthreads();
+    const int np = block_prefix(nreal, [&](int r) { return s_hi[r] - s_lo[r]; }, s_pre);
+    for (int g = tid; g < np; g += nthreads) {
+      const int r = find_real(s_pre, nreal, g);
+      const RealDesc &d = a.desc[r];
+      const int c = __ldcg(&a.ent[d.off + s_lo[r] + (g - s_pre[r])]);
+      double *hh = a.h + d.off;
+      hh[c] = __ldcg(&hh[c]) + d.u_dt;
+    }
+  };
+  for (int Lv = 1; Lv < maxlev; ++Lv) {
+    const int ngroups = level_groups(Lv);
+    for (int g0 = warp_global * kEroU; g0 < ngroups; g0 += nwarps * kEroU) {
+      int cc[kEroU], dd[kEroU], rr[kEroU];
+      uint32_t kk[kEroU];
+      bool ok[kEroU];
+#pragma unroll
+      for (int u = 0; u < kEroU; u++) {
+        const int g = g0 + u;
+        ok[u] = false;
+        rr[u] = 0;
+        cc[u] = 0;
+        dd[u] = 0;
+        kk[u] = 0;
+        if (g < ngroups) {
+          const int r = find_real(s_pre, nreal, g);
+          const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
+          rr[u] = r;
+          if (i < s_hi[r]) {
+            const int off = a.desc[r].off;
+            ok[u] = true;
+            cc[u] = __ldcg(&a.ent[off + i]);
+            dd[u] = __ldcg(&a.pdir[off + i]);
+            kk[u] = __ldcg(&a.acc[off + i]);
+          }
+        }
       }
-      const int n1 = c1 + nbr_off(d1 & 7, a.W);
-      const int n2 = c2 + nbr_off(d2 & 7, a.W);
-      const double *T1 = a.tab + (size_t)k1 * kTabStride + 4 * (d1 & 1);
-      const double *T2 = a.tab + (size_t)k2 * kTabStride + 4 * (d2 & 1);
-      const double hc1 = __ldcg(&a.h[c1]);
-      double hn1 = __ldcg(&a.h[n1]);
-      const double hc2 = __ldcg(&a.h[c2]);
-      double hn2 = __ldcg(&a.h[n2]);
-      if (d1 & 8) hn1 = hn1 + a.u_dt;
-      if (d2 & 8) hn2 = hn2 + a.u_dt;
-      const double r1 = erode_cell<NMODE>(a, T1, hc1 + a.u_dt, hn1);
-      if (!isfinite(r1)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-      a.h[c1] = r1;
-      if (two) {
-        const double r2 = erode_cell<NMODE>(a, T2, hc2 + a.u_dt, hn2);
-        if (!isfinite(r2)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-        a.h[c2] = r2;
+      double hc[kEroU], hn[kEroU];
+#pragma unroll
+      for (int u = 0; u < kEroU; u++) {
+        hc[u] = 0.0;
+        hn[u] = 0.0;
+        if (ok[u]) {
+          const RealDesc &d = a.desc[rr[u]];
+          const double *hh = a.h + d.off;
+          hc[u] = __ldcg(&hh[cc[u]]);
+          hn[u] = __ldcg(&hh[cc[u] + nbr_off(dd[u] & 7, d.W)]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEroU; u++) {
+        if (ok[u]) {
+          const RealDesc &d = a.desc[rr[u]];
+          const double *T = d.tab + (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
+          double hr = hn[u];
+          if (dd[u] & 8) hr = hr + d.u_dt;
+          const double hnew = erode_cell<NMODE>(d, a.neq, ctl, T, hc[u] + d.u_dt, hr);
+          if (!isfinite(hnew)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+          a.h[d.off + cc[u]] = hnew;
+        }
       }
     }
-    if (L == 2) uplift_pits(a, lvl0_end, tid, nthreads);
-    if (L + 1 < nlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (Lv == 2) uplift_pits();
+    if (Lv + 1 < maxlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
   }
-  if (nlev <= 2) {
-    if (nlev == 2 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
-    uplift_pits(a, lvl0_end, tid, nthreads);
+  if (maxlev <= 2) {
+    if (maxlev == 2 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    uplift_pits();
   }
   lap(2);
   if (tid == 0) atomicAdd(&ctl->steps_done, 1);
 }
 
-__global__ void k_check_finite(const double *__restrict__ h, int size, Ctl *ctl) {
+__global__ void k_check_finite(const double *__restrict__ h, long long n, Ctl *ctl) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < size; i += stride)
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     bad |= !isfinite(h[i]);
-  if (__syncthreads_or(bad) && threadIdx.x == 0)
-    raise_err(ctl, FS_ERR_NONFINITE, kPhaseNone);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) raise_err(ctl, FS_ERR_NONFINITE, kPhaseNone);
 }
 
 // Philox4x32-10 (Salmon, Moraes, Dror & Shaw, SC'11), counter = cell index,
@@ -769,8 +877,9 @@ __device__ __forceinline__ void philox4x32_10(uint32_t ctr[4], uint32_t key[2]) 
   }
 }
 
-__global__ void k_philox_field(double *__restrict__ h, int W, int H, int size,
-                               uint32_t key0, uint32_t key1) {
+__global__ void k_philox_field(double *__restrict__ h, int W, int H, uint32_t key0,
+                               uint32_t key1) {
+  const long long size = (long long)W * H;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < size; c += stride) {
     uint32_t ctr[4] = {(uint32_t)c, (uint32_t)((unsigned long long)c >> 32), 0u, 0u};
@@ -786,9 +895,32 @@ __global__ void k_philox_field(double *__restrict__ h, int W, int H, int size,
   }
 }
 
-// A wait on a count that no block ever completes; the bounded barrier must
-// give up after timeout_ns and report FS_ERR_TIMEOUT. Used by the tests of
-// the failure path only.
+// ent[0, nring) = the cells of rings 0 and 1 in ascending order: rows 0 and
+// 1, then x = 0, 1, W-2, W-1 of rows 2..H-3, then rows H-2 and H-1.
+__global__ void k_place_rings(int32_t *ent, int W, int H) {
+  const int mid_rows = H > 4 ? H - 4 : 0;
+  const int top = 2 * W;
+  const int nring = W * H - (W > 4 ? W - 4 : 0) * mid_rows;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nring; i += gridDim.x * blockDim.x) {
+    int c;
+    if (H <= 4 || W <= 4) {
+      c = i;  // no interior: every cell is a ring cell
+    } else if (i < top) {
+      c = i;
+    } else if (i < top + 4 * mid_rows) {
+      const int jj = i - top, row = 2 + jj / 4, q = jj % 4;
+      const int x = q < 2 ? q : W - 4 + q;
+      c = row * W + x;
+    } else {
+      c = (H - 2) * W + (i - top - 4 * mid_rows);
+    }
+    ent[i] = c;
+  }
+}
+
+// A wait on a count that no block ever completes; the bounded wait must give
+// up after timeout_ns and report FS_ERR_TIMEOUT. Used by the tests of the
+// failure path only.
 __global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
   if (threadIdx.x == 0) {
     const unsigned target = gridDim.x + 1;  // never reached
@@ -806,9 +938,34 @@ __global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
   }
 }
 
+int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
+}
+
 }  // namespace
 
+size_t walk_smem_bytes(int nreal) { return sizeof(int) * (4 * (size_t)nreal + 1); }
+
 int walk_threads() { return kWalkThreads; }
+
+const void *walk_kernel_ptr(int nmode) {
+  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne>);
+  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo>);
+  return reinterpret_cast<const void *>(&k_walk<kNGeneral>);
+}
+
+cudaError_t prepare_walk_kernels() {
+  const int bytes = (int)walk_smem_bytes(kMaxReal);
+  for (int nm = 0; nm < 3; nm++) {
+    cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 float tol_lower_float(double tol) {
   const double t = tol * (1.0 - 0x1p-20);
@@ -817,80 +974,95 @@ float tol_lower_float(double tol) {
   return f;
 }
 
-cudaError_t launch_receivers(const double *h, int8_t *rec, const Ctl *ctl, StepGeom g,
-                             double dr_orth, double dr_diag, cudaStream_t s) {
-  const int iw = g.W - 4, ih = g.H - 4;
-  if (iw <= 0 || ih <= 0) return cudaSuccess;
-  dim3 block(32, 8);
-  dim3 grid((iw + 31) / 32, (ih + 7) / 8);
-  k_receivers<<<grid, block, 0, s>>>(h, rec, g.W, g.H, dr_orth, dr_diag, ctl);
+int ring_cells(int W, int H) {
+  return W * H - (W > 4 ? W - 4 : 0) * (H > 4 ? H - 4 : 0);
+}
+
+int append_tiles(int kind, int r, int W, int H, Tile *out, int cap) {
+  // receivers: interior x, y in [2, W-3]; donors: x, y in [1, W-2]
+  const int lo = kind == 0 ? 2 : 1;
+  const int iw = W - 2 * lo, ih = H - 2 * lo;
+  if (iw <= 0 || ih <= 0) return 0;
+  const int tx = kind == 0 ? kRxTile : kDxTile, ty = kind == 0 ? kRyTile : kDyTile;
+  const int nx = (iw + tx - 1) / tx, ny = (ih + ty - 1) / ty;
+  if ((long long)nx * ny > cap) return -1;
+  int n = 0;
+  for (int y = 0; y < ny; y++)
+    for (int x = 0; x < nx; x++) out[n++] = Tile{r, lo + x * tx, lo + y * ty, 0};
+  return n;
+}
+
+void fill_table_range(double keq, double neq, double meq, double dt, double dr_orth,
+                      double dr_diag, double cell_area, long long k0, long long k1,
+                      double *rec) {
+  const double kd = keq * dt;
+  const double pl[2] = {std::pow(dr_orth, neq), std::pow(dr_diag, neq)};
+  for (long long k = k0; k < k1; k++) {
+    const double A = static_cast<double>(k) * cell_area;
+    const double pa = std::pow(A, meq);
+    double *r = rec + (k - k0) * kTabStride;
+    for (int cls = 0; cls < 2; cls++) {
+      const double F = kd * pa / pl[cls];
+      const double D = 1. + F;
+      r[4 * cls + 0] = F;
+      r[4 * cls + 1] = D;
+      r[4 * cls + 2] = 1. / D;
+      r[4 * cls + 3] = 0.;
+    }
+  }
+}
+
+cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s) {
+  if (a.nrtiles == 0) return cudaSuccess;
+  k_receivers_exact<<<a.nrtiles, dim3(32, 8), 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_receivers_fast(const double *h, int8_t *rec, int32_t *amb,
-                                  Ctl *ctl, StepGeom g, double dr_orth,
-                                  double dr_diag, cudaStream_t s) {
-  const int iw = g.W - 4, ih = g.H - 4;
-  if (iw <= 0 || ih <= 0) return cudaSuccess;
-  const float g_orth = (float)(1.0 / dr_orth), g_diag = (float)(1.0 / dr_diag);
-  const float gmax = g_orth > g_diag ? g_orth : g_diag;
-  dim3 block(32, 8);
-  dim3 grid((iw + kRxTile - 1) / kRxTile, (ih + kRyTile - 1) / kRyTile);
-  k_receivers_filter<<<grid, block, 0, s>>>(h, rec, amb, ctl, g.W, g.H, g_orth, g_diag, gmax);
+cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s) {
+  if (a.nrtiles == 0) return cudaSuccess;
+  k_receivers_filter<<<a.nrtiles, dim3(32, 8), 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_receivers_fixup<<<sms, 256, 0, s>>>(h, rec, amb, ctl, g.W, dr_orth, dr_diag);
+  k_receivers_fixup<<<sm_count(), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_donors_level0(const int8_t *rec, uint8_t *mask,
-                                 int32_t *ent, Ctl *ctl, StepGeom g, int nring,
-                                 cudaStream_t s) {
-  const int iw = g.W - 2, ih = g.H - 2;
-  if (iw <= 0 || ih <= 0) return cudaSuccess;
-  dim3 block(32, 8);
-  dim3 grid((iw + kDxTile - 1) / kDxTile, (ih + kDyTile - 1) / kDyTile);
-  k_donors_level0<<<grid, block, 0, s>>>(rec, mask, ent, ctl, g.W, g.H, nring);
+cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s) {
+  if (a.ndtiles == 0) return cudaSuccess;
+  k_donors_level0<<<a.ndtiles, dim3(32, 8), 0, s>>>(a);
   return cudaGetLastError();
 }
 
-const void *walk_kernel_ptr(int nmode) {
-  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne>);
-  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo>);
-  return reinterpret_cast<const void *>(&k_walk<kNGeneral>);
-}
-
-cudaError_t launch_walk(const WalkArgs &a, int blocks, cudaStream_t s) {
-  WalkArgs args = a;
+cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s) {
+  StepArgs args = a;
   void *params[] = {&args};
   return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode), dim3(blocks),
-                                     dim3(kWalkThreads), params, 0, s);
+                                     dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }
 
-cudaError_t launch_check_finite(const double *h, int size, Ctl *ctl,
-                                cudaStream_t s) {
-  int blocks = (size + 255) / 256;
+cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s) {
+  long long blocks = (n + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   if (blocks < 1) blocks = 1;
-  k_check_finite<<<blocks, 256, 0, s>>>(h, size, ctl);
+  k_check_finite<<<(int)blocks, 256, 0, s>>>(h, n, ctl);
   return cudaGetLastError();
 }
 
-cudaError_t launch_philox_field(double *h, StepGeom g, uint64_t seed,
-                                cudaStream_t s) {
-  int blocks = (g.size + 255) / 256;
+cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s) {
+  long long blocks = ((long long)W * H + 255) / 256;
   if (blocks > 8192) blocks = 8192;
   if (blocks < 1) blocks = 1;
-  k_philox_field<<<blocks, 256, 0, s>>>(h, g.W, g.H, g.size, (uint32_t)seed,
-                                       (uint32_t)(seed >> 32));
+  k_philox_field<<<(int)blocks, 256, 0, s>>>(h, W, H, (uint32_t)seed, (uint32_t)(seed >> 32));
   return cudaGetLastError();
 }
 
-cudaError_t launch_test_wait(Ctl *ctl, int blocks,
-                             unsigned long long timeout_ns, cudaStream_t s) {
+cudaError_t launch_place_rings(int32_t *ent, int W, int H, cudaStream_t s) {
+  k_place_rings<<<64, 256, 0, s>>>(ent, W, H);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns,
+                             cudaStream_t s) {
   k_test_wait<<<blocks, 32, 0, s>>>(ctl, timeout_ns);
   return cudaGetLastError();
 }

@@ -1,23 +1,26 @@
 // fs_model.cu -- host side of the C ABI declared in include/fastscape_gb300.h.
 //
-// A model owns its device buffers for its whole life (the reference
-// reallocates and frees its scratch on every run(), fastscape_RB.cpp:346-358
-// and :392-397) and one CUDA stream. Layout in HBM, for size = W*H cells:
-//   h       double[size]        elevation (the only state carried between
+// Every model is a batch of realizations on one CUDA stream (fs_create makes
+// a batch of one; fs_batch_create a ragged batch). A batch owns its device
+// buffers for its whole life (the reference reallocates and frees its
+// scratch on every run(), fastscape_RB.cpp:346-358 and :392-397). Layout in
+// HBM, for C = the batch's total cells (realization r at [off_r, off_r+size_r)):
+//   h       double[C]           elevation (the only state carried between
 //                               timesteps, as in the reference)
-//   rec     int8[size]          receiver direction code, -1 = NO_FLOW
-//   mask    uint8[size]         donor mask (bit k: neighbour k drains here)
-//   ent     int32[size]         cells grouped by level (the reference's stack)
-//   pdir    uint8[size]         receiver direction by level position
-//   nd      uint8[size]         donor count by level position
-//   kid     int32[size]         first donor's position by level position
-//   lvl_off int32[size+2]       level offsets into stack
-//   acc     uint32[size]        drainage cell counts by level position
+//   rec     int8[C]             receiver direction code, -1 rings, -2 pits
+//   mask    uint8[C]            donor mask (bit k: neighbour k drains here)
+//   ent     int32[C]            cells grouped by level (the reference's stack)
+//   pdir    uint8[C]            receiver direction by level position
+//   nd      uint8[C]            donor count by level position
+//   kid     int32[C]            first donor's position by level position
+//   acc     uint32[C]           drainage cell counts by level position
 //                               (accum = acc*cell_area)
-//   amb     int32[size]         cells queued for the FP64 receiver fix-up
-//   tab     double[8*tab_cap]   erosion table per drainage count k < tab_cap
-//                               (see fs_internal.h); grows on demand
-//   ctl     fs::Ctl             status word, counters, barrier
+//   amb     int32[C], amb_r     cells queued for the FP64 receiver fix-up
+//   lvl_off int32[C+2n]         level offsets, size_r+2 per realization
+//   tab_r   double[8*cap_r]     erosion table of realization r per drainage
+//                               count k < cap_r (fs_internal.h); grows on
+//                               demand
+//   desc, rctl, ctl, tiles      descriptors, counters, status, stencil tiles
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,14 +52,14 @@ int set_error(int status, const char *fmt, ...) {
 }
 
 int cuda_error(cudaError_t e, const char *what) {
-  return set_error(e == cudaErrorMemoryAllocation ? FS_ERR_NOMEM : FS_ERR_CUDA,
-                   "%s: %s", what, cudaGetErrorString(e));
+  return set_error(e == cudaErrorMemoryAllocation ? FS_ERR_NOMEM : FS_ERR_CUDA, "%s: %s", what,
+                   cudaGetErrorString(e));
 }
 
-#define FS_CUDA(call)                                      \
-  do {                                                     \
-    cudaError_t fs_e_ = (call);                            \
-    if (fs_e_ != cudaSuccess) return cuda_error(fs_e_, #call); \
+#define FS_CUDA(call)                                           \
+  do {                                                          \
+    cudaError_t fs_e_ = (call);                                 \
+    if (fs_e_ != cudaSuccess) return cuda_error(fs_e_, #call);  \
   } while (0)
 
 const double kSqrt2 = 1.414213562373095048801688724209698078569671875376948;
@@ -77,129 +80,64 @@ const char *status_name(int s) {
   }
 }
 
-bool finite_params(const fs_params &p) {
+bool valid_params(const fs_params &p) {
   const double v[9] = {p.keq, p.neq, p.meq, p.ueq, p.dt, p.dr_orth, p.dr_diag, p.tol, p.cell_area};
   for (double x : v)
     if (!std::isfinite(x)) return false;
   return p.dr_orth > 0 && p.dr_diag > 0 && p.cell_area > 0 && p.tol >= 0;
 }
 
+int nmode_of(double neq) {
+  return neq == 1.0 ? fs::kNOne : neq == 2.0 ? fs::kNTwo : fs::kNGeneral;
+}
+
 }  // namespace
 
 int fs::record_error(int status, const char *msg) { return set_error(status, "%s", msg); }
 
-struct fs_model {
-  int W = 0, H = 0, size = 0;
-  fs_params p{};
+// ---------------------------------------------------------------------------
+// Batch: the device state of n realizations and how to step it.
+// ---------------------------------------------------------------------------
+struct fs_batch {
+  int n = 0;
+  std::vector<int> W, H, size, off, lvl_base, nring;
+  std::vector<fs_params> p;
+  long long cells = 0, lvl_total = 0;
+  int nmode = fs::kNOne;
+  double neq = 1.0;
   int device = 0;
   cudaStream_t stream = nullptr;
-  double *d_h = nullptr;
-  int8_t *d_rec = nullptr;
-  uint8_t *d_mask = nullptr;
-  int32_t *d_ent = nullptr;
-  uint8_t *d_pdir = nullptr;
-  uint8_t *d_nd = nullptr;
-  int32_t *d_kid = nullptr;
-  int32_t *d_amb = nullptr;   // cells the receiver filter could not decide
-  int32_t *d_lvl = nullptr;
-  uint32_t *d_acc = nullptr;
-  double *d_tab = nullptr;
-  int tab_cap = 0;
-  fs::Ctl *d_ctl = nullptr;
-  fs::Ctl *h_ctl = nullptr;  // pinned mirror for status reads
-  int walk_blocks = 0;
-  int nring = 0;             // cells of rings 0 and 1 (always level 0)
-  int nmode = fs::kNGeneral;
-  double u_dt = 0;
+  double *h = nullptr;
+  int8_t *rec = nullptr;
+  uint8_t *mask = nullptr, *pdir = nullptr, *nd = nullptr;
+  int32_t *ent = nullptr, *kid = nullptr, *amb = nullptr, *amb_r = nullptr, *lvl = nullptr;
+  uint32_t *acc = nullptr;
+  fs::RealDesc *d_desc = nullptr;
+  fs::RealCtl *d_rctl = nullptr, *h_rctl = nullptr;
+  fs::Ctl *d_ctl = nullptr, *h_ctl = nullptr;
+  fs::Tile *d_rtiles = nullptr, *d_dtiles = nullptr;
+  int nrtiles = 0, ndtiles = 0;
+  std::vector<fs::RealDesc> desc;
+  std::vector<double *> tab;
+  std::vector<int> tab_cap;
+  int walk_occ = 1, walk_sms = 1, walk_bps = 2;  // walk blocks per SM in use
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
   bool timing = false;
-  bool exact_receivers = false;  // testing: FP64 reference formula for every cell
-  std::vector<cudaEvent_t> ev;  // timing mode: 3 per timestep + 1
+  bool exact_receivers = false;
+  bool use_graph = false;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_dirty = true;
+  std::vector<cudaEvent_t> ev;
   double phase_ms[4] = {0, 0, 0, 0};
 };
 
+struct fs_model {
+  fs_batch *b = nullptr;
+};
+
 namespace {
-
-void free_model(fs_model *m) {
-  if (!m) return;
-  int prev = 0;
-  cudaGetDevice(&prev);
-  cudaSetDevice(m->device);
-  if (m->stream) cudaStreamSynchronize(m->stream);
-  cudaFree(m->d_h);
-  cudaFree(m->d_rec);
-  cudaFree(m->d_mask);
-  cudaFree(m->d_ent);
-  cudaFree(m->d_pdir);
-  cudaFree(m->d_nd);
-  cudaFree(m->d_kid);
-  cudaFree(m->d_amb);
-  cudaFree(m->d_lvl);
-  cudaFree(m->d_acc);
-  cudaFree(m->d_tab);
-  cudaFree(m->d_ctl);
-  if (m->h_ctl) cudaFreeHost(m->h_ctl);
-  for (auto &e : m->ev) cudaEventDestroy(e);
-  if (m->stream) cudaStreamDestroy(m->stream);
-  cudaSetDevice(prev);
-  delete m;
-}
-
-// Erosion table records for counts k in [k0, k1): for each direction class
-// F = keq*dt*pow(k*cell_area, meq)/pow(dr_cls, neq) evaluated in exactly the
-// order of fastscape_RB.cpp:315 with the C library's pow (the reference's
-// accum[c] is k*cell_area exactly: integer multiples summed below 2^53), then
-// D = 1 + F and R = 1/D, both correctly rounded. Host arithmetic is IEEE
-// double without contraction, so the device sees the reference's bits.
-void fill_table(const fs_params &p, long long k0, long long k1, double *rec) {
-  const double kd = p.keq * p.dt;
-  const double pl[2] = {std::pow(p.dr_orth, p.neq), std::pow(p.dr_diag, p.neq)};
-  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
-  nt = std::min<unsigned>(nt, 64);
-  if (k1 - k0 < 65536) nt = 1;
-  auto work = [&](unsigned t) {
-    const long long lo = k0 + (k1 - k0) * t / nt;
-    const long long hi = k0 + (k1 - k0) * (t + 1) / nt;
-    for (long long k = lo; k < hi; k++) {
-      const double A = static_cast<double>(k) * p.cell_area;
-      const double pa = std::pow(A, p.meq);
-      double *r = rec + (k - k0) * fs::kTabStride;
-      for (int cls = 0; cls < 2; cls++) {
-        const double F = kd * pa / pl[cls];
-        const double D = 1. + F;
-        r[4 * cls + 0] = F;
-        r[4 * cls + 1] = D;
-        r[4 * cls + 2] = 1. / D;
-        r[4 * cls + 3] = 0.;
-      }
-    }
-  };
-  if (nt == 1) {
-    work(0);
-  } else {
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; t++) th.emplace_back(work, t);
-    for (auto &x : th) x.join();
-  }
-}
-
-// The reference field (fastscape_RB.cpp:111-130 via random.cpp:45-49),
-// generated with the same libstdc++ engine and distribution.
-void reference_field(std::vector<double> &h, int W, int H, uint32_t engine_seed) {
-  std::mt19937 eng(engine_seed);
-  std::uniform_real_distribution<double> d(0.0, 1.0);
-  h.resize(static_cast<size_t>(W) * H);
-  for (int y = 0; y < H; y++)
-    for (int x = 0; x < W; x++) {
-      const size_t c = static_cast<size_t>(y) * W + x;
-      double v = d(eng);
-      if (x == 0 || y == 0 || x == W - 1 || y == H - 1) v = 0;
-      if (x == 1 || y == 1 || x == W - 2 || y == H - 2) v = 0;
-      h[c] = v;
-    }
-}
 
 struct DeviceGuard {
   int prev = 0;
@@ -210,116 +148,621 @@ struct DeviceGuard {
   ~DeviceGuard() { cudaSetDevice(prev); }
 };
 
-int check_model(const fs_model *m) {
-  if (!m) return set_error(FS_ERR_ARG, "model is NULL");
-  return FS_OK;
+void free_batch(fs_batch *b) {
+  if (!b) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  void *bufs[] = {b->h, b->rec, b->mask, b->pdir, b->nd, b->ent, b->kid, b->amb, b->amb_r,
+                  b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles};
+  for (void *x : bufs) cudaFree(x);
+  for (double *t : b->tab) cudaFree(t);
+  if (b->h_ctl) cudaFreeHost(b->h_ctl);
+  if (b->h_rctl) cudaFreeHost(b->h_rctl);
+  for (auto &e : b->ev) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  cudaSetDevice(prev);
+  delete b;
 }
 
-// Reads the device status word and converts it to an ABI status.
-int collect_status(fs_model *m) {
-  FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  const int err = m->h_ctl->err;
-  if (err != 0)
-    return set_error(err, "timestep failed: %s (phase %d)", status_name(err), m->h_ctl->err_detail);
-  return FS_OK;
-}
-
-fs::WalkArgs walk_args(const fs_model *m, int do_erode) {
-  fs::WalkArgs a{};
-  a.h = m->d_h;
-  a.mask = m->d_mask;
-  a.ent = m->d_ent;
-  a.pdir = m->d_pdir;
-  a.nd = m->d_nd;
-  a.kid = m->d_kid;
-  a.acc = m->d_acc;
-  a.lvl_off = m->d_lvl;
-  a.tab = m->d_tab;
-  a.tab_cap = m->tab_cap;
-  a.ctl = m->d_ctl;
-  a.W = m->W;
-  a.size = m->size;
-  a.u_dt = do_erode ? m->u_dt : 0.0;
-  a.neq = m->p.neq;
-  a.tol = m->p.tol;
-  std::memcpy(&a.tol_bits, &m->p.tol, 8);
-  a.tol_lo_f = fs::tol_lower_float(m->p.tol);
-  a.nring = m->nring;
-  a.nmode = m->nmode;
-  a.do_erode = do_erode;
-  a.stamp = m->timing ? 1 : 0;
-  a.timeout_ns = m->timeout_ns;
-  return a;
-}
-
-// One timestep: receivers -> donors/level 0 -> level walk. With timing on,
-// events ev[3i..3i+3] bracket the three launches of timestep i.
-int one_step(fs_model *m, int i) {
-  const fs::StepGeom g{m->W, m->H, m->size};
-  if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i], m->stream));
-  FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(m->d_ctl) + fs::kCtlResetOffset, 0,
-                          fs::kCtlResetBytes, m->stream));
-  if (m->exact_receivers)
-    FS_CUDA(fs::launch_receivers(m->d_h, m->d_rec, m->d_ctl, g, m->p.dr_orth, m->p.dr_diag,
-                                 m->stream));
-  else
-    FS_CUDA(fs::launch_receivers_fast(m->d_h, m->d_rec, m->d_amb, m->d_ctl, g, m->p.dr_orth,
-                                      m->p.dr_diag, m->stream));
-  if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 1], m->stream));
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_ent, m->d_ctl, g, m->nring,
-                                   m->stream));
-  if (m->timing) FS_CUDA(cudaEventRecord(m->ev[3 * i + 2], m->stream));
-  FS_CUDA(fs::launch_walk(walk_args(m, 1), m->walk_blocks, m->stream));
-  return FS_OK;
-}
-
-int ensure_events(fs_model *m, size_t n) {
-  while (m->ev.size() < n) {
-    cudaEvent_t e;
-    FS_CUDA(cudaEventCreate(&e));
-    m->ev.push_back(e);
-  }
-  return FS_OK;
-}
-
-int harvest_events(fs_model *m, int k) {
-  FS_CUDA(cudaEventSynchronize(m->ev[3 * k]));
-  for (int i = 0; i < k; i++) {
-    for (int j = 0; j < 3; j++) {
-      float ms = 0;
-      FS_CUDA(cudaEventElapsedTime(&ms, m->ev[3 * i + j], m->ev[3 * i + j + 1]));
-      m->phase_ms[j] += ms;
-    }
-  }
-  float tot = 0;
-  FS_CUDA(cudaEventElapsedTime(&tot, m->ev[0], m->ev[3 * k]));
-  m->phase_ms[3] += tot;
-  return FS_OK;
-}
-
-// Makes the erosion table cover every drainage count below `need`+1
-// (doubling, capped at the grid size + 1).
-int grow_table(fs_model *m, long long need) {
-  long long cap = std::max<long long>(m->tab_cap, 1);
+// Erosion table of realization r for counts [0, cap), cap from doubling
+// until it exceeds `need`, at most size_r + 1. Evaluated on the host with
+// the C library's pow in the order of fastscape_RB.cpp:315 (the reference's
+// accum[c] is k*cell_area exactly: integer multiples summed below 2^53), so
+// the device sees the reference's bits. Parallel over host threads.
+int grow_table(fs_batch *b, int r, long long need) {
+  long long cap = std::max<long long>(b->tab_cap[r], 1);
   while (cap <= need) cap *= 2;
-  cap = std::min<long long>(cap, static_cast<long long>(m->size) + 1);
-  if (cap <= m->tab_cap) return set_error(FS_ERR_CUDA, "erosion table cannot grow past %d", m->tab_cap);
+  cap = std::min<long long>(cap, static_cast<long long>(b->size[r]) + 1);
+  if (cap <= b->tab_cap[r])
+    return set_error(FS_ERR_CUDA, "erosion table of realization %d cannot grow past %d", r,
+                     b->tab_cap[r]);
   std::vector<double> host(static_cast<size_t>(cap) * fs::kTabStride);
-  fill_table(m->p, 0, cap, host.data());
+  const fs_params &p = b->p[r];
+  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(nt, 64);
+  if (cap < 65536 * 2) nt = 1;
+  auto work = [&](unsigned t) {
+    const long long lo = cap * t / nt, hi = cap * (t + 1) / nt;
+    fs::fill_table_range(p.keq, p.neq, p.meq, p.dt, p.dr_orth, p.dr_diag, p.cell_area, lo, hi,
+                         host.data() + lo * fs::kTabStride);
+  };
+  if (nt == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
+  }
   double *d = nullptr;
   FS_CUDA(cudaMalloc(&d, host.size() * sizeof(double)));
-  cudaError_t e = cudaMemcpyAsync(d, host.data(), host.size() * sizeof(double),
-                                  cudaMemcpyHostToDevice, m->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  cudaError_t e =
+      cudaMemcpyAsync(d, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) {
     cudaFree(d);
     return cuda_error(e, "upload(erosion table)");
   }
-  cudaFree(m->d_tab);
-  m->d_tab = d;
-  m->tab_cap = static_cast<int>(cap);
+  cudaFree(b->tab[r]);
+  b->tab[r] = d;
+  b->tab_cap[r] = static_cast<int>(cap);
+  b->desc[r].tab = d;
+  b->desc[r].tab_cap = static_cast<int>(cap);
+  FS_CUDA(cudaMemcpyAsync(b->d_desc + r, &b->desc[r], sizeof(fs::RealDesc), cudaMemcpyHostToDevice,
+                          b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  b->graph_dirty = true;
   return FS_OK;
+}
+
+// The reference field (fastscape_RB.cpp:111-130 via random.cpp:45-49),
+// generated with the same libstdc++ engine and distribution.
+void reference_field(double *h, int W, int H, uint32_t engine_seed) {
+  std::mt19937 eng(engine_seed);
+  std::uniform_real_distribution<double> d(0.0, 1.0);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      double v = d(eng);
+      if (x == 0 || y == 0 || x == W - 1 || y == H - 1) v = 0;
+      if (x == 1 || y == 1 || x == W - 2 || y == H - 2) v = 0;
+      h[static_cast<size_t>(y) * W + x] = v;
+    }
+}
+
+fs::StepArgs step_args(const fs_batch *b, int do_erode) {
+  fs::StepArgs a{};
+  a.h = b->h;
+  a.rec = b->rec;
+  a.mask = b->mask;
+  a.ent = b->ent;
+  a.pdir = b->pdir;
+  a.nd = b->nd;
+  a.kid = b->kid;
+  a.acc = b->acc;
+  a.amb = b->amb;
+  a.amb_r = b->amb_r;
+  a.lvl_off = b->lvl;
+  a.desc = b->d_desc;
+  a.rctl = b->d_rctl;
+  a.ctl = b->d_ctl;
+  a.nreal = b->n;
+  a.rtiles = b->d_rtiles;
+  a.nrtiles = b->nrtiles;
+  a.dtiles = b->d_dtiles;
+  a.ndtiles = b->ndtiles;
+  a.nmode = b->nmode;
+  a.neq = b->neq;
+  a.do_erode = do_erode;
+  a.stamp = b->timing ? 1 : 0;
+  a.timeout_ns = b->timeout_ns;
+  return a;
+}
+
+// The launches of one timestep (no synchronization).
+cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
+  cudaError_t e = cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
+                                  fs::kCtlResetBytes, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream);
+  if (e == cudaSuccess)
+    e = b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
+                           : fs::launch_receivers_fast(a, b->stream);
+  if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
+  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream);
+  return e;
+}
+
+int ensure_events(fs_batch *b, size_t n) {
+  while (b->ev.size() < n) {
+    cudaEvent_t e;
+    FS_CUDA(cudaEventCreate(&e));
+    b->ev.push_back(e);
+  }
+  return FS_OK;
+}
+
+// One timestep with the phase events ev[3i..3i+3] around its launches.
+int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
+  FS_CUDA(cudaEventRecord(b->ev[3 * i], b->stream));
+  FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
+                          fs::kCtlResetBytes, b->stream));
+  FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
+  FS_CUDA(b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
+                             : fs::launch_receivers_fast(a, b->stream));
+  FS_CUDA(cudaEventRecord(b->ev[3 * i + 1], b->stream));
+  FS_CUDA(fs::launch_donors_level0(a, b->stream));
+  FS_CUDA(cudaEventRecord(b->ev[3 * i + 2], b->stream));
+  FS_CUDA(fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream));
+  return FS_OK;
+}
+
+int harvest_events(fs_batch *b, int k) {
+  FS_CUDA(cudaEventSynchronize(b->ev[3 * k]));
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < 3; j++) {
+      float ms = 0;
+      FS_CUDA(cudaEventElapsedTime(&ms, b->ev[3 * i + j], b->ev[3 * i + j + 1]));
+      b->phase_ms[j] += ms;
+    }
+  float tot = 0;
+  FS_CUDA(cudaEventElapsedTime(&tot, b->ev[0], b->ev[3 * k]));
+  b->phase_ms[3] += tot;
+  return FS_OK;
+}
+
+// Captures one timestep into a CUDA graph (re-captured whenever the
+// launch configuration or a descriptor changes). On any capture failure the
+// batch falls back to direct launches.
+int build_graph(fs_batch *b) {
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  const fs::StepArgs a = step_args(b, 1);
+  cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = launch_step(b, a);
+    e = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    b->use_graph = false;
+  }
+  b->graph_dirty = false;
+  return FS_OK;
+}
+
+int collect_status(fs_batch *b) {
+  FS_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  const int err = b->h_ctl->err;
+  if (err != 0)
+    return set_error(err, "timestep failed: %s (phase %d)", status_name(err), b->h_ctl->err_detail);
+  return FS_OK;
+}
+
+int read_rctl(const fs_batch *b) {
+  FS_CUDA(cudaMemcpyAsync(b->h_rctl, b->d_rctl, sizeof(fs::RealCtl) * b->n, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  return FS_OK;
+}
+
+// k timesteps of every realization; a timestep that outgrew an erosion table
+// stopped before changing h and the rest of the batch did nothing: grow the
+// table and carry on from there.
+int batch_step(fs_batch *b, int k) {
+  if (k < 0) return set_error(FS_ERR_ARG, "step count must be >= 0 (got %d)", k);
+  if (k == 0) return FS_OK;
+  DeviceGuard dg(b->device);
+  int done = 0;
+  while (done < k) {
+    const int batch = k - done;
+    const fs::StepArgs a = step_args(b, 1);
+    FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, fs::kCtlCallResetBytes, b->stream));
+    if (b->timing) {
+      if (int st = ensure_events(b, 3 * static_cast<size_t>(batch) + 1)) return st;
+      for (int i = 0; i < batch; i++)
+        if (int st = timed_step(b, a, i)) return st;
+      FS_CUDA(cudaEventRecord(b->ev[3 * batch], b->stream));
+      if (int st = harvest_events(b, batch)) return st;
+    } else {
+      if (b->use_graph && b->graph_dirty)
+        if (int st = build_graph(b)) return st;
+      for (int i = 0; i < batch; i++) {
+        if (b->use_graph && b->graph)
+          FS_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        else
+          FS_CUDA(launch_step(b, a));
+      }
+    }
+    if (int st = collect_status(b)) return st;
+    const int completed = b->h_ctl->steps_done;
+    done += completed;
+    b->steps += completed;
+    if (completed > 0) b->have_step = true;
+    if (b->h_ctl->abort_k > 0) {
+      if (int st = grow_table(b, b->h_ctl->abort_r, b->h_ctl->abort_k)) return st;
+    } else if (completed != batch) {
+      return set_error(FS_ERR_CUDA, "%d of %d timesteps completed without a status", completed,
+                       batch);
+    }
+  }
+  return FS_OK;
+}
+
+fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_params *params,
+                       int init_mode, const uint64_t *seeds, int *status) {
+  int dummy = 0;
+  if (!status) status = &dummy;
+  *status = FS_OK;
+  if (n < 1 || n > fs::kMaxReal) {
+    *status = set_error(FS_ERR_ARG, "batch size must be in [1, %d] (got %d)", fs::kMaxReal, n);
+    return nullptr;
+  }
+  if (!widths || !heights || !params) {
+    *status = set_error(FS_ERR_ARG, "widths, heights and params must not be NULL");
+    return nullptr;
+  }
+  if (init_mode < FS_INIT_ZERO || init_mode > FS_INIT_PHILOX) {
+    *status = set_error(FS_ERR_ARG, "unknown init_mode %d", init_mode);
+    return nullptr;
+  }
+  long long cells = 0;
+  for (int r = 0; r < n; r++) {
+    if (widths[r] < 3 || heights[r] < 3) {
+      *status = set_error(FS_ERR_ARG, "width and height must be >= 3 (realization %d: %d x %d)", r,
+                          widths[r], heights[r]);
+      return nullptr;
+    }
+    cells += static_cast<long long>(widths[r]) * heights[r];
+    if (!valid_params(params[r])) {
+      *status = set_error(FS_ERR_ARG,
+                          "parameters must be finite, dr and cell_area > 0, tol >= 0 (realization %d)", r);
+      return nullptr;
+    }
+    if (params[r].neq != params[0].neq) {
+      *status = set_error(FS_ERR_ARG, "all realizations of a batch must share n (neq)");
+      return nullptr;
+    }
+  }
+  if (cells + 2ll * n >= (1ll << 31) - 2) {
+    *status = set_error(FS_ERR_ARG, "batch of %lld cells exceeds 2^31-2", cells);
+    return nullptr;
+  }
+  fs_batch *b = new (std::nothrow) fs_batch();
+  if (!b) {
+    *status = set_error(FS_ERR_NOMEM, "host allocation failed");
+    return nullptr;
+  }
+  auto fail = [&](int st) -> fs_batch * {
+    *status = st;
+    free_batch(b);
+    return nullptr;
+  };
+  auto cu = [&](cudaError_t e, const char *what) -> bool {
+    if (e == cudaSuccess) return true;
+    *status = cuda_error(e, what);
+    return false;
+  };
+  b->n = n;
+  b->cells = cells;
+  b->neq = params[0].neq;
+  b->nmode = nmode_of(b->neq);
+  cudaGetDevice(&b->device);
+  long long o = 0, lb = 0;
+  for (int r = 0; r < n; r++) {
+    b->W.push_back(widths[r]);
+    b->H.push_back(heights[r]);
+    b->size.push_back(widths[r] * heights[r]);
+    b->off.push_back(static_cast<int>(o));
+    b->lvl_base.push_back(static_cast<int>(lb));
+    b->nring.push_back(fs::ring_cells(widths[r], heights[r]));
+    b->p.push_back(params[r]);
+    o += b->size.back();
+    lb += b->size.back() + 2;
+  }
+  b->lvl_total = lb;
+  b->tab.assign(n, nullptr);
+  b->tab_cap.assign(n, 0);
+  const size_t C = static_cast<size_t>(cells);
+  if (!cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cu(cudaMalloc(&b->h, C * sizeof(double)), "cudaMalloc(h)") ||
+      !cu(cudaMalloc(&b->rec, C), "cudaMalloc(rec)") ||
+      !cu(cudaMalloc(&b->mask, C), "cudaMalloc(mask)") ||
+      !cu(cudaMalloc(&b->pdir, C), "cudaMalloc(pdir)") ||
+      !cu(cudaMalloc(&b->nd, C), "cudaMalloc(nd)") ||
+      !cu(cudaMalloc(&b->ent, C * sizeof(int32_t)), "cudaMalloc(ent)") ||
+      !cu(cudaMalloc(&b->kid, C * sizeof(int32_t)), "cudaMalloc(kid)") ||
+      !cu(cudaMalloc(&b->amb, C * sizeof(int32_t)), "cudaMalloc(amb)") ||
+      !cu(cudaMalloc(&b->amb_r, C * sizeof(int32_t)), "cudaMalloc(amb_r)") ||
+      !cu(cudaMalloc(&b->acc, C * sizeof(uint32_t)), "cudaMalloc(acc)") ||
+      !cu(cudaMalloc(&b->lvl, static_cast<size_t>(lb) * sizeof(int32_t)), "cudaMalloc(lvl)") ||
+      !cu(cudaMalloc(&b->d_desc, n * sizeof(fs::RealDesc)), "cudaMalloc(desc)") ||
+      !cu(cudaMalloc(&b->d_rctl, n * sizeof(fs::RealCtl)), "cudaMalloc(rctl)") ||
+      !cu(cudaMalloc(&b->d_ctl, sizeof(fs::Ctl)), "cudaMalloc(ctl)") ||
+      !cu(cudaMallocHost(&b->h_ctl, sizeof(fs::Ctl)), "cudaMallocHost(ctl)") ||
+      !cu(cudaMallocHost(&b->h_rctl, n * sizeof(fs::RealCtl)), "cudaMallocHost(rctl)"))
+    return fail(*status);
+  // Rings keep NO_FLOW forever (fastscape_RB.cpp:361-362) and ring-0 cells
+  // never have donors: receivers and masks are written for the interior only.
+  if (!cu(cudaMemsetAsync(b->rec, 0xff, C, b->stream), "memset(rec)") ||
+      !cu(cudaMemsetAsync(b->mask, 0, C, b->stream), "memset(mask)") ||
+      !cu(cudaMemsetAsync(b->acc, 0, C * sizeof(uint32_t), b->stream), "memset(acc)") ||
+      !cu(cudaMemsetAsync(b->lvl, 0, static_cast<size_t>(lb) * sizeof(int32_t), b->stream),
+          "memset(lvl)") ||
+      !cu(cudaMemsetAsync(b->d_rctl, 0, n * sizeof(fs::RealCtl), b->stream), "memset(rctl)") ||
+      !cu(cudaMemsetAsync(b->d_ctl, 0, sizeof(fs::Ctl), b->stream), "memset(ctl)"))
+    return fail(*status);
+  // Descriptors; the erosion tables start at min(65536, size+1) records.
+  b->desc.resize(n);
+  for (int r = 0; r < n; r++) {
+    fs::RealDesc &d = b->desc[r];
+    const fs_params &p = b->p[r];
+    d = fs::RealDesc{};
+    d.W = b->W[r];
+    d.H = b->H[r];
+    d.size = b->size[r];
+    d.off = b->off[r];
+    d.lvl_base = b->lvl_base[r];
+    d.nring = b->nring[r];
+    d.u_dt = p.ueq * p.dt;
+    d.tol = p.tol;
+    std::memcpy(&d.tol_bits, &p.tol, sizeof(double));
+    d.tol_lo_f = fs::tol_lower_float(p.tol);
+    d.g_orth = static_cast<float>(1.0 / p.dr_orth);
+    d.g_diag = static_cast<float>(1.0 / p.dr_diag);
+    d.gmax = std::max(d.g_orth, d.g_diag);
+    d.dr_orth = p.dr_orth;
+    d.dr_diag = p.dr_diag;
+  }
+  if (!cu(cudaMemcpyAsync(b->d_desc, b->desc.data(), n * sizeof(fs::RealDesc),
+                          cudaMemcpyHostToDevice, b->stream),
+          "upload(desc)"))
+    return fail(*status);
+  for (int r = 0; r < n; r++)
+    if (int st = grow_table(b, r, std::min<long long>(b->size[r], 65535))) return fail(st);
+  // Stencil tiles of every realization.
+  {
+    std::vector<fs::Tile> rt, dt;
+    for (int r = 0; r < n; r++) {
+      for (int kind = 0; kind < 2; kind++) {
+        std::vector<fs::Tile> &v = kind == 0 ? rt : dt;
+        const size_t at = v.size();
+        v.resize(at + static_cast<size_t>(b->W[r] / 32 + 2) * (b->H[r] / 32 + 2));
+        const int got = fs::append_tiles(kind, r, b->W[r], b->H[r], v.data() + at,
+                                         static_cast<int>(v.size() - at));
+        v.resize(at + std::max(got, 0));
+      }
+    }
+    b->nrtiles = static_cast<int>(rt.size());
+    b->ndtiles = static_cast<int>(dt.size());
+    if (!cu(cudaMalloc(&b->d_rtiles, std::max<size_t>(1, rt.size()) * sizeof(fs::Tile)),
+            "cudaMalloc(rtiles)") ||
+        !cu(cudaMalloc(&b->d_dtiles, std::max<size_t>(1, dt.size()) * sizeof(fs::Tile)),
+            "cudaMalloc(dtiles)") ||
+        (!rt.empty() && !cu(cudaMemcpyAsync(b->d_rtiles, rt.data(), rt.size() * sizeof(fs::Tile),
+                                            cudaMemcpyHostToDevice, b->stream),
+                            "upload(rtiles)")) ||
+        (!dt.empty() && !cu(cudaMemcpyAsync(b->d_dtiles, dt.data(), dt.size() * sizeof(fs::Tile),
+                                            cudaMemcpyHostToDevice, b->stream),
+                            "upload(dtiles)")) ||
+        !cu(cudaStreamSynchronize(b->stream), "sync"))
+      return fail(*status);
+  }
+  // Rings 0 and 1 are the head of level 0 in every timestep; initial fields.
+  std::vector<double> host;
+  for (int r = 0; r < n; r++) {
+    if (!cu(fs::launch_place_rings(b->ent + b->off[r], b->W[r], b->H[r], b->stream), "rings"))
+      return fail(*status);
+    const uint64_t seed = seeds ? seeds[r] : 0;
+    double *hr = b->h + b->off[r];
+    if (init_mode == FS_INIT_REFERENCE || init_mode == FS_INIT_MT19937) {
+      host.resize(b->size[r]);
+      const uint32_t es = init_mode == FS_INIT_REFERENCE ? static_cast<uint32_t>(seed * 0u)
+                                                         : static_cast<uint32_t>(seed);
+      reference_field(host.data(), b->W[r], b->H[r], es);
+      if (!cu(cudaMemcpyAsync(hr, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice,
+                              b->stream),
+              "upload(h)") ||
+          !cu(cudaStreamSynchronize(b->stream), "sync"))
+        return fail(*status);
+    } else if (init_mode == FS_INIT_PHILOX) {
+      if (!cu(fs::launch_philox_field(hr, b->W[r], b->H[r], seed, b->stream), "philox"))
+        return fail(*status);
+    } else if (!cu(cudaMemsetAsync(hr, 0, b->size[r] * sizeof(double), b->stream), "memset(h)")) {
+      return fail(*status);
+    }
+  }
+  int occ = 0;
+  if (!cu(fs::prepare_walk_kernels(), "walk smem attribute") ||
+      !cu(cudaDeviceGetAttribute(&b->walk_sms, cudaDevAttrMultiProcessorCount, b->device), "attr") ||
+      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(b->nmode),
+                                                        fs::walk_threads(),
+                                                        fs::walk_smem_bytes(n)),
+          "occupancy"))
+    return fail(*status);
+  if (occ < 1) return fail(set_error(FS_ERR_CUDA, "walk kernel cannot be resident"));
+  b->walk_occ = occ;
+  b->walk_bps = std::min(occ, 2);
+  if (!cu(cudaStreamSynchronize(b->stream), "sync")) return fail(*status);
+  return b;
+}
+
+int check_r(const fs_batch *b, int r) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (r < 0 || r >= b->n) return set_error(FS_ERR_ARG, "realization %d out of range [0, %d)", r, b->n);
+  return FS_OK;
+}
+
+int get_elevation(const fs_batch *b, int r, double *out) {
+  if (int st = check_r(b, r)) return st;
+  if (!out) return set_error(FS_ERR_ARG, "out is NULL");
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemcpyAsync(out, b->h + b->off[r], sizeof(double) * b->size[r], cudaMemcpyDeviceToHost,
+                          b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  return FS_OK;
+}
+
+int set_elevation(fs_batch *b, int r, const double *in) {
+  if (int st = check_r(b, r)) return st;
+  if (!in) return set_error(FS_ERR_ARG, "in is NULL");
+  DeviceGuard dg(b->device);
+  double *hr = b->h + b->off[r];
+  FS_CUDA(cudaMemcpyAsync(hr, in, sizeof(double) * b->size[r], cudaMemcpyHostToDevice, b->stream));
+  FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, fs::kCtlCallResetBytes, b->stream));
+  FS_CUDA(fs::launch_check_finite(hr, b->size[r], b->d_ctl, b->stream));
+  const int st = collect_status(b);
+  if (st == FS_ERR_NONFINITE)
+    return set_error(FS_ERR_NONFINITE, "set_elevation: input holds NaN or Inf");
+  return st;
+}
+
+int get_accumulation(const fs_batch *b, int r, double *out) {
+  if (int st = check_r(b, r)) return st;
+  if (!out) return set_error(FS_ERR_ARG, "out is NULL");
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  const int n = b->size[r];
+  std::vector<uint32_t> acc(n);
+  std::vector<int32_t> ent(n);
+  FS_CUDA(cudaMemcpyAsync(acc.data(), b->acc + b->off[r], sizeof(uint32_t) * n,
+                          cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaMemcpyAsync(ent.data(), b->ent + b->off[r], sizeof(int32_t) * n,
+                          cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < n; i++) out[ent[i]] = static_cast<double>(acc[i]) * b->p[r].cell_area;
+  return FS_OK;
+}
+
+int get_receivers(const fs_batch *b, int r, int32_t *dir) {
+  if (int st = check_r(b, r)) return st;
+  if (!dir) return set_error(FS_ERR_ARG, "dir is NULL");
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  std::vector<int8_t> v(b->size[r]);
+  FS_CUDA(cudaMemcpyAsync(v.data(), b->rec + b->off[r], b->size[r], cudaMemcpyDeviceToHost,
+                          b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->size[r]; i++) dir[i] = v[i] < 0 ? FS_NO_FLOW : v[i];
+  return FS_OK;
+}
+
+int get_levels(const fs_batch *b, int r, int32_t *level_id, int32_t *nlevels) {
+  if (int st = check_r(b, r)) return st;
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  if (int st = read_rctl(b)) return st;
+  const int nl = b->h_rctl[r].nlevels;
+  if (nlevels) *nlevels = nl;
+  if (!level_id) return FS_OK;
+  const int n = b->size[r];
+  std::vector<int32_t> ent(n), off(nl + 1);
+  FS_CUDA(cudaMemcpyAsync(ent.data(), b->ent + b->off[r], sizeof(int32_t) * n,
+                          cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaMemcpyAsync(off.data(), b->lvl + b->lvl_base[r], sizeof(int32_t) * (nl + 1),
+                          cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < n; i++) level_id[i] = -1;
+  for (int L = 0; L < nl; L++)
+    for (int s = off[L]; s < off[L + 1]; s++) level_id[ent[s]] = L;
+  return FS_OK;
+}
+
+int get_donor_mask(const fs_batch *b, int r, uint8_t *mask) {
+  if (int st = check_r(b, r)) return st;
+  if (!mask) return set_error(FS_ERR_ARG, "mask is NULL");
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemcpyAsync(mask, b->mask + b->off[r], b->size[r], cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  return FS_OK;
+}
+
+int get_phase_times(const fs_batch *b, double *ms, int reset) {
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  if (ms) {
+    for (int i = 0; i < 4; i++) ms[i] = b->phase_ms[i];
+    for (int i = 0; i < 3; i++) ms[4 + i] = b->h_ctl->walk_ns[i] * 1e-6;
+  }
+  if (reset) {
+    for (double &x : const_cast<fs_batch *>(b)->phase_ms) x = 0;
+    FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + offsetof(fs::Ctl, walk_ns), 0,
+                            sizeof(b->h_ctl->walk_ns), b->stream));
+    FS_CUDA(cudaStreamSynchronize(b->stream));
+  }
+  return FS_OK;
+}
+
+// Autotuner: times each candidate launch configuration -- walk blocks per SM
+// (1 .. occupancy limit, at most 2) with and without the captured graph --
+// on the batch's own state over `probe` timesteps, restoring the elevation
+// after every probe, and keeps the fastest.
+int autotune(fs_batch *b, int probe, int *chosen) {
+  DeviceGuard dg(b->device);
+  double *save = nullptr;
+  FS_CUDA(cudaMalloc(&save, b->cells * sizeof(double)));
+  auto release = [&]() { cudaFree(save); };
+  cudaError_t e = cudaMemcpyAsync(save, b->h, b->cells * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  b->stream);
+  if (e != cudaSuccess) {
+    release();
+    return cuda_error(e, "autotune save");
+  }
+  const bool timing = b->timing;
+  const long long steps = b->steps;
+  b->timing = false;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int best_bps = b->walk_bps;
+  bool best_graph = false;
+  int st = FS_OK;
+  for (int bps = 1; bps <= std::min(b->walk_occ, 2) && st == FS_OK; bps++) {
+    for (int gr = 0; gr < 2 && st == FS_OK; gr++) {
+      b->walk_bps = bps;
+      b->use_graph = gr == 1;
+      b->graph_dirty = true;
+      if ((st = batch_step(b, 1)) != FS_OK) break;  // warm (and build the graph)
+      cudaEventRecord(e0, b->stream);
+      if ((st = batch_step(b, probe)) != FS_OK) break;
+      cudaEventRecord(e1, b->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_bps = bps;
+        best_graph = gr == 1 && b->use_graph;
+      }
+      cudaMemcpyAsync(b->h, save, b->cells * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(b->stream);
+  release();
+  b->timing = timing;
+  b->steps = steps;
+  b->walk_bps = best_bps;
+  b->use_graph = best_graph;
+  b->graph_dirty = true;
+  if (chosen) {
+    chosen[0] = best_bps;
+    chosen[1] = best_graph ? 1 : 0;
+  }
+  return st;
 }
 
 }  // namespace
@@ -352,17 +795,18 @@ void fs_params_workload(fs_params *out, double dx) {
   out->cell_area = dx * dx;
 }
 
-fs_model *fs_create(int width, int height, const fs_params *params, int init_mode,
-                    uint64_t seed, int *status) {
+// ---- single model: a batch of one ----------------------------------------
+
+fs_model *fs_create(int width, int height, const fs_params *params, int init_mode, uint64_t seed,
+                    int *status) {
   int dummy = 0;
   if (!status) status = &dummy;
-  *status = FS_OK;
   if (width < 3 || height < 3) {
     *status = set_error(FS_ERR_ARG, "width and height must be >= 3 (got %d x %d)", width, height);
     return nullptr;
   }
-  if ((long long)width * height >= (1ll << 31) - 2) {
-    *status = set_error(FS_ERR_ARG, "grid of %lld cells exceeds 2^31-2", (long long)width * height);
+  if ((long long)width * height >= (1ll << 31) - 4) {
+    *status = set_error(FS_ERR_ARG, "grid of %lld cells exceeds 2^31-4", (long long)width * height);
     return nullptr;
   }
   fs_params p;
@@ -370,7 +814,7 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
     p = *params;
   else
     fs_params_workload(&p, 100.0);
-  if (!finite_params(p)) {
+  if (!valid_params(p)) {
     *status = set_error(FS_ERR_ARG, "parameters must be finite, dr and cell_area > 0, tol >= 0");
     return nullptr;
   }
@@ -383,277 +827,114 @@ fs_model *fs_create(int width, int height, const fs_params *params, int init_mod
     *status = set_error(FS_ERR_NOMEM, "host allocation failed");
     return nullptr;
   }
-  m->W = width;
-  m->H = height;
-  m->size = width * height;
-  m->p = p;
-  m->u_dt = p.ueq * p.dt;
-  m->nmode = (p.neq == 1.0) ? fs::kNOne : (p.neq == 2.0) ? fs::kNTwo : fs::kNGeneral;
-  cudaGetDevice(&m->device);
-  auto fail = [&](int st) -> fs_model * {
-    *status = st;
-    free_model(m);
+  m->b = batch_create(1, &width, &height, &p, init_mode, &seed, status);
+  if (!m->b) {
+    delete m;
     return nullptr;
-  };
-  auto cu = [&](cudaError_t e, const char *what) -> bool {
-    if (e == cudaSuccess) return true;
-    *status = cuda_error(e, what);
-    return false;
-  };
-  const size_t n = static_cast<size_t>(m->size);
-  if (!cu(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
-      !cu(cudaMalloc(&m->d_h, n * sizeof(double)), "cudaMalloc(h)") ||
-      !cu(cudaMalloc(&m->d_rec, n), "cudaMalloc(rec)") ||
-      !cu(cudaMalloc(&m->d_mask, n), "cudaMalloc(mask)") ||
-      !cu(cudaMalloc(&m->d_ent, n * sizeof(int32_t)), "cudaMalloc(ent)") ||
-      !cu(cudaMalloc(&m->d_pdir, n), "cudaMalloc(pdir)") ||
-      !cu(cudaMalloc(&m->d_nd, n), "cudaMalloc(nd)") ||
-      !cu(cudaMalloc(&m->d_kid, n * sizeof(int32_t)), "cudaMalloc(kid)") ||
-      !cu(cudaMalloc(&m->d_amb, n * sizeof(int32_t)), "cudaMalloc(amb)") ||
-      !cu(cudaMalloc(&m->d_lvl, (n + 2) * sizeof(int32_t)), "cudaMalloc(lvl)") ||
-      !cu(cudaMalloc(&m->d_acc, n * sizeof(uint32_t)), "cudaMalloc(acc)") ||
-      !cu(cudaMalloc(&m->d_ctl, sizeof(fs::Ctl)), "cudaMalloc(ctl)") ||
-      !cu(cudaMallocHost(&m->h_ctl, sizeof(fs::Ctl)), "cudaMallocHost(ctl)"))
-    return fail(*status);
-  // Rings keep NO_FLOW forever (fastscape_RB.cpp:361-362): receivers are
-  // only ever written for interior cells.
-  if (!cu(cudaMemsetAsync(m->d_rec, 0xff, n, m->stream), "memset(rec)") ||
-      !cu(cudaMemsetAsync(m->d_mask, 0, n, m->stream), "memset(mask)") ||
-      !cu(cudaMemsetAsync(m->d_acc, 0, n * sizeof(uint32_t), m->stream), "memset(acc)") ||
-      !cu(cudaMemsetAsync(m->d_lvl, 0, (n + 2) * sizeof(int32_t), m->stream), "memset(lvl)") ||
-      !cu(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream), "memset(ctl)"))
-    return fail(*status);
-
-  if (int st = grow_table(m, std::min<long long>(m->size, 65535))) return fail(st);
-  {
-    // Rings 0 and 1 never get a receiver: they are the head of level 0 in
-    // every timestep, in ascending order, written once here.
-    std::vector<int32_t> ring;
-    for (int y = 0; y < m->H; y++)
-      for (int x = 0; x < m->W; x++)
-        if (x <= 1 || y <= 1 || x >= m->W - 2 || y >= m->H - 2) ring.push_back(y * m->W + x);
-    m->nring = static_cast<int>(ring.size());
-    if (!cu(cudaMemcpyAsync(m->d_ent, ring.data(), ring.size() * sizeof(int32_t),
-                            cudaMemcpyHostToDevice, m->stream), "upload(ring)") ||
-        !cu(cudaStreamSynchronize(m->stream), "sync"))
-      return fail(*status);
   }
-
-  const fs::StepGeom g{m->W, m->H, m->size};
-  if (init_mode == FS_INIT_REFERENCE || init_mode == FS_INIT_MT19937) {
-    std::vector<double> h;
-    const uint32_t es = (init_mode == FS_INIT_REFERENCE) ? static_cast<uint32_t>(seed * 0u)
-                                                         : static_cast<uint32_t>(seed);
-    reference_field(h, m->W, m->H, es);
-    if (!cu(cudaMemcpyAsync(m->d_h, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, m->stream),
-            "upload(h)") ||
-        !cu(cudaStreamSynchronize(m->stream), "sync"))
-      return fail(*status);
-  } else if (init_mode == FS_INIT_PHILOX) {
-    if (!cu(fs::launch_philox_field(m->d_h, g, seed, m->stream), "philox"))
-      return fail(*status);
-  } else {
-    if (!cu(cudaMemsetAsync(m->d_h, 0, n * sizeof(double), m->stream), "memset(h)"))
-      return fail(*status);
-  }
-
-  int occ = 0, sms = 0;
-  if (!cu(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device), "attr") ||
-      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(m->nmode),
-                                                        fs::walk_threads(), 0),
-          "occupancy"))
-    return fail(*status);
-  if (occ < 1) return fail(set_error(FS_ERR_CUDA, "walk kernel cannot be resident"));
-  m->walk_blocks = sms * std::min(occ, 2);
-  if (!cu(cudaStreamSynchronize(m->stream), "sync")) return fail(*status);
   return m;
 }
 
-void fs_destroy(fs_model *m) { free_model(m); }
+void fs_destroy(fs_model *m) {
+  if (!m) return;
+  free_batch(m->b);
+  delete m;
+}
+
+#define FS_MODEL(m)                                           \
+  if (!(m) || !(m)->b) return set_error(FS_ERR_ARG, "model is NULL")
 
 int fs_step(fs_model *m, int k) {
-  if (int st = check_model(m)) return st;
-  if (k < 0) return set_error(FS_ERR_ARG, "step count must be >= 0 (got %d)", k);
-  if (k == 0) return FS_OK;
-  DeviceGuard dg(m->device);
-  int done = 0;
-  while (done < k) {
-    const int batch = k - done;
-    if (m->timing)
-      if (int st = ensure_events(m, 3 * static_cast<size_t>(batch) + 1)) return st;
-    FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, fs::kCtlCallResetBytes, m->stream));
-    for (int i = 0; i < batch; i++) {
-      if (int st = one_step(m, i)) return st;
-    }
-    if (m->timing) {
-      FS_CUDA(cudaEventRecord(m->ev[3 * batch], m->stream));
-      if (int st = harvest_events(m, batch)) return st;
-    }
-    if (int st = collect_status(m)) return st;
-    const int completed = m->h_ctl->steps_done;
-    done += completed;
-    m->steps += completed;
-    if (completed > 0) m->have_step = true;
-    if (m->h_ctl->abort_k > 0) {
-      // A drainage count outgrew the erosion table; that timestep stopped
-      // before changing h and the remaining ones did nothing. Grow and redo.
-      if (int st = grow_table(m, m->h_ctl->abort_k)) return st;
-    } else if (completed != batch) {
-      return set_error(FS_ERR_CUDA, "%d of %d timesteps completed without a status", completed,
-                       batch);
-    }
-  }
-  return FS_OK;
+  FS_MODEL(m);
+  return batch_step(m->b, k);
 }
 
 int fs_run(fs_model *m, int nstep) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (nstep < -1) return set_error(FS_ERR_ARG, "nstep must be >= -1 (got %d)", nstep);
-  return fs_step(m, nstep + 1);
+  return batch_step(m->b, nstep + 1);
 }
 
 int fs_get_elevation(const fs_model *m, double *out) {
-  if (int st = check_model(m)) return st;
-  if (!out) return set_error(FS_ERR_ARG, "out is NULL");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(out, m->d_h, sizeof(double) * m->size, cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  return FS_OK;
+  FS_MODEL(m);
+  return get_elevation(m->b, 0, out);
 }
 
 int fs_set_elevation(fs_model *m, const double *in) {
-  if (int st = check_model(m)) return st;
-  if (!in) return set_error(FS_ERR_ARG, "in is NULL");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(m->d_h, in, sizeof(double) * m->size, cudaMemcpyHostToDevice, m->stream));
-  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, fs::kCtlCallResetBytes, m->stream));
-  FS_CUDA(fs::launch_check_finite(m->d_h, m->size, m->d_ctl, m->stream));
-  const int st = collect_status(m);
-  if (st == FS_ERR_NONFINITE)
-    return set_error(FS_ERR_NONFINITE, "fs_set_elevation: input holds NaN or Inf");
-  return st;
+  FS_MODEL(m);
+  return set_elevation(m->b, 0, in);
 }
 
 int fs_get_accumulation(const fs_model *m, double *out) {
-  if (int st = check_model(m)) return st;
-  if (!out) return set_error(FS_ERR_ARG, "out is NULL");
-  if (!m->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
-  DeviceGuard dg(m->device);
-  std::vector<uint32_t> acc(m->size);
-  std::vector<int32_t> ent(m->size);
-  FS_CUDA(cudaMemcpyAsync(acc.data(), m->d_acc, sizeof(uint32_t) * m->size, cudaMemcpyDeviceToHost,
-                          m->stream));
-  FS_CUDA(cudaMemcpyAsync(ent.data(), m->d_ent, sizeof(int32_t) * m->size, cudaMemcpyDeviceToHost,
-                          m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  for (int i = 0; i < m->size; i++) out[ent[i]] = static_cast<double>(acc[i]) * m->p.cell_area;
-  return FS_OK;
+  FS_MODEL(m);
+  return get_accumulation(m->b, 0, out);
 }
 
 int fs_get_receivers(const fs_model *m, int32_t *dir) {
-  if (int st = check_model(m)) return st;
-  if (!dir) return set_error(FS_ERR_ARG, "dir is NULL");
-  if (!m->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
-  DeviceGuard dg(m->device);
-  std::vector<int8_t> r(m->size);
-  FS_CUDA(cudaMemcpyAsync(r.data(), m->d_rec, m->size, cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  for (int i = 0; i < m->size; i++) dir[i] = r[i] < 0 ? FS_NO_FLOW : r[i];
-  return FS_OK;
+  FS_MODEL(m);
+  return get_receivers(m->b, 0, dir);
 }
 
 int fs_get_receiver_index(const fs_model *m, int64_t *idx) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!idx) return set_error(FS_ERR_ARG, "idx is NULL");
-  std::vector<int32_t> dir(m->size);
-  if (int st = fs_get_receivers(m, dir.data())) return st;
-  const long long W = m->W;
+  const fs_batch *b = m->b;
+  std::vector<int32_t> dir(b->size[0]);
+  if (int st = get_receivers(b, 0, dir.data())) return st;
+  const long long W = b->W[0];
   const long long off[8] = {-1, -W - 1, -W, -W + 1, 1, W + 1, W, W - 1};
-  for (int i = 0; i < m->size; i++) idx[i] = dir[i] < 0 ? i : i + off[dir[i]];
+  for (int i = 0; i < b->size[0]; i++) idx[i] = dir[i] < 0 ? i : i + off[dir[i]];
   return FS_OK;
 }
 
 int fs_get_levels(const fs_model *m, int32_t *level_id, int32_t *nlevels) {
-  if (int st = check_model(m)) return st;
-  if (!m->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  const int nl = m->h_ctl->nlevels;
-  if (nlevels) *nlevels = nl;
-  if (!level_id) return FS_OK;
-  std::vector<int32_t> stack(m->size), off(nl + 1);
-  FS_CUDA(cudaMemcpyAsync(stack.data(), m->d_ent, sizeof(int32_t) * m->size,
-                          cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaMemcpyAsync(off.data(), m->d_lvl, sizeof(int32_t) * (nl + 1), cudaMemcpyDeviceToHost,
-                          m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  for (int i = 0; i < m->size; i++) level_id[i] = -1;
-  for (int L = 0; L < nl; L++)
-    for (int s = off[L]; s < off[L + 1]; s++) level_id[stack[s]] = L;
-  return FS_OK;
+  FS_MODEL(m);
+  return get_levels(m->b, 0, level_id, nlevels);
 }
 
 int fs_get_donor_mask(const fs_model *m, uint8_t *mask) {
-  if (int st = check_model(m)) return st;
-  if (!mask) return set_error(FS_ERR_ARG, "mask is NULL");
-  if (!m->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(mask, m->d_mask, m->size, cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  return FS_OK;
+  FS_MODEL(m);
+  return get_donor_mask(m->b, 0, mask);
 }
 
 int fs_get_shape(const fs_model *m, int *width, int *height) {
-  if (int st = check_model(m)) return st;
-  if (width) *width = m->W;
-  if (height) *height = m->H;
+  FS_MODEL(m);
+  if (width) *width = m->b->W[0];
+  if (height) *height = m->b->H[0];
   return FS_OK;
 }
 
 int fs_get_params(const fs_model *m, fs_params *out) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!out) return set_error(FS_ERR_ARG, "out is NULL");
-  *out = m->p;
+  *out = m->b->p[0];
   return FS_OK;
 }
 
-int64_t fs_steps_executed(const fs_model *m) { return m ? m->steps : -1; }
+int64_t fs_steps_executed(const fs_model *m) { return m && m->b ? m->b->steps : -1; }
 
 int fs_set_timing(fs_model *m, int enable) {
-  if (int st = check_model(m)) return st;
-  m->timing = enable != 0;
+  FS_MODEL(m);
+  m->b->timing = enable != 0;
   return FS_OK;
 }
 
 int fs_get_phase_times(const fs_model *m, double *ms, int reset) {
-  if (int st = check_model(m)) return st;
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  if (ms) {
-    for (int i = 0; i < 4; i++) ms[i] = m->phase_ms[i];
-    for (int i = 0; i < 3; i++) ms[4 + i] = m->h_ctl->walk_ns[i] * 1e-6;
-  }
-  if (reset) {
-    for (double &x : const_cast<fs_model *>(m)->phase_ms) x = 0;
-    FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(m->d_ctl) + offsetof(fs::Ctl, walk_ns), 0,
-                            sizeof(m->h_ctl->walk_ns), m->stream));
-    FS_CUDA(cudaStreamSynchronize(m->stream));
-  }
-  return FS_OK;
+  FS_MODEL(m);
+  return get_phase_times(m->b, ms, reset);
 }
 
 int fs_set_barrier_timeout(fs_model *m, double ms) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!(ms > 0) || ms > 3.6e6) return set_error(FS_ERR_ARG, "timeout must be in (0, 3.6e6] ms");
-  m->timeout_ns = static_cast<unsigned long long>(ms * 1e6);
+  m->b->timeout_ns = static_cast<unsigned long long>(ms * 1e6);
+  m->b->graph_dirty = true;
   return FS_OK;
 }
 
 int fs_synchronize(const fs_model *m) {
-  if (int st = check_model(m)) return st;
-  FS_CUDA(cudaStreamSynchronize(m->stream));
+  FS_MODEL(m);
+  FS_CUDA(cudaStreamSynchronize(m->b->stream));
   return FS_OK;
 }
 
@@ -666,7 +947,79 @@ size_t fs_last_error(char *buf, size_t n) {
   return g_last_error.size();
 }
 
-const char *fs_version(void) { return "fastscape-gb300 0.1 (sm_103a)"; }
+const char *fs_version(void) { return "fastscape-gb300 0.2 (sm_103a)"; }
+
+// ---- batches ------------------------------------------------------------
+
+fs_batch *fs_batch_create(int n, const int *widths, const int *heights, const fs_params *params,
+                          int init_mode, const uint64_t *seeds, int *status) {
+  return batch_create(n, widths, heights, params, init_mode, seeds, status);
+}
+
+void fs_batch_destroy(fs_batch *b) { free_batch(b); }
+
+int fs_batch_step(fs_batch *b, int k) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  return batch_step(b, k);
+}
+
+int fs_batch_run(fs_batch *b, int nstep) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (nstep < -1) return set_error(FS_ERR_ARG, "nstep must be >= -1 (got %d)", nstep);
+  return batch_step(b, nstep + 1);
+}
+
+int fs_batch_get_elevation(const fs_batch *b, int r, double *out) { return get_elevation(b, r, out); }
+
+int fs_batch_set_elevation(fs_batch *b, int r, const double *in) { return set_elevation(b, r, in); }
+
+int fs_batch_get_accumulation(const fs_batch *b, int r, double *out) {
+  return get_accumulation(b, r, out);
+}
+
+int fs_batch_get_receivers(const fs_batch *b, int r, int32_t *dir) { return get_receivers(b, r, dir); }
+
+int fs_batch_get_levels(const fs_batch *b, int r, int32_t *level_id, int32_t *nlevels) {
+  return get_levels(b, r, level_id, nlevels);
+}
+
+int fs_batch_info(const fs_batch *b, int *n, int64_t *cells) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (n) *n = b->n;
+  if (cells) *cells = b->cells;
+  return FS_OK;
+}
+
+int fs_batch_set_timing(fs_batch *b, int enable) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  b->timing = enable != 0;
+  return FS_OK;
+}
+
+int fs_batch_get_phase_times(const fs_batch *b, double *ms, int reset) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  return get_phase_times(b, ms, reset);
+}
+
+int fs_batch_use_graph(fs_batch *b, int enable) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  b->use_graph = enable != 0;
+  b->graph_dirty = true;
+  return FS_OK;
+}
+
+int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (probe_steps < 1 || probe_steps > 100)
+    return set_error(FS_ERR_ARG, "probe_steps must be in [1, 100]");
+  return autotune(b, probe_steps, chosen);
+}
+
+int fs_batch_synchronize(const fs_batch *b) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  return FS_OK;
+}
 
 // ---- testing hooks (declared in include/fastscape_gb300_testing.h) -------
 
@@ -675,66 +1028,71 @@ const char *fs_version(void) { return "fastscape-gb300 0.1 (sm_103a)"; }
 // to check the ordering's cycle detection with receivers that the receiver
 // kernel itself can never produce.
 int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!dir) return set_error(FS_ERR_ARG, "dir is NULL");
-  std::vector<int8_t> r(m->size);
-  for (int i = 0; i < m->size; i++) {
-    const int y = i / m->W, x = i % m->W;
-    const bool interior = x >= 2 && x < m->W - 2 && y >= 2 && y < m->H - 2;
+  fs_batch *b = m->b;
+  const int W = b->W[0], H = b->H[0], n = b->size[0];
+  std::vector<int8_t> v(n);
+  for (int i = 0; i < n; i++) {
+    const int y = i / W, x = i % W;
+    const bool interior = x >= 2 && x < W - 2 && y >= 2 && y < H - 2;
     if (dir[i] < -1 || dir[i] > 7 || (!interior && dir[i] != -1))
       return set_error(FS_ERR_ARG, "invalid receiver code %d at cell %d", dir[i], i);
-    r[i] = static_cast<int8_t>(interior && dir[i] == FS_NO_FLOW ? fs::kPit : dir[i]);
+    v[i] = static_cast<int8_t>(interior && dir[i] == FS_NO_FLOW ? fs::kPit : dir[i]);
   }
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(m->d_rec, r.data(), m->size, cudaMemcpyHostToDevice, m->stream));
-  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream));
-  const fs::StepGeom g{m->W, m->H, m->size};
-  FS_CUDA(fs::launch_donors_level0(m->d_rec, m->d_mask, m->d_ent, m->d_ctl, g, m->nring,
-                                   m->stream));
-  FS_CUDA(fs::launch_walk(walk_args(m, 0), m->walk_blocks, m->stream));
-  m->have_step = true;
-  return collect_status(m);
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemcpyAsync(b->rec, v.data(), n, cudaMemcpyHostToDevice, b->stream));
+  FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, sizeof(fs::Ctl), b->stream));
+  FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
+  const fs::StepArgs a = step_args(b, 0);
+  FS_CUDA(fs::launch_donors_level0(a, b->stream));
+  FS_CUDA(fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream));
+  b->have_step = true;
+  return collect_status(b);
 }
 
 // Selects the receiver kernel: 1 = the FP64 reference formula for every
 // cell, 0 = the FP32 filter with FP64 fix-up (default). Both give identical
 // receivers; the switch exists to test that.
 int fs_test_set_receiver_path(fs_model *m, int exact) {
-  if (int st = check_model(m)) return st;
-  m->exact_receivers = exact != 0;
+  FS_MODEL(m);
+  m->b->exact_receivers = exact != 0;
+  m->b->graph_dirty = true;
   return FS_OK;
 }
 
 // Number of cells the receiver filter queued for the FP64 fix-up in the last
 // timestep.
 int fs_test_receiver_fixups(const fs_model *m, int32_t *count) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!count) return set_error(FS_ERR_ARG, "count is NULL");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, m->stream));
-  FS_CUDA(cudaStreamSynchronize(m->stream));
-  *count = m->h_ctl->amb;
+  const fs_batch *b = m->b;
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  *count = b->h_ctl->amb;
   return FS_OK;
 }
 
 // Current capacity of the erosion table (drainage counts below it are
 // covered).
 int fs_test_table_capacity(const fs_model *m, int32_t *cap) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!cap) return set_error(FS_ERR_ARG, "cap is NULL");
-  *cap = m->tab_cap;
+  *cap = m->b->tab_cap[0];
   return FS_OK;
 }
 
 // Runs a bounded wait on a count that is never reached and returns its
 // status (FS_ERR_TIMEOUT when the limit works). The GPU stays usable.
 int fs_test_barrier_timeout(fs_model *m, double ms) {
-  if (int st = check_model(m)) return st;
+  FS_MODEL(m);
   if (!(ms > 0) || ms > 10000) return set_error(FS_ERR_ARG, "ms must be in (0, 10000]");
-  DeviceGuard dg(m->device);
-  FS_CUDA(cudaMemsetAsync(m->d_ctl, 0, sizeof(fs::Ctl), m->stream));
-  FS_CUDA(fs::launch_test_wait(m->d_ctl, 4, static_cast<unsigned long long>(ms * 1e6), m->stream));
-  return collect_status(m);
+  fs_batch *b = m->b;
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, sizeof(fs::Ctl), b->stream));
+  FS_CUDA(fs::launch_test_wait(b->d_ctl, 4, static_cast<unsigned long long>(ms * 1e6), b->stream));
+  return collect_status(b);
 }
 
 }  // extern "C"

@@ -166,6 +166,44 @@ size_t fs_last_error(char *buf, size_t n);
 /* Library version string. */
 const char *fs_version(void);
 
+/* ---- Ragged batches ------------------------------------------------------
+ * Many independent realizations, each with its own grid size and constants
+ * (all sharing the slope exponent n), advanced together: one launch sequence
+ * per timestep for the whole batch, all realizations walking their levels in
+ * lock step so one grid barrier per level serves every realization. The
+ * reference has no batch; each realization behaves exactly like a model of
+ * its own (same results bit for bit). */
+typedef struct fs_batch fs_batch;
+
+/* n realizations; widths[r] x heights[r] cells with params[r]; seeds may be
+ * NULL (all 0). At most 4096 realizations and 2^31-2 cells in total. */
+fs_batch *fs_batch_create(int n, const int *widths, const int *heights,
+                          const fs_params *params, int init_mode,
+                          const uint64_t *seeds, int *status);
+void fs_batch_destroy(fs_batch *b);
+/* Exactly k timesteps of every realization. */
+int fs_batch_step(fs_batch *b, int k);
+/* nstep+1 timesteps of every realization (the reference's run semantics). */
+int fs_batch_run(fs_batch *b, int nstep);
+int fs_batch_get_elevation(const fs_batch *b, int r, double *out);
+int fs_batch_set_elevation(fs_batch *b, int r, const double *in);
+int fs_batch_get_accumulation(const fs_batch *b, int r, double *out);
+int fs_batch_get_receivers(const fs_batch *b, int r, int32_t *dir);
+int fs_batch_get_levels(const fs_batch *b, int r, int32_t *level_id,
+                        int32_t *nlevels);
+/* Number of realizations and total cells. */
+int fs_batch_info(const fs_batch *b, int *n, int64_t *cells);
+int fs_batch_set_timing(fs_batch *b, int enable);
+int fs_batch_get_phase_times(const fs_batch *b, double *ms, int reset);
+/* Replays each timestep from a captured CUDA graph (1) or launches it
+ * directly (0, default). */
+int fs_batch_use_graph(fs_batch *b, int enable);
+/* Times every launch configuration (walk blocks per SM, graph or direct)
+ * over probe_steps timesteps of the batch's own state, restores the state
+ * and keeps the fastest; chosen[0] = blocks per SM, chosen[1] = graph. */
+int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen);
+int fs_batch_synchronize(const fs_batch *b);
+
 /* Largest grid (width*height cells) fs_step_noalloc accepts. */
 #define FS_NOALLOC_MAX_CELLS 262144
 
@@ -177,7 +215,7 @@ const char *fs_version(void);
  * may not allocate device memory while running (a host application that
  * owns all device memory through its own pool, a latency-critical loop where
  * cudaMalloc/cudaFree would synchronize the device, a plugin with a fixed
- * footprint). All scratch (~23 MB) is one static device array in the
+ * footprint). All scratch (~24 MB) is one static device array in the
  * library, held on every GPU that loads it until the process exits, shared
  * by all calls and keeping the last call's contents: calls that overlap on
  * the GPU race and must be serialized by the caller. Grids larger than

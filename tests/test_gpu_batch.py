@@ -1,0 +1,125 @@
+"""Ragged batches (fs_batch_*): every realization of a batch must evolve
+exactly like a model of its own -- bit for bit, receivers, level ids,
+accumulation and elevation -- whatever its neighbours in the batch, with
+direct launches or a replayed CUDA graph, and after the autotuner ran."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Params
+
+pytestmark = pytest.mark.gpu
+
+
+def ensemble(n, seed, smin=5, smax=160, neq=1.0):
+    """Sides log-uniform, K log-U[1e-6,1e-5], m U[0.3,0.6], U log-U[1e-4,5e-3]
+    (the ensemble workload's distributions at small sizes)."""
+    import importlib
+    pkg = importlib.import_module("barnes2019-landscape_gb300")
+    rng = np.random.default_rng(seed)
+    ws, hs, ps = [], [], []
+    for _ in range(n):
+        ws.append(int(np.exp(rng.uniform(np.log(smin), np.log(smax)))))
+        hs.append(int(np.exp(rng.uniform(np.log(smin), np.log(smax)))))
+        p = pkg.workload_params(keq=float(10 ** rng.uniform(-6, -5)),
+                                meq=float(rng.uniform(0.3, 0.6)),
+                                ueq=float(10 ** rng.uniform(-4, np.log10(5e-3))), neq=neq)
+        ps.append(p)
+    return ws, hs, ps
+
+
+def compare_with_singles(pkg, b, ws, hs, ps, singles, tag):
+    for r in range(len(ws)):
+        m = singles[r]
+        assert np.array_equal(b.receivers(r), m.receivers()), f"{tag} rec r={r}"
+        lb, nb = b.levels(r)
+        lm, nm = m.levels()
+        assert nb == nm and np.array_equal(lb, lm), f"{tag} levels r={r}"
+        assert np.array_equal(b.accumulation(r), m.accumulation()), f"{tag} acc r={r}"
+        assert np.array_equal(b.getH(r), m.getH()), f"{tag} h r={r}"
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_equals_independent_models(pkg, graph):
+    ws, hs, ps = ensemble(9, 11)
+    seeds = list(range(100, 109))
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=seeds) as b:
+        b.use_graph(graph)
+        singles = [pkg.FastScape_RBP(w, h, params=p, init=pkg.INIT_PHILOX, seed=s)
+                   for w, h, p, s in zip(ws, hs, ps, seeds)]
+        for r in range(len(ws)):
+            assert np.array_equal(b.getH(r), singles[r].getH())
+        for k in (1, 4, 7):
+            b.step(k)
+            for m in singles:
+                m.step(k)
+            compare_with_singles(pkg, b, ws, hs, ps, singles, f"k={k}")
+        for m in singles:
+            m.close()
+
+
+def test_batch_against_oracle(pkg, oracle):
+    ws, hs, ps = ensemble(5, 3, smin=6, smax=90)
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[1, 2, 3, 4, 5]) as b:
+        hs0 = [b.getH(r) for r in range(len(ws))]
+        b.step(6)
+        for r in range(len(ws)):
+            h = hs0[r].copy()
+            oracle.steps(h, ws[r], hs[r], Params(*ps[r].as_tuple()), 6)
+            assert np.array_equal(b.getH(r), h), f"r={r}"
+
+
+def test_batch_reference_constants(pkg):
+    """n = 2 everywhere (the reference's exponent) also batches exactly."""
+    ws, hs, ps = ensemble(4, 5, neq=2.0)
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[7, 8, 9, 10]) as b:
+        singles = [pkg.FastScape_RBP(w, h, params=p, init=pkg.INIT_PHILOX, seed=s)
+                   for w, h, p, s in zip(ws, hs, ps, [7, 8, 9, 10])]
+        b.step(5)
+        for m in singles:
+            m.step(5)
+        compare_with_singles(pkg, b, ws, hs, ps, singles, "n=2")
+
+
+def test_autotune_keeps_state(pkg):
+    ws, hs, ps = ensemble(6, 21, smin=40, smax=300)
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=list(range(6))) as a, \
+            pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=list(range(6))) as b:
+        a.step(2)
+        b.step(2)
+        before = [a.getH(r) for r in range(6)]
+        choice = a.autotune(probe_steps=2)
+        assert choice["walk_blocks_per_sm"] in (1, 2)
+        for r in range(6):
+            assert np.array_equal(a.getH(r), before[r])
+        a.step(5)
+        b.step(5)
+        for r in range(6):
+            assert np.array_equal(a.getH(r), b.getH(r))
+
+
+def test_batch_run_semantics_and_errors(pkg):
+    ws, hs, ps = ensemble(3, 8)
+    with pkg.FastScapeBatch(ws, hs, ps, seeds=[1, 2, 3]) as b:
+        b.run(3)
+        assert b.cells() == sum(w * h for w, h in zip(ws, hs))
+        with pytest.raises(pkg.FastScapeError):
+            b.getH(3)
+    p1 = pkg.workload_params()
+    p2 = pkg.workload_params(neq=2.0)
+    with pytest.raises(pkg.FastScapeError):
+        pkg.FastScapeBatch([10, 10], [10, 10], [p1, p2])
+
+
+def test_large_and_small_mixed(pkg):
+    """A 1000x900 realization beside tiny ones; the tiny ones finish their
+    levels early and must not disturb the big one."""
+    ws = [1000, 5, 7, 64]
+    hs = [900, 5, 40, 3]
+    ps = [pkg.workload_params()] * 4
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[4, 5, 6, 7]) as b:
+        singles = [pkg.FastScape_RBP(w, h, params=p, init=pkg.INIT_PHILOX, seed=s)
+                   for w, h, p, s in zip(ws, hs, ps, [4, 5, 6, 7])]
+        b.step(3)
+        for m in singles:
+            m.step(3)
+        compare_with_singles(pkg, b, ws, hs, ps, singles, "mixed")
