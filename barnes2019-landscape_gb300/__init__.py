@@ -329,6 +329,8 @@ class FastScapeBatch:
         self.close()
 
     def size(self, r: int) -> int:
+        if not 0 <= int(r) < self.n:
+            raise FastScapeError(-1, f"realization {r} out of range [0, {self.n})")
         return self.widths[r] * self.heights[r]
 
     def cells(self) -> int:

@@ -5,7 +5,8 @@ arch=compute_103a,code=sm_103a``) with ``-fmad=false`` (the timestep must
 not contract multiply-adds, to keep the reference's rounding) and links
 ``lib/libfastscape_gb300.so`` with the CUDA runtime linked statically.
 Objects go to ``_build/`` next to this file. Translation units compile in
-parallel. Usage: ``python build_ext.py [--force] [--verbose]``.
+parallel. Also builds ``bin/fastscape_gb300``, the command-line program with
+the reference's interface. Usage: ``python build_ext.py [--force] [--verbose]``.
 """
 from __future__ import annotations
 
@@ -21,6 +22,8 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libfastscape_gb300.so"
+BINDIR = PKG / "bin"
+CLI = BINDIR / "fastscape_gb300"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -80,7 +83,23 @@ def build(force: bool = False, verbose: bool = False) -> Path:
               ["-Xcompiler", "-fPIC", "-lpthread"]
         subprocess.run(cmd, check=True)
         os.replace(tmp, LIB)
+    build_cli(force)
     return LIB
+
+
+def build_cli(force: bool = False) -> Path:
+    """The reference-style command-line program, linked to the library."""
+    BINDIR.mkdir(exist_ok=True)
+    src = CSRC / "fs_cli.cpp"
+    deps = [src, LIB, ROOT / "include" / "fastscape_gb300.hpp", ROOT / "include" / "fastscape_gb300.h"]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    tmp = CLI.with_suffix(".tmp")
+    cmd = ["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", str(src), "-o", str(tmp),
+           f"-L{LIBDIR}", "-lfastscape_gb300", "-Wl,-rpath,$ORIGIN/../lib"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":
