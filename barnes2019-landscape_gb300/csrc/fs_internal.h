@@ -150,7 +150,7 @@ cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s);
 int walk_threads();
-const void *walk_kernel_ptr(int nmode);
+const void *walk_kernel_ptr(int nmode, bool single);
 cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
 cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s);
 cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s);

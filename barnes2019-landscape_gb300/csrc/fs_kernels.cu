@@ -499,8 +499,8 @@ __device__ __forceinline__ double erode_cell(const RealDesc &d, double neq, Ctl 
 // memory and maps global work items (expansion chunks, 32-entry groups) to
 // realizations through a prefix over the batch.
 // ---------------------------------------------------------------------------
-template <int NMODE>
-__global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
+template <int NMODE, bool SINGLE>
+__global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
   extern __shared__ int smem[];
   const int nreal = a.nreal;
   int *s_lo = smem;               // per realization: current range start
@@ -511,6 +511,12 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
   if (stopped(ctl)) return;
+  // A batch of one keeps its descriptor in registers and skips the
+  // realization lookups.
+  RealDesc d0;
+  if (SINGLE) d0 = a.desc[0];
+  auto desc = [&](int r) -> const RealDesc & { return SINGLE ? d0 : a.desc[r]; };
+  auto real_of = [&](int g) -> int { return SINGLE ? 0 : find_real(s_pre, nreal, g); };
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nthreads = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -536,7 +542,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
   // rotates over three words so a block that reads the size of level k after
   // the barrier never races with the reset for level k+2.
   for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
-    const RealDesc &d = a.desc[r];
+    const RealDesc &d = desc(r);
     s_lo[r] = 0;
     s_hi[r] = d.nring + ld_volatile_i32(&a.rctl[r].top);
     s_nlev[r] = 1;
@@ -554,8 +560,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
     const int nchunks = block_prefix(
         nreal, [&](int r) { return (s_hi[r] - s_lo[r] + kChunk - 1) / kChunk; }, s_pre);
     for (int g = blockIdx.x; g < nchunks; g += gridDim.x) {
-      const int r = find_real(s_pre, nreal, g);
-      const RealDesc &d = a.desc[r];
+      const int r = real_of(g);
+      const RealDesc &d = desc(r);
       const int hi = s_hi[r];
       const int base = s_lo[r] + (g - s_pre[r]) * kChunk;
       const int wbase = base + wid * (32 * kPer);
@@ -641,9 +647,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         s_hi[r] += added;
         s_nlev[r] = L + 2;
         any = 1;
-        if (s_hi[r] > a.desc[r].size) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
-        if (blockIdx.x == 0 && s_hi[r] <= a.desc[r].size)
-          a.lvl_off[a.desc[r].lvl_base + L + 2] = s_hi[r];
+        if (s_hi[r] > desc(r).size) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+        if (blockIdx.x == 0 && s_hi[r] <= desc(r).size)
+          a.lvl_off[desc(r).lvl_base + L + 2] = s_hi[r];
       }
     }
     if (!__syncthreads_or(any)) break;
@@ -660,7 +666,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         a.rctl[r].nlevels = s_nlev[r];
         a.rctl[r].total = s_hi[r];
       }
-      bad |= s_hi[r] != a.desc[r].size;
+      bad |= s_hi[r] != desc(r).size;
     }
     if (__syncthreads_or(bad)) {
       if (tid == 0) raise_err(ctl, FS_ERR_ORDER, kPhaseOrder);
@@ -675,7 +681,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
     __syncthreads();  // every warp is done with the previous ranges
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
       if (Lv < s_nlev[r]) {
-        const int b = a.desc[r].lvl_base;
+        const int b = desc(r).lvl_base;
         s_lo[r] = __ldcg(&a.lvl_off[b + Lv]);
         s_hi[r] = __ldcg(&a.lvl_off[b + Lv + 1]);
       } else {
@@ -710,11 +716,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         rr[u] = 0;
         ii[u] = -1;
         if (g < ngroups) {
-          const int r = find_real(s_pre, nreal, g);
+          const int r = real_of(g);
           const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
           rr[u] = r;
           if (i < s_hi[r]) {
-            const int off = a.desc[r].off;
+            const int off = desc(r).off;
             ii[u] = i;
             n[u] = __ldcg(&a.nd[off + i]);
             k = __ldcg(&a.kid[off + i]);
@@ -728,7 +734,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         }
         incl[u] = v;
         tot[u] = __shfl_sync(kFull, v, 31);
-        run[u] = a.desc[rr[u]].off + __shfl_sync(kFull, k, 0);
+        run[u] = desc(rr[u]).off + __shfl_sync(kFull, k, 0);
       }
 #pragma unroll
       for (int u = 0; u < kAccU; u++)
@@ -748,7 +754,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
           }
         }
         if (ii[u] >= 0) {
-          const RealDesc &d = a.desc[rr[u]];
+          const RealDesc &d = desc(rr[u]);
           a.acc[d.off + ii[u]] = s;
           if (a.do_erode && Lv > 0 && s >= (uint32_t)d.tab_cap) {
             if (atomicMax(&ctl->abort_k, (int)s) < (int)s) ctl->abort_r = rr[u];
@@ -772,15 +778,15 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
     // pits of realization r: level-0 positions [nring, lvl_off[1])
     __syncthreads();  // every warp is done with the level's ranges
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
-      const RealDesc &d = a.desc[r];
+      const RealDesc &d = desc(r);
       s_lo[r] = d.nring;
       s_hi[r] = __ldcg(&a.lvl_off[d.lvl_base + 1]);
     }
     __syncthreads();
     const int np = block_prefix(nreal, [&](int r) { return s_hi[r] - s_lo[r]; }, s_pre);
     for (int g = tid; g < np; g += nthreads) {
-      const int r = find_real(s_pre, nreal, g);
-      const RealDesc &d = a.desc[r];
+      const int r = real_of(g);
+      const RealDesc &d = desc(r);
       const int c = __ldcg(&a.ent[d.off + s_lo[r] + (g - s_pre[r])]);
       double *hh = a.h + d.off;
       hh[c] = __ldcg(&hh[c]) + d.u_dt;
@@ -801,11 +807,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         dd[u] = 0;
         kk[u] = 0;
         if (g < ngroups) {
-          const int r = find_real(s_pre, nreal, g);
+          const int r = real_of(g);
           const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
           rr[u] = r;
           if (i < s_hi[r]) {
-            const int off = a.desc[r].off;
+            const int off = desc(r).off;
             ok[u] = true;
             cc[u] = __ldcg(&a.ent[off + i]);
             dd[u] = __ldcg(&a.pdir[off + i]);
@@ -819,7 +825,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
         hc[u] = 0.0;
         hn[u] = 0.0;
         if (ok[u]) {
-          const RealDesc &d = a.desc[rr[u]];
+          const RealDesc &d = desc(rr[u]);
           const double *hh = a.h + d.off;
           hc[u] = __ldcg(&hh[cc[u]]);
           hn[u] = __ldcg(&hh[cc[u] + nbr_off(dd[u] & 7, d.W)]);
@@ -828,7 +834,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(StepArgs a) {
 #pragma unroll
       for (int u = 0; u < kEroU; u++) {
         if (ok[u]) {
-          const RealDesc &d = a.desc[rr[u]];
+          const RealDesc &d = desc(rr[u]);
           const double *T = d.tab + (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
           double hr = hn[u];
           if (dd[u] & 8) hr = hr + d.u_dt;
@@ -951,19 +957,25 @@ size_t walk_smem_bytes(int nreal) { return sizeof(int) * (4 * (size_t)nreal + 1)
 
 int walk_threads() { return kWalkThreads; }
 
-const void *walk_kernel_ptr(int nmode) {
-  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne>);
-  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo>);
-  return reinterpret_cast<const void *>(&k_walk<kNGeneral>);
+const void *walk_kernel_ptr(int nmode, bool single) {
+  if (single) {
+    if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne, true>);
+    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo, true>);
+    return reinterpret_cast<const void *>(&k_walk<kNGeneral, true>);
+  }
+  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne, false>);
+  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo, false>);
+  return reinterpret_cast<const void *>(&k_walk<kNGeneral, false>);
 }
 
 cudaError_t prepare_walk_kernels() {
   const int bytes = (int)walk_smem_bytes(kMaxReal);
-  for (int nm = 0; nm < 3; nm++) {
-    cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm),
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess) return e;
-  }
+  for (int nm = 0; nm < 3; nm++)
+    for (int single = 0; single < 2; single++) {
+      cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0),
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e != cudaSuccess) return e;
+    }
   return cudaSuccess;
 }
 
@@ -1036,7 +1048,7 @@ cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s) {
 cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
-  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode), dim3(blocks),
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1), dim3(blocks),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }
 

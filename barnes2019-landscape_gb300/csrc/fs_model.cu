@@ -584,7 +584,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
   int occ = 0;
   if (!cu(fs::prepare_walk_kernels(), "walk smem attribute") ||
       !cu(cudaDeviceGetAttribute(&b->walk_sms, cudaDevAttrMultiProcessorCount, b->device), "attr") ||
-      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(b->nmode),
+      !cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(b->nmode, n == 1),
                                                         fs::walk_threads(),
                                                         fs::walk_smem_bytes(n)),
           "occupancy"))

@@ -110,7 +110,7 @@ int setup_device(int dev, DeviceState &d) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
   for (int nm = 0; nm < 3; nm++) {
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(nm),
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::walk_kernel_ptr(nm, true),
                                                       fs::walk_threads(), fs::walk_smem_bytes(1));
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (occ < 1) return fail(FS_ERR_CUDA, "walk kernel cannot be resident");

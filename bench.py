@@ -319,17 +319,15 @@ def run_ensemble(args, dist, rank, ws, local):
     b.step(args.warmup)
     tune = b.autotune(probe_steps=2)
     b.step(1)
-    b.synchronize()
-    barrier(dist)
-    t0 = time.perf_counter()
-    with Clocks(local) as clk:
-        b.step(args.steps)
-        b.synchronize()
-    dt = max_over_ranks(dist, time.perf_counter() - t0)
     b.set_timing(True)
     b.phase_times(reset=True)
-    b.step(2)
-    t = b.phase_times(reset=True)
+    b.synchronize()
+    barrier(dist)
+    with Clocks(local) as clk:
+        b.step(args.steps)
+    barrier(dist)
+    t = b.phase_times(reset=True) / args.steps * 2   # per 2 timesteps, like below
+    dt = max_over_ranks(dist, t[3] / 2 * 1e-3 * args.steps)
     b.close()
     per_step = dt / args.steps
     value = ws * len(sides) / (ENSEMBLE_STEPS * per_step)

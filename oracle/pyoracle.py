@@ -192,6 +192,7 @@ class RefHarness:
         L.fsref_nlevel.argtypes = [C.c_int, vp]
         L.fsref_nlevel.restype = C.c_int
         L.fsref_run.argtypes = [C.c_int, vp, C.c_int]
+        L.fsref_print_dem.argtypes = [C.c_int, vp, C.c_char_p]
 
     def set_params(self, p: Params):
         if self.text != "param":
@@ -244,6 +245,10 @@ class RefModel:
 
     def run(self, nstep):
         self.hr.lib.fsref_run(self.v, self.obj, nstep)
+
+    def print_dem(self, path):
+        """The reference's PrintDEM of the current elevation."""
+        self.hr.lib.fsref_print_dem(self.v, self.obj, str(path).encode())
 
     def get(self, name):
         L, ip = self.hr.lib, C.c_int32

@@ -181,6 +181,11 @@ void fsref_get_accum(int variant, void *obj, double *out) {
   FSREF_DISPATCH(variant, obj, std::memcpy(out, m.accum.data(), sizeof(double) * m.size));
 }
 
+// The reference's PrintDEM (fastscape_RB.cpp:20-40) of the current h.
+void fsref_print_dem(int variant, void *obj, const char *path) {
+  FSREF_DISPATCH(variant, obj, fsref_rb::PrintDEM(path, m.h, m.width, m.height));
+}
+
 // The reference's own run(): nstep+1 timesteps, prints its `p`/`t` lines.
 void fsref_run(int variant, void *obj, int nstep) {
   FSREF_DISPATCH(variant, obj, m.run(nstep));

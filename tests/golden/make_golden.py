@@ -125,6 +125,16 @@ def main():
             save(f"known_{kname}_{pname}", W=W, H=H, nsteps=2, variant=0,
                  params=params_array(p), **rec)
 
+    # the reference's own DEM output (PrintDEM after run(nstep)), as its CLI
+    # writes it: compare.sh's artefact
+    for name, hr, p, W, nstep in [("dem_refconst_40_30", pristine, REFERENCE_PARAMS, 40, 30),
+                                  ("dem_workload_33_25", param, wl, 33, 25)]:
+        m = hr.model(W, W, p, 0)
+        m.run(nstep)
+        path = HERE / f"{name}.dem"
+        m.print_dem(path)
+        written.append(path)
+
     # the reference's own generator stream: first draws of the field for
     # seeds that seed_rand turns into engine seed 0
     m = pristine.model(16, 16, REFERENCE_PARAMS, 0, seed=999)
