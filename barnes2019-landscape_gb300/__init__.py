@@ -39,12 +39,12 @@ ABI_SYMBOLS = [
     "fs_params_reference", "fs_params_workload", "fs_create", "fs_destroy",
     "fs_run", "fs_step", "fs_get_elevation", "fs_set_elevation",
     "fs_get_accumulation", "fs_get_receivers", "fs_get_receiver_index",
-    "fs_get_levels", "fs_get_donor_mask", "fs_get_shape", "fs_get_params",
+    "fs_get_levels", "fs_get_donor_mask", "fs_get_stack_dfs", "fs_get_shape", "fs_get_params",
     "fs_steps_executed", "fs_set_timing", "fs_get_phase_times",
     "fs_set_barrier_timeout", "fs_synchronize", "fs_last_error", "fs_version",
     "fs_batch_create", "fs_batch_destroy", "fs_batch_step", "fs_batch_run",
     "fs_batch_get_elevation", "fs_batch_set_elevation", "fs_batch_get_accumulation",
-    "fs_batch_get_receivers", "fs_batch_get_levels", "fs_batch_info",
+    "fs_batch_get_receivers", "fs_batch_get_levels", "fs_batch_get_stack_dfs", "fs_batch_info",
     "fs_batch_set_timing", "fs_batch_get_phase_times", "fs_batch_use_graph",
     "fs_batch_autotune", "fs_batch_synchronize",
     "fs_step_noalloc",
@@ -115,6 +115,8 @@ def library() -> C.CDLL:
     L.fs_get_receiver_index.argtypes = [vp, C.POINTER(C.c_int64)]
     L.fs_get_levels.argtypes = [vp, i32p, i32p]
     L.fs_get_donor_mask.argtypes = [vp, C.POINTER(C.c_uint8)]
+    L.fs_get_stack_dfs.argtypes = [vp, i32p, i32p, i32p]
+    L.fs_batch_get_stack_dfs.argtypes = [vp, C.c_int, i32p, i32p, i32p]
     L.fs_get_shape.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fs_get_params.argtypes = [vp, pp]
     L.fs_steps_executed.argtypes = [vp]
@@ -249,6 +251,16 @@ class FastScape_RBP:
         n = C.c_int32(0)
         check(library().fs_get_levels(self._m, _p(out, C.c_int32), C.byref(n)))
         return out, n.value
+
+    def stack_dfs(self):
+        """(stack, stack_start) of the Braun-Willett order
+        (fastscape_BW.cpp:201-221, fastscape_BW+P.cpp:223-240)."""
+        stack = np.empty(self.size, np.int32)
+        starts = np.empty(self.size + 1, np.int32)
+        n = C.c_int32(0)
+        check(library().fs_get_stack_dfs(self._m, _p(stack, C.c_int32), _p(starts, C.c_int32),
+                                         C.byref(n)))
+        return stack, starts[:n.value + 1].copy()
 
     def donor_mask(self) -> np.ndarray:
         out = np.empty(self.size, np.uint8)

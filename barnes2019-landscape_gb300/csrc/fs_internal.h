@@ -158,6 +158,23 @@ cudaError_t launch_place_rings(int32_t *ent, int W, int H, cudaStream_t s);
 cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns,
                              cudaStream_t s);
 
+// One realization's level-walk arrays, for the Braun-Willett order.
+struct DfsArgs {
+  const int8_t *rec;
+  const int32_t *ent;
+  const uint8_t *nd;
+  const int32_t *kid;
+  const uint8_t *pdir;
+  const uint32_t *acc;
+  int W, size;
+};
+// Scratch ints launch_dfs_order needs for a realization of `size` cells.
+size_t dfs_scratch_ints(int size);
+// The Braun-Willett (depth-first) order into out[size], given the level
+// offsets on the host.
+cudaError_t launch_dfs_order(const DfsArgs &d, const int32_t *lvl_host, int nlev,
+                             int32_t *scratch, int32_t *out, cudaStream_t s);
+
 // Host helpers shared by the entry points.
 float tol_lower_float(double tol);
 int ring_cells(int W, int H);

@@ -944,6 +944,94 @@ __global__ void k_test_wait(Ctl *ctl, unsigned long long timeout_ns) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// 5. The Braun-Willett order (fastscape_BW.cpp:201-221) of the last
+// timestep's receiver forest, from the level-walk arrays: a depth-first
+// preorder with roots (NO_FLOW cells) in ascending index and each cell's
+// donors in ascending index. A cell's preorder position is its parent's
+// position + 1 + the subtree sizes (drainage counts) of the siblings before
+// it; a root's is the total subtree size of the roots before it. Computed
+// level by level, top down, then scattered.
+// ---------------------------------------------------------------------------
+
+// cellacc[ent[i]] = acc[i] over one realization.
+__global__ void k_scatter_counts(const int32_t *__restrict__ ent, const uint32_t *__restrict__ acc,
+                                 int n, int32_t *__restrict__ cellacc) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    cellacc[ent[i]] = (int32_t)acc[i];
+}
+
+// v[c] = subtree size of c if c is a root, else 0; then an exclusive scan in
+// three launches (block sums, one block over the sums, block scans + offsets).
+constexpr int kScanBlock = 1024;
+__global__ void k_root_sizes_blocksum(const int8_t *__restrict__ rec,
+                                      const int32_t *__restrict__ cellacc, int n,
+                                      int32_t *__restrict__ v, int32_t *__restrict__ bsum) {
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  const int x = (i < n && rec[i] < 0) ? cellacc[i] : 0;
+  if (i < n) v[i] = x;
+  int total;
+  block_excl_scan(x, total, threadIdx.x, kScanBlock);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(int32_t *bsum, int nb) {
+  // one block: each thread scans a contiguous slice, then the slices
+  const int per = (nb + kScanBlock - 1) / kScanBlock;
+  const int b0 = threadIdx.x * per;
+  int s = 0;
+  for (int b = b0; b < b0 + per && b < nb; b++) s += bsum[b];
+  int total;
+  int run = block_excl_scan(s, total, threadIdx.x, kScanBlock);
+  for (int b = b0; b < b0 + per && b < nb; b++) {
+    const int x = bsum[b];
+    bsum[b] = run;
+    run += x;
+  }
+}
+
+__global__ void k_scan_apply(int32_t *__restrict__ v, const int32_t *__restrict__ bsum, int n) {
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  const int x = i < n ? v[i] : 0;
+  int total;
+  const int e = block_excl_scan(x, total, threadIdx.x, kScanBlock);
+  if (i < n) v[i] = bsum[blockIdx.x] + e;
+}
+
+// Level 0: dpos[i] = rootpos[ent[i]].
+__global__ void k_dfs_level0(const int32_t *__restrict__ ent, const int32_t *__restrict__ rootpos,
+                             int n0, int32_t *__restrict__ dpos) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += gridDim.x * blockDim.x)
+    dpos[i] = rootpos[ent[i]];
+}
+
+// Donors of the entries [b, e): positions after their parent in ascending
+// cell-index order (the donor-list order of fastscape_BW.cpp:188-198).
+__global__ void k_dfs_level(const uint8_t *__restrict__ nd, const int32_t *__restrict__ kid,
+                            const uint8_t *__restrict__ pdir, const uint32_t *__restrict__ acc,
+                            int b, int e, int W, int32_t *__restrict__ dpos) {
+  for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+    const int n = nd[i];
+    if (!n) continue;
+    const int k0 = kid[i];
+    const int p = dpos[i];
+    for (int q = 0; q < n; q++) {
+      // the donor's offset from its receiver is minus its receiver offset
+      const int oq = -nbr_off(pdir[k0 + q] & 7, W);
+      int pos = p + 1;
+      for (int s = 0; s < n; s++)
+        if (-nbr_off(pdir[k0 + s] & 7, W) < oq) pos += (int)acc[k0 + s];
+      dpos[k0 + q] = pos;
+    }
+  }
+}
+
+__global__ void k_dfs_scatter(const int32_t *__restrict__ ent, const int32_t *__restrict__ dpos,
+                              int n, int32_t *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[dpos[i]] = ent[i];
+}
+
 int sm_count() {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -1076,6 +1164,31 @@ cudaError_t launch_place_rings(int32_t *ent, int W, int H, cudaStream_t s) {
 cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns,
                              cudaStream_t s) {
   k_test_wait<<<blocks, 32, 0, s>>>(ctl, timeout_ns);
+  return cudaGetLastError();
+}
+
+size_t dfs_scratch_ints(int size) {
+  return 3 * (size_t)size + (size_t)(size + kScanBlock - 1) / kScanBlock + 1;
+}
+
+cudaError_t launch_dfs_order(const DfsArgs &d, const int32_t *lvl_host, int nlev,
+                             int32_t *scratch, int32_t *out, cudaStream_t s) {
+  const int n = d.size;
+  int32_t *cellacc = scratch, *v = scratch + n, *dpos = scratch + 2 * (size_t)n;
+  int32_t *bsum = scratch + 3 * (size_t)n;
+  const int nb = (n + kScanBlock - 1) / kScanBlock;
+  const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_scatter_counts<<<g, 256, 0, s>>>(d.ent, d.acc, n, cellacc);
+  k_root_sizes_blocksum<<<nb, kScanBlock, 0, s>>>(d.rec, cellacc, n, v, bsum);
+  k_scan_sums<<<1, kScanBlock, 0, s>>>(bsum, nb);
+  k_scan_apply<<<nb, kScanBlock, 0, s>>>(v, bsum, n);
+  k_dfs_level0<<<g, 256, 0, s>>>(d.ent, v, lvl_host[1], dpos);
+  for (int L = 0; L + 1 < nlev; L++) {
+    const int b = lvl_host[L], e = lvl_host[L + 1];
+    const int gl = (e - b + 255) / 256 < 4096 ? (e - b + 255) / 256 : 4096;
+    if (gl > 0) k_dfs_level<<<gl, 256, 0, s>>>(d.nd, d.kid, d.pdir, d.acc, b, e, d.W, dpos);
+  }
+  k_dfs_scatter<<<g, 256, 0, s>>>(d.ent, dpos, n, out);
   return cudaGetLastError();
 }
 

@@ -677,6 +677,50 @@ int get_levels(const fs_batch *b, int r, int32_t *level_id, int32_t *nlevels) {
   return FS_OK;
 }
 
+// The Braun-Willett order of the last timestep (fastscape_BW.cpp:201-221),
+// computed on the device from the level walk; stack_start (may be NULL)
+// gets the first position of each root and a final size entry
+// (fastscape_BW+P.cpp:223-240).
+int get_stack_dfs(const fs_batch *b, int r, int32_t *stack, int32_t *stack_start,
+                  int32_t *nroots) {
+  if (int st = check_r(b, r)) return st;
+  if (!stack) return set_error(FS_ERR_ARG, "stack is NULL");
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  if (int st = read_rctl(b)) return st;
+  const int nl = b->h_rctl[r].nlevels;
+  const int n = b->size[r];
+  std::vector<int32_t> off(nl + 1);
+  FS_CUDA(cudaMemcpyAsync(off.data(), b->lvl + b->lvl_base[r], sizeof(int32_t) * (nl + 1),
+                          cudaMemcpyDeviceToHost, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  int32_t *scratch = nullptr, *out = nullptr;
+  FS_CUDA(cudaMalloc(&scratch, fs::dfs_scratch_ints(n) * sizeof(int32_t)));
+  cudaError_t e = cudaMalloc(&out, n * sizeof(int32_t));
+  const int o = b->off[r];
+  const fs::DfsArgs d{b->rec + o, b->ent + o, b->nd + o, b->kid + o, b->pdir + o, b->acc + o,
+                      b->W[r], n};
+  if (e == cudaSuccess) e = fs::launch_dfs_order(d, off.data(), nl, scratch, out, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(stack, out, n * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream);
+  std::vector<int8_t> rec(n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(rec.data(), b->rec + o, n, cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  cudaFree(scratch);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_error(e, "depth-first order");
+  int k = 0;
+  for (int p = 0; p < n; p++)
+    if (rec[stack[p]] < 0) {
+      if (stack_start) stack_start[k] = p;
+      k++;
+    }
+  if (stack_start) stack_start[k] = n;
+  if (nroots) *nroots = k;
+  return FS_OK;
+}
+
 int get_donor_mask(const fs_batch *b, int r, uint8_t *mask) {
   if (int st = check_r(b, r)) return st;
   if (!mask) return set_error(FS_ERR_ARG, "mask is NULL");
@@ -897,6 +941,11 @@ int fs_get_donor_mask(const fs_model *m, uint8_t *mask) {
   return get_donor_mask(m->b, 0, mask);
 }
 
+int fs_get_stack_dfs(const fs_model *m, int32_t *stack, int32_t *stack_start, int32_t *nroots) {
+  FS_MODEL(m);
+  return get_stack_dfs(m->b, 0, stack, stack_start, nroots);
+}
+
 int fs_get_shape(const fs_model *m, int *width, int *height) {
   FS_MODEL(m);
   if (width) *width = m->b->W[0];
@@ -981,6 +1030,11 @@ int fs_batch_get_receivers(const fs_batch *b, int r, int32_t *dir) { return get_
 
 int fs_batch_get_levels(const fs_batch *b, int r, int32_t *level_id, int32_t *nlevels) {
   return get_levels(b, r, level_id, nlevels);
+}
+
+int fs_batch_get_stack_dfs(const fs_batch *b, int r, int32_t *stack, int32_t *stack_start,
+                           int32_t *nroots) {
+  return get_stack_dfs(b, r, stack, stack_start, nroots);
 }
 
 int fs_batch_info(const fs_batch *b, int *n, int64_t *cells) {

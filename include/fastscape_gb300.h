@@ -137,6 +137,17 @@ int fs_get_levels(const fs_model *m, int32_t *level_id, int32_t *nlevels);
  * the order NW(1), N(2), NE(3), W(0), E(4), SW(7), S(6), SE(5). */
 int fs_get_donor_mask(const fs_model *m, uint8_t *mask);
 
+/* The Braun-Willett order of the last timestep's receivers
+ * (fastscape_BW.cpp:201-221): a depth-first preorder of the receiver forest,
+ * roots (FS_NO_FLOW cells) in ascending index, each cell followed by its
+ * donors' subtrees in ascending index -- identical to the reference BW's
+ * stack. stack holds width*height entries; stack_start (may be NULL; at
+ * least width*height+1 entries) receives each root's first position and a
+ * final width*height, the stack_start of fastscape_BW+P.cpp:223-240;
+ * *nroots the number of roots. Computed on the device from the level walk. */
+int fs_get_stack_dfs(const fs_model *m, int32_t *stack, int32_t *stack_start,
+                     int32_t *nroots);
+
 /* Grid geometry and counters. */
 int fs_get_shape(const fs_model *m, int *width, int *height);
 int fs_get_params(const fs_model *m, fs_params *out);
@@ -191,6 +202,8 @@ int fs_batch_get_accumulation(const fs_batch *b, int r, double *out);
 int fs_batch_get_receivers(const fs_batch *b, int r, int32_t *dir);
 int fs_batch_get_levels(const fs_batch *b, int r, int32_t *level_id,
                         int32_t *nlevels);
+int fs_batch_get_stack_dfs(const fs_batch *b, int r, int32_t *stack,
+                           int32_t *stack_start, int32_t *nroots);
 /* Number of realizations and total cells. */
 int fs_batch_info(const fs_batch *b, int *n, int64_t *cells);
 int fs_batch_set_timing(fs_batch *b, int enable);

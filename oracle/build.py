@@ -96,7 +96,8 @@ def _translation_unit(ref: Path, param: bool) -> str:
         parts.append("#define FSREF_PARAM_BUILD 1\n")
     parts.append(f'#line {harness[:pre_start].count(chr(10)) + 1} "{HERE / "ref_harness.cpp"}"\n')
     parts.append(prelude)
-    for ns, fname in (("fsref_rb", "fastscape_RB.cpp"), ("fsref_rbp", "fastscape_RB+P.cpp")):
+    for ns, fname in (("fsref_rb", "fastscape_RB.cpp"), ("fsref_rbp", "fastscape_RB+P.cpp"),
+                      ("fsref_bw", "fastscape_BW.cpp")):
         text = (ref / fname).read_text()
         if param:
             text = _patch_constants(text, fname)
@@ -114,7 +115,7 @@ def build_ref(force: bool = False) -> list[Path]:
     if not (ref / "fastscape_RB.cpp").exists():
         return []
     REF_OUT.mkdir(exist_ok=True)
-    sources = [ref / "fastscape_RB.cpp", ref / "fastscape_RB+P.cpp",
+    sources = [ref / "fastscape_RB.cpp", ref / "fastscape_RB+P.cpp", ref / "fastscape_BW.cpp",
                ref / "random.cpp", ref / "CumulativeTimer.cpp",
                HERE / "ref_harness.cpp", Path(__file__)]
     flagsets = {

@@ -161,6 +161,44 @@ int fso_order(const int32_t *rec, const int32_t *ndon, const int32_t *donor,
   return nlevel;
 }
 
+/* fastscape_BW.cpp:201-221; stack_start as fastscape_BW+P.cpp:223-240 */
+int fso_order_bw(const int32_t *rec, const int32_t *ndon, const int32_t *donor,
+                 int W, int H, int32_t *stack, int32_t *stack_start) {
+  const long size = (long)W * H;
+  /* explicit DFS stack of (cell, next donor slot) instead of recursion */
+  int32_t *node = (int32_t *)malloc(size * sizeof(int32_t));
+  int8_t *next = (int8_t *)malloc(size);
+  long nstack = 0;
+  int nroots = 0;
+  for (long c = 0; c < size; c++) {
+    if (rec[c] != NO_FLOW) continue;
+    if (stack_start) stack_start[nroots] = (int32_t)nstack;
+    nroots++;
+    stack[nstack++] = (int32_t)c;
+    long depth = 0;
+    node[0] = (int32_t)c;
+    next[0] = 0;
+    depth = 1;
+    while (depth > 0) {
+      const long u = node[depth - 1];
+      if (next[depth - 1] < ndon[u]) {
+        const int32_t v = donor[8 * u + next[depth - 1]];
+        next[depth - 1]++;
+        stack[nstack++] = v;
+        node[depth] = v;
+        next[depth] = 0;
+        depth++;
+      } else {
+        depth--;
+      }
+    }
+  }
+  if (stack_start) stack_start[nroots] = (int32_t)nstack;
+  free(node);
+  free(next);
+  return nroots;
+}
+
 /* fastscape_RB.cpp:262-279 */
 void fso_flowacc(const int32_t *rec, const int32_t *stack, int W, int H,
                  const fso_params *p, double *accum) {

@@ -63,6 +63,15 @@ void fso_donors(const int32_t *rec, int W, int H, int32_t *ndon,
 int fso_order(const int32_t *rec, const int32_t *ndon, const int32_t *donor,
               int W, int H, int32_t *stack, int32_t *levels);
 
+/* fastscape_BW.cpp:201-221 (and the stack_start of fastscape_BW+P.cpp:
+ * 223-240): the Braun-Willett order, a depth-first preorder of the receiver
+ * forest -- roots (NO_FLOW cells) in ascending index, each followed by its
+ * donors' subtrees in donor-list order. stack holds W*H; stack_start (may be
+ * NULL) receives each root's first position plus a final W*H entry.
+ * Iterative (the reference recurses). Returns the number of roots. */
+int fso_order_bw(const int32_t *rec, const int32_t *ndon, const int32_t *donor,
+                 int W, int H, int32_t *stack, int32_t *stack_start);
+
 /* fastscape_RB.cpp:262-279. */
 void fso_flowacc(const int32_t *rec, const int32_t *stack, int W, int H,
                  const fso_params *p, double *accum);

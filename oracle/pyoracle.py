@@ -84,6 +84,8 @@ class Oracle:
         L.fso_erode_levels.argtypes = [dp, ip, ip, ip, C.c_int, dp, C.c_int, C.c_int, pp]
         L.fso_run.argtypes = [dp, C.c_int, C.c_int, pp, C.c_int, C.c_int]
         L.fso_level_ids.argtypes = [ip, ip, C.c_int, C.c_int, C.c_int, ip]
+        L.fso_order_bw.argtypes = [ip, ip, ip, C.c_int, C.c_int, ip, ip]
+        L.fso_order_bw.restype = C.c_int
         L.fso_omp_threads.restype = C.c_int
 
     # -- primitives -------------------------------------------------------
@@ -131,6 +133,21 @@ class Oracle:
         return dict(rec=rec, ndon=ndon, donor=donor.reshape(size, 8), stack=stack,
                     levels=levels[:nlevel].copy(), nlevel=nlevel, accum=accum,
                     h_uplifted=h_upl, h=h, level_id=level_id)
+
+    def order_bw(self, rec: np.ndarray, W: int, H: int):
+        """Braun-Willett DFS stack and root starts from receiver codes
+        (fastscape_BW.cpp:201-221)."""
+        size = W * H
+        ip = C.c_int32
+        rec = np.ascontiguousarray(rec, np.int32)
+        ndon = np.empty(size, np.int32)
+        donor = np.zeros(8 * size, np.int32)
+        self.lib.fso_donors(_ptr(rec, ip), W, H, _ptr(ndon, ip), _ptr(donor, ip))
+        stack = np.empty(size, np.int32)
+        starts = np.empty(size + 1, np.int32)
+        n = self.lib.fso_order_bw(_ptr(rec, ip), _ptr(ndon, ip), _ptr(donor, ip), W, H,
+                                  _ptr(stack, ip), _ptr(starts, ip))
+        return stack, starts[:n + 1].copy()
 
     def run(self, h: np.ndarray, W: int, H: int, p: Params, nstep: int,
             parallel=False) -> np.ndarray:
@@ -270,6 +287,14 @@ class RefModel:
         out = np.empty(self.size, np.int32)
         getattr(L, f"fsref_get_{name}")(self.v, self.obj, _ptr(out, ip))
         return out
+
+    def bw_phases(self):
+        """One timestep of the Braun-Willett variant (variant 2); returns
+        receivers, its DFS stack and the eroded h."""
+        self.prepare()
+        for i in range(6):
+            self.phase(i)
+        return dict(rec=self.get("rec"), stack=self.get("stack"), h=self.get_h())
 
     def phases(self):
         """One timestep; returns the intermediates like Oracle.phases."""

@@ -4,10 +4,11 @@
 // the reference sources read from where they lie (never copied), and writes
 // the result only to oracle/_ref/. Nothing in the product path loads it.
 //
-// build_ref.py emits one translation unit:
+// oracle/build.py emits one translation unit:
 //     <this file's PRELUDE section>
 //     namespace fsref_rb  { <fastscape_RB.cpp>   }
 //     namespace fsref_rbp { <fastscape_RB+P.cpp> }
+//     namespace fsref_bw  { <fastscape_BW.cpp>   }
 //     <this file's DRIVER section>
 // The standard headers, random.hpp and CumulativeTimer.hpp are included
 // first, so the includes inside the reference files are no-ops and the two
@@ -66,6 +67,15 @@ void prepare_common(M &m) {
 
 void prepare(fsref_rb::FastScape_RB &m) { prepare_common(m); }
 
+// fastscape_BW.cpp:307-315 (no level table in the Braun-Willett variant).
+void prepare(fsref_bw::FastScape_BW &m) {
+  m.accum.assign(m.size, 0.0);
+  m.rec.assign(m.size, -1);
+  m.ndon.assign(m.size, 0);
+  m.donor.assign(8 * static_cast<size_t>(m.size), 0);
+  m.stack.assign(m.size, 0);
+}
+
 // fastscape_RB+P.cpp:368-370 also sets the capacities used by its asserts.
 void prepare(fsref_rbp::FastScape_RBP &m) {
   m.stack_width = m.size;
@@ -88,14 +98,26 @@ void phase(M &m, int p) {
 
 }  // namespace
 
+// Variants 0 (RB) and 1 (RB+P), which have a level table.
 #define FSREF_DISPATCH(variant, obj, EXPR)                                   \
   do {                                                                       \
     if ((variant) == 0) {                                                    \
       auto &m = *static_cast<fsref_rb::FastScape_RB *>(obj);                 \
       EXPR;                                                                  \
-    } else {                                                                 \
+    } else if ((variant) == 1) {                                             \
       auto &m = *static_cast<fsref_rbp::FastScape_RBP *>(obj);               \
       EXPR;                                                                  \
+    }                                                                        \
+  } while (0)
+
+// All three variants, 2 being BW (fastscape_BW.cpp, the DFS stack order).
+#define FSREF_DISPATCH3(variant, obj, EXPR)                                  \
+  do {                                                                       \
+    if ((variant) == 2) {                                                    \
+      auto &m = *static_cast<fsref_bw::FastScape_BW *>(obj);                 \
+      EXPR;                                                                  \
+    } else {                                                                 \
+      FSREF_DISPATCH(variant, obj, EXPR);                                    \
     }                                                                        \
   } while (0)
 
@@ -117,18 +139,21 @@ void fsref_seed(unsigned long seed) { seed_rand(seed); }
 
 void *fsref_create(int variant, int W, int H) {
   if (variant == 0) return new fsref_rb::FastScape_RB(W, H);
+  if (variant == 2) return new fsref_bw::FastScape_BW(W, H);
   return new fsref_rbp::FastScape_RBP(W, H);
 }
 
 void fsref_destroy(int variant, void *obj) {
   if (variant == 0)
     delete static_cast<fsref_rb::FastScape_RB *>(obj);
+  else if (variant == 2)
+    delete static_cast<fsref_bw::FastScape_BW *>(obj);
   else
     delete static_cast<fsref_rbp::FastScape_RBP *>(obj);
 }
 
 void fsref_constants(int variant, void *obj, double *out) {
-  FSREF_DISPATCH(variant, obj, {
+  FSREF_DISPATCH3(variant, obj, {
     out[0] = m.keq; out[1] = m.neq; out[2] = m.meq; out[3] = m.ueq;
     out[4] = m.dt; out[5] = m.dr[0]; out[6] = m.dr[1]; out[7] = m.tol;
     out[8] = m.cell_area;
@@ -136,23 +161,23 @@ void fsref_constants(int variant, void *obj, double *out) {
 }
 
 void fsref_get_h(int variant, void *obj, double *out) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(out, m.h.data(), sizeof(double) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(out, m.h.data(), sizeof(double) * m.size));
 }
 
 void fsref_set_h(int variant, void *obj, const double *in) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(m.h.data(), in, sizeof(double) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(m.h.data(), in, sizeof(double) * m.size));
 }
 
 void fsref_prepare(int variant, void *obj) {
-  FSREF_DISPATCH(variant, obj, prepare(m));
+  FSREF_DISPATCH3(variant, obj, prepare(m));
 }
 
 void fsref_phase(int variant, void *obj, int p) {
-  FSREF_DISPATCH(variant, obj, phase(m, p));
+  FSREF_DISPATCH3(variant, obj, phase(m, p));
 }
 
 void fsref_step(int variant, void *obj) {
-  FSREF_DISPATCH(variant, obj, for (int p = 0; p < 6; p++) phase(m, p));
+  FSREF_DISPATCH3(variant, obj, for (int p = 0; p < 6; p++) phase(m, p));
 }
 
 int fsref_nlevel(int variant, void *obj) {
@@ -162,33 +187,33 @@ int fsref_nlevel(int variant, void *obj) {
 }
 
 void fsref_get_rec(int variant, void *obj, int32_t *out) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(out, m.rec.data(), sizeof(int) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(out, m.rec.data(), sizeof(int) * m.size));
 }
 void fsref_get_ndon(int variant, void *obj, int32_t *out) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(out, m.ndon.data(), sizeof(int) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(out, m.ndon.data(), sizeof(int) * m.size));
 }
 void fsref_get_donor(int variant, void *obj, int32_t *out) {
-  FSREF_DISPATCH(variant, obj,
-                 std::memcpy(out, m.donor.data(), sizeof(int) * 8 * static_cast<size_t>(m.size)));
+  FSREF_DISPATCH3(variant, obj,
+                  std::memcpy(out, m.donor.data(), sizeof(int) * 8 * static_cast<size_t>(m.size)));
 }
 void fsref_get_stack(int variant, void *obj, int32_t *out) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(out, m.stack.data(), sizeof(int) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(out, m.stack.data(), sizeof(int) * m.size));
 }
 void fsref_get_levels(int variant, void *obj, int32_t *out, int n) {
   FSREF_DISPATCH(variant, obj, std::memcpy(out, m.levels.data(), sizeof(int) * n));
 }
 void fsref_get_accum(int variant, void *obj, double *out) {
-  FSREF_DISPATCH(variant, obj, std::memcpy(out, m.accum.data(), sizeof(double) * m.size));
+  FSREF_DISPATCH3(variant, obj, std::memcpy(out, m.accum.data(), sizeof(double) * m.size));
 }
 
 // The reference's PrintDEM (fastscape_RB.cpp:20-40) of the current h.
 void fsref_print_dem(int variant, void *obj, const char *path) {
-  FSREF_DISPATCH(variant, obj, fsref_rb::PrintDEM(path, m.h, m.width, m.height));
+  FSREF_DISPATCH3(variant, obj, fsref_rb::PrintDEM(path, m.h, m.width, m.height));
 }
 
 // The reference's own run(): nstep+1 timesteps, prints its `p`/`t` lines.
 void fsref_run(int variant, void *obj, int nstep) {
-  FSREF_DISPATCH(variant, obj, m.run(nstep));
+  FSREF_DISPATCH3(variant, obj, m.run(nstep));
   std::cout.flush();
 }
 

@@ -235,3 +235,29 @@ def test_table_growth_large_basin(pkg, oracle, n):
         pkg.check(pkg.library().fs_test_table_capacity(m.handle, C.byref(cap)))
         assert cap.value > 65536 and ref["accum"].max() / p.cell_area > 65536
         assert m.steps_executed() == 3
+
+
+@pytest.mark.parametrize("W,H,n", [(64, 64, 1), (301, 157, 1), (90, 90, 2)])
+def test_braun_willett_order(pkg, oracle, W, H, n):
+    """fs_get_stack_dfs equals the reference Braun-Willett stack order
+    (fastscape_BW.cpp:201-221, pinned against the reference by
+    tests/test_oracle_pin.py::test_bw_dfs_order) and its stack_start."""
+    p = pkg.workload_params() if n == 1 else pkg.reference_params()
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_PHILOX, seed=W) as m:
+        for _ in range(3):
+            m.step(1)
+            stack, starts = m.stack_dfs()
+            want, want_starts = oracle.order_bw(m.receivers(), W, H)
+            assert np.array_equal(stack, want)
+            assert np.array_equal(starts, want_starts)
+
+
+def test_braun_willett_order_valley(pkg, oracle):
+    """Deep trees (hundreds of levels) through one basin."""
+    W, H = 200, 180
+    with pkg.FastScape_RBP(W, H, params=pkg.workload_params(), init=pkg.INIT_ZERO) as m:
+        m.setH(valley(W, H))
+        m.step(2)
+        stack, starts = m.stack_dfs()
+        want, want_starts = oracle.order_bw(m.receivers(), W, H)
+        assert np.array_equal(stack, want) and np.array_equal(starts, want_starts)

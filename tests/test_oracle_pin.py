@@ -70,3 +70,22 @@ def test_reference_run_semantics(oracle):
     h = oracle.terrain(40, 40, 0)
     oracle.steps(h, 40, 40, workload_params(), 8, parallel=True)
     assert np.array_equal(m.get_h(), h)
+
+
+@pytest.mark.parametrize("W,H,text", [(30, 30, "pristine"), (57, 41, "param"), (5, 5, "param")])
+def test_bw_dfs_order(oracle, W, H, text):
+    """fso_order_bw == the reference Braun-Willett FastScape_BW's stack
+    (fastscape_BW.cpp:201-221), over several timesteps; its elevations equal
+    the level-ordered RB's."""
+    from oracle.pyoracle import REFERENCE_PARAMS
+    p = REFERENCE_PARAMS if text == "pristine" else workload_params()
+    bw = RefHarness(text, "exact").model(W, H, p, 2)
+    h = oracle.terrain(W, H, 0)
+    for s in range(5):
+        r = bw.bw_phases()
+        q = oracle.phases(h, W, H, p)
+        stack, starts = oracle.order_bw(q["rec"], W, H)
+        assert np.array_equal(r["rec"], q["rec"])
+        assert np.array_equal(r["stack"], stack), f"step {s}"
+        assert np.array_equal(r["h"], q["h"]), f"step {s}"
+        assert starts[-1] == W * H and np.all(q["rec"][stack[starts[:-1]]] == -1)
