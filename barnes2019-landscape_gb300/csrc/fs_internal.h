@@ -78,15 +78,25 @@ struct Tile {
 constexpr int kPit = -2;
 
 // Erosion table: one 64-byte record per drainage count k (cells), holding
-// for each direction class (0 orthogonal, 1 diagonal) at doubles 4*cls+0..2:
+// for each direction class (0 orthogonal, 1 diagonal) at doubles 4*cls+0..3:
 //   F = keq*dt*pow(k*cell_area, meq)/pow(dr_cls, neq)  (fastscape_RB.cpp:315)
 //   D = 1 + F          (the n = 1 Newton denominator, fastscape_RB.cpp:322)
 //   R = RN(1/D)        (reciprocal for the correctly rounded division)
+//   -R                 (the same, negated)
 constexpr int kTabStride = 8;
 
-// Tiles: receivers over the interior [2, W-3]^2, donors over [1, W-2]^2.
+// Tiles: receivers over the interior [2, W-3]^2; donors over [1, W-2]^2
+// with tiles starting at x = 0, 128, 256, ... (four cells per thread, so a
+// row of a realization whose byte offset is a multiple of 4 is stored in
+// whole words).
 constexpr int kRxTile = 32, kRyTile = 32;
-constexpr int kDxTile = 32, kDyTile = 64;
+constexpr int kDxTile = 128, kDyTile = 32;
+
+// The donor kernel reads rec as aligned 32-bit words around each tile row,
+// up to 8 bytes before the first and 144 bytes past the last byte of a
+// realization: rec buffers keep kRecPad readable bytes on both sides that no
+// kernel writes while the donor kernel runs.
+constexpr size_t kRecPad = 256;
 
 // Where an error was detected (Ctl::err_detail).
 enum ErrPhase : int {
@@ -107,8 +117,7 @@ enum NMode : int {
 // Arrays indexed by position i in the level order (the reference's stack):
 //   ent[i]   cell index (local); level 0 starts with the two rings (fixed)
 //            followed by the pits of this timestep
-//   pdir[i]  receiver direction of ent[i] (0..7), bit 3 set when that
-//            receiver is a pit (levels >= 1 only)
+//   pdir[i]  receiver direction of ent[i] (0..7)
 //   nd[i]    number of donors of ent[i]
 //   kid[i]   position of its first donor (local); its donors are contiguous
 //   acc[i]   drainage cell count of ent[i]

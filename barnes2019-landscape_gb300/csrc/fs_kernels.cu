@@ -171,6 +171,30 @@ __device__ __forceinline__ long long abs_bits(double x) {
   return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll;
 }
 
+// FP64 add / multiply of bit patterns held in integer registers. Keeping
+// elevations as integers between the FP64 instructions avoids the FP64
+// moves the compiler otherwise emits for merges, selects and negations of
+// doubles (each an instruction on this part's narrow FP64 pipe).
+__device__ __forceinline__ uint64_t fadd_bits(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "add.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+
+__device__ __forceinline__ uint64_t fmul_bits(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "mul.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+
+constexpr uint64_t kSignBit = 0x8000000000000000ull;
+
 // ---------------------------------------------------------------------------
 // 1. Receivers: fastscape_RB.cpp:160-182. slope = (h[c]-h[n])/dr[n], strict
 // '>' against a running maximum that starts at 0, so the first maximum in
@@ -221,7 +245,8 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 // a_n = fl(fl(f_c - f_n) * g_n) with g_n = fl(1/dr_n); then for the exact
 // reference slope q_n = RN(RN(h_c-h_n)/dr_n):
 //   |a_n - q_n| <= 2^-20 * gmax * (M + 2^-100) =: E/2,
-// M = max |f| over the 3x3 window, gmax = max g_n. So
+// M >= max |f| over the 3x3 window (the kernel takes the maximum over the
+// whole staged tile, which only widens the bound), gmax = max g_n. So
 //   best - second > 2E  and best > E  => q_best is the unique maximum > 0;
 //   best < -E                         => every q_n < 0 (NO_FLOW);
 // otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
@@ -229,8 +254,7 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 // Truncation of a double to FP32 with integer operations only (no FP64
 // pipe): rebias the exponent, keep the top 23 fraction bits. Values below
 // 2^-126 flush to signed zero; |x| >= 2^128, Inf and NaN give NaN.
-__device__ __forceinline__ float trunc_to_float(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+__device__ __forceinline__ float trunc_bits_to_float(unsigned long long b) {
   const unsigned hi = (unsigned)(b >> 32);
   const unsigned sign = hi & 0x80000000u;
   const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
@@ -240,79 +264,93 @@ __device__ __forceinline__ float trunc_to_float(double x) {
   return __uint_as_float(sign | ((unsigned)e << 23) | frac);
 }
 
+__device__ __forceinline__ float trunc_to_float(double x) {
+  return trunc_bits_to_float((unsigned long long)__double_as_longlong(x));
+}
+
 __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   if (stopped(a.ctl)) return;
   __shared__ float s[kRyTile + 2][kRxTile + 3];
+  __shared__ unsigned s_wmax[8];
   const Tile t = a.rtiles[blockIdx.x];
   const RealDesc &d = a.desc[t.r];
   const int W = d.W, H = d.H;
   const double *h = a.h + d.off;
   int8_t *rec = a.rec + d.off;
   const int x0 = t.x0 - 1, y0 = t.y0 - 1;  // grid coordinates of s[0][0]
-  for (int ly = threadIdx.y; ly < kRyTile + 2; ly += 8) {
-    const int gy = y0 + ly;
-    for (int lx = threadIdx.x; lx < kRxTile + 2; lx += 32) {
-      const int gx = x0 + lx;
-      s[ly][lx] = (gx < W && gy < H) ? trunc_to_float(h[gy * W + gx]) : 0.f;
-    }
+  // Stage the tile and its halo; M = max |f| and whether any value is NaN
+  // (|h| >= 2^128, Inf, NaN) are taken over the whole tile.
+  float m = 0.f;
+  bool bad = false;
+  constexpr int kSw = kRxTile + 2, kSn = (kRyTile + 2) * kSw;
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < kSn; i += 256) {
+    const int ly = i / kSw, lx = i - ly * kSw;
+    const int gx = x0 + lx, gy = y0 + ly;
+    const float f = (gx < W && gy < H) ? trunc_to_float(h[gy * W + gx]) : 0.f;
+    s[ly][lx] = f;
+    m = fmaxf(m, fabsf(f));
+    bad |= !(f == f);
   }
-  __syncthreads();
-  const float g_orth = d.g_orth, g_diag = d.g_diag, gmax = d.gmax;
-  const int lane = threadIdx.x;
+  const unsigned wm = __reduce_max_sync(kFull, __float_as_uint(m));  // m >= 0: bits order
+  if (threadIdx.x == 0) s_wmax[threadIdx.y] = wm;
+  const bool tile_bad = __syncthreads_or(bad) != 0;
+  float M = 0.f;
+#pragma unroll
+  for (int w = 0; w < 8; w++) M = fmaxf(M, __uint_as_float(s_wmax[w]));
+  const float g_orth = d.g_orth, g_diag = d.g_diag;
+  const float E = 0x1p-19f * d.gmax * (M + 0x1p-100f);
   const int lx = threadIdx.x + 1;
   const int gx = x0 + lx;
+  unsigned qbits = 0;  // bit r: the cell of row pass r is queued
 #pragma unroll 1
   for (int r = 0; r < kRyTile / 8; r++) {
     const int ly = threadIdx.y + 8 * r + 1;
     const int gy = y0 + ly;
     const bool valid = gx < W - 2 && gy < H - 2;
-    bool queue = false;
     if (valid) {
       const float fc = s[ly][lx];
       const float f[8] = {s[ly][lx - 1], s[ly - 1][lx - 1], s[ly - 1][lx],
                           s[ly - 1][lx + 1], s[ly][lx + 1], s[ly + 1][lx + 1],
                           s[ly + 1][lx], s[ly + 1][lx - 1]};
+      // Largest and second largest approximate slope; the first maximum in
+      // neighbour order keeps bn (an exact tie leaves best == second, which
+      // queues the cell). Without NaN in the tile no slope is NaN (an
+      // overflowing difference is +-Inf, and Inf - Inf below only queues).
       float best = -INFINITY, second = -INFINITY;
       int bn = 0;
-      float M = fabsf(fc);
-      bool bad = !(fc == fc);
 #pragma unroll
       for (int n = 0; n < 8; n++) {
         const float av = (fc - f[n]) * ((n & 1) ? g_diag : g_orth);
-        M = fmaxf(M, fabsf(f[n]));
-        bad |= !(av == av);
-        if (av > best) {
-          second = best;
-          best = av;
-          bn = n;
-        } else if (av > second) {
-          second = av;
-        }
+        bn = av > best ? n : bn;
+        second = fmaxf(second, fminf(best, av));
+        best = fmaxf(best, av);
       }
-      const float E = 0x1p-19f * gmax * (M + 0x1p-100f);
-      int code = 0;
-      queue = true;
-      if (!bad) {
-        if (best - second > 2.f * E && best > E) {
-          code = bn;
-          queue = false;
-        } else if (best < -E) {
-          code = kPit;
-          queue = false;
-        }
+      int code = -1;
+      if (!tile_bad) {
+        if (best - second > 2.f * E && best > E) code = bn;
+        else if (best < -E) code = kPit;
       }
-      if (!queue) rec[gy * W + gx] = (int8_t)code;
+      if (code != -1) rec[gy * W + gx] = (int8_t)code;
+      else qbits |= 1u << r;
     }
-    const unsigned bq = __ballot_sync(kFull, queue);
-    if (bq) {
-      int base = 0;
-      if (lane == 0) base = atomicAdd(&a.ctl->amb, __popc(bq));
-      base = __shfl_sync(kFull, base, 0);
-      if (queue) {
-        const int q = base + __popc(bq & ((1u << lane) - 1u));
-        a.amb[q] = d.off + gy * W + gx;
-        a.amb_r[q] = t.r;
-      }
+  }
+  // The queued cells of the tile, placed with one atomic per tile (a
+  // counter shared by the whole grid would serialise on one address).
+  int total;
+  const int tt = threadIdx.y * 32 + threadIdx.x;
+  const int excl = block_excl_scan(__popc(qbits), total, tt, 256);
+  if (total == 0) return;
+  __shared__ int s_qbase;
+  if (tt == 0) s_qbase = atomicAdd(&a.ctl->amb, total);
+  __syncthreads();
+  int q = s_qbase + excl;
+#pragma unroll 1
+  for (int r = 0; r < kRyTile / 8; r++) {
+    if (qbits >> r & 1u) {
+      const int gy = y0 + threadIdx.y + 8 * r + 1;
+      a.amb[q] = d.off + gy * W + gx;
+      a.amb_r[q] = t.r;
+      ++q;
     }
   }
 }
@@ -335,57 +373,106 @@ __global__ void __launch_bounds__(256) k_receivers_fixup(StepArgs a) {
 // Level 0 = every cell without a receiver (fastscape_RB.cpp:221-227): the
 // two outer rings, which never change and sit at ent[0, nring) of their
 // realization from creation on, and the interior pits, appended here with
-// one atomic per 32x64 tile.
+// one atomic per tile.
+//
+// Four cells per thread, as bytes of one 32-bit word: a tile's rows are
+// staged as aligned words of rec, each thread extracts the words of its
+// cells' left, centre and right neighbours with funnel shifts, and a
+// byte-wise equality test against the direction code gives the eight mask
+// bits of four cells at once.
 // ---------------------------------------------------------------------------
+
+// 0x80 in every byte of x equal to the byte t, 0 in the others (no carry
+// crosses a byte: (y & 0x7F) + 0x7F <= 0xFE).
+__device__ __forceinline__ unsigned bytes_eq(unsigned x, unsigned t) {
+  const unsigned y = x ^ (t * 0x01010101u);
+  return ~(((y & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | y) & 0x80808080u;
+}
+
+constexpr int kDRows = kDyTile / 8;       // consecutive rows per thread
+constexpr int kDWords = kDxTile / 4 + 4;  // staged words per row
+
 __global__ void __launch_bounds__(256) k_donors_level0(StepArgs a) {
   if (stopped(a.ctl)) return;
-  __shared__ int8_t sr[kDyTile + 2][kDxTile + 4];
+  __shared__ unsigned S[kDyTile + 2][kDWords];
+  __shared__ int s_sh[kDyTile + 2];
   __shared__ int s_base;
   const Tile t = a.dtiles[blockIdx.x];
   const RealDesc &d = a.desc[t.r];
   const int W = d.W, H = d.H;
   const int8_t *rec = a.rec + d.off;
-  const int x0 = t.x0 - 1, y0 = t.y0 - 1;  // grid coordinates of sr[0][0]
   const int tt = threadIdx.y * 32 + threadIdx.x;
+  // Staged row ly = grid row y0-1+ly (clamped to the grid: rows past it only
+  // feed cells that are not written), as the aligned words from the one
+  // holding byte x0-4 on; s_sh = position of byte x0-4 in the first word.
+  // The reads stay within kRecPad bytes of the realization.
   for (int ly = threadIdx.y; ly < kDyTile + 2; ly += 8) {
-    const int gy = y0 + ly;
-    for (int lx = threadIdx.x; lx < kDxTile + 2; lx += 32) {
-      const int gx = x0 + lx;
-      sr[ly][lx] = (gx < W && gy < H) ? rec[gy * W + gx] : (int8_t)FS_NO_FLOW;
-    }
+    const int gy = min(t.y0 - 1 + ly, H - 1);
+    const uintptr_t first = reinterpret_cast<uintptr_t>(rec + (size_t)gy * W + t.x0) - 4;
+    const unsigned *src = reinterpret_cast<const unsigned *>(first & ~(uintptr_t)3);
+    for (int j = threadIdx.x; j < kDWords; j += 32) S[ly][j] = __ldg(src + j);
+    if (threadIdx.x == 0) s_sh[ly] = (int)(first & 3);
   }
   __syncthreads();
-  const int lx = threadIdx.x + 1;
-  const int gx = x0 + lx;
-  constexpr int kRows = kDyTile / 8;
-  unsigned pit_bits = 0;
+  const int gx0 = t.x0 + 4 * threadIdx.x;   // the thread's first cell
+  const int ly0 = 1 + kDRows * threadIdx.y;  // its first staged row
+  // left / centre / right neighbour words of the four cells in staged row ly
+  auto words = [&](int ly, unsigned &L, unsigned &C, unsigned &R) {
+    const int p = 3 + s_sh[ly] + 4 * threadIdx.x;  // byte of the first left neighbour
+    const int sh = (p & 3) * 8;
+    const unsigned *w = &S[ly][p >> 2];
+    const unsigned w0 = w[0], w1 = w[1], w2 = w[2];
+    L = __funnelshift_r(w0, w1, sh);
+    C = __funnelshift_rc(w0, w1, sh + 8);
+    R = sh <= 16 ? __funnelshift_rc(w0, w1, sh + 16) : __funnelshift_r(w1, w2, sh - 16);
+  };
+  unsigned vx = 0;  // 0xFF in the bytes of cells with 1 <= x <= W-2
 #pragma unroll
-  for (int r = 0; r < kRows; r++) {
-    const int ly = threadIdx.y + 8 * r + 1;
-    const int gy = y0 + ly;
-    if (gx <= W - 2 && gy <= H - 2) {
-      unsigned m = 0;
-      m |= (sr[ly][lx - 1] == 4) ? 1u : 0u;         // W  neighbour drains E
-      m |= (sr[ly - 1][lx - 1] == 5) ? 2u : 0u;     // NW drains SE
-      m |= (sr[ly - 1][lx] == 6) ? 4u : 0u;         // N  drains S
-      m |= (sr[ly - 1][lx + 1] == 7) ? 8u : 0u;     // NE drains SW
-      m |= (sr[ly][lx + 1] == 0) ? 16u : 0u;        // E  drains W
-      m |= (sr[ly + 1][lx + 1] == 1) ? 32u : 0u;    // SE drains NW
-      m |= (sr[ly + 1][lx] == 2) ? 64u : 0u;        // S  drains N
-      m |= (sr[ly + 1][lx - 1] == 3) ? 128u : 0u;   // SW drains NE
-      a.mask[d.off + gy * W + gx] = (uint8_t)m;
-      if (sr[ly][lx] == kPit) pit_bits |= 1u << r;
+  for (int j = 0; j < 4; j++)
+    if (gx0 + j >= 1 && gx0 + j <= W - 2) vx |= 0xFFu << (8 * j);
+  unsigned UL, UC, UR, ML, MC, MR, DL, DC, DR;
+  words(ly0 - 1, UL, UC, UR);
+  words(ly0, ML, MC, MR);
+  uint8_t *mask = a.mask + d.off;
+  unsigned pits[kDRows];
+  int npit = 0;
+#pragma unroll
+  for (int i = 0; i < kDRows; i++) {
+    const int gy = t.y0 + kDRows * threadIdx.y + i;
+    words(ly0 + i + 1, DL, DC, DR);
+    const unsigned m = (bytes_eq(ML, 4) >> 7) | (bytes_eq(UL, 5) >> 6) |   // W, NW
+                       (bytes_eq(UC, 6) >> 5) | (bytes_eq(UR, 7) >> 4) |   // N, NE
+                       (bytes_eq(MR, 0) >> 3) | (bytes_eq(DR, 1) >> 2) |   // E, SE
+                       (bytes_eq(DC, 2) >> 1) | bytes_eq(DL, 3);           // S, SW
+    const unsigned v = gy <= H - 2 ? vx : 0u;
+    pits[i] = bytes_eq(MC, (unsigned)(uint8_t)kPit) & v;
+    npit += __popc(pits[i]);
+    if (v) {
+      uint8_t *row = mask + (size_t)gy * W + gx0;
+      if (v == 0xFFFFFFFFu && (reinterpret_cast<uintptr_t>(row) & 3) == 0) {
+        *reinterpret_cast<unsigned *>(row) = m;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if ((v >> (8 * j)) & 1u) row[j] = (uint8_t)(m >> (8 * j));
+      }
     }
+    UL = ML; UC = MC; UR = MR;
+    ML = DL; MC = DC; MR = DR;
   }
   int total;
-  const int excl = block_excl_scan(__popc(pit_bits), total, tt, 256);
+  const int excl = block_excl_scan(npit, total, tt, 256);
   if (total == 0) return;
   if (tt == 0) s_base = d.off + d.nring + atomicAdd(&a.rctl[t.r].top, total);
   __syncthreads();
   int pos = s_base + excl;
 #pragma unroll
-  for (int r = 0; r < kRows; r++)
-    if (pit_bits >> r & 1u) a.ent[pos++] = (y0 + threadIdx.y + 8 * r + 1) * W + gx;
+  for (int i = 0; i < kDRows; i++) {
+    const int gy = t.y0 + kDRows * threadIdx.y + i;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if ((pits[i] >> (8 * j + 7)) & 1u) a.ent[pos++] = gy * W + gx0 + j;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -415,6 +502,38 @@ __device__ __forceinline__ double div_rn(double num, double D, double R) {
   return num / D;
 }
 
+// -RN(num/D) on bit patterns, given D > 0, R = RN(1/D) and Rn = -R: the
+// div_rn sequence with every quotient carried negated (RN is symmetric, so
+// q0n = RN(num*Rn) = -q0 and q1n = RN(r0*Rn + q0n) = -q1 exactly), which
+// puts the negations into the operands instead of separate instructions.
+// The caller adds the result to h0 directly. The IEEE division fallback is
+// volatile PTX in a branch; the numerator and result stay in integer
+// registers.
+__device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double R,
+                                                    double Rn) {
+  const double num = __longlong_as_double(numb);
+  const double q0n = num * Rn;
+  const double r0 = fma(q0n, D, num);
+  const double q1n = fma(r0, Rn, q0n);
+  const double r1 = fma(q1n, D, num);
+  // Magnitudes are compared with the sign shifted out (x << 1) rather than
+  // masked: the compiler turns a sign mask of a double into an FP64
+  // absolute value.
+  const uint64_t q1b = (uint64_t)__double_as_longlong(q1n);
+  const int e = (int)((q1b << 1) >> 53);
+  if (e >= 64 && e <= 1980 && (q1b << 12) != 0) {
+    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1076) << 52));
+    if (((uint64_t)__double_as_longlong(r1) << 1) < (thr << 1)) return q1b;
+  }
+  uint64_t r;
+  asm volatile(
+      "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(numb), "l"((uint64_t)__double_as_longlong(D)));
+  return r ^ kSignBit;
+}
+
 // pow(x, n) and pow(x, n-1) for the Newton update of fastscape_RB.cpp:322.
 template <int NMODE>
 __device__ __forceinline__ void powers(double x, double neq, double &pn, double &pn1) {
@@ -430,47 +549,58 @@ __device__ __forceinline__ void powers(double x, double neq, double &pn, double 
   }
 }
 
-// Erosion of one cell: fastscape_RB.cpp:315-326 with h0 the uplifted
-// elevation, hn the receiver's final elevation and T the table record of the
-// cell's drainage count and direction class (T[0] = fact).
+// Erosion of one cell for n = 1 (fastscape_RB.cpp:315-326) on bit
+// patterns: h0 the uplifted elevation, hn the receiver's final elevation,
+// Tb the table record of the cell's drainage count and direction class
+// (fact, D = 1 + fact, R = 1/D).
+//
+// First iterate: hnew - h0 = +0, pow(x,1) = x and pow(x,0) = 1, so
+// hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)).
+__device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
+                                                  const unsigned long long *Tb, uint64_t h0,
+                                                  uint64_t hn) {
+  const uint64_t factb = Tb[0];
+  const double D = __longlong_as_double(Tb[1]), R = __longlong_as_double(Tb[2]);
+  const uint64_t num = fmul_bits(factb, fadd_bits(h0, hn ^ kSignBit));
+  const uint64_t qn = neg_div_rn_bits(num, D, R, __longlong_as_double(Tb[3]));  // -q
+  const uint64_t hnew = fadd_bits(h0, qn);
+  // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
+  // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
+  // truncated magnitudes (each within 2^-23 relative, flushed below
+  // 2^-126) with 2^-21 of slack proves it for almost every cell without
+  // the subtraction; the rest evaluate diff and follow the loop in FP64.
+  const float qf = fabsf(trunc_bits_to_float(qn));
+  const float hf = fabsf(trunc_bits_to_float(h0));
+  if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= d.tol_lo_f) return hnew;
+  const double fact = __longlong_as_double(factb), h0d = __longlong_as_double(h0),
+               hnd = __longlong_as_double(hn);
+  double x = __longlong_as_double(hnew);
+  double diff = x - h0d, hp = x;
+  int it = 1;
+  // fabs(diff) > tol as an integer compare of the magnitudes' bits (both
+  // non-negative; a NaN diff stops the loop, as fabs(NaN) > tol is false)
+  while (abs_bits(diff) > d.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
+    const double num2 = (x - h0d) + fact * (x - hnd);
+    x -= div_rn(num2, D, R);
+    diff = x - hp;
+    hp = x;
+    if (++it >= kNewtonMaxIt) {
+      raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
+      break;
+    }
+  }
+  return (uint64_t)__double_as_longlong(x);
+}
+
+// Erosion of one cell for n != 1: fastscape_RB.cpp:315-326 with h0 the
+// uplifted elevation, hn the receiver's final elevation and T the table
+// record of the cell's drainage count and direction class (T[0] = fact).
 template <int NMODE>
 __device__ __forceinline__ double erode_cell(const RealDesc &d, double neq, Ctl *ctl,
                                              const double *T, double h0, double hn) {
   const double fact = T[0];
   double hnew, hp, diff;
   int it;
-  if (NMODE == kNOne) {
-    // First iterate: hnew - h0 = +0, pow(x,1) = x and pow(x,0) = 1, so
-    // hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)) with D = RN(1+fact).
-    const double D = T[1], R = T[2];
-    const double num = fact * (h0 - hn);
-    const double q = div_rn(num, D, R);
-    hnew = h0 - q;
-    // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
-    // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
-    // truncated magnitudes (each within 2^-23 relative, flushed below
-    // 2^-126) with 2^-21 of slack proves it for almost every cell without
-    // the FP64 subtraction; the rest evaluate diff and follow the loop.
-    const float qf = fabsf(trunc_to_float(q));
-    const float hf = fabsf(trunc_to_float(h0));
-    if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= d.tol_lo_f) return hnew;
-    diff = hnew - h0;
-    hp = hnew;
-    it = 1;
-    // fabs(diff) > tol as an integer compare of the magnitudes' bits (both
-    // non-negative; a NaN diff stops the loop, as fabs(NaN) > tol is false)
-    while (abs_bits(diff) > d.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
-      const double num2 = (hnew - h0) + fact * (hnew - hn);
-      hnew -= div_rn(num2, D, R);
-      diff = hnew - hp;
-      hp = hnew;
-      if (++it >= kNewtonMaxIt) {
-        raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
-        break;
-      }
-    }
-    return hnew;
-  }
   hnew = h0;
   hp = h0;
   diff = 2 * d.tol;
@@ -624,13 +754,10 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
           if (rr < q_hi) {
             for (int skip = rr - ofirst; skip > 0; --skip) om &= om - 1;
             const int k = __ffs(om) - 1;
-            // level-1 entries remember whether their receiver is a pit
-            // (a level-0 entry past the rings)
-            const unsigned pit = (L == 0 && wbase + 32 * q + o >= d.nring) ? 8u : 0u;
             const int pos = cbase + rr;
             if (pos < d.size) {
               ent[pos] = oc + nbr_off(k, d.W);
-              a.pdir[d.off + pos] = (uint8_t)(((k + 4) & 7) | pit);
+              a.pdir[d.off + pos] = (uint8_t)((k + 4) & 7);
             } else {
               raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
             }
@@ -759,6 +886,12 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
           if (a.do_erode && Lv > 0 && s >= (uint32_t)d.tab_cap) {
             if (atomicMax(&ctl->abort_k, (int)s) < (int)s) ctl->abort_r = rr[u];
           }
+          if (Lv == 0 && a.do_erode && ii[u] >= d.nring) {
+            // a pit (level 0 past the rings): uplift it (fastscape_RB.cpp:291-295)
+            unsigned long long *hh = reinterpret_cast<unsigned long long *>(a.h + d.off);
+            const int c = __ldcg(&a.ent[d.off + ii[u]]);
+            hh[c] = fadd_bits(__ldcg(&hh[c]), (uint64_t)__double_as_longlong(d.u_dt));
+          }
         }
       }
     }
@@ -766,32 +899,16 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
   }
   lap(1);
   if (!a.do_erode) return;
+  // The pits were uplifted in the level-0 pass above (reached only when no
+  // count exceeded an erosion table, so no timestep that the host repeats
+  // has changed h); level 1 reads them after this barrier.
+  if (maxlev > 1 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
 
   // ---- uplift + erosion: fastscape_RB.cpp:285-296 and :306-328 in the
   // level order of fastscape_RB+P.cpp:319-350. Eroded cells are uplifted on
-  // their first read; level-1 cells add the uplift of a pit receiver on
-  // read, and the pits themselves are uplifted once no level-1 cell can read
-  // them any more (during level 2, or after a barrier when level 1 is the
-  // deepest). No barrier is needed before level 1: it reads counts complete
-  // since the barrier after accumulation level 1 and never-written h.
-  auto uplift_pits = [&]() {
-    // pits of realization r: level-0 positions [nring, lvl_off[1])
-    __syncthreads();  // every warp is done with the level's ranges
-    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
-      const RealDesc &d = desc(r);
-      s_lo[r] = d.nring;
-      s_hi[r] = __ldcg(&a.lvl_off[d.lvl_base + 1]);
-    }
-    __syncthreads();
-    const int np = block_prefix(nreal, [&](int r) { return s_hi[r] - s_lo[r]; }, s_pre);
-    for (int g = tid; g < np; g += nthreads) {
-      const int r = real_of(g);
-      const RealDesc &d = desc(r);
-      const int c = __ldcg(&a.ent[d.off + s_lo[r] + (g - s_pre[r])]);
-      double *hh = a.h + d.off;
-      hh[c] = __ldcg(&hh[c]) + d.u_dt;
-    }
-  };
+  // their first read (uplift of every interior cell precedes erosion in the
+  // reference; a cell's h is read first by its own erosion, its receiver's
+  // h is final).
   for (int Lv = 1; Lv < maxlev; ++Lv) {
     const int ngroups = level_groups(Lv);
     for (int g0 = warp_global * kEroU; g0 < ngroups; g0 += nwarps * kEroU) {
@@ -819,37 +936,43 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
           }
         }
       }
-      double hc[kEroU], hn[kEroU];
+      // elevations as bit patterns (integer registers, see fadd_bits)
+      uint64_t hc[kEroU], hn[kEroU];
 #pragma unroll
       for (int u = 0; u < kEroU; u++) {
-        hc[u] = 0.0;
-        hn[u] = 0.0;
+        hc[u] = 0;
+        hn[u] = 0;
         if (ok[u]) {
           const RealDesc &d = desc(rr[u]);
-          const double *hh = a.h + d.off;
+          const unsigned long long *hh =
+              reinterpret_cast<const unsigned long long *>(a.h + d.off);
           hc[u] = __ldcg(&hh[cc[u]]);
-          hn[u] = __ldcg(&hh[cc[u] + nbr_off(dd[u] & 7, d.W)]);
+          hn[u] = __ldcg(&hh[cc[u] + nbr_off(dd[u], d.W)]);
         }
       }
 #pragma unroll
       for (int u = 0; u < kEroU; u++) {
         if (ok[u]) {
           const RealDesc &d = desc(rr[u]);
-          const double *T = d.tab + (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
-          double hr = hn[u];
-          if (dd[u] & 8) hr = hr + d.u_dt;
-          const double hnew = erode_cell<NMODE>(d, a.neq, ctl, T, hc[u] + d.u_dt, hr);
-          if (!isfinite(hnew)) raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-          a.h[d.off + cc[u]] = hnew;
+          const size_t rec_at = (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
+          const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
+          const uint64_t hr = hn[u];
+          const uint64_t h0 = fadd_bits(hc[u], udt);
+          uint64_t hnew;
+          if (NMODE == kNOne) {
+            hnew = erode_cell_n1(d, ctl, reinterpret_cast<const unsigned long long *>(d.tab) + rec_at,
+                                 h0, hr);
+          } else {
+            hnew = (uint64_t)__double_as_longlong(erode_cell<NMODE>(d, a.neq, ctl, d.tab + rec_at,
+                                                  __longlong_as_double(h0), __longlong_as_double(hr)));
+          }
+          if (((hnew >> 52) & 0x7FF) == 0x7FF)  // Inf or NaN
+            raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+          reinterpret_cast<unsigned long long *>(a.h + d.off)[cc[u]] = hnew;
         }
       }
     }
-    if (Lv == 2) uplift_pits();
     if (Lv + 1 < maxlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
-  }
-  if (maxlev <= 2) {
-    if (maxlev == 2 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
-    uplift_pits();
   }
   lap(2);
   if (tid == 0) atomicAdd(&ctl->steps_done, 1);
@@ -1080,15 +1203,18 @@ int ring_cells(int W, int H) {
 
 int append_tiles(int kind, int r, int W, int H, Tile *out, int cap) {
   // receivers: interior x, y in [2, W-3]; donors: x, y in [1, W-2]
+  // (donor tiles start at x = 0 and cover x in [0, W-2]; x = 0 is skipped)
   const int lo = kind == 0 ? 2 : 1;
+  const int xlo = kind == 0 ? 2 : 0;
   const int iw = W - 2 * lo, ih = H - 2 * lo;
   if (iw <= 0 || ih <= 0) return 0;
   const int tx = kind == 0 ? kRxTile : kDxTile, ty = kind == 0 ? kRyTile : kDyTile;
-  const int nx = (iw + tx - 1) / tx, ny = (ih + ty - 1) / ty;
+  const int xw = W - lo - xlo;  // columns [xlo, W-1-lo]
+  const int nx = (xw + tx - 1) / tx, ny = (ih + ty - 1) / ty;
   if ((long long)nx * ny > cap) return -1;
   int n = 0;
   for (int y = 0; y < ny; y++)
-    for (int x = 0; x < nx; x++) out[n++] = Tile{r, lo + x * tx, lo + y * ty, 0};
+    for (int x = 0; x < nx; x++) out[n++] = Tile{r, xlo + x * tx, lo + y * ty, 0};
   return n;
 }
 
@@ -1107,7 +1233,7 @@ void fill_table_range(double keq, double neq, double meq, double dt, double dr_o
       r[4 * cls + 0] = F;
       r[4 * cls + 1] = D;
       r[4 * cls + 2] = 1. / D;
-      r[4 * cls + 3] = 0.;
+      r[4 * cls + 3] = -(1. / D);
     }
   }
 }
@@ -1123,7 +1249,7 @@ cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s) {
   k_receivers_filter<<<a.nrtiles, dim3(32, 8), 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_receivers_fixup<<<sm_count(), 256, 0, s>>>(a);
+  k_receivers_fixup<<<8 * sm_count(), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -109,6 +109,7 @@ struct fs_batch {
   cudaStream_t stream = nullptr;
   double *h = nullptr;
   int8_t *rec = nullptr;
+  int8_t *rec_alloc = nullptr;  // rec - kRecPad
   uint8_t *mask = nullptr, *pdir = nullptr, *nd = nullptr;
   int32_t *ent = nullptr, *kid = nullptr, *amb = nullptr, *amb_r = nullptr, *lvl = nullptr;
   uint32_t *acc = nullptr;
@@ -155,7 +156,7 @@ void free_batch(fs_batch *b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  void *bufs[] = {b->h, b->rec, b->mask, b->pdir, b->nd, b->ent, b->kid, b->amb, b->amb_r,
+  void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->nd, b->ent, b->kid, b->amb, b->amb_r,
                   b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles};
   for (void *x : bufs) cudaFree(x);
   for (double *t : b->tab) cudaFree(t);
@@ -475,7 +476,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
   const size_t C = static_cast<size_t>(cells);
   if (!cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
       !cu(cudaMalloc(&b->h, C * sizeof(double)), "cudaMalloc(h)") ||
-      !cu(cudaMalloc(&b->rec, C), "cudaMalloc(rec)") ||
+      !cu(cudaMalloc(&b->rec_alloc, C + 2 * fs::kRecPad), "cudaMalloc(rec)") ||
       !cu(cudaMalloc(&b->mask, C), "cudaMalloc(mask)") ||
       !cu(cudaMalloc(&b->pdir, C), "cudaMalloc(pdir)") ||
       !cu(cudaMalloc(&b->nd, C), "cudaMalloc(nd)") ||
@@ -491,6 +492,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
       !cu(cudaMallocHost(&b->h_ctl, sizeof(fs::Ctl)), "cudaMallocHost(ctl)") ||
       !cu(cudaMallocHost(&b->h_rctl, n * sizeof(fs::RealCtl)), "cudaMallocHost(rctl)"))
     return fail(*status);
+  b->rec = b->rec_alloc + fs::kRecPad;
   // Rings keep NO_FLOW forever (fastscape_RB.cpp:361-362) and ring-0 cells
   // never have donors: receivers and masks are written for the interior only.
   if (!cu(cudaMemsetAsync(b->rec, 0xff, C, b->stream), "memset(rec)") ||

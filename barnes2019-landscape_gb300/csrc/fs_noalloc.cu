@@ -57,8 +57,10 @@ constexpr size_t kOffAmb = align256(kOffKid + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAmbR = align256(kOffAmb + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffLvl = align256(kOffAmbR + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAcc = align256(kOffLvl + (kMaxCells + 2) * sizeof(int32_t));
-constexpr size_t kOffRec = align256(kOffAcc + kMaxCells * sizeof(uint32_t));
-constexpr size_t kOffMask = align256(kOffRec + kMaxCells);
+// rec keeps fs::kRecPad bytes on both sides (read, never written, by the
+// donor kernel); acc before it is not written while that kernel runs.
+constexpr size_t kOffRec = align256(kOffAcc + kMaxCells * sizeof(uint32_t) + fs::kRecPad);
+constexpr size_t kOffMask = align256(kOffRec + kMaxCells + fs::kRecPad);
 constexpr size_t kOffPdir = align256(kOffMask + kMaxCells);
 constexpr size_t kOffNd = align256(kOffPdir + kMaxCells);
 constexpr size_t kScratchBytes = align256(kOffNd + kMaxCells);

@@ -357,6 +357,70 @@ def run_ensemble(args, dist, rank, ws, local):
         dist.destroy_process_group()
 
 
+SWEEP_SIDES = (100, 200, 400, 700, 1000, 1500, 2000, 3000, 4000, 5000, 7000, 10000,
+               14000, 20000)
+SWEEP_NSTEP = 120          # run(120): 121 timesteps, the reference's sweep length
+
+
+def run_sweep(args, dist, rank, ws, local):
+    """Size sweep mirroring the reference's scaling runs (edge 100 ... 20000,
+    run(120) = 121 timesteps, reference initial field, workload constants).
+    Per size: device-resident cell-steps/s (CUDA events over run(120)), the
+    reference-style wall time of run(120) from the host, and the CPU
+    restatement of fastscape_RB+P on a bounded sample (sizes <= 10000)."""
+    import __graft_entry__ as ge
+    import torch  # noqa: F401
+    pkg = ge.load()
+    if ws > 1:
+        torch.cuda.set_device(local)
+    sides = [int(s) for s in args.sizes.split(",")] if args.sizes else list(SWEEP_SIDES)
+    p = pkg.workload_params()
+    rows = []
+    for side in sides:
+        m = pkg.FastScape_RBP(side, side, params=p, init=pkg.INIT_REFERENCE, seed=123)
+        m.step(args.warmup)
+        m.set_timing(True)
+        m.phase_times(reset=True)
+        m.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        m.run(SWEEP_NSTEP)
+        m.synchronize()
+        wall = max_over_ranks(dist, time.perf_counter() - t0)
+        t = m.phase_times(reset=True)
+        dev_s = max_over_ranks(dist, float(t[3]) * 1e-3)
+        nstep = SWEEP_NSTEP + 1
+        nl = m.levels()[1]
+        m.close()
+        row = {"side": side, "cells": side * side, "timesteps": nstep, "levels": int(nl),
+               "ms_per_step": 1e3 * dev_s / nstep,
+               "cell_steps_per_s": ws * side * side * nstep / dev_s,
+               "run_wall_s": wall,
+               "run_cell_steps_per_s": ws * side * side * nstep / wall,
+               "kernel_ms": {"receivers": t[0] / nstep, "donors_level0": t[1] / nstep,
+                             "walk": t[2] / nstep}}
+        if rank == 0 and ws == 1 and not args.no_cpu_baseline and side <= 10000:
+            nst = int(max(1, min(nstep, 4e7 / (side * side))))
+            v, kind, thr, _ = cpu_sample(side, nst, prefer_reference=False)
+            row["cpu"] = {"cell_steps_per_s": v, "kind": kind, "cores": thr, "timesteps": nst}
+        rows.append(row)
+        if rank == 0:
+            print(json.dumps({"sweep_row": row}), flush=True)
+    if rank == 0:
+        best = max(rows, key=lambda r: r["cell_steps_per_s"])
+        print(json.dumps({
+            "metric": "cell-steps/s by grid size (run(120), FP64)",
+            "value": best["cell_steps_per_s"], "unit": UNIT, "n_gpus": ws,
+            "steps": SWEEP_NSTEP + 1, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "size sweep, edge " + ",".join(map(str, sides)) +
+                                   ", reference initial field, K 2e-6 m 0.4 n 1 U 2e-3 "
+                                   "dt 1000 dx 100", "best_side": best["side"]},
+            "sweep": rows}), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,10 +431,11 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="grid", choices=["grid", "ensemble"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep"],
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
-                         "256-realization batch")
+                         "256-realization batch; sweep: grid sizes 100..20000")
     ap.add_argument("--realizations", type=int, default=256)
+    ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -381,6 +446,9 @@ def main():
         return
     if args.workload == "ensemble":
         run_ensemble(args, dist, rank, ws, local)
+        return
+    if args.workload == "sweep":
+        run_sweep(args, dist, rank, ws, local)
         return
 
     import __graft_entry__ as ge
@@ -408,7 +476,8 @@ def main():
     total_ms = max_over_ranks(dist, float(t[3]))
     cells = side * side
     value = ws * cells * args.steps / (total_ms * 1e-3)
-    launches = 3 * args.steps
+    # receivers filter + fix-up, donors/level 0, walk: four launches a timestep
+    launches = 4 * args.steps
 
     # ---- roofline of the dominant kernel ----------------------------------
     peak, peak_kind = load_peaks()
