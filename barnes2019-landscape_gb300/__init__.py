@@ -46,7 +46,8 @@ ABI_SYMBOLS = [
     "fs_batch_get_elevation", "fs_batch_set_elevation", "fs_batch_get_accumulation",
     "fs_batch_get_receivers", "fs_batch_get_levels", "fs_batch_get_stack_dfs", "fs_batch_info",
     "fs_batch_set_timing", "fs_batch_get_phase_times", "fs_batch_use_graph",
-    "fs_batch_autotune", "fs_batch_synchronize",
+    "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
+    "fs_autotune", "fs_launch_config",
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_receiver_fixups",
@@ -144,6 +145,9 @@ def library() -> C.CDLL:
     L.fs_batch_get_phase_times.argtypes = [vp, dp, C.c_int]
     L.fs_batch_use_graph.argtypes = [vp, C.c_int]
     L.fs_batch_autotune.argtypes = [vp, C.c_int, ip]
+    L.fs_batch_launch_config.argtypes = [vp, ip, ip, ip]
+    L.fs_autotune.argtypes = [vp, C.c_int, ip]
+    L.fs_launch_config.argtypes = [vp, ip, ip, ip]
     L.fs_batch_synchronize.argtypes = [vp]
     L.fs_step_noalloc.argtypes = [vp, C.c_int, C.c_int, pp, C.c_int, vp]
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
@@ -282,6 +286,19 @@ class FastScape_RBP:
         check(library().fs_get_phase_times(self._m, _p(out, C.c_double), int(reset)))
         return out
 
+    def autotune(self, probe_steps: int = 2):
+        """Picks the fastest launch configuration (kernel blocks per SM,
+        graph replay) on the model's own state, which it restores."""
+        out = (C.c_int * 2)()
+        check(library().fs_autotune(self._m, int(probe_steps), out))
+        return self.launch_config()
+
+    def launch_config(self):
+        o, e, g = C.c_int(), C.c_int(), C.c_int()
+        check(library().fs_launch_config(self._m, C.byref(o), C.byref(e), C.byref(g)))
+        return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
+                "graph": bool(g.value)}
+
     def set_barrier_timeout(self, ms: float) -> None:
         check(library().fs_set_barrier_timeout(self._m, float(ms)))
 
@@ -395,9 +412,16 @@ class FastScapeBatch:
         check(library().fs_batch_use_graph(self._b, int(bool(on))))
 
     def autotune(self, probe_steps: int = 2):
+        """Picks the fastest launch configuration; returns it."""
         out = (C.c_int * 2)()
         check(library().fs_batch_autotune(self._b, int(probe_steps), out))
-        return {"walk_blocks_per_sm": out[0], "graph": bool(out[1])}
+        return self.launch_config()
+
+    def launch_config(self):
+        o, e, g = C.c_int(), C.c_int(), C.c_int()
+        check(library().fs_batch_launch_config(self._b, C.byref(o), C.byref(e), C.byref(g)))
+        return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
+                "graph": bool(g.value)}
 
     def synchronize(self) -> None:
         check(library().fs_batch_synchronize(self._b))

@@ -29,9 +29,10 @@ struct Ctl {
   unsigned long long walk_ns[3];  // accumulated walk time: ordering,
                                   // accumulation, erosion (block 0's clock)
   // --- reset before every timestep (from `bar` on) ---
-  unsigned int bar;        // grid-barrier arrival counter
+  unsigned int bar;        // grid-barrier arrival counter (k_order)
   int amb;                 // cells queued by the receiver filter
-  int pad1[2];
+  unsigned int bar2;       // grid-barrier arrival counter (k_erode)
+  int pad1;
 };
 constexpr size_t kCtlResetOffset = offsetof(Ctl, bar);
 constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
@@ -157,9 +158,14 @@ size_t walk_smem_bytes(int nreal);
 cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
-cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s);
+// The level walk: k_order with order_bps blocks per SM (2 or 3; each has
+// its own register budget), then (when a.do_erode) k_erode with erode_bps
+// blocks per SM; both cooperative launches over `sms` SMs.
+cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
+                        cudaStream_t s);
 int walk_threads();
-const void *walk_kernel_ptr(int nmode, bool single);
+const void *walk_kernel_ptr(int nmode, bool single);    // k_erode
+const void *order_kernel_ptr(bool single, int bps);     // k_order for bps 2 or 3
 cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
 cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s);
 cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s);

@@ -1,21 +1,22 @@
 // fs_kernels.cu -- sm_103a kernels of the FastScape timestep, over a batch
 // of realizations (a single model is a batch of one).
 //
-// One timestep = four launches on the stream:
+// One timestep = five launches on the stream:
 //   1. k_receivers_filter  D8 steepest descent over the interior
 //      + k_receivers_fixup (fastscape_RB.cpp:160-182): FP32 proof of the
 //                          receiver, FP64 reference formula for the cells
 //                          the proof cannot settle
 //   2. k_donors_level0     donor masks (pull form of fastscape_RB.cpp:188-203)
 //                          and the level-0 frontier (fastscape_RB.cpp:221-227)
-//   3. k_walk              persistent cooperative kernel: level-by-level
-//                          ordering (:229-251), flow accumulation back down
-//                          the levels (:262-279), uplift (:285-296) and the
-//                          implicit erosion solved upward from base level
-//                          (:306-328, in the level order of
-//                          fastscape_RB+P.cpp:319-350). All realizations
-//                          walk their levels in lock step, so one grid
-//                          barrier per level serves the whole batch.
+//   3. k_order             persistent cooperative kernel: level-by-level
+//                          ordering (:229-251) and flow accumulation back
+//                          down the levels (:262-279); uplifts the pits
+//   4. k_erode             persistent cooperative kernel: uplift (:285-296)
+//                          and the implicit erosion solved upward from base
+//                          level (:306-328, in the level order of
+//                          fastscape_RB+P.cpp:319-350).
+//   In both, all realizations walk their levels in lock step, so one grid
+//   barrier per level serves the whole batch.
 //
 // Floating point follows the reference's operation order exactly; the whole
 // file is compiled with -fmad=false so no multiply-add is contracted, and
@@ -69,18 +70,19 @@ __device__ __forceinline__ bool stopped(const Ctl *ctl) {
 // completes when bar reaches epoch*gridDim.x. Every wait is bounded by
 // `timeout_ns` of wall time; on timeout, or when another block has already
 // raised an error, it returns false and the caller leaves the kernel.
-__device__ bool grid_barrier(Ctl *ctl, unsigned &epoch, unsigned long long timeout_ns) {
+__device__ bool grid_barrier(Ctl *ctl, unsigned *bar, unsigned &epoch,
+                             unsigned long long timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     ++epoch;
     const unsigned target = epoch * gridDim.x;
     __threadfence();
-    atomicAdd(&ctl->bar, 1u);
+    atomicAdd(bar, 1u);
     int ok = 1;
     const unsigned long long t0 = globaltimer_ns();
     unsigned spins = 0;
-    while (ld_acquire_u32(&ctl->bar) < target) {
+    while (ld_acquire_u32(bar) < target) {
       if (ld_volatile_i32(&ctl->err) != 0) { ok = 0; break; }
       if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
         raise_err(ctl, FS_ERR_TIMEOUT, kPhaseBarrier);
@@ -629,8 +631,8 @@ __device__ __forceinline__ double erode_cell(const RealDesc &d, double neq, Ctl 
 // memory and maps global work items (expansion chunks, 32-entry groups) to
 // realizations through a prefix over the batch.
 // ---------------------------------------------------------------------------
-template <int NMODE, bool SINGLE>
-__global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
+template <bool SINGLE, int MINB>
+__global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
   extern __shared__ int smem[];
   const int nreal = a.nreal;
   int *s_lo = smem;               // per realization: current range start
@@ -765,7 +767,7 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
         }
       }
     }
-    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
     int any = 0;
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
       const int added = ld_volatile_i32(&a.rctl[r].lvlcnt[j]);
@@ -895,14 +897,62 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
         }
       }
     }
-    if (Lv > 0 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (Lv > 0 && !grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
   }
   lap(1);
-  if (!a.do_erode) return;
-  // The pits were uplifted in the level-0 pass above (reached only when no
-  // count exceeded an erosion table, so no timestep that the host repeats
-  // has changed h); level 1 reads them after this barrier.
-  if (maxlev > 1 && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+}
+
+// Uplift and erosion (fastscape_RB.cpp:285-296, :306-328) level by level
+// from base level, after k_order has placed the levels and the drainage
+// counts (and uplifted the pits). A kernel of its own: the ordering and
+// accumulation run with more resident threads than the register-hungry FP64
+// erosion allows.
+template <int NMODE, bool SINGLE>
+__global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
+  extern __shared__ int smem[];
+  const int nreal = a.nreal;
+  int *s_lo = smem;
+  int *s_hi = s_lo + nreal;
+  int *s_nlev = s_hi + nreal;
+  int *s_pre = s_nlev + nreal;
+  __shared__ int s_maxlev;
+  unsigned epoch = 0;
+  Ctl *ctl = a.ctl;
+  if (stopped(ctl)) return;
+  RealDesc d0;
+  if (SINGLE) d0 = a.desc[0];
+  auto desc = [&](int r) -> const RealDesc & { return SINGLE ? d0 : a.desc[r]; };
+  auto real_of = [&](int g) -> int { return SINGLE ? 0 : find_real(s_pre, nreal, g); };
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = tid >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  const bool stamp = a.stamp && tid == 0;
+  const unsigned long long t_start = stamp ? globaltimer_ns() : 0;
+  if (threadIdx.x == 0) s_maxlev = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+    s_nlev[r] = __ldcg(&a.rctl[r].nlevels);
+    atomicMax(&s_maxlev, s_nlev[r]);
+  }
+  __syncthreads();
+  const int maxlev = s_maxlev;
+
+  // Level Lv of every realization as [s_lo[r], s_hi[r]) (empty past its
+  // depth), and the prefix of its 32-entry groups over the batch.
+  auto level_groups = [&](int Lv) -> int {
+    __syncthreads();  // every warp is done with the previous ranges
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      if (Lv < s_nlev[r]) {
+        const int b = desc(r).lvl_base;
+        s_lo[r] = __ldcg(&a.lvl_off[b + Lv]);
+        s_hi[r] = __ldcg(&a.lvl_off[b + Lv + 1]);
+      } else {
+        s_lo[r] = s_hi[r] = 0;
+      }
+    }
+    __syncthreads();
+    return block_prefix(nreal, [&](int r) { return (s_hi[r] - s_lo[r] + 31) >> 5; }, s_pre);
+  };
 
   // ---- uplift + erosion: fastscape_RB.cpp:285-296 and :306-328 in the
   // level order of fastscape_RB+P.cpp:319-350. Eroded cells are uplifted on
@@ -972,9 +1022,9 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_walk(StepArgs a) {
         }
       }
     }
-    if (Lv + 1 < maxlev && !grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (Lv + 1 < maxlev && !grid_barrier(ctl, &ctl->bar2, epoch, a.timeout_ns)) return;
   }
-  lap(2);
+  if (stamp) atomicAdd(&ctl->walk_ns[2], globaltimer_ns() - t_start);
   if (tid == 0) atomicAdd(&ctl->steps_done, 1);
 }
 
@@ -1170,23 +1220,37 @@ int walk_threads() { return kWalkThreads; }
 
 const void *walk_kernel_ptr(int nmode, bool single) {
   if (single) {
-    if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne, true>);
-    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo, true>);
-    return reinterpret_cast<const void *>(&k_walk<kNGeneral, true>);
+    if (nmode == kNOne) return reinterpret_cast<const void *>(&k_erode<kNOne, true>);
+    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, true>);
+    return reinterpret_cast<const void *>(&k_erode<kNGeneral, true>);
   }
-  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_walk<kNOne, false>);
-  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_walk<kNTwo, false>);
-  return reinterpret_cast<const void *>(&k_walk<kNGeneral, false>);
+  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_erode<kNOne, false>);
+  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, false>);
+  return reinterpret_cast<const void *>(&k_erode<kNGeneral, false>);
+}
+
+const void *order_kernel_ptr(bool single, int bps) {
+  if (bps >= 3)
+    return single ? reinterpret_cast<const void *>(&k_order<true, 3>)
+                  : reinterpret_cast<const void *>(&k_order<false, 3>);
+  return single ? reinterpret_cast<const void *>(&k_order<true, 2>)
+                : reinterpret_cast<const void *>(&k_order<false, 2>);
 }
 
 cudaError_t prepare_walk_kernels() {
   const int bytes = (int)walk_smem_bytes(kMaxReal);
-  for (int nm = 0; nm < 3; nm++)
-    for (int single = 0; single < 2; single++) {
+  for (int single = 0; single < 2; single++) {
+    for (int nm = 0; nm < 3; nm++) {
       cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
       if (e != cudaSuccess) return e;
     }
+    for (int bps = 2; bps <= 3; bps++) {
+      cudaError_t e = cudaFuncSetAttribute(order_kernel_ptr(single != 0, bps),
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e != cudaSuccess) return e;
+    }
+  }
   return cudaSuccess;
 }
 
@@ -1259,10 +1323,16 @@ cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_walk(const StepArgs &a, int blocks, cudaStream_t s) {
+cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
+                        cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
-  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1), dim3(blocks),
+  const bool single = a.nreal == 1;
+  cudaError_t e = cudaLaunchCooperativeKernel(order_kernel_ptr(single, order_bps),
+                                              dim3(sms * order_bps), dim3(kWalkThreads), params,
+                                              walk_smem_bytes(a.nreal), s);
+  if (e != cudaSuccess || !a.do_erode) return e;
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, single), dim3(sms * erode_bps),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }
 

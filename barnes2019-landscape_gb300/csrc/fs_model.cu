@@ -121,7 +121,8 @@ struct fs_batch {
   std::vector<fs::RealDesc> desc;
   std::vector<double *> tab;
   std::vector<int> tab_cap;
-  int walk_occ = 1, walk_sms = 1, walk_bps = 2;  // walk blocks per SM in use
+  int walk_occ = 1, walk_sms = 1, walk_bps = 2;  // k_erode blocks per SM: limit, SMs, in use
+  int order_max = 2, order_bps = 2;              // k_order blocks per SM: limit (2 or 3), in use
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
@@ -271,7 +272,7 @@ cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
     e = b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
                            : fs::launch_receivers_fast(a, b->stream);
   if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
-  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream);
+  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream);
   return e;
 }
 
@@ -295,7 +296,7 @@ int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
   FS_CUDA(cudaEventRecord(b->ev[3 * i + 1], b->stream));
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
   FS_CUDA(cudaEventRecord(b->ev[3 * i + 2], b->stream));
-  FS_CUDA(fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream));
+  FS_CUDA(fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream));
   return FS_OK;
 }
 
@@ -594,6 +595,22 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
   if (occ < 1) return fail(set_error(FS_ERR_CUDA, "walk kernel cannot be resident"));
   b->walk_occ = occ;
   b->walk_bps = std::min(occ, 2);
+  // k_order: the variant with 3 blocks per SM where all three fit (a large
+  // batch's shared memory may not allow it), else the 2-block one.
+  for (int bps = 3; bps >= 2; bps--) {
+    int o = 0;
+    if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fs::order_kernel_ptr(n == 1, bps),
+                                                          fs::walk_threads(),
+                                                          fs::walk_smem_bytes(n)),
+            "occupancy"))
+      return fail(*status);
+    if (o >= bps) {
+      b->order_max = bps;
+      break;
+    }
+    if (bps == 2) return fail(set_error(FS_ERR_CUDA, "order kernel cannot be resident"));
+  }
+  b->order_bps = b->order_max;
   if (!cu(cudaStreamSynchronize(b->stream), "sync")) return fail(*status);
   return b;
 }
@@ -772,27 +789,32 @@ int autotune(fs_batch *b, int probe, int *chosen) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int best_bps = b->walk_bps;
+  int best_bps = b->walk_bps, best_obps = b->order_bps;
   bool best_graph = false;
   int st = FS_OK;
-  for (int bps = 1; bps <= std::min(b->walk_occ, 2) && st == FS_OK; bps++) {
-    for (int gr = 0; gr < 2 && st == FS_OK; gr++) {
-      b->walk_bps = bps;
-      b->use_graph = gr == 1;
-      b->graph_dirty = true;
-      if ((st = batch_step(b, 1)) != FS_OK) break;  // warm (and build the graph)
-      cudaEventRecord(e0, b->stream);
-      if ((st = batch_step(b, probe)) != FS_OK) break;
-      cudaEventRecord(e1, b->stream);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best) {
-        best = ms;
-        best_bps = bps;
-        best_graph = gr == 1 && b->use_graph;
+  for (int obps = 2; obps <= b->order_max && st == FS_OK; obps++) {
+    for (int bps = 1; bps <= std::min(b->walk_occ, 2) && st == FS_OK; bps++) {
+      for (int gr = 0; gr < 2 && st == FS_OK; gr++) {
+        b->order_bps = obps;
+        b->walk_bps = bps;
+        b->use_graph = gr == 1;
+        b->graph_dirty = true;
+        if ((st = batch_step(b, 1)) != FS_OK) break;  // warm (and build the graph)
+        cudaEventRecord(e0, b->stream);
+        if ((st = batch_step(b, probe)) != FS_OK) break;
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+          best = ms;
+          best_bps = bps;
+          best_obps = obps;
+          best_graph = gr == 1 && b->use_graph;
+        }
+        cudaMemcpyAsync(b->h, save, b->cells * sizeof(double), cudaMemcpyDeviceToDevice,
+                        b->stream);
       }
-      cudaMemcpyAsync(b->h, save, b->cells * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
     }
   }
   cudaEventDestroy(e0);
@@ -802,6 +824,7 @@ int autotune(fs_batch *b, int probe, int *chosen) {
   b->timing = timing;
   b->steps = steps;
   b->walk_bps = best_bps;
+  b->order_bps = best_obps;
   b->use_graph = best_graph;
   b->graph_dirty = true;
   if (chosen) {
@@ -1071,6 +1094,24 @@ int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen) {
   return autotune(b, probe_steps, chosen);
 }
 
+int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps, int *graph) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (order_bps) *order_bps = b->order_bps;
+  if (erode_bps) *erode_bps = b->walk_bps;
+  if (graph) *graph = b->use_graph ? 1 : 0;
+  return FS_OK;
+}
+
+int fs_autotune(fs_model *m, int probe_steps, int *chosen) {
+  FS_MODEL(m);
+  return fs_batch_autotune(m->b, probe_steps, chosen);
+}
+
+int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *graph) {
+  FS_MODEL(m);
+  return fs_batch_launch_config(m->b, order_bps, erode_bps, graph);
+}
+
 int fs_batch_synchronize(const fs_batch *b) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
   FS_CUDA(cudaStreamSynchronize(b->stream));
@@ -1102,7 +1143,7 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
   FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
   const fs::StepArgs a = step_args(b, 0);
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
-  FS_CUDA(fs::launch_walk(a, b->walk_sms * b->walk_bps, b->stream));
+  FS_CUDA(fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream));
   b->have_step = true;
   return collect_status(b);
 }

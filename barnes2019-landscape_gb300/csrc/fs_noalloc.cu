@@ -76,7 +76,9 @@ static fs::Tile g_host_tiles[2][kMaxTiles];
 struct DeviceState {
   bool ready = false;
   unsigned char *base = nullptr;  // device address of g_scratch
-  int walk_blocks[3] = {0, 0, 0};
+  int sms = 0;
+  int erode_bps[3] = {0, 0, 0};  // k_erode blocks per SM for each n mode
+  int order_bps = 2;
   bool tab_valid = false;
   fs_params tab_params{};
 };
@@ -116,8 +118,20 @@ int setup_device(int dev, DeviceState &d) {
                                                       fs::walk_threads(), fs::walk_smem_bytes(1));
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (occ < 1) return fail(FS_ERR_CUDA, "walk kernel cannot be resident");
-    d.walk_blocks[nm] = sms * (occ < 2 ? occ : 2);
+    d.erode_bps[nm] = occ < 2 ? occ : 2;
   }
+  int occ = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::order_kernel_ptr(true, 3),
+                                                    fs::walk_threads(), fs::walk_smem_bytes(1));
+  if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+  d.order_bps = occ >= 3 ? 3 : 2;
+  if (d.order_bps == 2) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::order_kernel_ptr(true, 2),
+                                                      fs::walk_threads(), fs::walk_smem_bytes(1));
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+    if (occ < 2) return fail(FS_ERR_CUDA, "order kernel cannot be resident");
+  }
+  d.sms = sms;
   d.base = static_cast<unsigned char *>(ptr);
   d.ready = true;
   return FS_OK;
@@ -245,7 +259,7 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
     if (e == cudaSuccess) e = cudaMemsetAsync(rctl, 0, sizeof(fs::RealCtl), s);
     if (e == cudaSuccess) e = fs::launch_receivers_fast(a, s);
     if (e == cudaSuccess) e = fs::launch_donors_level0(a, s);
-    if (e == cudaSuccess) e = fs::launch_walk(a, d.walk_blocks[a.nmode], s);
+    if (e == cudaSuccess) e = fs::launch_walk(a, d.sms, d.order_bps, d.erode_bps[a.nmode], s);
     if (e != cudaSuccess) return cuda_fail(e, "timestep launch");
   }
   fs::Ctl h_ctl;

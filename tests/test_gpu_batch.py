@@ -88,13 +88,29 @@ def test_autotune_keeps_state(pkg):
         b.step(2)
         before = [a.getH(r) for r in range(6)]
         choice = a.autotune(probe_steps=2)
-        assert choice["walk_blocks_per_sm"] in (1, 2)
+        assert choice["erode_blocks_per_sm"] in (1, 2)
+        assert choice["order_blocks_per_sm"] in (2, 3)
         for r in range(6):
             assert np.array_equal(a.getH(r), before[r])
         a.step(5)
         b.step(5)
         for r in range(6):
             assert np.array_equal(a.getH(r), b.getH(r))
+
+
+def test_single_model_autotune_keeps_state(pkg):
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(300, 200, params=p, init=pkg.INIT_PHILOX, seed=4) as a, \
+            pkg.FastScape_RBP(300, 200, params=p, init=pkg.INIT_PHILOX, seed=4) as b:
+        a.step(3)
+        b.step(3)
+        h = a.getH()
+        cfg = a.autotune(probe_steps=2)
+        assert cfg["order_blocks_per_sm"] in (2, 3) and cfg["erode_blocks_per_sm"] in (1, 2)
+        assert np.array_equal(a.getH(), h)
+        a.step(4)
+        b.step(4)
+        assert np.array_equal(a.getH(), b.getH())
 
 
 def test_batch_run_semantics_and_errors(pkg):
