@@ -278,7 +278,8 @@ class FastScape_RBP:
         check(library().fs_set_timing(self._m, int(bool(on))))
 
     TIMERS = ("receivers", "donors_level0", "walk", "total",
-              "walk_order", "walk_accumulation", "walk_erosion")
+              "walk_order", "walk_accumulation", "walk_erosion",
+              "order_kernel", "erode_kernel")
 
     def phase_times(self, reset: bool = False):
         """Device milliseconds per timer in TIMERS (fs_get_phase_times)."""

@@ -163,6 +163,8 @@ cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
 // blocks per SM; both cooperative launches over `sms` SMs.
 cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
                         cudaStream_t s);
+cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_order
+cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_erode
 int walk_threads();
 const void *walk_kernel_ptr(int nmode, bool single);    // k_erode
 const void *order_kernel_ptr(bool single, int bps);     // k_order for bps 2 or 3

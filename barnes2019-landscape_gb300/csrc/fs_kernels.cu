@@ -1323,17 +1323,25 @@ cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
-                        cudaStream_t s) {
+cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
-  const bool single = a.nreal == 1;
-  cudaError_t e = cudaLaunchCooperativeKernel(order_kernel_ptr(single, order_bps),
-                                              dim3(sms * order_bps), dim3(kWalkThreads), params,
-                                              walk_smem_bytes(a.nreal), s);
-  if (e != cudaSuccess || !a.do_erode) return e;
-  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, single), dim3(sms * erode_bps),
+  return cudaLaunchCooperativeKernel(order_kernel_ptr(a.nreal == 1, bps), dim3(sms * bps),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
+}
+
+cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s) {
+  StepArgs args = a;
+  void *params[] = {&args};
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1), dim3(sms * bps),
+                                     dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
+}
+
+cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
+                        cudaStream_t s) {
+  cudaError_t e = launch_order(a, sms, order_bps, s);
+  if (e != cudaSuccess || !a.do_erode) return e;
+  return launch_erode(a, sms, erode_bps, s);
 }
 
 cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s) {

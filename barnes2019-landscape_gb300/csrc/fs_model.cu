@@ -132,7 +132,7 @@ struct fs_batch {
   cudaGraphExec_t graph = nullptr;
   bool graph_dirty = true;
   std::vector<cudaEvent_t> ev;
-  double phase_ms[4] = {0, 0, 0, 0};
+  double phase_ms[FS_NUM_TIMERS] = {};  // event timers (indices 0-3, 7, 8)
 };
 
 struct fs_model {
@@ -285,31 +285,41 @@ int ensure_events(fs_batch *b, size_t n) {
   return FS_OK;
 }
 
-// One timestep with the phase events ev[3i..3i+3] around its launches.
+// Events per timed timestep: start, after the receivers, after the donors,
+// between the two level-walk kernels (the next timestep's start, or the
+// final event, closes the erosion kernel).
+constexpr int kEvPerStep = 4;
+
+// One timestep with the phase events ev[4i..4i+4] around its launches.
 int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
-  FS_CUDA(cudaEventRecord(b->ev[3 * i], b->stream));
+  cudaEvent_t *ev = &b->ev[kEvPerStep * i];
+  FS_CUDA(cudaEventRecord(ev[0], b->stream));
   FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
                           fs::kCtlResetBytes, b->stream));
   FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
   FS_CUDA(b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
                              : fs::launch_receivers_fast(a, b->stream));
-  FS_CUDA(cudaEventRecord(b->ev[3 * i + 1], b->stream));
+  FS_CUDA(cudaEventRecord(ev[1], b->stream));
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
-  FS_CUDA(cudaEventRecord(b->ev[3 * i + 2], b->stream));
-  FS_CUDA(fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream));
+  FS_CUDA(cudaEventRecord(ev[2], b->stream));
+  FS_CUDA(fs::launch_order(a, b->walk_sms, b->order_bps, b->stream));
+  FS_CUDA(cudaEventRecord(ev[3], b->stream));
+  FS_CUDA(fs::launch_erode(a, b->walk_sms, b->walk_bps, b->stream));
   return FS_OK;
 }
 
 int harvest_events(fs_batch *b, int k) {
-  FS_CUDA(cudaEventSynchronize(b->ev[3 * k]));
+  FS_CUDA(cudaEventSynchronize(b->ev[kEvPerStep * k]));
+  static const int slot[kEvPerStep] = {0, 1, 7, 8};  // receivers, donors, k_order, k_erode
   for (int i = 0; i < k; i++)
-    for (int j = 0; j < 3; j++) {
+    for (int j = 0; j < kEvPerStep; j++) {
       float ms = 0;
-      FS_CUDA(cudaEventElapsedTime(&ms, b->ev[3 * i + j], b->ev[3 * i + j + 1]));
-      b->phase_ms[j] += ms;
+      FS_CUDA(cudaEventElapsedTime(&ms, b->ev[kEvPerStep * i + j], b->ev[kEvPerStep * i + j + 1]));
+      b->phase_ms[slot[j]] += ms;
+      if (j >= 2) b->phase_ms[2] += ms;  // the level walk: both kernels
     }
   float tot = 0;
-  FS_CUDA(cudaEventElapsedTime(&tot, b->ev[0], b->ev[3 * k]));
+  FS_CUDA(cudaEventElapsedTime(&tot, b->ev[0], b->ev[kEvPerStep * k]));
   b->phase_ms[3] += tot;
   return FS_OK;
 }
@@ -370,10 +380,10 @@ int batch_step(fs_batch *b, int k) {
     const fs::StepArgs a = step_args(b, 1);
     FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, fs::kCtlCallResetBytes, b->stream));
     if (b->timing) {
-      if (int st = ensure_events(b, 3 * static_cast<size_t>(batch) + 1)) return st;
+      if (int st = ensure_events(b, kEvPerStep * static_cast<size_t>(batch) + 1)) return st;
       for (int i = 0; i < batch; i++)
         if (int st = timed_step(b, a, i)) return st;
-      FS_CUDA(cudaEventRecord(b->ev[3 * batch], b->stream));
+      FS_CUDA(cudaEventRecord(b->ev[kEvPerStep * batch], b->stream));
       if (int st = harvest_events(b, batch)) return st;
     } else {
       if (b->use_graph && b->graph_dirty)
@@ -755,7 +765,7 @@ int get_phase_times(const fs_batch *b, double *ms, int reset) {
   FS_CUDA(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(fs::Ctl), cudaMemcpyDeviceToHost, b->stream));
   FS_CUDA(cudaStreamSynchronize(b->stream));
   if (ms) {
-    for (int i = 0; i < 4; i++) ms[i] = b->phase_ms[i];
+    for (int i = 0; i < FS_NUM_TIMERS; i++) ms[i] = b->phase_ms[i];
     for (int i = 0; i < 3; i++) ms[4 + i] = b->h_ctl->walk_ns[i] * 1e-6;
   }
   if (reset) {

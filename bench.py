@@ -52,12 +52,18 @@ RUN_NSTEP = 20            # run(20) executes 21 timesteps
 ALG_BYTES = {
     "receivers": 8 + 1,                     # h read, rec write
     "donors_level0": 1 + 1,                 # rec read, mask write (+ pit list)
-    "walk": (4 + 1 + 4 + 1 + 4 + 1) + (1 + 4 + 4 + 4) + (4 + 1 + 4 + 8 + 8),
-    # ordering: entry read, mask read, entry + direction write, first-donor
-    # position + donor count write; accumulation: donor count, first-donor
-    # position, donors' counts read once, count write; erosion: entry,
-    # direction, count, h read, h write.
+    "order": (4 + 1 + 4 + 1 + 4 + 1) + (1 + 4 + 4 + 4),
+    # k_order -- ordering: entry read, mask read, entry + direction write,
+    # first-donor position + donor count write; accumulation: donor count,
+    # first-donor position, donors' counts read once, count write
+    "erode": 4 + 1 + 4 + 8 + 8,
+    # k_erode: entry, direction, count, h read, h write
 }
+# k_erode is bound by the FP64 pipe: 8 FP64 operations per eroded cell
+# (uplift, h0 - hn, fact*dh, four for the division, h0 - q). Peak measured
+# here with a probe kernel: 1.59 FP64 lanes/clock/SM x 152 SMs x 2.07 GHz.
+ERODE_FP64_PER_CELL = 8
+FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12
 STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
 
 
@@ -333,8 +339,10 @@ def run_ensemble(args, dist, rank, ws, local):
     value = ws * len(sides) / (ENSEMBLE_STEPS * per_step)
     if rank == 0:
         peak, peak_kind = load_peaks()
-        walk_ms = t[2] / 2
-        achieved = ALG_BYTES["walk"] * cells / (walk_ms * 1e-3) / 1e9
+        kern = {"receivers": t[0] / 2, "donors_level0": t[1] / 2, "order": t[7] / 2,
+                "erode": t[8] / 2}
+        dom = max(("order", "erode"), key=kern.get)
+        achieved = ALG_BYTES[dom] * cells / (kern[dom] * 1e-3) / 1e9
         print(json.dumps({
             "metric": "ensemble realizations/s (200-timestep runs)", "value": value,
             "unit": "realizations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -345,11 +353,10 @@ def run_ensemble(args, dist, rank, ws, local):
                                    "U log-U[1e-4,5e-3], n 1, dt 1000, dx 100",
                        "cells_per_step": cells, "cell_steps_per_s": cells / per_step,
                        "autotune": tune, "l2": "inputs larger than L2"},
-            "roofline": {"bound": "hbm", "kernel": "walk", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "peak_source": f"{peak_kind} hbm_gbs",
-                         "kernel_ms": {"receivers": t[0] / 2, "donors_level0": t[1] / 2,
-                                       "walk": walk_ms}},
+                         "alg_bytes_per_cell": ALG_BYTES[dom],
+                         "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": kern},
             "gpu_launches": 5 * args.steps,
             "clocks": clk.summary(),
         }), flush=True)
@@ -398,7 +405,7 @@ def run_sweep(args, dist, rank, ws, local):
                "run_wall_s": wall,
                "run_cell_steps_per_s": ws * side * side * nstep / wall,
                "kernel_ms": {"receivers": t[0] / nstep, "donors_level0": t[1] / nstep,
-                             "walk": t[2] / nstep}}
+                             "order": t[7] / nstep, "erode": t[8] / nstep}}
         if rank == 0 and ws == 1 and not args.no_cpu_baseline and side <= 10000:
             nst = int(max(1, min(nstep, 4e7 / (side * side))))
             v, kind, thr, _ = cpu_sample(side, nst, prefer_reference=False)
@@ -484,7 +491,7 @@ def main():
 
     # ---- roofline of the dominant kernel ----------------------------------
     peak, peak_kind = load_peaks()
-    kern = {"receivers": t[0], "donors_level0": t[1], "walk": t[2]}
+    kern = {"receivers": t[0], "donors_level0": t[1], "order": t[7], "erode": t[8]}
     dom = max(kern, key=kern.get)
     per_launch_ms = kern[dom] / args.steps
     achieved = ALG_BYTES[dom] * cells / (per_launch_ms * 1e-3) / 1e9
@@ -495,13 +502,24 @@ def main():
                 "walk_split_ms": {"ordering": t[4] / args.steps,
                                   "accumulation": t[5] / args.steps,
                                   "erosion": t[6] / args.steps}}
+    # the erosion kernel against the FP64 pipe (eroded cells: all but level 0)
+    lid, _ = m.levels()
+    eroded = int(np.count_nonzero(lid >= 1))
+    del lid
+    erode_tf = ERODE_FP64_PER_CELL * eroded / (t[8] / args.steps * 1e-3) / 1e12
+    roofline["erode_fp64"] = {"bound": "fp64", "achieved": erode_tf, "peak": FP64_PEAK_TFLOPS,
+                              "unit": "TFLOP/s", "frac": erode_tf / FP64_PEAK_TFLOPS,
+                              "ops_per_eroded_cell": ERODE_FP64_PER_CELL,
+                              "eroded_cells": eroded,
+                              "peak_source": "probe-kernel FP64 rate (no FP64 figure in "
+                                             "MEASURED_PEAKS.json)"}
     step_rf = cells * args.steps / (total_ms * 1e-3) * STEP_ALG_BYTES / 1e9
     prof = ROOT / "profiles" / "traffic.json"
     if prof.exists():
         try:
             tr = json.loads(prof.read_text())
-            if dom in tr:
-                roofline["traffic"] = tr[dom]["bytes_per_launch_at_10000"]
+            if dom in tr:   # ncu bytes per cell (profiles/kernels_step_4000.md) x cells
+                roofline["traffic"] = tr[dom]["bytes_per_cell"] * cells
         except (ValueError, KeyError):
             pass
 

@@ -156,11 +156,12 @@ int64_t fs_steps_executed(const fs_model *m);
 /* Device time in milliseconds accumulated over timed fs_step/fs_run calls
  * since the last reset, measured with CUDA events on the model's stream
  * (enabled by fs_set_timing(m, 1)). ms[] holds FS_NUM_TIMERS values:
- *   0 receiver kernel, 1 donor/level-0 kernel, 2 level-walk kernel,
- *   3 whole timed calls (first event to last),
- *   4..6 split of the level walk measured inside it (ordering,
- *        accumulation, uplift+erosion). */
-#define FS_NUM_TIMERS 7
+ *   0 receiver kernels, 1 donor/level-0 kernel, 2 level walk (both of
+ *   its kernels), 3 whole timed calls (first event to last),
+ *   4..6 split of the level walk measured inside it by the GPU clock
+ *        (ordering, accumulation, uplift+erosion),
+ *   7 ordering/accumulation kernel, 8 erosion kernel (events). */
+#define FS_NUM_TIMERS 9
 int fs_set_timing(fs_model *m, int enable);
 int fs_get_phase_times(const fs_model *m, double *ms, int reset);
 
