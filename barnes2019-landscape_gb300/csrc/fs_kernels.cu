@@ -35,6 +35,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
+constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kPer = 8;   // entries per thread per expansion chunk
 constexpr int kChunk = kPer * kWalkThreads;
 constexpr int kAccU = 4;  // 32-entry groups per warp per accumulation pass
@@ -639,7 +640,9 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
   int *s_hi = s_lo + nreal;       // and end (local positions)
   int *s_nlev = s_hi + nreal;     // levels found so far
   int *s_pre = s_nlev + nreal;    // prefix over the batch, nreal+1
-  __shared__ int s_base;
+  __shared__ int s_cw[2][kWalkWarps];  // warp totals / prefixes of a chunk
+  __shared__ int s_cbase[2];           // the chunk's first position
+  int cbuf = 0;
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
   if (stopped(ctl)) return;
@@ -724,13 +727,26 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         incl[q] = wtot + v;  // inclusive, relative to the warp's first donor
         wtot += __shfl_sync(kFull, v, 31);
       }
-      int total;
-      const int wexcl = block_excl_scan(lane == 0 ? wtot : 0, total, threadIdx.x, kWalkThreads);
-      const int wstart = __shfl_sync(kFull, wexcl, 0);
-      if (threadIdx.x == 0) s_base = total ? atomicAdd(&a.rctl[r].lvlcnt[j], total) : 0;
+      // Place the chunk: prefix of the warp totals and one atomic, with two
+      // barriers; the shared words alternate between two buffers so the next
+      // chunk can fill one while this chunk's readers finish with the other.
+      if (lane == 0) s_cw[cbuf][wid] = wtot;
       __syncthreads();
-      const int cbase = hi + s_base + wstart;  // position of the warp's first donor
+      if (wid == 0) {
+        int w = lane < kWalkWarps ? s_cw[cbuf][lane] : 0;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+          const int x = __shfl_up_sync(kFull, w, dd);
+          if (lane >= dd) w += x;
+        }
+        if (lane < kWalkWarps) s_cw[cbuf][lane] = w;  // inclusive prefix over warps
+        const int total = __shfl_sync(kFull, w, kWalkWarps - 1);
+        if (lane == 0) s_cbase[cbuf] = total ? atomicAdd(&a.rctl[r].lvlcnt[j], total) : 0;
+      }
       __syncthreads();
+      // position of the warp's first donor
+      const int cbase = hi + s_cbase[cbuf] + (wid ? s_cw[cbuf][wid - 1] : 0);
+      cbuf ^= 1;
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
         const int i = wbase + 32 * q + lane;
