@@ -643,6 +643,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
   __shared__ int s_cw[2][kWalkWarps];  // warp totals / prefixes of a chunk
   __shared__ int s_cbase[2];           // the chunk's first position
   int cbuf = 0;
+  __shared__ uint8_t s_own[kWalkWarps][32 * 8];  // (lane, direction) per donor slot of a pass
   unsigned epoch = 0;
   Ctl *ctl = a.ctl;
   if (stopped(ctl)) return;
@@ -755,24 +756,28 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
           a.kid[d.off + i] = cbase + incl[q] - n_d;
           a.nd[d.off + i] = (uint8_t)n_d;
         }
+        // The pass's donors go to positions cbase + [q_lo, q_lo + q_n) in
+        // entry order. Each lane records (its lane, direction) for the slots
+        // of its donors in the warp's shared bytes; then lane t writes slot t
+        // of every 32, coalesced.
         const int q_lo = __shfl_sync(kFull, incl[q] - n_d, 0);
-        const int q_hi = __shfl_sync(kFull, incl[q], 31);
-        for (int r0 = q_lo; r0 < q_hi; r0 += 32) {
-          const int rr = r0 + lane;
-          // owner = number of lanes whose inclusive count is <= rr
-          int o = 0;
-#pragma unroll
-          for (int step = 16; step >= 1; step >>= 1) {
-            const int v = __shfl_sync(kFull, incl[q], o + step - 1);
-            if (v <= rr) o += step;
+        const int q_n = __shfl_sync(kFull, incl[q], 31) - q_lo;  // <= 32 * 8
+        {
+          unsigned m = ms[q];
+          int slot = incl[q] - n_d - q_lo;
+          while (m) {
+            s_own[wid][slot++] = (uint8_t)((lane << 3) | (__ffs(m) - 1));
+            m &= m - 1;
           }
-          const int oc = __shfl_sync(kFull, cs[q], o);
-          unsigned om = __shfl_sync(kFull, ms[q], o);
-          const int ofirst = __shfl_sync(kFull, incl[q] - __popc(ms[q]), o);
-          if (rr < q_hi) {
-            for (int skip = rr - ofirst; skip > 0; --skip) om &= om - 1;
-            const int k = __ffs(om) - 1;
-            const int pos = cbase + rr;
+        }
+        __syncwarp();
+        for (int r0 = 0; r0 < q_n; r0 += 32) {
+          const int rr = r0 + lane;
+          const unsigned pk = rr < q_n ? s_own[wid][rr] : 0u;
+          const int k = pk & 7;
+          const int oc = __shfl_sync(kFull, cs[q], pk >> 3);
+          if (rr < q_n) {
+            const int pos = cbase + q_lo + rr;
             if (pos < d.size) {
               ent[pos] = oc + nbr_off(k, d.W);
               a.pdir[d.off + pos] = (uint8_t)((k + 4) & 7);
@@ -781,6 +786,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
             }
           }
         }
+        __syncwarp();  // s_own is refilled by the next pass
       }
     }
     if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
@@ -886,18 +892,32 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         v0[u] = lane < tot[u] ? __ldcg(&a.acc[run[u] + lane]) : 0u;
 #pragma unroll
       for (int u = 0; u < kAccU; u++) {
-        const int first = incl[u] - n[u];
-        uint32_t s = 1;
+        // The donors of the group's entries are the run [0, tot); entry i's
+        // are [first, last) of it. Its count is 1 + E(last) - E(first), E(x)
+        // the sum of the run's counts before x, read from a warp scan of
+        // each 32-donor chunk plus the chunks before it.
+        const int first = incl[u] - n[u], last = incl[u];
+        uint32_t eF = 0, eL = 0, carry = 0;
         for (int r0 = 0; r0 < tot[u]; r0 += 32) {
-          uint32_t v = v0[u];
-          if (r0 > 0) v = r0 + lane < tot[u] ? __ldcg(&a.acc[run[u] + r0 + lane]) : 0u;
+          uint32_t c = v0[u];
+          if (r0 > 0) c = r0 + lane < tot[u] ? __ldcg(&a.acc[run[u] + r0 + lane]) : 0u;
+          uint32_t S = c;
 #pragma unroll
-          for (int q = 0; q < 8; q++) {
-            const int rq = first + q - r0;
-            const uint32_t x = __shfl_sync(kFull, v, rq & 31);
-            if (q < n[u] && rq >= 0 && rq < 32) s += x;
+          for (int dd = 1; dd < 32; dd <<= 1) {
+            const uint32_t x = __shfl_up_sync(kFull, S, dd);
+            if (lane >= dd) S += x;
           }
+          const uint32_t ex = S - c;  // exclusive within the chunk
+          const int xf = first - r0, xl = last - r0;
+          const uint32_t gf = __shfl_sync(kFull, ex, xf & 31);
+          const uint32_t gl = __shfl_sync(kFull, ex, xl & 31);
+          if (xf >= 0 && xf < 32) eF = carry + gf;
+          if (xl >= 0 && xl < 32) eL = carry + gl;
+          carry += __shfl_sync(kFull, S, 31);
         }
+        if (first >= tot[u]) eF = carry;  // at the run's end
+        if (last >= tot[u]) eL = carry;
+        const uint32_t s = 1u + (eL - eF);
         if (ii[u] >= 0) {
           const RealDesc &d = desc(rr[u]);
           a.acc[d.off + ii[u]] = s;
