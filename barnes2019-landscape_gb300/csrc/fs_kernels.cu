@@ -703,6 +703,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       const int wbase = base + wid * (32 * kPer);
       int32_t *ent = a.ent + d.off;
       const uint8_t *mask = a.mask + d.off;
+      const int offk = nbr_off(lane & 7, d.W);  // lane k < 8: offset of direction k
       int cs[kPer];
       unsigned ms[kPer];
       int incl[kPer];
@@ -776,10 +777,11 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
           const unsigned pk = rr < q_n ? s_own[wid][rr] : 0u;
           const int k = pk & 7;
           const int oc = __shfl_sync(kFull, cs[q], pk >> 3);
+          const int ok = __shfl_sync(kFull, offk, k);
           if (rr < q_n) {
             const int pos = cbase + q_lo + rr;
             if (pos < d.size) {
-              ent[pos] = oc + nbr_off(k, d.W);
+              ent[pos] = oc + ok;
               a.pdir[d.off + pos] = (uint8_t)((k + 4) & 7);
             } else {
               raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
@@ -961,6 +963,7 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   auto real_of = [&](int g) -> int { return SINGLE ? 0 : find_real(s_pre, nreal, g); };
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
+  const int offk0 = SINGLE ? nbr_off(lane & 7, d0.W) : 0;
   const int warp_global = tid >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
   const bool stamp = a.stamp && tid == 0;
   const unsigned long long t_start = stamp ? globaltimer_ns() : 0;
@@ -1028,12 +1031,15 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
       for (int u = 0; u < kEroU; u++) {
         hc[u] = 0;
         hn[u] = 0;
+        // a group lies in one realization: lane k < 8 holds direction k's offset
+        const int offk = SINGLE ? offk0 : nbr_off(lane & 7, desc(rr[u]).W);
+        const int ro = __shfl_sync(kFull, offk, dd[u] & 7);
         if (ok[u]) {
           const RealDesc &d = desc(rr[u]);
           const unsigned long long *hh =
               reinterpret_cast<const unsigned long long *>(a.h + d.off);
           hc[u] = __ldcg(&hh[cc[u]]);
-          hn[u] = __ldcg(&hh[cc[u] + nbr_off(dd[u], d.W)]);
+          hn[u] = __ldcg(&hh[cc[u] + ro]);
         }
       }
 #pragma unroll
