@@ -304,17 +304,21 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   const float E = 0x1p-19f * d.gmax * (M + 0x1p-100f);
   const int lx = threadIdx.x + 1;
   const int gx = x0 + lx;
-  unsigned qbits = 0;  // bit r: the cell of row pass r is queued
-#pragma unroll 1
-  for (int r = 0; r < kRyTile / 8; r++) {
-    const int ly = threadIdx.y + 8 * r + 1;
+  unsigned qbits = 0;  // bit r: the cell of row lyb + r is queued
+  // Each thread takes 4 consecutive rows of its column, sliding a 3x3
+  // window down: 3 new shared loads per row.
+  constexpr int kRows = kRyTile / 8;
+  const int lyb = kRows * threadIdx.y + 1;
+  float u0 = s[lyb - 1][lx - 1], u1 = s[lyb - 1][lx], u2 = s[lyb - 1][lx + 1];
+  float m0 = s[lyb][lx - 1], m1 = s[lyb][lx], m2 = s[lyb][lx + 1];
+#pragma unroll
+  for (int r = 0; r < kRows; r++) {
+    const int ly = lyb + r;
+    const float d0 = s[ly + 1][lx - 1], d1 = s[ly + 1][lx], d2 = s[ly + 1][lx + 1];
     const int gy = y0 + ly;
-    const bool valid = gx < W - 2 && gy < H - 2;
-    if (valid) {
-      const float fc = s[ly][lx];
-      const float f[8] = {s[ly][lx - 1], s[ly - 1][lx - 1], s[ly - 1][lx],
-                          s[ly - 1][lx + 1], s[ly][lx + 1], s[ly + 1][lx + 1],
-                          s[ly + 1][lx], s[ly + 1][lx - 1]};
+    if (gx < W - 2 && gy < H - 2) {
+      const float fc = m1;
+      const float f[8] = {m0, u0, u1, u2, m2, d2, d1, d0};  // W NW N NE E SE S SW
       // Largest and second largest approximate slope; the first maximum in
       // neighbour order keeps bn (an exact tie leaves best == second, which
       // queues the cell). Without NaN in the tile no slope is NaN (an
@@ -336,6 +340,8 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
       if (code != -1) rec[gy * W + gx] = (int8_t)code;
       else qbits |= 1u << r;
     }
+    u0 = m0; u1 = m1; u2 = m2;
+    m0 = d0; m1 = d1; m2 = d2;
   }
   // The queued cells of the tile, placed with one atomic per tile (a
   // counter shared by the whole grid would serialise on one address).
@@ -350,7 +356,7 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
 #pragma unroll 1
   for (int r = 0; r < kRyTile / 8; r++) {
     if (qbits >> r & 1u) {
-      const int gy = y0 + threadIdx.y + 8 * r + 1;
+      const int gy = y0 + kRows * threadIdx.y + r + 1;
       a.amb[q] = d.off + gy * W + gx;
       a.amb_r[q] = t.r;
       ++q;
