@@ -286,13 +286,29 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   float m = 0.f;
   bool bad = false;
   constexpr int kSw = kRxTile + 2, kSn = (kRyTile + 2) * kSw;
-  for (int i = threadIdx.y * 32 + threadIdx.x; i < kSn; i += 256) {
+  constexpr int kSPer = (kSn + 255) / 256;  // staged values per thread
+  // all of a thread's loads in flight before the first is used
+  unsigned long long hv[kSPer];
+  const int t0 = threadIdx.y * 32 + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < kSPer; k++) {
+    const int i = t0 + 256 * k;
     const int ly = i / kSw, lx = i - ly * kSw;
     const int gx = x0 + lx, gy = y0 + ly;
-    const float f = (gx < W && gy < H) ? trunc_to_float(h[gy * W + gx]) : 0.f;
-    s[ly][lx] = f;
-    m = fmaxf(m, fabsf(f));
-    bad |= !(f == f);
+    hv[k] = 0;  // bits of +0.0
+    if (i < kSn && gx < W && gy < H)
+      hv[k] = __ldg(reinterpret_cast<const unsigned long long *>(h) + (gy * W + gx));
+  }
+#pragma unroll
+  for (int k = 0; k < kSPer; k++) {
+    const int i = t0 + 256 * k;
+    if (i < kSn) {
+      const int ly = i / kSw, lx = i - ly * kSw;
+      const float f = trunc_bits_to_float(hv[k]);
+      s[ly][lx] = f;
+      m = fmaxf(m, fabsf(f));
+      bad |= !(f == f);
+    }
   }
   const unsigned wm = __reduce_max_sync(kFull, __float_as_uint(m));  // m >= 0: bits order
   if (threadIdx.x == 0) s_wmax[threadIdx.y] = wm;
@@ -415,12 +431,33 @@ __global__ void __launch_bounds__(256) k_donors_level0(StepArgs a) {
   // feed cells that are not written), as the aligned words from the one
   // holding byte x0-4 on; s_sh = position of byte x0-4 in the first word.
   // The reads stay within kRecPad bytes of the realization.
-  for (int ly = threadIdx.y; ly < kDyTile + 2; ly += 8) {
-    const int gy = min(t.y0 - 1 + ly, H - 1);
-    const uintptr_t first = reinterpret_cast<uintptr_t>(rec + (size_t)gy * W + t.x0) - 4;
-    const unsigned *src = reinterpret_cast<const unsigned *>(first & ~(uintptr_t)3);
-    for (int j = threadIdx.x; j < kDWords; j += 32) S[ly][j] = __ldg(src + j);
-    if (threadIdx.x == 0) s_sh[ly] = (int)(first & 3);
+  // (all of a thread's loads in flight before the first is stored)
+  constexpr int kSRows = (kDyTile + 2 + 7) / 8;
+  static_assert(kDWords > 32 && kDWords <= 64, "two words per lane and row");
+  unsigned wv[kSRows][2];
+  int shv[kSRows];
+#pragma unroll
+  for (int k = 0; k < kSRows; k++) {
+    const int ly = threadIdx.y + 8 * k;
+    wv[k][0] = wv[k][1] = 0;
+    shv[k] = 0;
+    if (ly < kDyTile + 2) {
+      const int gy = min(t.y0 - 1 + ly, H - 1);
+      const uintptr_t first = reinterpret_cast<uintptr_t>(rec + (size_t)gy * W + t.x0) - 4;
+      const unsigned *src = reinterpret_cast<const unsigned *>(first & ~(uintptr_t)3);
+      wv[k][0] = __ldg(src + threadIdx.x);
+      if (threadIdx.x + 32 < kDWords) wv[k][1] = __ldg(src + 32 + threadIdx.x);
+      shv[k] = (int)(first & 3);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kSRows; k++) {
+    const int ly = threadIdx.y + 8 * k;
+    if (ly < kDyTile + 2) {
+      S[ly][threadIdx.x] = wv[k][0];
+      if (threadIdx.x + 32 < kDWords) S[ly][32 + threadIdx.x] = wv[k][1];
+      if (threadIdx.x == 0) s_sh[ly] = shv[k];
+    }
   }
   __syncthreads();
   const int gx0 = t.x0 + 4 * threadIdx.x;   // the thread's first cell
