@@ -150,6 +150,39 @@ def test_workload_1000_full_run(pkg, oracle):
     assert nl >= 2 and acc.min() == p.cell_area
 
 
+@pytest.mark.slow
+def test_workload_10000_full_run(pkg, oracle):
+    """The 10000x10000 workload: run(20) = 21 timesteps, final elevation
+    bit-identical to the oracle (OpenMP restatement of fastscape_RB+P, about
+    a minute on the host cores), plus size-independent checks of the last
+    timestep's receivers, level ids and accumulation."""
+    W = H = 10000
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_REFERENCE) as m:
+        m.run(20)
+        got = m.getH()
+        rec = m.receivers()
+        lid, nl = m.levels()
+        acc = m.accumulation()
+    # every cell drains to exactly one root: the roots' drainage areas add
+    # up to the grid; a non-root cell sits one level above its receiver
+    roots = rec == -1
+    assert np.count_nonzero(lid[roots] == 0) == np.count_nonzero(roots)
+    assert np.sum(acc[roots] / p.cell_area, dtype=np.float64) == W * H
+    off = np.array([-1, -W - 1, -W, -W + 1, 1, W + 1, W, W - 1], dtype=np.int64)
+    for y0 in range(0, H, 1000):
+        sl = slice(y0 * W, (y0 + 1000) * W)
+        r = rec[sl]
+        c = np.nonzero(r >= 0)[0] + y0 * W
+        assert np.array_equal(lid[c], lid[c + off[rec[c]]] + 1)
+        assert np.all(acc[c] < acc[c + off[rec[c]]])
+    assert nl == lid.max() + 1
+    del rec, lid, acc
+    h = oracle.terrain(W, H, 0)
+    oracle.run(h, W, H, Params(*p.as_tuple()), 20, parallel=True)
+    assert np.array_equal(got, h)
+
+
 def test_run_then_run_equals_one_run(pkg):
     """State carried between run() calls is only h (fastscape_RB.cpp:334-340)."""
     W = 200
