@@ -312,7 +312,8 @@ def ensemble_spec(pkg, n: int, seed: int = 2019):
 
 def run_ensemble(args, dist, rank, ws, local):
     """Batched ragged ensemble: realizations/s of 200-timestep runs, one
-    batched launch sequence per timestep (autotuned, graph-replayed)."""
+    batched launch sequence per timestep (autotuned). The timed region is the
+    whole run from the initial fields, so deepening level structures count."""
     import __graft_entry__ as ge
     import torch  # noqa: F401
     pkg = ge.load()
@@ -322,21 +323,24 @@ def run_ensemble(args, dist, rank, ws, local):
     b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX,
                            seeds=list(range(1000 * rank, 1000 * rank + len(sides))))
     cells = b.cells()
-    b.step(args.warmup)
+    # warm-up: the autotuner's probe timesteps (8 launch configurations x 3),
+    # after which it restores the initial fields
     tune = b.autotune(probe_steps=2)
-    b.step(1)
+    warm = 8 * 3
+    nsteps = args.ensemble_steps
     b.set_timing(True)
     b.phase_times(reset=True)
     b.synchronize()
     barrier(dist)
     with Clocks(local) as clk:
-        b.step(args.steps)
+        b.step(nsteps)                       # the whole run from the initial fields
     barrier(dist)
-    t = b.phase_times(reset=True) / args.steps * 2   # per 2 timesteps, like below
-    dt = max_over_ranks(dist, t[3] / 2 * 1e-3 * args.steps)
+    t = b.phase_times(reset=True) / nsteps * 2   # per 2 timesteps, like below
+    dt = max_over_ranks(dist, t[3] / 2 * 1e-3 * nsteps)
+    levels = max(b.levels(r)[1] for r in range(len(sides)))
     b.close()
-    per_step = dt / args.steps
-    value = ws * len(sides) / (ENSEMBLE_STEPS * per_step)
+    per_step = dt / nsteps
+    value = ws * len(sides) / (nsteps * per_step)
     if rank == 0:
         peak, peak_kind = load_peaks()
         kern = {"receivers": t[0] / 2, "donors_level0": t[1] / 2, "order": t[7] / 2,
@@ -344,20 +348,22 @@ def run_ensemble(args, dist, rank, ws, local):
         dom = max(("order", "erode"), key=kern.get)
         achieved = ALG_BYTES[dom] * cells / (kern[dom] * 1e-3) / 1e9
         print(json.dumps({
-            "metric": "ensemble realizations/s (200-timestep runs)", "value": value,
-            "unit": "realizations/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "metric": f"ensemble realizations/s ({nsteps}-timestep runs)", "value": value,
+            "unit": "realizations/s", "n_gpus": ws, "steps": nsteps, "warmup": warm,
             "ms_per_step": 1e3 * per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"ragged ensemble of {len(sides)} realizations, sides "
                                    "log-U[256,2048], K log-U[1e-6,1e-5], m U[0.3,0.6], "
                                    "U log-U[1e-4,5e-3], n 1, dt 1000, dx 100",
                        "cells_per_step": cells, "cell_steps_per_s": cells / per_step,
-                       "autotune": tune, "l2": "inputs larger than L2"},
+                       "autotune": tune, "l2": "inputs larger than L2",
+                       "timed": f"the whole {nsteps}-timestep run from the initial fields",
+                       "levels_at_end": levels},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "alg_bytes_per_cell": ALG_BYTES[dom],
                          "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": kern},
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": 5 * nsteps,
             "clocks": clk.summary(),
         }), flush=True)
     if dist is not None:
@@ -442,6 +448,8 @@ def main():
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
                          "256-realization batch; sweep: grid sizes 100..20000")
     ap.add_argument("--realizations", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=ENSEMBLE_STEPS,
+                    help="ensemble: timesteps of the timed run (the metric's run length)")
     ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
     args = ap.parse_args()
     if args.warmup < 3:
