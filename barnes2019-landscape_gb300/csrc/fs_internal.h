@@ -122,6 +122,7 @@ enum NMode : int {
 //   nd[i]    number of donors of ent[i]
 //   kid[i]   position of its first donor (local); its donors are contiguous
 //   acc[i]   drainage cell count of ent[i]
+//   par[i]   position of ent[i]'s receiver (levels >= 1)
 struct StepArgs {
   double *h;
   int8_t *rec;
@@ -131,6 +132,7 @@ struct StepArgs {
   uint8_t *nd;
   int32_t *kid;
   uint32_t *acc;
+  int32_t *par;
   int32_t *amb;            // queued cells (global index) of the filter
   int32_t *amb_r;          // and their realization
   int32_t *lvl_off;        // per realization: size+2 local level offsets

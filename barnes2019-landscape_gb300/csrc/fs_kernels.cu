@@ -799,6 +799,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         if (i < hi) {
           a.kid[d.off + i] = cbase + incl[q] - n_d;
           a.nd[d.off + i] = (uint8_t)n_d;
+          a.acc[d.off + i] = 1u;  // the cell itself; donors add theirs below
         }
         // The pass's donors go to positions cbase + [q_lo, q_lo + q_n) in
         // entry order. Each lane records (its lane, direction) for the slots
@@ -826,6 +827,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
             if (pos < d.size) {
               ent[pos] = oc + ok;
               a.pdir[d.off + pos] = (uint8_t)((k + 4) & 7);
+              a.par[d.off + pos] = wbase + 32 * q + (int)(pk >> 3);  // receiver's position
             } else {
               raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
             }
@@ -888,97 +890,71 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
     return block_prefix(nreal, [&](int r) { return (s_hi[r] - s_lo[r] + 31) >> 5; }, s_pre);
   };
 
-  // ---- accumulation: fastscape_RB.cpp:262-279, pulled level by level ----
-  // acc[i] = 1 + sum of the donors' counts, read from the contiguous run
-  // [kid[i], kid[i] + nd[i]) of the next level; the reference's accum is
-  // acc*cell_area (exact: integer multiples of cell_area). A warp takes
-  // kAccU 32-entry groups (a group lies inside one expansion chunk, so its
-  // donors form one contiguous run starting at kid of its first entry),
-  // loads the runs coalesced -- all groups' first 32 donors in flight
-  // together -- and each lane sums its own donors with shuffles. A count at
-  // level >= 1 beyond its realization's erosion table stops the timestep
-  // before any elevation changes; the host grows the table and repeats it.
-  for (int Lv = maxlev - 1; Lv >= 0; --Lv) {
-    if (Lv == 0 && ld_volatile_i32(&ctl->abort_k) != 0) return;
+  // ---- accumulation: fastscape_RB.cpp:262-279, pushed level by level ----
+  // acc[i] = 1 + the counts of i's donors (the reference's accum is
+  // acc*cell_area, exact: integer multiples of cell_area). The ordering set
+  // every acc to 1; from the deepest level up, each entry -- whose count is
+  // final, its donors having pushed before the last barrier -- adds its
+  // count to its receiver's (position par[i]) with a fire-and-forget
+  // reduction. Integer sums are exact in any order. A count at level >= 1
+  // beyond its realization's erosion table stops the timestep before any
+  // elevation changes; the host grows the table and repeats it.
+  for (int Lv = maxlev - 1; Lv >= 1; --Lv) {
     const int ngroups = level_groups(Lv);
     for (int g0 = warp_global * kAccU; g0 < ngroups; g0 += nwarps * kAccU) {
-      int n[kAccU], incl[kAccU], run[kAccU], tot[kAccU], ii[kAccU], rr[kAccU];
-      uint32_t v0[kAccU];
+      uint32_t v[kAccU];
+      int pp[kAccU], rr[kAccU];
+      bool ok[kAccU];
 #pragma unroll
-      for (int u = 0; u < kAccU; u++) {
+      for (int u = 0; u < kAccU; u++) {  // all loads in flight first
         const int g = g0 + u;
-        int k = 0;
-        n[u] = 0;
+        ok[u] = false;
+        v[u] = 0;
+        pp[u] = 0;
         rr[u] = 0;
-        ii[u] = -1;
         if (g < ngroups) {
           const int r = real_of(g);
           const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
           rr[u] = r;
           if (i < s_hi[r]) {
             const int off = desc(r).off;
-            ii[u] = i;
-            n[u] = __ldcg(&a.nd[off + i]);
-            k = __ldcg(&a.kid[off + i]);
+            ok[u] = true;
+            v[u] = __ldcg(&a.acc[off + i]);
+            pp[u] = __ldcg(&a.par[off + i]);
           }
         }
-        int v = n[u];
-#pragma unroll
-        for (int dd = 1; dd < 32; dd <<= 1) {
-          const int x = __shfl_up_sync(kFull, v, dd);
-          if (lane >= dd) v += x;
-        }
-        incl[u] = v;
-        tot[u] = __shfl_sync(kFull, v, 31);
-        run[u] = desc(rr[u]).off + __shfl_sync(kFull, k, 0);
       }
 #pragma unroll
-      for (int u = 0; u < kAccU; u++)
-        v0[u] = lane < tot[u] ? __ldcg(&a.acc[run[u] + lane]) : 0u;
-#pragma unroll
       for (int u = 0; u < kAccU; u++) {
-        // The donors of the group's entries are the run [0, tot); entry i's
-        // are [first, last) of it. Its count is 1 + E(last) - E(first), E(x)
-        // the sum of the run's counts before x, read from a warp scan of
-        // each 32-donor chunk plus the chunks before it.
-        const int first = incl[u] - n[u], last = incl[u];
-        uint32_t eF = 0, eL = 0, carry = 0;
-        for (int r0 = 0; r0 < tot[u]; r0 += 32) {
-          uint32_t c = v0[u];
-          if (r0 > 0) c = r0 + lane < tot[u] ? __ldcg(&a.acc[run[u] + r0 + lane]) : 0u;
-          uint32_t S = c;
-#pragma unroll
-          for (int dd = 1; dd < 32; dd <<= 1) {
-            const uint32_t x = __shfl_up_sync(kFull, S, dd);
-            if (lane >= dd) S += x;
-          }
-          const uint32_t ex = S - c;  // exclusive within the chunk
-          const int xf = first - r0, xl = last - r0;
-          const uint32_t gf = __shfl_sync(kFull, ex, xf & 31);
-          const uint32_t gl = __shfl_sync(kFull, ex, xl & 31);
-          if (xf >= 0 && xf < 32) eF = carry + gf;
-          if (xl >= 0 && xl < 32) eL = carry + gl;
-          carry += __shfl_sync(kFull, S, 31);
-        }
-        if (first >= tot[u]) eF = carry;  // at the run's end
-        if (last >= tot[u]) eL = carry;
-        const uint32_t s = 1u + (eL - eF);
-        if (ii[u] >= 0) {
+        if (ok[u]) {
           const RealDesc &d = desc(rr[u]);
-          a.acc[d.off + ii[u]] = s;
-          if (a.do_erode && Lv > 0 && s >= (uint32_t)d.tab_cap) {
-            if (atomicMax(&ctl->abort_k, (int)s) < (int)s) ctl->abort_r = rr[u];
-          }
-          if (Lv == 0 && a.do_erode && ii[u] >= d.nring) {
-            // a pit (level 0 past the rings): uplift it (fastscape_RB.cpp:291-295)
-            unsigned long long *hh = reinterpret_cast<unsigned long long *>(a.h + d.off);
-            const int c = __ldcg(&a.ent[d.off + ii[u]]);
-            hh[c] = fadd_bits(__ldcg(&hh[c]), (uint64_t)__double_as_longlong(d.u_dt));
+          atomicAdd(&a.acc[d.off + pp[u]], v[u]);
+          if (a.do_erode && v[u] >= (uint32_t)d.tab_cap) {
+            if (atomicMax(&ctl->abort_k, (int)v[u]) < (int)v[u]) ctl->abort_r = rr[u];
           }
         }
       }
     }
-    if (Lv > 0 && !grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
+    if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
+  }
+  // Level 0: counts final. With no table exceeded, uplift the pits (level 0
+  // past the rings; fastscape_RB.cpp:291-295) -- the erosion kernel reads
+  // them after the kernel boundary.
+  if (a.do_erode && ld_volatile_i32(&ctl->abort_k) == 0) {
+    __syncthreads();  // every warp is done with the last level's ranges
+    for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+      s_lo[r] = desc(r).nring;
+      s_hi[r] = __ldcg(&a.lvl_off[desc(r).lvl_base + 1]);
+    }
+    __syncthreads();
+    const int np = block_prefix(nreal, [&](int r) { return s_hi[r] - s_lo[r]; }, s_pre);
+    for (int g = tid; g < np; g += nthreads) {
+      const int r = real_of(g);
+      const RealDesc &d = desc(r);
+      unsigned long long *hh = reinterpret_cast<unsigned long long *>(a.h + d.off);
+      const int c = __ldcg(&a.ent[d.off + s_lo[r] + (g - s_pre[r])]);
+      hh[c] = fadd_bits(__ldcg(&hh[c]), (uint64_t)__double_as_longlong(d.u_dt));
+    }
   }
   lap(1);
 }

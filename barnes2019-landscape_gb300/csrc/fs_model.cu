@@ -111,7 +111,8 @@ struct fs_batch {
   int8_t *rec = nullptr;
   int8_t *rec_alloc = nullptr;  // rec - kRecPad
   uint8_t *mask = nullptr, *pdir = nullptr, *nd = nullptr;
-  int32_t *ent = nullptr, *kid = nullptr, *amb = nullptr, *amb_r = nullptr, *lvl = nullptr;
+  int32_t *ent = nullptr, *kid = nullptr, *par = nullptr, *amb = nullptr, *amb_r = nullptr,
+          *lvl = nullptr;
   uint32_t *acc = nullptr;
   fs::RealDesc *d_desc = nullptr;
   fs::RealCtl *d_rctl = nullptr, *h_rctl = nullptr;
@@ -157,7 +158,7 @@ void free_batch(fs_batch *b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->nd, b->ent, b->kid, b->amb, b->amb_r,
+  void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->nd, b->ent, b->kid, b->par, b->amb, b->amb_r,
                   b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles};
   for (void *x : bufs) cudaFree(x);
   for (double *t : b->tab) cudaFree(t);
@@ -242,6 +243,7 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.pdir = b->pdir;
   a.nd = b->nd;
   a.kid = b->kid;
+  a.par = b->par;
   a.acc = b->acc;
   a.amb = b->amb;
   a.amb_r = b->amb_r;
@@ -493,6 +495,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
       !cu(cudaMalloc(&b->nd, C), "cudaMalloc(nd)") ||
       !cu(cudaMalloc(&b->ent, C * sizeof(int32_t)), "cudaMalloc(ent)") ||
       !cu(cudaMalloc(&b->kid, C * sizeof(int32_t)), "cudaMalloc(kid)") ||
+      !cu(cudaMalloc(&b->par, C * sizeof(int32_t)), "cudaMalloc(par)") ||
       !cu(cudaMalloc(&b->amb, C * sizeof(int32_t)), "cudaMalloc(amb)") ||
       !cu(cudaMalloc(&b->amb_r, C * sizeof(int32_t)), "cudaMalloc(amb_r)") ||
       !cu(cudaMalloc(&b->acc, C * sizeof(uint32_t)), "cudaMalloc(acc)") ||

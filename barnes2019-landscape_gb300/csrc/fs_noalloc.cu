@@ -14,8 +14,9 @@
 // Limits and sharing:
 //   * grids of at most FS_NOALLOC_MAX_CELLS cells (width*height); larger
 //     grids are rejected with FS_ERR_ARG;
-//   * the scratch array (~24 MB: receivers, donor masks, level lists and
-//     offsets, drainage counts, the erosion table for every possible count,
+//   * the scratch array (~25 MB: receivers, donor masks, level lists and
+//     offsets, receiver positions, drainage counts, the erosion table for
+//     every possible count,
 //     stencil tiles, descriptors and the control block) lives in the library
 //     image, so every GPU that loads the library holds it until the process
 //     exits;
@@ -53,7 +54,8 @@ constexpr size_t kOffDtiles = align256(kOffRtiles + kMaxTiles * sizeof(fs::Tile)
 constexpr size_t kOffTab = align256(kOffDtiles + kMaxTiles * sizeof(fs::Tile));
 constexpr size_t kOffEnt = align256(kOffTab + kTabRecords * fs::kTabStride * sizeof(double));
 constexpr size_t kOffKid = align256(kOffEnt + kMaxCells * sizeof(int32_t));
-constexpr size_t kOffAmb = align256(kOffKid + kMaxCells * sizeof(int32_t));
+constexpr size_t kOffPar = align256(kOffKid + kMaxCells * sizeof(int32_t));
+constexpr size_t kOffAmb = align256(kOffPar + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAmbR = align256(kOffAmb + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffLvl = align256(kOffAmbR + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAcc = align256(kOffLvl + (kMaxCells + 2) * sizeof(int32_t));
@@ -219,6 +221,7 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   a.pdir = reinterpret_cast<uint8_t *>(d.base + kOffPdir);
   a.nd = reinterpret_cast<uint8_t *>(d.base + kOffNd);
   a.kid = reinterpret_cast<int32_t *>(d.base + kOffKid);
+  a.par = reinterpret_cast<int32_t *>(d.base + kOffPar);
   a.acc = reinterpret_cast<uint32_t *>(d.base + kOffAcc);
   a.amb = reinterpret_cast<int32_t *>(d.base + kOffAmb);
   a.amb_r = reinterpret_cast<int32_t *>(d.base + kOffAmbR);
