@@ -117,10 +117,9 @@ enum NMode : int {
 
 // Arrays indexed by position i in the level order (the reference's stack):
 //   ent[i]   cell index (local); level 0 starts with the two rings (fixed)
-//            followed by the pits of this timestep
+//            followed by the pits of this timestep; each level lists the
+//            donors of the level before it, a receiver's donors contiguous
 //   pdir[i]  receiver direction of ent[i] (0..7)
-//   nd[i]    number of donors of ent[i]
-//   kid[i]   position of its first donor (local); its donors are contiguous
 //   acc[i]   drainage cell count of ent[i]
 //   par[i]   position of ent[i]'s receiver (levels >= 1)
 struct StepArgs {
@@ -129,8 +128,6 @@ struct StepArgs {
   uint8_t *mask;
   int32_t *ent;
   uint8_t *pdir;
-  uint8_t *nd;
-  int32_t *kid;
   uint32_t *acc;
   int32_t *par;
   int32_t *amb;            // queued cells (global index) of the filter
@@ -181,8 +178,7 @@ cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns
 struct DfsArgs {
   const int8_t *rec;
   const int32_t *ent;
-  const uint8_t *nd;
-  const int32_t *kid;
+  const int32_t *par;
   const uint8_t *pdir;
   const uint32_t *acc;
   int W, size;

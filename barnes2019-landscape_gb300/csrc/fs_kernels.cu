@@ -797,8 +797,6 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         const int i = wbase + 32 * q + lane;
         const int n_d = __popc(ms[q]);
         if (i < hi) {
-          a.kid[d.off + i] = cbase + incl[q] - n_d;
-          a.nd[d.off + i] = (uint8_t)n_d;
           a.acc[d.off + i] = 1u;  // the cell itself; donors add theirs below
         }
         // The pass's donors go to positions cbase + [q_lo, q_lo + q_n) in
@@ -1241,13 +1239,24 @@ __global__ void k_dfs_level0(const int32_t *__restrict__ ent, const int32_t *__r
 
 // Donors of the entries [b, e): positions after their parent in ascending
 // cell-index order (the donor-list order of fastscape_BW.cpp:188-198).
-__global__ void k_dfs_level(const uint8_t *__restrict__ nd, const int32_t *__restrict__ kid,
+// First and one-past-last donor position of every receiver, from the
+// donors' receiver positions (a receiver's donors are contiguous, so they
+// start where par changes): kid / kend for positions of levels >= 1.
+__global__ void k_dfs_links(const int32_t *__restrict__ par, int b1, int n,
+                            int32_t *__restrict__ kid, int32_t *__restrict__ kend) {
+  for (int j = b1 + blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int p = par[j];
+    if (j == b1 || par[j - 1] != p) kid[p] = j;
+    if (j == n - 1 || par[j + 1] != p) kend[p] = j + 1;
+  }
+}
+
+__global__ void k_dfs_level(const int32_t *__restrict__ kid, const int32_t *__restrict__ kend,
                             const uint8_t *__restrict__ pdir, const uint32_t *__restrict__ acc,
                             int b, int e, int W, int32_t *__restrict__ dpos) {
   for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
-    const int n = nd[i];
-    if (!n) continue;
-    const int k0 = kid[i];
+    const int k0 = kid[i], n = kend[i] - k0;
+    if (n <= 0) continue;
     const int p = dpos[i];
     for (int q = 0; q < n; q++) {
       // the donor's offset from its receiver is minus its receiver offset
@@ -1433,25 +1442,29 @@ cudaError_t launch_test_wait(Ctl *ctl, int blocks, unsigned long long timeout_ns
 }
 
 size_t dfs_scratch_ints(int size) {
-  return 3 * (size_t)size + (size_t)(size + kScanBlock - 1) / kScanBlock + 1;
+  return 5 * (size_t)size + (size_t)(size + kScanBlock - 1) / kScanBlock + 1;
 }
 
 cudaError_t launch_dfs_order(const DfsArgs &d, const int32_t *lvl_host, int nlev,
                              int32_t *scratch, int32_t *out, cudaStream_t s) {
   const int n = d.size;
   int32_t *cellacc = scratch, *v = scratch + n, *dpos = scratch + 2 * (size_t)n;
-  int32_t *bsum = scratch + 3 * (size_t)n;
+  int32_t *kid = scratch + 3 * (size_t)n, *kend = scratch + 4 * (size_t)n;
+  int32_t *bsum = scratch + 5 * (size_t)n;
   const int nb = (n + kScanBlock - 1) / kScanBlock;
   const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  cudaError_t e = cudaMemsetAsync(kid, 0, 2 * (size_t)n * sizeof(int32_t), s);
+  if (e != cudaSuccess) return e;
+  if (nlev > 1 && lvl_host[1] < n) k_dfs_links<<<g, 256, 0, s>>>(d.par, lvl_host[1], n, kid, kend);
   k_scatter_counts<<<g, 256, 0, s>>>(d.ent, d.acc, n, cellacc);
   k_root_sizes_blocksum<<<nb, kScanBlock, 0, s>>>(d.rec, cellacc, n, v, bsum);
   k_scan_sums<<<1, kScanBlock, 0, s>>>(bsum, nb);
   k_scan_apply<<<nb, kScanBlock, 0, s>>>(v, bsum, n);
   k_dfs_level0<<<g, 256, 0, s>>>(d.ent, v, lvl_host[1], dpos);
   for (int L = 0; L + 1 < nlev; L++) {
-    const int b = lvl_host[L], e = lvl_host[L + 1];
-    const int gl = (e - b + 255) / 256 < 4096 ? (e - b + 255) / 256 : 4096;
-    if (gl > 0) k_dfs_level<<<gl, 256, 0, s>>>(d.nd, d.kid, d.pdir, d.acc, b, e, d.W, dpos);
+    const int b = lvl_host[L], e2 = lvl_host[L + 1];
+    const int gl = (e2 - b + 255) / 256 < 4096 ? (e2 - b + 255) / 256 : 4096;
+    if (gl > 0) k_dfs_level<<<gl, 256, 0, s>>>(kid, kend, d.pdir, d.acc, b, e2, d.W, dpos);
   }
   k_dfs_scatter<<<g, 256, 0, s>>>(d.ent, dpos, n, out);
   return cudaGetLastError();

@@ -11,10 +11,9 @@
 //   mask    uint8[C]            donor mask (bit k: neighbour k drains here)
 //   ent     int32[C]            cells grouped by level (the reference's stack)
 //   pdir    uint8[C]            receiver direction by level position
-//   nd      uint8[C]            donor count by level position
-//   kid     int32[C]            first donor's position by level position
 //   acc     uint32[C]           drainage cell counts by level position
 //                               (accum = acc*cell_area)
+//   par     int32[C]            receiver's position by level position
 //   amb     int32[C], amb_r     cells queued for the FP64 receiver fix-up
 //   lvl_off int32[C+2n]         level offsets, size_r+2 per realization
 //   tab_r   double[8*cap_r]     erosion table of realization r per drainage
@@ -110,9 +109,8 @@ struct fs_batch {
   double *h = nullptr;
   int8_t *rec = nullptr;
   int8_t *rec_alloc = nullptr;  // rec - kRecPad
-  uint8_t *mask = nullptr, *pdir = nullptr, *nd = nullptr;
-  int32_t *ent = nullptr, *kid = nullptr, *par = nullptr, *amb = nullptr, *amb_r = nullptr,
-          *lvl = nullptr;
+  uint8_t *mask = nullptr, *pdir = nullptr;
+  int32_t *ent = nullptr, *par = nullptr, *amb = nullptr, *amb_r = nullptr, *lvl = nullptr;
   uint32_t *acc = nullptr;
   fs::RealDesc *d_desc = nullptr;
   fs::RealCtl *d_rctl = nullptr, *h_rctl = nullptr;
@@ -158,7 +156,7 @@ void free_batch(fs_batch *b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->nd, b->ent, b->kid, b->par, b->amb, b->amb_r,
+  void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->ent, b->par, b->amb, b->amb_r,
                   b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles};
   for (void *x : bufs) cudaFree(x);
   for (double *t : b->tab) cudaFree(t);
@@ -241,8 +239,6 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.mask = b->mask;
   a.ent = b->ent;
   a.pdir = b->pdir;
-  a.nd = b->nd;
-  a.kid = b->kid;
   a.par = b->par;
   a.acc = b->acc;
   a.amb = b->amb;
@@ -492,9 +488,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
       !cu(cudaMalloc(&b->rec_alloc, C + 2 * fs::kRecPad), "cudaMalloc(rec)") ||
       !cu(cudaMalloc(&b->mask, C), "cudaMalloc(mask)") ||
       !cu(cudaMalloc(&b->pdir, C), "cudaMalloc(pdir)") ||
-      !cu(cudaMalloc(&b->nd, C), "cudaMalloc(nd)") ||
       !cu(cudaMalloc(&b->ent, C * sizeof(int32_t)), "cudaMalloc(ent)") ||
-      !cu(cudaMalloc(&b->kid, C * sizeof(int32_t)), "cudaMalloc(kid)") ||
       !cu(cudaMalloc(&b->par, C * sizeof(int32_t)), "cudaMalloc(par)") ||
       !cu(cudaMalloc(&b->amb, C * sizeof(int32_t)), "cudaMalloc(amb)") ||
       !cu(cudaMalloc(&b->amb_r, C * sizeof(int32_t)), "cudaMalloc(amb_r)") ||
@@ -730,7 +724,7 @@ int get_stack_dfs(const fs_batch *b, int r, int32_t *stack, int32_t *stack_start
   FS_CUDA(cudaMalloc(&scratch, fs::dfs_scratch_ints(n) * sizeof(int32_t)));
   cudaError_t e = cudaMalloc(&out, n * sizeof(int32_t));
   const int o = b->off[r];
-  const fs::DfsArgs d{b->rec + o, b->ent + o, b->nd + o, b->kid + o, b->pdir + o, b->acc + o,
+  const fs::DfsArgs d{b->rec + o, b->ent + o, b->par + o, b->pdir + o, b->acc + o,
                       b->W[r], n};
   if (e == cudaSuccess) e = fs::launch_dfs_order(d, off.data(), nl, scratch, out, b->stream);
   if (e == cudaSuccess)

@@ -14,7 +14,7 @@
 // Limits and sharing:
 //   * grids of at most FS_NOALLOC_MAX_CELLS cells (width*height); larger
 //     grids are rejected with FS_ERR_ARG;
-//   * the scratch array (~25 MB: receivers, donor masks, level lists and
+//   * the scratch array (~24 MB: receivers, donor masks, level lists and
 //     offsets, receiver positions, drainage counts, the erosion table for
 //     every possible count,
 //     stencil tiles, descriptors and the control block) lives in the library
@@ -53,8 +53,7 @@ constexpr size_t kOffRtiles = align256(kOffDesc + sizeof(fs::RealDesc));
 constexpr size_t kOffDtiles = align256(kOffRtiles + kMaxTiles * sizeof(fs::Tile));
 constexpr size_t kOffTab = align256(kOffDtiles + kMaxTiles * sizeof(fs::Tile));
 constexpr size_t kOffEnt = align256(kOffTab + kTabRecords * fs::kTabStride * sizeof(double));
-constexpr size_t kOffKid = align256(kOffEnt + kMaxCells * sizeof(int32_t));
-constexpr size_t kOffPar = align256(kOffKid + kMaxCells * sizeof(int32_t));
+constexpr size_t kOffPar = align256(kOffEnt + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAmb = align256(kOffPar + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffAmbR = align256(kOffAmb + kMaxCells * sizeof(int32_t));
 constexpr size_t kOffLvl = align256(kOffAmbR + kMaxCells * sizeof(int32_t));
@@ -64,8 +63,7 @@ constexpr size_t kOffAcc = align256(kOffLvl + (kMaxCells + 2) * sizeof(int32_t))
 constexpr size_t kOffRec = align256(kOffAcc + kMaxCells * sizeof(uint32_t) + fs::kRecPad);
 constexpr size_t kOffMask = align256(kOffRec + kMaxCells + fs::kRecPad);
 constexpr size_t kOffPdir = align256(kOffMask + kMaxCells);
-constexpr size_t kOffNd = align256(kOffPdir + kMaxCells);
-constexpr size_t kScratchBytes = align256(kOffNd + kMaxCells);
+constexpr size_t kScratchBytes = align256(kOffPdir + kMaxCells);
 
 // The scratch. Host code must not use this name as a device address (on the
 // host it is only a stand-in); the address comes from cudaGetSymbolAddress.
@@ -219,8 +217,6 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   a.mask = reinterpret_cast<uint8_t *>(d.base + kOffMask);
   a.ent = reinterpret_cast<int32_t *>(d.base + kOffEnt);
   a.pdir = reinterpret_cast<uint8_t *>(d.base + kOffPdir);
-  a.nd = reinterpret_cast<uint8_t *>(d.base + kOffNd);
-  a.kid = reinterpret_cast<int32_t *>(d.base + kOffKid);
   a.par = reinterpret_cast<int32_t *>(d.base + kOffPar);
   a.acc = reinterpret_cast<uint32_t *>(d.base + kOffAcc);
   a.amb = reinterpret_cast<int32_t *>(d.base + kOffAmb);

@@ -52,11 +52,10 @@ RUN_NSTEP = 20            # run(20) executes 21 timesteps
 ALG_BYTES = {
     "receivers": 8 + 1,                     # h read, rec write
     "donors_level0": 1 + 1,                 # rec read, mask write (+ pit list)
-    "order": (4 + 1 + 4 + 1 + 4 + 1 + 4 + 4) + (4 + 4 + 4),
+    "order": (4 + 1 + 4 + 1 + 4 + 4) + (4 + 4 + 4),
     # k_order -- ordering: entry read, mask read, entry + direction +
-    # receiver-position write, first-donor position + donor count + unit
-    # count write; accumulation: own count and receiver position read,
-    # reduction into the receiver's count
+    # receiver-position write, unit count write; accumulation: own count
+    # and receiver position read, reduction into the receiver's count
     "erode": 4 + 1 + 4 + 8 + 8,
     # k_erode: entry, direction, count, h read, h write
 }
