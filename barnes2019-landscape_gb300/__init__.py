@@ -279,7 +279,7 @@ class FastScape_RBP:
 
     TIMERS = ("receivers", "donors_level0", "walk", "total",
               "walk_order", "walk_accumulation", "walk_erosion",
-              "order_kernel", "erode_kernel")
+              "order_kernel", "erode_kernel", "accum_kernel")
 
     def phase_times(self, reset: bool = False):
         """Device milliseconds per timer in TIMERS (fs_get_phase_times)."""

@@ -32,7 +32,7 @@ struct Ctl {
   unsigned int bar;        // grid-barrier arrival counter (k_order)
   int amb;                 // cells queued by the receiver filter
   unsigned int bar2;       // grid-barrier arrival counter (k_erode)
-  int pad1;
+  unsigned int bar3;       // grid-barrier arrival counter (k_accum)
 };
 constexpr size_t kCtlResetOffset = offsetof(Ctl, bar);
 constexpr size_t kCtlResetBytes = sizeof(Ctl) - kCtlResetOffset;
@@ -158,15 +158,18 @@ cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s);
 cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
 // The level walk: k_order with order_bps blocks per SM (2 or 3; each has
-// its own register budget), then (when a.do_erode) k_erode with erode_bps
-// blocks per SM; both cooperative launches over `sms` SMs.
-cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
-                        cudaStream_t s);
+// its own register budget), k_accum with accum_bps, then (when a.do_erode)
+// k_erode with erode_bps blocks per SM; cooperative launches over `sms` SMs.
+cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int accum_bps,
+                        int erode_bps, cudaStream_t s);
 cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_order
+cudaError_t launch_accum(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_accum
 cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_erode
 int walk_threads();
 const void *walk_kernel_ptr(int nmode, bool single);    // k_erode
 const void *order_kernel_ptr(bool single, int bps);     // k_order for bps 2 or 3
+const void *accum_kernel_ptr(bool single);              // k_accum
+constexpr int kAccumMaxBps = 4;                         // k_accum's register budget
 cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
 cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s);
 cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s);

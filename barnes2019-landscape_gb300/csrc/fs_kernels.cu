@@ -1,7 +1,7 @@
 // fs_kernels.cu -- sm_103a kernels of the FastScape timestep, over a batch
 // of realizations (a single model is a batch of one).
 //
-// One timestep = five launches on the stream:
+// One timestep = six launches on the stream:
 //   1. k_receivers_filter  D8 steepest descent over the interior
 //      + k_receivers_fixup (fastscape_RB.cpp:160-182): FP32 proof of the
 //                          receiver, FP64 reference formula for the cells
@@ -9,9 +9,10 @@
 //   2. k_donors_level0     donor masks (pull form of fastscape_RB.cpp:188-203)
 //                          and the level-0 frontier (fastscape_RB.cpp:221-227)
 //   3. k_order             persistent cooperative kernel: level-by-level
-//                          ordering (:229-251) and flow accumulation back
-//                          down the levels (:262-279); uplifts the pits
-//   4. k_erode             persistent cooperative kernel: uplift (:285-296)
+//                          ordering (:229-251)
+//   4. k_accum             persistent cooperative kernel: flow accumulation
+//                          back down the levels (:262-279); uplifts the pits
+//   5. k_erode             persistent cooperative kernel: uplift (:285-296)
 //                          and the implicit erosion solved upward from base
 //                          level (:306-328, in the level order of
 //                          fastscape_RB+P.cpp:319-350).
@@ -870,6 +871,42 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
     }
   }
   lap(0);
+}
+
+// Accumulation (fastscape_RB.cpp:262-279) level by level back down to base
+// level, then the pits' uplift, after k_order has placed the levels. A
+// kernel of its own: its little per-thread state lets it run 4 blocks of
+// 512 threads per SM, hiding more of the latency of its loads.
+template <bool SINGLE>
+__global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
+  extern __shared__ int smem[];
+  const int nreal = a.nreal;
+  int *s_lo = smem;
+  int *s_hi = s_lo + nreal;
+  int *s_nlev = s_hi + nreal;
+  int *s_pre = s_nlev + nreal;
+  __shared__ int s_maxlev;
+  unsigned epoch = 0;
+  Ctl *ctl = a.ctl;
+  if (stopped(ctl)) return;
+  RealDesc d0;
+  if (SINGLE) d0 = a.desc[0];
+  auto desc = [&](int r) -> const RealDesc & { return SINGLE ? d0 : a.desc[r]; };
+  auto real_of = [&](int g) -> int { return SINGLE ? 0 : find_real(s_pre, nreal, g); };
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nthreads = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = tid >> 5, nwarps = nthreads >> 5;
+  const bool stamp = a.stamp && tid == 0;
+  const unsigned long long t_start = stamp ? globaltimer_ns() : 0;
+  if (threadIdx.x == 0) s_maxlev = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
+    s_nlev[r] = __ldcg(&a.rctl[r].nlevels);
+    atomicMax(&s_maxlev, s_nlev[r]);
+  }
+  __syncthreads();
+  const int maxlev = s_maxlev;
 
   // Level Lv of every realization as [s_lo[r], s_hi[r]) (empty past its
   // depth), and the prefix of its 32-entry groups over the batch.
@@ -933,7 +970,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         }
       }
     }
-    if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
+    if (!grid_barrier(ctl, &ctl->bar3, epoch, a.timeout_ns)) return;
   }
   // Level 0: counts final. With no table exceeded, uplift the pits (level 0
   // past the rings; fastscape_RB.cpp:291-295) -- the erosion kernel reads
@@ -954,7 +991,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       hh[c] = fadd_bits(__ldcg(&hh[c]), (uint64_t)__double_as_longlong(d.u_dt));
     }
   }
-  lap(1);
+  if (stamp) atomicAdd(&ctl->walk_ns[1], globaltimer_ns() - t_start);
 }
 
 // Uplift and erosion (fastscape_RB.cpp:285-296, :306-328) level by level
@@ -1307,6 +1344,11 @@ const void *order_kernel_ptr(bool single, int bps) {
                 : reinterpret_cast<const void *>(&k_order<false, 2>);
 }
 
+const void *accum_kernel_ptr(bool single) {
+  return single ? reinterpret_cast<const void *>(&k_accum<true>)
+                : reinterpret_cast<const void *>(&k_accum<false>);
+}
+
 cudaError_t prepare_walk_kernels() {
   const int bytes = (int)walk_smem_bytes(kMaxReal);
   for (int single = 0; single < 2; single++) {
@@ -1320,6 +1362,9 @@ cudaError_t prepare_walk_kernels() {
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
       if (e != cudaSuccess) return e;
     }
+    cudaError_t e = cudaFuncSetAttribute(accum_kernel_ptr(single != 0),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
@@ -1407,9 +1452,17 @@ cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s) {
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }
 
-cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int erode_bps,
-                        cudaStream_t s) {
+cudaError_t launch_accum(const StepArgs &a, int sms, int bps, cudaStream_t s) {
+  StepArgs args = a;
+  void *params[] = {&args};
+  return cudaLaunchCooperativeKernel(accum_kernel_ptr(a.nreal == 1), dim3(sms * bps),
+                                     dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
+}
+
+cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int accum_bps,
+                        int erode_bps, cudaStream_t s) {
   cudaError_t e = launch_order(a, sms, order_bps, s);
+  if (e == cudaSuccess) e = launch_accum(a, sms, accum_bps, s);
   if (e != cudaSuccess || !a.do_erode) return e;
   return launch_erode(a, sms, erode_bps, s);
 }

@@ -122,6 +122,7 @@ struct fs_batch {
   std::vector<int> tab_cap;
   int walk_occ = 1, walk_sms = 1, walk_bps = 2;  // k_erode blocks per SM: limit, SMs, in use
   int order_max = 2, order_bps = 2;              // k_order blocks per SM: limit (2 or 3), in use
+  int accum_bps = 1;                             // k_accum blocks per SM
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
@@ -270,7 +271,7 @@ cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
     e = b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
                            : fs::launch_receivers_fast(a, b->stream);
   if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
-  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream);
+  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->accum_bps, b->walk_bps, b->stream);
   return e;
 }
 
@@ -284,11 +285,11 @@ int ensure_events(fs_batch *b, size_t n) {
 }
 
 // Events per timed timestep: start, after the receivers, after the donors,
-// between the two level-walk kernels (the next timestep's start, or the
-// final event, closes the erosion kernel).
-constexpr int kEvPerStep = 4;
+// after the ordering, after the accumulation (the next timestep's start, or
+// the final event, closes the erosion kernel).
+constexpr int kEvPerStep = 5;
 
-// One timestep with the phase events ev[4i..4i+4] around its launches.
+// One timestep with the phase events ev[5i..5i+5] around its launches.
 int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
   cudaEvent_t *ev = &b->ev[kEvPerStep * i];
   FS_CUDA(cudaEventRecord(ev[0], b->stream));
@@ -302,19 +303,22 @@ int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
   FS_CUDA(cudaEventRecord(ev[2], b->stream));
   FS_CUDA(fs::launch_order(a, b->walk_sms, b->order_bps, b->stream));
   FS_CUDA(cudaEventRecord(ev[3], b->stream));
+  FS_CUDA(fs::launch_accum(a, b->walk_sms, b->accum_bps, b->stream));
+  FS_CUDA(cudaEventRecord(ev[4], b->stream));
   FS_CUDA(fs::launch_erode(a, b->walk_sms, b->walk_bps, b->stream));
   return FS_OK;
 }
 
 int harvest_events(fs_batch *b, int k) {
   FS_CUDA(cudaEventSynchronize(b->ev[kEvPerStep * k]));
-  static const int slot[kEvPerStep] = {0, 1, 7, 8};  // receivers, donors, k_order, k_erode
+  // receivers, donors, k_order, k_accum, k_erode
+  static const int slot[kEvPerStep] = {0, 1, 7, 9, 8};
   for (int i = 0; i < k; i++)
     for (int j = 0; j < kEvPerStep; j++) {
       float ms = 0;
       FS_CUDA(cudaEventElapsedTime(&ms, b->ev[kEvPerStep * i + j], b->ev[kEvPerStep * i + j + 1]));
       b->phase_ms[slot[j]] += ms;
-      if (j >= 2) b->phase_ms[2] += ms;  // the level walk: both kernels
+      if (j >= 2) b->phase_ms[2] += ms;  // the level walk: its three kernels
     }
   float tot = 0;
   FS_CUDA(cudaEventElapsedTime(&tot, b->ev[0], b->ev[kEvPerStep * k]));
@@ -618,6 +622,16 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
     if (bps == 2) return fail(set_error(FS_ERR_CUDA, "order kernel cannot be resident"));
   }
   b->order_bps = b->order_max;
+  {
+    int o = 0;
+    if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fs::accum_kernel_ptr(n == 1),
+                                                          fs::walk_threads(),
+                                                          fs::walk_smem_bytes(n)),
+            "occupancy"))
+      return fail(*status);
+    if (o < 1) return fail(set_error(FS_ERR_CUDA, "accumulation kernel cannot be resident"));
+    b->accum_bps = std::min(o, fs::kAccumMaxBps);
+  }
   if (!cu(cudaStreamSynchronize(b->stream), "sync")) return fail(*status);
   return b;
 }
@@ -1150,7 +1164,7 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
   FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
   const fs::StepArgs a = step_args(b, 0);
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
-  FS_CUDA(fs::launch_walk(a, b->walk_sms, b->order_bps, b->walk_bps, b->stream));
+  FS_CUDA(fs::launch_walk(a, b->walk_sms, b->order_bps, b->accum_bps, b->walk_bps, b->stream));
   b->have_step = true;
   return collect_status(b);
 }

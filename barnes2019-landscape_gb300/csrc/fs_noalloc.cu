@@ -79,6 +79,7 @@ struct DeviceState {
   int sms = 0;
   int erode_bps[3] = {0, 0, 0};  // k_erode blocks per SM for each n mode
   int order_bps = 2;
+  int accum_bps = 1;
   bool tab_valid = false;
   fs_params tab_params{};
 };
@@ -131,6 +132,11 @@ int setup_device(int dev, DeviceState &d) {
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (occ < 2) return fail(FS_ERR_CUDA, "order kernel cannot be resident");
   }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs::accum_kernel_ptr(true),
+                                                    fs::walk_threads(), fs::walk_smem_bytes(1));
+  if (e != cudaSuccess) return cuda_fail(e, "occupancy");
+  if (occ < 1) return fail(FS_ERR_CUDA, "accumulation kernel cannot be resident");
+  d.accum_bps = occ < fs::kAccumMaxBps ? occ : fs::kAccumMaxBps;
   d.sms = sms;
   d.base = static_cast<unsigned char *>(ptr);
   d.ready = true;
@@ -258,7 +264,7 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
     if (e == cudaSuccess) e = cudaMemsetAsync(rctl, 0, sizeof(fs::RealCtl), s);
     if (e == cudaSuccess) e = fs::launch_receivers_fast(a, s);
     if (e == cudaSuccess) e = fs::launch_donors_level0(a, s);
-    if (e == cudaSuccess) e = fs::launch_walk(a, d.sms, d.order_bps, d.erode_bps[a.nmode], s);
+    if (e == cudaSuccess) e = fs::launch_walk(a, d.sms, d.order_bps, d.accum_bps, d.erode_bps[a.nmode], s);
     if (e != cudaSuccess) return cuda_fail(e, "timestep launch");
   }
   fs::Ctl h_ctl;

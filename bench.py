@@ -13,7 +13,8 @@ ordering, accumulation, uplift, erosion.
              host buffers: fs_set_elevation (pinned host -> device), fs_run(20)
              (21 timesteps, the reference's run semantics) and
              fs_get_elevation (device -> pinned host), all inside the timed
-             region.
+             region (host clock; the median of --e2e-calls calls after one
+             warm-up call).
   roofline   the dominant kernel's algorithmic bytes per launch / its mean
              launch time (CUDA events), against the measured HBM copy peak.
   cpu_baseline  the oracle's fastscape_RB+P restatement (OpenMP on every host
@@ -52,10 +53,12 @@ RUN_NSTEP = 20            # run(20) executes 21 timesteps
 ALG_BYTES = {
     "receivers": 8 + 1,                     # h read, rec write
     "donors_level0": 1 + 1,                 # rec read, mask write (+ pit list)
-    "order": (4 + 1 + 4 + 1 + 4 + 4) + (4 + 4 + 4),
-    # k_order -- ordering: entry read, mask read, entry + direction +
-    # receiver-position write, unit count write; accumulation: own count
-    # and receiver position read, reduction into the receiver's count
+    "order": 4 + 1 + 4 + 1 + 4 + 4,
+    # k_order: entry read, mask read, entry + direction + receiver-position
+    # write, unit count write
+    "accum": 4 + 4 + 4,
+    # k_accum: own count and receiver position read, reduction into the
+    # receiver's count
     "erode": 4 + 1 + 4 + 8 + 8,
     # k_erode: entry, direction, count, h read, h write
 }
@@ -344,8 +347,8 @@ def run_ensemble(args, dist, rank, ws, local):
     if rank == 0:
         peak, peak_kind = load_peaks()
         kern = {"receivers": t[0] / 2, "donors_level0": t[1] / 2, "order": t[7] / 2,
-                "erode": t[8] / 2}
-        dom = max(("order", "erode"), key=kern.get)
+                "accum": t[9] / 2, "erode": t[8] / 2}
+        dom = max(("order", "accum", "erode"), key=kern.get)
         achieved = ALG_BYTES[dom] * cells / (kern[dom] * 1e-3) / 1e9
         print(json.dumps({
             "metric": f"ensemble realizations/s ({nsteps}-timestep runs)", "value": value,
@@ -363,7 +366,7 @@ def run_ensemble(args, dist, rank, ws, local):
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "alg_bytes_per_cell": ALG_BYTES[dom],
                          "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": kern},
-            "gpu_launches": 5 * nsteps,
+            "gpu_launches": 6 * nsteps,
             "clocks": clk.summary(),
         }), flush=True)
     if dist is not None:
@@ -411,7 +414,8 @@ def run_sweep(args, dist, rank, ws, local):
                "run_wall_s": wall,
                "run_cell_steps_per_s": ws * side * side * nstep / wall,
                "kernel_ms": {"receivers": t[0] / nstep, "donors_level0": t[1] / nstep,
-                             "order": t[7] / nstep, "erode": t[8] / nstep}}
+                             "order": t[7] / nstep, "accum": t[9] / nstep,
+                             "erode": t[8] / nstep}}
         if rank == 0 and ws == 1 and not args.no_cpu_baseline and side <= 10000:
             nst = int(max(1, min(nstep, 4e7 / (side * side))))
             v, kind, thr, _ = cpu_sample(side, nst, prefer_reference=False)
@@ -441,7 +445,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--side", type=int, default=SIDE)
-    ap.add_argument("--e2e-calls", type=int, default=2)
+    ap.add_argument("--e2e-calls", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep"],
@@ -493,13 +497,14 @@ def main():
     total_ms = max_over_ranks(dist, float(t[3]))
     cells = side * side
     value = ws * cells * args.steps / (total_ms * 1e-3)
-    # receivers filter + fix-up, donors/level 0, ordering/accumulation,
-    # erosion: five launches a timestep
-    launches = 5 * args.steps
+    # receivers filter + fix-up, donors/level 0, ordering, accumulation,
+    # erosion: six launches a timestep
+    launches = 6 * args.steps
 
     # ---- roofline of the dominant kernel ----------------------------------
     peak, peak_kind = load_peaks()
-    kern = {"receivers": t[0], "donors_level0": t[1], "order": t[7], "erode": t[8]}
+    kern = {"receivers": t[0], "donors_level0": t[1], "order": t[7], "accum": t[9],
+            "erode": t[8]}
     dom = max(kern, key=kern.get)
     per_launch_ms = kern[dom] / args.steps
     achieved = ALG_BYTES[dom] * cells / (per_launch_ms * 1e-3) / 1e9
@@ -538,16 +543,19 @@ def main():
     dp = C.POINTER(C.c_double)
     hptr = hbuf.ctypes.data_as(dp)
     optr = obuf.ctypes.data_as(dp)
-    pkg.check(lib.fs_set_elevation(m.handle, hptr))
-    pkg.check(lib.fs_run(m.handle, RUN_NSTEP))   # warm-up of the e2e path
-    barrier(dist)
-    t0 = time.perf_counter()
+    pkg.check(lib.fs_set_elevation(m.handle, hptr))   # warm-up of the e2e path
+    pkg.check(lib.fs_run(m.handle, RUN_NSTEP))
+    pkg.check(lib.fs_get_elevation(m.handle, optr))
+    call_s = []
     for _ in range(args.e2e_calls):
+        barrier(dist)
+        t0 = time.perf_counter()
         pkg.check(lib.fs_set_elevation(m.handle, hptr))
         pkg.check(lib.fs_run(m.handle, RUN_NSTEP))
         pkg.check(lib.fs_get_elevation(m.handle, optr))
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e_value = ws * cells * (RUN_NSTEP + 1) * args.e2e_calls / e2e_s
+        call_s.append(max_over_ranks(dist, time.perf_counter() - t0))
+    e2e_s = statistics.median(call_s)   # one call; host-side jitter is not the library's
+    e2e_value = ws * cells * (RUN_NSTEP + 1) / e2e_s
     checksum = float(np.sum(obuf))
     m.close()
 
@@ -576,7 +584,8 @@ def main():
                               "achieved_gbs": step_rf, "frac": step_rf / peak},
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": 8 * cells, "d2h_bytes_per_step": 8 * cells,
-                    "calls": args.e2e_calls, "checksum": checksum},
+                    "calls": args.e2e_calls, "call_ms": [1e3 * x for x in call_s],
+                    "statistic": "median call", "checksum": checksum},
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,

@@ -160,8 +160,8 @@ int64_t fs_steps_executed(const fs_model *m);
  *   its kernels), 3 whole timed calls (first event to last),
  *   4..6 split of the level walk measured inside it by the GPU clock
  *        (ordering, accumulation, uplift+erosion),
- *   7 ordering/accumulation kernel, 8 erosion kernel (events). */
-#define FS_NUM_TIMERS 9
+ *   7 ordering kernel, 8 erosion kernel, 9 accumulation kernel (events). */
+#define FS_NUM_TIMERS 10
 int fs_set_timing(fs_model *m, int enable);
 int fs_get_phase_times(const fs_model *m, double *ms, int reset);
 

@@ -212,7 +212,7 @@ def test_timing_counters(pkg):
         t = m.phase_times(reset=True)
         assert np.all(t > 0)
         assert t[3] >= t[0] + t[1] + t[2] * 0.99
-        assert t[2] == pytest.approx(t[7] + t[8], rel=1e-9)   # the two walk kernels
+        assert t[2] == pytest.approx(t[7] + t[8] + t[9], rel=1e-9)  # the walk's kernels
         assert np.all(m.phase_times() == 0)
 
 
