@@ -961,9 +961,37 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
       }
 #pragma unroll
       for (int u = 0; u < kAccU; u++) {
+        if (!SINGLE) {  // batches: one reduction per donor (measured faster there)
+          if (ok[u]) {
+            const RealDesc &d = desc(rr[u]);
+            atomicAdd(&a.acc[d.off + pp[u]], v[u]);
+            if (a.do_erode && v[u] >= (uint32_t)d.tab_cap) {
+              if (atomicMax(&ctl->abort_k, (int)v[u]) < (int)v[u]) ctl->abort_r = rr[u];
+            }
+          }
+          continue;
+        }
+        // Donors of one receiver are consecutive: sum each run of equal
+        // receiver positions in the group (a warp scan minus its value
+        // before the run) and let the run's last lane reduce it into the
+        // receiver -- one reduction per receiver and group instead of one
+        // per donor. Lanes past the level keep runs of their own.
+        const int p = ok[u] ? pp[u] : -1 - lane;
+        const int pu = __shfl_up_sync(kFull, p, 1), pd = __shfl_down_sync(kFull, p, 1);
+        const bool head = lane == 0 || pu != p, tail = lane == 31 || pd != p;
+        const unsigned heads = __ballot_sync(kFull, head) & (0xFFFFFFFFu >> (31 - lane));
+        const int hl = 31 - __clz(heads);  // first lane of this lane's run
+        uint32_t S = v[u];
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+          const uint32_t x = __shfl_up_sync(kFull, S, dd);
+          if (lane >= dd) S += x;
+        }
+        const uint32_t before = __shfl_sync(kFull, S, (hl + 31) & 31);
+        const uint32_t run = S - (hl > 0 ? before : 0u);
         if (ok[u]) {
           const RealDesc &d = desc(rr[u]);
-          atomicAdd(&a.acc[d.off + pp[u]], v[u]);
+          if (tail) atomicAdd(&a.acc[d.off + p], run);
           if (a.do_erode && v[u] >= (uint32_t)d.tab_cap) {
             if (atomicMax(&ctl->abort_k, (int)v[u]) < (int)v[u]) ctl->abort_r = rr[u];
           }
