@@ -139,3 +139,34 @@ def test_large_and_small_mixed(pkg):
         for m in singles:
             m.step(3)
         compare_with_singles(pkg, b, ws, hs, ps, singles, "mixed")
+
+
+def test_batch_table_growth_in_one_realization(pkg):
+    """A realization whose drainage counts outgrow its erosion table (a
+    valley draining ~W*H cells to one outlet) stops the whole batch's
+    timestep before any elevation changes; the host grows that table and
+    redoes it. Every realization must still match its single model."""
+    W, H = 420, 400
+    yy, xx = np.divmod(np.arange(W * H), W)
+    hv = 1.0 + 0.5 * np.abs(xx - W // 2) + 0.05 * yy
+    hv[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    ws0, hs0, ps0 = ensemble(4, 11, smin=20, smax=200)
+    ws, hs = [ws0[0], W, ws0[1], ws0[2]], [hs0[0], H, hs0[1], hs0[2]]
+    p = pkg.workload_params()
+    ps = [ps0[0], p, ps0[1], ps0[2]]
+    with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[3, 0, 4, 5]) as b:
+        b.setH(1, hv)
+        singles = []
+        for r in range(4):
+            m = pkg.FastScape_RBP(ws[r], hs[r], params=ps[r], init=pkg.INIT_PHILOX,
+                                  seed=[3, 0, 4, 5][r])
+            if r == 1:
+                m.setH(hv)
+            singles.append(m)
+        b.step(3)
+        for m in singles:
+            m.step(3)
+        compare_with_singles(pkg, b, ws, hs, ps, singles, "valley")
+        assert b.accumulation(1).max() / p.cell_area > 65536
+        for m in singles:
+            m.close()
