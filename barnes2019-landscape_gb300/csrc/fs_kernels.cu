@@ -549,28 +549,33 @@ __device__ __forceinline__ double div_rn(double num, double D, double R) {
   return num / D;
 }
 
-// -RN(num/D) on bit patterns, given D > 0, R = RN(1/D) and Rn = -R: the
-// div_rn sequence with every quotient carried negated (RN is symmetric, so
-// q0n = RN(num*Rn) = -q0 and q1n = RN(r0*Rn + q0n) = -q1 exactly), which
-// puts the negations into the operands instead of separate instructions.
-// The caller adds the result to h0 directly. The IEEE division fallback is
-// volatile PTX in a branch; the numerator and result stay in integer
-// registers.
-__device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double R,
-                                                    double Rn) {
+// -RN(num/D) on bit patterns, given D >= 1 and Rn = -R, R = RN(1/D), in
+// three FP64 operations. q0 = RN(num*R) and r0 = num - q0*D by a fused
+// multiply-add; when q0 is not a power of two, its exponent is far from the
+// range limits and |r0| < D*ulp(q0), q0 lies within one ulp of num/D, r0 is
+// exact, and by Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1),
+// 1990) q1 = RN(q0 + r0*R) is the correctly rounded quotient
+// (tests/native/division_check.cpp replays this on the host against the
+// IEEE division, near rounding midpoints included). (A q0 more
+// than an ulp away makes |num - q0*D| >= D*ulp(q0), which its rounding
+// keeps, so the test is never passed wrongly.) Every quotient is carried
+// negated -- RN is symmetric; q0n = RN(num*Rn) = -q0 -- which puts the
+// negations into the operands; the caller adds the result to h0. Anything
+// else takes the IEEE division, volatile PTX in a branch; the numerator and
+// result stay in integer registers.
+__device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double Rn) {
   const double num = __longlong_as_double(numb);
   const double q0n = num * Rn;
   const double r0 = fma(q0n, D, num);
-  const double q1n = fma(r0, Rn, q0n);
-  const double r1 = fma(q1n, D, num);
   // Magnitudes are compared with the sign shifted out (x << 1) rather than
   // masked: the compiler turns a sign mask of a double into an FP64
   // absolute value.
-  const uint64_t q1b = (uint64_t)__double_as_longlong(q1n);
-  const int e = (int)((q1b << 1) >> 53);
-  if (e >= 64 && e <= 1980 && (q1b << 12) != 0) {
-    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1076) << 52));
-    if (((uint64_t)__double_as_longlong(r1) << 1) < (thr << 1)) return q1b;
+  const uint64_t q0b = (uint64_t)__double_as_longlong(q0n);
+  const int e = (int)((q0b << 1) >> 53);
+  if (e >= 64 && e <= 1980 && (q0b << 12) != 0) {
+    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1075) << 52));
+    if (((uint64_t)__double_as_longlong(r0) << 1) < (thr << 1))
+      return (uint64_t)__double_as_longlong(fma(r0, Rn, q0n));
   }
   uint64_t r;
   asm volatile(
@@ -609,7 +614,7 @@ __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
   const uint64_t factb = Tb[0];
   const double D = __longlong_as_double(Tb[1]), R = __longlong_as_double(Tb[2]);
   const uint64_t num = fmul_bits(factb, fadd_bits(h0, hn ^ kSignBit));
-  const uint64_t qn = neg_div_rn_bits(num, D, R, __longlong_as_double(Tb[3]));  // -q
+  const uint64_t qn = neg_div_rn_bits(num, D, __longlong_as_double(Tb[3]));  // -q
   const uint64_t hnew = fadd_bits(h0, qn);
   // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
   // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on

@@ -62,10 +62,10 @@ ALG_BYTES = {
     "erode": 4 + 1 + 4 + 8 + 8,
     # k_erode: entry, direction, count, h read, h write
 }
-# k_erode is bound by the FP64 pipe: 8 FP64 operations per eroded cell
-# (uplift, h0 - hn, fact*dh, four for the division, h0 - q). Peak measured
+# k_erode is bound by the FP64 pipe: 7 FP64 operations per eroded cell
+# (uplift, h0 - hn, fact*dh, three for the division, h0 - q). Peak measured
 # here with a probe kernel: 1.59 FP64 lanes/clock/SM x 152 SMs x 2.07 GHz.
-ERODE_FP64_PER_CELL = 8
+ERODE_FP64_PER_CELL = 7
 FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12
 STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
 
@@ -445,7 +445,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--side", type=int, default=SIDE)
-    ap.add_argument("--e2e-calls", type=int, default=3)
+    ap.add_argument("--e2e-calls", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep"],

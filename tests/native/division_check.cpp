@@ -1,0 +1,77 @@
+// Host restatement of the erosion kernel's quotient (neg_div_rn_bits in
+// fs_kernels.cu): q0 = RN(num * R) with R = RN(1/D), r0 = num - q0*D by a
+// fused multiply-add, q1 = RN(q0 + r0*R), accepted when q0 is not a power of
+// two, its exponent is far from the range limits and |r0| < D*ulp(q0) --
+// then q0 is within one ulp of num/D, r0 is exact, and by Markstein's theorem
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990) q1 = RN(num/D). The check
+// compares every accepted q1 with the IEEE quotient on random operands and
+// on operands built next to rounding midpoints (num = RN(D * midpoint)),
+// D of all significand shapes, and reports the acceptance rate.
+// Usage: division_check <cases> <seed>; exit 1 on the first mismatch.
+#include <cinttypes>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+
+static double dbl(uint64_t u) { double d; std::memcpy(&d, &u, 8); return d; }
+static uint64_t bits(double d) { uint64_t u; std::memcpy(&u, &d, 8); return u; }
+
+// Returns true and *q = RN(num/D) when the fast path accepts.
+static bool fast_quotient(double num, double D, double R, double *q) {
+  const double Rn = -R;
+  const double q0n = num * Rn;
+  const double r0 = std::fma(q0n, D, num);
+  const uint64_t q0b = bits(q0n);
+  const int e = (int)((q0b << 1) >> 53);
+  if (e >= 64 && e <= 1980 && (q0b << 12) != 0) {
+    const uint64_t thr = (uint64_t)((int64_t)bits(D) + ((int64_t)(e - 1075) << 52));
+    if ((bits(r0) << 1) < (thr << 1)) {
+      *q = -std::fma(r0, Rn, q0n);
+      return true;
+    }
+  }
+  return false;
+}
+
+int main(int argc, char **argv) {
+  const long n = argc > 1 ? std::atol(argv[1]) : 10000000;
+  std::mt19937_64 g(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
+  long accepted = 0;
+  for (long i = 0; i < n; i++) {
+    // D = 1 + F, F from tiny to huge; significands of every shape
+    double D;
+    switch (i % 4) {
+      case 0: D = 1.0 + std::ldexp((double)(g() >> 11), -53 + (int)(g() % 80) - 40); break;
+      case 1: D = dbl((uint64_t)(1023 + g() % 40) << 52 | (g() & ((1ull << 52) - 1))); break;
+      case 2: D = dbl((uint64_t)(1023 + g() % 40) << 52 | (((1ull << 52) - 1) ^ ((1ull << (g() % 52)) - 1))); break;
+      default: D = dbl((uint64_t)(1023 + g() % 40) << 52 | ((1ull << (g() % 52)) | (g() & 0xFF))); break;
+    }
+    if (!(D >= 1.0) || !std::isfinite(D)) continue;
+    const double R = 1.0 / D;
+    double num;
+    if (i & 1) {
+      // next to a midpoint: num = RN(D * (m + ulp(m)/2)), m a double
+      const double m = dbl((uint64_t)(1023 + (int)(g() % 200) - 100) << 52 | (g() & ((1ull << 52) - 1)));
+      int e; std::frexp(m, &e);
+      num = std::fma(D, m, D * std::ldexp(1.0, e - 54));
+      if (i % 3 == 0) num = dbl(bits(num) + (int)(g() % 5) - 2);
+    } else {
+      num = dbl((uint64_t)(1023 + (int)(g() % 400) - 200) << 52 | (g() & ((1ull << 52) - 1)));
+    }
+    if (g() & 1) num = -num;
+    double q;
+    if (fast_quotient(num, D, R, &q)) {
+      accepted++;
+      const double ex = num / D;
+      if (bits(q) != bits(ex)) {
+        std::printf("MISMATCH num=%a D=%a fast=%a ieee=%a\n", num, D, q, ex);
+        return 1;
+      }
+    }
+  }
+  std::printf("%ld cases, %ld accepted by the fast path, all equal to the IEEE quotient\n", n,
+              accepted);
+  return 0;
+}
