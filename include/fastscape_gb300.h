@@ -240,7 +240,7 @@ int fs_batch_synchronize(const fs_batch *b);
  * may not allocate device memory while running (a host application that
  * owns all device memory through its own pool, a latency-critical loop where
  * cudaMalloc/cudaFree would synchronize the device, a plugin with a fixed
- * footprint). All scratch (~25 MB) is one static device array in the
+ * footprint). All scratch (~24 MB) is one static device array in the
  * library, held on every GPU that loads it until the process exits, shared
  * by all calls and keeping the last call's contents: calls that overlap on
  * the GPU race and must be serialized by the caller. Grids larger than
