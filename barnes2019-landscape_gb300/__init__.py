@@ -46,6 +46,7 @@ ABI_SYMBOLS = [
     "fs_batch_get_elevation", "fs_batch_set_elevation", "fs_batch_get_accumulation",
     "fs_batch_get_receivers", "fs_batch_get_levels", "fs_batch_get_stack_dfs", "fs_batch_info",
     "fs_batch_set_timing", "fs_batch_get_phase_times", "fs_batch_use_graph",
+    "fs_batch_use_int_sub", "fs_use_int_sub",
     "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
     "fs_autotune", "fs_launch_config",
     "fs_step_noalloc",
@@ -144,10 +145,12 @@ def library() -> C.CDLL:
     L.fs_batch_set_timing.argtypes = [vp, C.c_int]
     L.fs_batch_get_phase_times.argtypes = [vp, dp, C.c_int]
     L.fs_batch_use_graph.argtypes = [vp, C.c_int]
+    L.fs_batch_use_int_sub.argtypes = [vp, C.c_int]
+    L.fs_use_int_sub.argtypes = [vp, C.c_int]
     L.fs_batch_autotune.argtypes = [vp, C.c_int, ip]
-    L.fs_batch_launch_config.argtypes = [vp, ip, ip, ip]
+    L.fs_batch_launch_config.argtypes = [vp, ip, ip, ip, ip]
     L.fs_autotune.argtypes = [vp, C.c_int, ip]
-    L.fs_launch_config.argtypes = [vp, ip, ip, ip]
+    L.fs_launch_config.argtypes = [vp, ip, ip, ip, ip]
     L.fs_batch_synchronize.argtypes = [vp]
     L.fs_step_noalloc.argtypes = [vp, C.c_int, C.c_int, pp, C.c_int, vp]
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
@@ -294,11 +297,17 @@ class FastScape_RBP:
         check(library().fs_autotune(self._m, int(probe_steps), out))
         return self.launch_config()
 
+    def use_int_sub(self, on: bool = True) -> None:
+        """n = 1: the erosion's elevation subtractions in integer arithmetic
+        (same results; fs_autotune chooses by speed)."""
+        check(library().fs_use_int_sub(self._m, int(bool(on))))
+
     def launch_config(self):
-        o, e, g = C.c_int(), C.c_int(), C.c_int()
-        check(library().fs_launch_config(self._m, C.byref(o), C.byref(e), C.byref(g)))
+        o, e, g, i = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(library().fs_launch_config(self._m, C.byref(o), C.byref(e), C.byref(g),
+                                         C.byref(i)))
         return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
-                "graph": bool(g.value)}
+                "graph": bool(g.value), "erode_int_sub": bool(i.value)}
 
     def set_barrier_timeout(self, ms: float) -> None:
         check(library().fs_set_barrier_timeout(self._m, float(ms)))
@@ -412,6 +421,9 @@ class FastScapeBatch:
     def use_graph(self, on: bool = True) -> None:
         check(library().fs_batch_use_graph(self._b, int(bool(on))))
 
+    def use_int_sub(self, on: bool = True) -> None:
+        check(library().fs_batch_use_int_sub(self._b, int(bool(on))))
+
     def autotune(self, probe_steps: int = 2):
         """Picks the fastest launch configuration; returns it."""
         out = (C.c_int * 2)()
@@ -419,10 +431,11 @@ class FastScapeBatch:
         return self.launch_config()
 
     def launch_config(self):
-        o, e, g = C.c_int(), C.c_int(), C.c_int()
-        check(library().fs_batch_launch_config(self._b, C.byref(o), C.byref(e), C.byref(g)))
+        o, e, g, i = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(library().fs_batch_launch_config(self._b, C.byref(o), C.byref(e), C.byref(g),
+                                               C.byref(i)))
         return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
-                "graph": bool(g.value)}
+                "graph": bool(g.value), "erode_int_sub": bool(i.value)}
 
     def synchronize(self) -> None:
         check(library().fs_batch_synchronize(self._b))

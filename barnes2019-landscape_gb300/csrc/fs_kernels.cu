@@ -28,6 +28,7 @@
 #include <cstdint>
 
 #include "fastscape_gb300.h"
+#include "fs_bits.h"
 #include "fs_internal.h"
 
 namespace fs {
@@ -198,6 +199,51 @@ __device__ __forceinline__ uint64_t fmul_bits(uint64_t a, uint64_t b) {
 }
 
 constexpr uint64_t kSignBit = 0x8000000000000000ull;
+
+// FP64 addition in a branch taken by few cells: volatile, so that the
+// compiler does not execute it speculatively for the others.
+__device__ __forceinline__ uint64_t fadd_bits_volatile(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm volatile(
+      "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "add.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+
+// The erosion's FP64 pipe is its bottleneck while its integer pipes idle, so
+// some of its additions run in integer arithmetic (fs_bits.h, each
+// bit-identical to the hardware's RN operation on the operands it accepts;
+// the rest take the FP64 addition).
+//
+// The uplift h + U*dt of an eroded cell: two positive normal operands (every
+// cell of a landscape above base level). Off the cell's critical path (it
+// does not wait for the receiver's elevation), so always worth it.
+__device__ __forceinline__ uint64_t uplift_bits(uint64_t h, uint64_t udt) {
+  if (add_pos_operand(h) && add_pos_operand(udt)) return add_pos_rn_bits(h, udt);
+  return fadd_bits_volatile(h, udt);
+}
+
+// RN(x - y) of a cell's and its receiver's elevation: the exact integer
+// difference when y >= x/2 (sub_near_bits), else in FP64.
+__device__ __forceinline__ uint64_t sub_near(uint64_t x, uint64_t y) {
+  if (add_pos_operand(x) && add_pos_operand(y) && x > y) {
+    const uint64_t r = sub_near_bits(x, y);
+    if (r) return r;
+  }
+  return fadd_bits_volatile(x, y ^ kSignBit);
+}
+
+// RN(x - y) of an elevation and its erosion: in integer arithmetic when y's
+// exponent is at least 2 below x's (sub_far_bits), else in FP64.
+__device__ __forceinline__ uint64_t sub_far(uint64_t x, uint64_t y) {
+  if (add_pos_operand(x) && add_pos_operand(y)) {
+    const uint64_t r = sub_far_bits(x, y);
+    if (r) return r;
+  }
+  return fadd_bits_volatile(x, y ^ kSignBit);
+}
 
 // ---------------------------------------------------------------------------
 // 1. Receivers: fastscape_RB.cpp:160-182. slope = (h[c]-h[n])/dr[n], strict
@@ -607,15 +653,21 @@ __device__ __forceinline__ void powers(double x, double neq, double &pn, double 
 // (fact, D = 1 + fact, R = 1/D).
 //
 // First iterate: hnew - h0 = +0, pow(x,1) = x and pow(x,0) = 1, so
-// hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)).
+// hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)). With ISUB the two
+// subtractions run in integer arithmetic: that relieves the FP64 pipe but
+// lengthens the cell's dependency chain after the receiver's elevation
+// arrives, which pays where the pipe, not latency, limits the erosion (the
+// autotuner decides per workload).
+template <bool ISUB>
 __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
                                                   const unsigned long long *Tb, uint64_t h0,
                                                   uint64_t hn) {
   const uint64_t factb = Tb[0];
   const double D = __longlong_as_double(Tb[1]), R = __longlong_as_double(Tb[2]);
-  const uint64_t num = fmul_bits(factb, fadd_bits(h0, hn ^ kSignBit));
+  const uint64_t dh = ISUB ? sub_near(h0, hn) : fadd_bits(h0, hn ^ kSignBit);
+  const uint64_t num = fmul_bits(factb, dh);
   const uint64_t qn = neg_div_rn_bits(num, D, __longlong_as_double(Tb[3]));  // -q
-  const uint64_t hnew = fadd_bits(h0, qn);
+  const uint64_t hnew = ISUB ? sub_far(h0, qn ^ kSignBit) : fadd_bits(h0, qn);
   // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
   // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
   // truncated magnitudes (each within 2^-23 relative, flushed below
@@ -1032,7 +1084,7 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
 // counts (and uplifted the pits). A kernel of its own: the ordering and
 // accumulation run with more resident threads than the register-hungry FP64
 // erosion allows.
-template <int NMODE, bool SINGLE>
+template <int NMODE, bool SINGLE, bool ISUB>
 __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   extern __shared__ int smem[];
   const int nreal = a.nreal;
@@ -1136,11 +1188,12 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
           const size_t rec_at = (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
           const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
           const uint64_t hr = hn[u];
-          const uint64_t h0 = fadd_bits(hc[u], udt);
+          const uint64_t h0 = uplift_bits(hc[u], udt);
           uint64_t hnew;
           if (NMODE == kNOne) {
-            hnew = erode_cell_n1(d, ctl, reinterpret_cast<const unsigned long long *>(d.tab) + rec_at,
-                                 h0, hr);
+            hnew = erode_cell_n1<ISUB>(d, ctl,
+                                       reinterpret_cast<const unsigned long long *>(d.tab) + rec_at,
+                                       h0, hr);
           } else {
             hnew = (uint64_t)__double_as_longlong(erode_cell<NMODE>(d, a.neq, ctl, d.tab + rec_at,
                                                   __longlong_as_double(h0), __longlong_as_double(hr)));
@@ -1358,15 +1411,19 @@ size_t walk_smem_bytes(int nreal) { return sizeof(int) * (4 * (size_t)nreal + 1)
 
 int walk_threads() { return kWalkThreads; }
 
-const void *walk_kernel_ptr(int nmode, bool single) {
+const void *walk_kernel_ptr(int nmode, bool single, bool isub) {
   if (single) {
-    if (nmode == kNOne) return reinterpret_cast<const void *>(&k_erode<kNOne, true>);
-    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, true>);
-    return reinterpret_cast<const void *>(&k_erode<kNGeneral, true>);
+    if (nmode == kNOne)
+      return isub ? reinterpret_cast<const void *>(&k_erode<kNOne, true, true>)
+                  : reinterpret_cast<const void *>(&k_erode<kNOne, true, false>);
+    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, true, false>);
+    return reinterpret_cast<const void *>(&k_erode<kNGeneral, true, false>);
   }
-  if (nmode == kNOne) return reinterpret_cast<const void *>(&k_erode<kNOne, false>);
-  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, false>);
-  return reinterpret_cast<const void *>(&k_erode<kNGeneral, false>);
+  if (nmode == kNOne)
+    return isub ? reinterpret_cast<const void *>(&k_erode<kNOne, false, true>)
+                : reinterpret_cast<const void *>(&k_erode<kNOne, false, false>);
+  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, false, false>);
+  return reinterpret_cast<const void *>(&k_erode<kNGeneral, false, false>);
 }
 
 const void *order_kernel_ptr(bool single, int bps) {
@@ -1386,9 +1443,11 @@ cudaError_t prepare_walk_kernels() {
   const int bytes = (int)walk_smem_bytes(kMaxReal);
   for (int single = 0; single < 2; single++) {
     for (int nm = 0; nm < 3; nm++) {
-      cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0),
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-      if (e != cudaSuccess) return e;
+      for (int isub = 0; isub < 2; isub++) {
+        cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0, isub != 0),
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+      }
     }
     for (int bps = 2; bps <= 3; bps++) {
       cudaError_t e = cudaFuncSetAttribute(order_kernel_ptr(single != 0, bps),
@@ -1481,7 +1540,8 @@ cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s) {
 cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
-  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1), dim3(sms * bps),
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1, a.erode_isub != 0),
+                                     dim3(sms * bps),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }
 

@@ -123,6 +123,7 @@ struct fs_batch {
   int walk_occ = 1, walk_sms = 1, walk_bps = 2;  // k_erode blocks per SM: limit, SMs, in use
   int order_max = 2, order_bps = 2;              // k_order blocks per SM: limit (2 or 3), in use
   int accum_bps = 1;                             // k_accum blocks per SM
+  int erode_isub = 0;                            // k_erode's integer subtractions (n = 1)
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
@@ -256,6 +257,7 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.nmode = b->nmode;
   a.neq = b->neq;
   a.do_erode = do_erode;
+  a.erode_isub = b->erode_isub;
   a.stamp = b->timing ? 1 : 0;
   a.timeout_ns = b->timeout_ns;
   return a;
@@ -788,10 +790,11 @@ int get_phase_times(const fs_batch *b, double *ms, int reset) {
   return FS_OK;
 }
 
-// Autotuner: times each candidate launch configuration -- walk blocks per SM
-// (1 .. occupancy limit, at most 2) with and without the captured graph --
-// on the batch's own state over `probe` timesteps, restoring the elevation
-// after every probe, and keeps the fastest.
+// Autotuner: times each candidate launch configuration -- ordering and
+// erosion blocks per SM with and without the captured graph, then for n = 1
+// the fastest of these with the erosion's integer subtractions -- on the
+// batch's own state over `probe` timesteps, restoring the elevation after
+// every probe, and keeps the fastest.
 int autotune(fs_batch *b, int probe, int *chosen) {
   DeviceGuard dg(b->device);
   double *save = nullptr;
@@ -810,32 +813,48 @@ int autotune(fs_batch *b, int probe, int *chosen) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int best_bps = b->walk_bps, best_obps = b->order_bps;
+  int best_bps = b->walk_bps, best_obps = b->order_bps, best_isub = 0;
   bool best_graph = false;
   int st = FS_OK;
+  // One probe: a warm-up timestep (which also builds the graph), then
+  // `probe` timed ones; the elevation is restored afterwards.
+  auto time_config = [&](int obps, int bps, bool graph, int isub, float *ms) -> int {
+    b->order_bps = obps;
+    b->walk_bps = bps;
+    b->use_graph = graph;
+    b->erode_isub = isub;
+    b->graph_dirty = true;
+    int r = batch_step(b, 1);
+    if (r == FS_OK) {
+      cudaEventRecord(e0, b->stream);
+      r = batch_step(b, probe);
+      cudaEventRecord(e1, b->stream);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(ms, e0, e1);
+    }
+    cudaMemcpyAsync(b->h, save, b->cells * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+    return r;
+  };
   for (int obps = 2; obps <= b->order_max && st == FS_OK; obps++) {
     for (int bps = 1; bps <= std::min(b->walk_occ, 2) && st == FS_OK; bps++) {
       for (int gr = 0; gr < 2 && st == FS_OK; gr++) {
-        b->order_bps = obps;
-        b->walk_bps = bps;
-        b->use_graph = gr == 1;
-        b->graph_dirty = true;
-        if ((st = batch_step(b, 1)) != FS_OK) break;  // warm (and build the graph)
-        cudaEventRecord(e0, b->stream);
-        if ((st = batch_step(b, probe)) != FS_OK) break;
-        cudaEventRecord(e1, b->stream);
-        cudaEventSynchronize(e1);
         float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
+        if ((st = time_config(obps, bps, gr == 1, 0, &ms)) != FS_OK) break;
         if (ms < best) {
           best = ms;
           best_bps = bps;
           best_obps = obps;
           best_graph = gr == 1 && b->use_graph;
         }
-        cudaMemcpyAsync(b->h, save, b->cells * sizeof(double), cudaMemcpyDeviceToDevice,
-                        b->stream);
       }
+    }
+  }
+  if (st == FS_OK && b->nmode == fs::kNOne) {
+    float ms = 0;
+    st = time_config(best_obps, best_bps, best_graph, 1, &ms);
+    if (st == FS_OK && ms < best) {
+      best = ms;
+      best_isub = 1;
     }
   }
   cudaEventDestroy(e0);
@@ -847,6 +866,7 @@ int autotune(fs_batch *b, int probe, int *chosen) {
   b->walk_bps = best_bps;
   b->order_bps = best_obps;
   b->use_graph = best_graph;
+  b->erode_isub = best_isub;
   b->graph_dirty = true;
   if (chosen) {
     chosen[0] = best_bps;
@@ -1108,6 +1128,13 @@ int fs_batch_use_graph(fs_batch *b, int enable) {
   return FS_OK;
 }
 
+int fs_batch_use_int_sub(fs_batch *b, int enable) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  b->erode_isub = enable != 0 && b->nmode == fs::kNOne ? 1 : 0;
+  b->graph_dirty = true;
+  return FS_OK;
+}
+
 int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
   if (probe_steps < 1 || probe_steps > 100)
@@ -1115,11 +1142,13 @@ int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen) {
   return autotune(b, probe_steps, chosen);
 }
 
-int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps, int *graph) {
+int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps, int *graph,
+                           int *erode_int_sub) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
   if (order_bps) *order_bps = b->order_bps;
   if (erode_bps) *erode_bps = b->walk_bps;
   if (graph) *graph = b->use_graph ? 1 : 0;
+  if (erode_int_sub) *erode_int_sub = b->erode_isub;
   return FS_OK;
 }
 
@@ -1128,9 +1157,15 @@ int fs_autotune(fs_model *m, int probe_steps, int *chosen) {
   return fs_batch_autotune(m->b, probe_steps, chosen);
 }
 
-int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *graph) {
+int fs_use_int_sub(fs_model *m, int enable) {
   FS_MODEL(m);
-  return fs_batch_launch_config(m->b, order_bps, erode_bps, graph);
+  return fs_batch_use_int_sub(m->b, enable);
+}
+
+int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *graph,
+                     int *erode_int_sub) {
+  FS_MODEL(m);
+  return fs_batch_launch_config(m->b, order_bps, erode_bps, graph, erode_int_sub);
 }
 
 int fs_batch_synchronize(const fs_batch *b) {

@@ -62,10 +62,15 @@ ALG_BYTES = {
     "erode": 4 + 1 + 4 + 8 + 8,
     # k_erode: entry, direction, count, h read, h write
 }
-# k_erode is bound by the FP64 pipe: 7 FP64 operations per eroded cell
-# (uplift, h0 - hn, fact*dh, three for the division, h0 - q). Peak measured
-# here with a probe kernel: 1.59 FP64 lanes/clock/SM x 152 SMs x 2.07 GHz.
-ERODE_FP64_PER_CELL = 7
+# k_erode leans on the FP64 pipe: per eroded cell fact*dh and the three
+# operations of the division, plus h0 - hn and h0 - q unless those run in
+# integer arithmetic (the autotuner's erode_int_sub); the uplift always runs
+# in integer arithmetic. Peak measured here with a probe kernel: 1.59 FP64
+# lanes/clock/SM x 152 SMs x 2.07 GHz.
+def erode_fp64_per_cell(int_sub: bool) -> int:
+    return 4 if int_sub else 6
+
+
 FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12
 STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
 
@@ -326,7 +331,7 @@ def run_ensemble(args, dist, rank, ws, local):
     b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX,
                            seeds=list(range(1000 * rank, 1000 * rank + len(sides))))
     cells = b.cells()
-    # warm-up: the autotuner's probe timesteps (8 launch configurations x 3),
+    # warm-up: the autotuner's probe timesteps (9 launch configurations x 3),
     # after which it restores the initial fields
     tune = b.autotune(probe_steps=2)
     warm = 8 * 3
@@ -519,10 +524,11 @@ def main():
     lid, _ = m.levels()
     eroded = int(np.count_nonzero(lid >= 1))
     del lid
-    erode_tf = ERODE_FP64_PER_CELL * eroded / (t[8] / args.steps * 1e-3) / 1e12
+    fp64_ops = erode_fp64_per_cell(bool(tune.get("erode_int_sub")))
+    erode_tf = fp64_ops * eroded / (t[8] / args.steps * 1e-3) / 1e12
     roofline["erode_fp64"] = {"bound": "fp64", "achieved": erode_tf, "peak": FP64_PEAK_TFLOPS,
                               "unit": "TFLOP/s", "frac": erode_tf / FP64_PEAK_TFLOPS,
-                              "ops_per_eroded_cell": ERODE_FP64_PER_CELL,
+                              "ops_per_eroded_cell": fp64_ops,
                               "eroded_cells": eroded,
                               "peak_source": "probe-kernel FP64 rate (no FP64 figure in "
                                              "MEASURED_PEAKS.json)"}

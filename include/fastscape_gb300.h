@@ -168,7 +168,9 @@ int fs_get_phase_times(const fs_model *m, double *ms, int reset);
 /* fs_batch_autotune / fs_batch_launch_config for a single model (a batch
  * of one). No reference counterpart: the reference has no launch shapes. */
 int fs_autotune(fs_model *m, int probe_steps, int *chosen);
-int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *graph);
+int fs_use_int_sub(fs_model *m, int enable);
+int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *graph,
+                     int *erode_int_sub);
 
 /* Limit (milliseconds) on every grid-wide barrier wait; default 2000. */
 int fs_set_barrier_timeout(fs_model *m, double ms);
@@ -217,16 +219,23 @@ int fs_batch_get_phase_times(const fs_batch *b, double *ms, int reset);
 /* Replays each timestep from a captured CUDA graph (1) or launches it
  * directly (0, default). */
 int fs_batch_use_graph(fs_batch *b, int enable);
-/* Times every launch configuration (blocks per SM of the two level-walk
- * kernels, graph or direct) over probe_steps timesteps of the batch's own
- * state, restores the state and keeps the fastest; chosen[0] = erosion
- * kernel blocks per SM, chosen[1] = graph (fs_batch_launch_config reports
- * all three choices). */
+/* With n = 1, the erosion subtracts elevations in integer arithmetic (1) or
+ * on the FP64 pipe (0, default); identical results, different speed
+ * (fs_batch_autotune picks). Ignored for n != 1. */
+int fs_batch_use_int_sub(fs_batch *b, int enable);
+/* Times every launch configuration (blocks per SM of the ordering and
+ * erosion kernels, graph or direct; for n = 1 then the best of these with
+ * the erosion's elevation subtractions in integer arithmetic) over
+ * probe_steps timesteps of the batch's own state, restores the state and
+ * keeps the fastest; chosen[0] = erosion kernel blocks per SM, chosen[1] =
+ * graph (fs_batch_launch_config reports every choice). Results do not depend
+ * on the configuration. */
 int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen);
-/* The launch configuration in use: blocks per SM of the ordering /
- * accumulation kernel and of the erosion kernel, graph replay (0/1). */
+/* The launch configuration in use: blocks per SM of the ordering kernel and
+ * of the erosion kernel, graph replay (0/1), integer subtractions in the
+ * erosion (0/1). Any pointer may be NULL. */
 int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps,
-                           int *graph);
+                           int *graph, int *erode_int_sub);
 int fs_batch_synchronize(const fs_batch *b);
 
 /* Largest grid (width*height cells) fs_step_noalloc accepts. */

@@ -38,12 +38,14 @@ def compare_with_singles(pkg, b, ws, hs, ps, singles, tag):
         assert np.array_equal(b.getH(r), m.getH()), f"{tag} h r={r}"
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_independent_models(pkg, graph):
+@pytest.mark.parametrize("graph,int_sub", [(False, False), (True, False), (True, True)])
+def test_batch_equals_independent_models(pkg, graph, int_sub):
     ws, hs, ps = ensemble(9, 11)
     seeds = list(range(100, 109))
     with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=seeds) as b:
         b.use_graph(graph)
+        b.use_int_sub(int_sub)
+        assert b.launch_config()["erode_int_sub"] == int_sub
         singles = [pkg.FastScape_RBP(w, h, params=p, init=pkg.INIT_PHILOX, seed=s)
                    for w, h, p, s in zip(ws, hs, ps, seeds)]
         for r in range(len(ws)):
@@ -57,9 +59,11 @@ def test_batch_equals_independent_models(pkg, graph):
             m.close()
 
 
-def test_batch_against_oracle(pkg, oracle):
+@pytest.mark.parametrize("int_sub", [False, True])
+def test_batch_against_oracle(pkg, oracle, int_sub):
     ws, hs, ps = ensemble(5, 3, smin=6, smax=90)
     with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[1, 2, 3, 4, 5]) as b:
+        b.use_int_sub(int_sub)
         hs0 = [b.getH(r) for r in range(len(ws))]
         b.step(6)
         for r in range(len(ws)):
@@ -89,6 +93,7 @@ def test_autotune_keeps_state(pkg):
         before = [a.getH(r) for r in range(6)]
         choice = a.autotune(probe_steps=2)
         assert choice["erode_blocks_per_sm"] in (1, 2)
+        assert choice["erode_int_sub"] in (False, True)
         assert choice["order_blocks_per_sm"] in (2, 3)
         for r in range(6):
             assert np.array_equal(a.getH(r), before[r])

@@ -112,6 +112,54 @@ def test_oracle_trajectory(pkg, oracle, W, H, steps, seed, n):
             assert_step_equal(m, W, H, ref, f"step {s}", exact_h=(n == 1))
 
 
+@pytest.mark.parametrize("W,H,steps,seed", [(64, 64, 10, 3), (333, 250, 6, 5)])
+def test_oracle_trajectory_integer_subtractions(pkg, oracle, W, H, steps, seed):
+    """The erosion with its elevation subtractions in integer arithmetic,
+    bit-identical to the oracle. The terrain mixes the cases each integer
+    path declines (negative and zero elevations, receivers below half the
+    cell's elevation, erosion close to the elevation itself) with ordinary
+    cells, so both the integer paths and their FP64 fallbacks run."""
+    rng = np.random.default_rng(seed)
+    p = pkg.workload_params()
+    op = Params(*p.as_tuple())
+    h = rng.uniform(0, 3, W * H)
+    kind = rng.integers(0, 6, W * H)
+    h[kind == 1] *= 1e-3                          # near zero: large relative drops
+    h[kind == 2] = -rng.uniform(0, 5, (kind == 2).sum())   # negative elevations
+    h[kind == 3] = 0.0
+    h[kind == 4] = rng.uniform(100, 3000, (kind == 4).sum())  # steep cliffs
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+        m.use_int_sub(True)
+        assert m.launch_config()["erode_int_sub"]
+        m.setH(h)
+        for s in range(steps):
+            m.step(1)
+            ref = oracle.phases(h, W, H, op)
+            assert_step_equal(m, W, H, ref, f"step {s}")
+
+
+def test_workload_1000_integer_subtractions(pkg, oracle):
+    """run(120) of the 1000x1000 workload with the integer subtractions:
+    bit-identical to the oracle, like the default erosion."""
+    W = 1000
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(W, W, params=p, init=pkg.INIT_REFERENCE) as m:
+        m.use_int_sub(True)
+        m.run(120)
+        got = m.getH()
+    h = oracle.terrain(W, W, 0)
+    oracle.run(h, W, W, Params(*p.as_tuple()), 120, parallel=True)
+    assert np.array_equal(got, h)
+
+
+def test_integer_subtractions_ignored_for_general_n(pkg):
+    with pkg.FastScape_RBP(64, 64, params=pkg.reference_params(), init=pkg.INIT_PHILOX) as m:
+        m.use_int_sub(True)
+        assert not m.launch_config()["erode_int_sub"]
+
+
 def test_reference_field_generator(pkg, oracle):
     for W, H in [(16, 16), (101, 37)]:
         with pkg.FastScape_RBP(W, H, init=pkg.INIT_REFERENCE, seed=123) as m:
