@@ -41,7 +41,6 @@ constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kPer = 8;   // entries per thread per expansion chunk
 constexpr int kChunk = kPer * kWalkThreads;
 constexpr int kAccU = 4;  // 32-entry groups per warp per accumulation pass
-constexpr int kEroU = 2;  // 32-entry groups per warp per erosion pass
 constexpr int kNewtonMaxIt = 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -658,15 +657,24 @@ __device__ __forceinline__ void powers(double x, double neq, double &pn, double 
 // lengthens the cell's dependency chain after the receiver's elevation
 // arrives, which pays where the pipe, not latency, limits the erosion (the
 // autotuner decides per workload).
+// The fields of a table record the n = 1 erosion reads up front.
+struct TabN1 {
+  uint64_t fact, D, Rn;
+};
+
+__device__ __forceinline__ TabN1 load_tab_n1(const unsigned long long *Tb) {
+  return TabN1{__ldg(Tb + 0), __ldg(Tb + 1), __ldg(Tb + 3)};
+}
+
 template <bool ISUB>
 __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
-                                                  const unsigned long long *Tb, uint64_t h0,
-                                                  uint64_t hn) {
-  const uint64_t factb = Tb[0];
-  const double D = __longlong_as_double(Tb[1]), R = __longlong_as_double(Tb[2]);
+                                                  const unsigned long long *Tb, TabN1 t,
+                                                  uint64_t h0, uint64_t hn) {
+  const uint64_t factb = t.fact;
+  const double D = __longlong_as_double(t.D);
   const uint64_t dh = ISUB ? sub_near(h0, hn) : fadd_bits(h0, hn ^ kSignBit);
   const uint64_t num = fmul_bits(factb, dh);
-  const uint64_t qn = neg_div_rn_bits(num, D, __longlong_as_double(Tb[3]));  // -q
+  const uint64_t qn = neg_div_rn_bits(num, D, __longlong_as_double(t.Rn));  // -q
   const uint64_t hnew = ISUB ? sub_far(h0, qn ^ kSignBit) : fadd_bits(h0, qn);
   // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
   // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
@@ -676,6 +684,7 @@ __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
   const float qf = fabsf(trunc_bits_to_float(qn));
   const float hf = fabsf(trunc_bits_to_float(h0));
   if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= d.tol_lo_f) return hnew;
+  const double R = __longlong_as_double(__ldg(Tb + 2));
   const double fact = __longlong_as_double(factb), h0d = __longlong_as_double(h0),
                hnd = __longlong_as_double(hn);
   double x = __longlong_as_double(hnew);
@@ -1139,69 +1148,75 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   // h is final).
   for (int Lv = 1; Lv < maxlev; ++Lv) {
     const int ngroups = level_groups(Lv);
-    for (int g0 = warp_global * kEroU; g0 < ngroups; g0 += nwarps * kEroU) {
-      int cc[kEroU], dd[kEroU], rr[kEroU];
-      uint32_t kk[kEroU];
-      bool ok[kEroU];
-#pragma unroll
-      for (int u = 0; u < kEroU; u++) {
-        const int g = g0 + u;
-        ok[u] = false;
-        rr[u] = 0;
-        cc[u] = 0;
-        dd[u] = 0;
-        kk[u] = 0;
-        if (g < ngroups) {
-          const int r = real_of(g);
-          const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
-          rr[u] = r;
-          if (i < s_hi[r]) {
-            const int off = desc(r).off;
-            ok[u] = true;
-            cc[u] = __ldcg(&a.ent[off + i]);
-            dd[u] = __ldcg(&a.pdir[off + i]);
-            kk[u] = __ldcg(&a.acc[off + i]);
-          }
+    // A warp erodes one 32-entry group per iteration, in a software
+    // pipeline: the entries (cell, receiver direction, drainage count) of the
+    // group two iterations ahead and the elevations of the next group are
+    // loaded before this group's erosion, so the chain entry -> elevation ->
+    // erosion of one group overlaps the erosion of the groups before it.
+    struct Entry {
+      int c, dir, r;
+      uint32_t k;
+      bool ok;
+    };
+    struct Heights {
+      uint64_t hc, hn;  // bit patterns in integer registers (see fadd_bits)
+    };
+    auto load_entry = [&](int g) -> Entry {
+      Entry e{0, 0, 0, 0u, false};
+      if (g < ngroups) {
+        const int r = real_of(g);
+        const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
+        e.r = r;
+        if (i < s_hi[r]) {
+          const int off = desc(r).off;
+          e.ok = true;
+          e.c = __ldcg(&a.ent[off + i]);
+          e.dir = __ldcg(&a.pdir[off + i]);
+          e.k = __ldcg(&a.acc[off + i]);
         }
       }
-      // elevations as bit patterns (integer registers, see fadd_bits)
-      uint64_t hc[kEroU], hn[kEroU];
-#pragma unroll
-      for (int u = 0; u < kEroU; u++) {
-        hc[u] = 0;
-        hn[u] = 0;
-        // a group lies in one realization: lane k < 8 holds direction k's offset
-        const int offk = SINGLE ? offk0 : nbr_off(lane & 7, desc(rr[u]).W);
-        const int ro = __shfl_sync(kFull, offk, dd[u] & 7);
-        if (ok[u]) {
-          const RealDesc &d = desc(rr[u]);
-          const unsigned long long *hh =
-              reinterpret_cast<const unsigned long long *>(a.h + d.off);
-          hc[u] = __ldcg(&hh[cc[u]]);
-          hn[u] = __ldcg(&hh[cc[u] + ro]);
-        }
+      return e;
+    };
+    auto gather = [&](const Entry &e) -> Heights {
+      Heights g{0, 0};
+      // a group lies in one realization: lane k < 8 holds direction k's offset
+      const int offk = SINGLE ? offk0 : nbr_off(lane & 7, desc(e.r).W);
+      const int ro = __shfl_sync(kFull, offk, e.dir & 7);
+      if (e.ok) {
+        const unsigned long long *hh =
+            reinterpret_cast<const unsigned long long *>(a.h + desc(e.r).off);
+        g.hc = __ldcg(&hh[e.c]);
+        g.hn = __ldcg(&hh[e.c + ro]);
       }
-#pragma unroll
-      for (int u = 0; u < kEroU; u++) {
-        if (ok[u]) {
-          const RealDesc &d = desc(rr[u]);
-          const size_t rec_at = (size_t)kk[u] * kTabStride + 4 * (dd[u] & 1);
-          const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
-          const uint64_t hr = hn[u];
-          const uint64_t h0 = uplift_bits(hc[u], udt);
-          uint64_t hnew;
-          if (NMODE == kNOne) {
-            hnew = erode_cell_n1<ISUB>(d, ctl,
-                                       reinterpret_cast<const unsigned long long *>(d.tab) + rec_at,
-                                       h0, hr);
-          } else {
-            hnew = (uint64_t)__double_as_longlong(erode_cell<NMODE>(d, a.neq, ctl, d.tab + rec_at,
-                                                  __longlong_as_double(h0), __longlong_as_double(hr)));
-          }
-          if (((hnew >> 52) & 0x7FF) == 0x7FF)  // Inf or NaN
-            raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-          reinterpret_cast<unsigned long long *>(a.h + d.off)[cc[u]] = hnew;
+      return g;
+    };
+    const int gstride = nwarps;
+    Entry e1 = load_entry(warp_global);
+    Entry e2 = load_entry(warp_global + gstride);
+    Heights h1 = gather(e1);
+    for (int g = warp_global; g < ngroups; g += gstride) {
+      const Entry e = e1;
+      const Heights hg = h1;
+      e1 = e2;
+      e2 = load_entry(g + 2 * gstride);
+      h1 = gather(e1);
+      if (e.ok) {
+        const RealDesc &d = desc(e.r);
+        const size_t rec_at = (size_t)e.k * kTabStride + 4 * (e.dir & 1);
+        const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
+        const uint64_t h0 = uplift_bits(hg.hc, udt);
+        uint64_t hnew;
+        if (NMODE == kNOne) {
+          const unsigned long long *Tb = reinterpret_cast<const unsigned long long *>(d.tab) + rec_at;
+          hnew = erode_cell_n1<ISUB>(d, ctl, Tb, load_tab_n1(Tb), h0, hg.hn);
+        } else {
+          hnew = (uint64_t)__double_as_longlong(
+              erode_cell<NMODE>(d, a.neq, ctl, d.tab + rec_at, __longlong_as_double(h0),
+                                __longlong_as_double(hg.hn)));
         }
+        if (((hnew >> 52) & 0x7FF) == 0x7FF)  // Inf or NaN
+          raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+        reinterpret_cast<unsigned long long *>(a.h + d.off)[e.c] = hnew;
       }
     }
     if (Lv + 1 < maxlev && !grid_barrier(ctl, &ctl->bar2, epoch, a.timeout_ns)) return;
