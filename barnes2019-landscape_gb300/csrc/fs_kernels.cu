@@ -40,7 +40,6 @@ constexpr int kWalkThreads = 512;
 constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kPer = 8;   // entries per thread per expansion chunk
 constexpr int kChunk = kPer * kWalkThreads;
-constexpr int kAccU = 4;  // 32-entry groups per warp per accumulation pass
 constexpr int kNewtonMaxIt = 1000;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -380,20 +379,29 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
     const int gy = y0 + ly;
     if (gx < W - 2 && gy < H - 2) {
       const float fc = m1;
-      const float f[8] = {m0, u0, u1, u2, m2, d2, d1, d0};  // W NW N NE E SE S SW
-      // Largest and second largest approximate slope; the first maximum in
-      // neighbour order keeps bn (an exact tie leaves best == second, which
-      // queues the cell). Without NaN in the tile no slope is NaN (an
+      // Largest and second largest approximate slope. Within a direction
+      // class (orthogonal W N E S = codes 0 2 4 6, diagonal NW NE SE SW =
+      // 1 3 5 7) a_n = fl(fl(fc - f_n) * g) does not increase with f_n
+      // (rounding is monotone), so the class's largest and second largest
+      // slopes are those of its smallest and second smallest f -- the same
+      // values as over all eight slopes. bn is the direction of the largest;
+      // it is used only when the largest exceeds every other slope, when its
+      // f is the unique minimum of its class (a tie leaves best == second,
+      // which queues the cell). Without NaN in the tile no slope is NaN (an
       // overflowing difference is +-Inf, and Inf - Inf below only queues).
-      float best = -INFINITY, second = -INFINITY;
-      int bn = 0;
-#pragma unroll
-      for (int n = 0; n < 8; n++) {
-        const float av = (fc - f[n]) * ((n & 1) ? g_diag : g_orth);
-        bn = av > best ? n : bn;
-        second = fmaxf(second, fminf(best, av));
-        best = fmaxf(best, av);
-      }
+      const float lo1 = fminf(m0, m2), hi1 = fmaxf(m0, m2);  // W, E
+      const float lo2 = fminf(u1, d1), hi2 = fmaxf(u1, d1);  // N, S
+      const float lo3 = fminf(u0, u2), hi3 = fmaxf(u0, u2);  // NW, NE
+      const float lo4 = fminf(d2, d0), hi4 = fmaxf(d2, d0);  // SE, SW
+      const float omin = fminf(lo1, lo2), osec = fminf(fmaxf(lo1, lo2), fminf(hi1, hi2));
+      const float dmin = fminf(lo3, lo4), dsec = fminf(fmaxf(lo3, lo4), fminf(hi3, hi4));
+      const int oi = lo2 < lo1 ? (d1 < u1 ? 6 : 2) : (m2 < m0 ? 4 : 0);
+      const int di = lo4 < lo3 ? (d0 < d2 ? 7 : 5) : (u2 < u0 ? 3 : 1);
+      const float bo = (fc - omin) * g_orth, so = (fc - osec) * g_orth;
+      const float bd = (fc - dmin) * g_diag, sd = (fc - dsec) * g_diag;
+      const float best = fmaxf(bo, bd);
+      const float second = fmaxf(fminf(bo, bd), fmaxf(so, sd));
+      const int bn = bo > bd ? oi : di;
       int code = -1;
       if (!tile_bad) {
         if (best - second > 2.f * E && best > E) code = bn;
@@ -1002,29 +1010,52 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
   // elevation changes; the host grows the table and repeats it.
   for (int Lv = maxlev - 1; Lv >= 1; --Lv) {
     const int ngroups = level_groups(Lv);
-    for (int g0 = warp_global * kAccU; g0 < ngroups; g0 += nwarps * kAccU) {
+    // 32-entry groups per warp per iteration. A single grid sums runs of
+    // donors in the warp (more work per group) and loads the next groups
+    // before reducing these; a batch reduces per donor and keeps more groups'
+    // loads in flight instead (each measured faster for its case).
+    constexpr int kAccU = SINGLE ? 2 : 4;
+    struct Group {
       uint32_t v[kAccU];
-      int pp[kAccU], rr[kAccU];
+      int p[kAccU], r[kAccU];
       bool ok[kAccU];
+    };
+    auto load_group = [&](int g0) -> Group {
+      Group G;
 #pragma unroll
       for (int u = 0; u < kAccU; u++) {  // all loads in flight first
         const int g = g0 + u;
-        ok[u] = false;
-        v[u] = 0;
-        pp[u] = 0;
-        rr[u] = 0;
+        G.ok[u] = false;
+        G.v[u] = 0;
+        G.p[u] = 0;
+        G.r[u] = 0;
         if (g < ngroups) {
           const int r = real_of(g);
           const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
-          rr[u] = r;
+          G.r[u] = r;
           if (i < s_hi[r]) {
             const int off = desc(r).off;
-            ok[u] = true;
-            v[u] = __ldcg(&a.acc[off + i]);
-            pp[u] = __ldcg(&a.par[off + i]);
+            G.ok[u] = true;
+            G.v[u] = __ldcg(&a.acc[off + i]);
+            G.p[u] = __ldcg(&a.par[off + i]);
           }
         }
       }
+      return G;
+    };
+    Group nxt;
+    if (SINGLE) nxt = load_group(warp_global * kAccU);
+    for (int g0 = warp_global * kAccU; g0 < ngroups; g0 += nwarps * kAccU) {
+      Group G;
+      if (SINGLE) {
+        G = nxt;
+        nxt = load_group(g0 + nwarps * kAccU);
+      } else {
+        G = load_group(g0);
+      }
+      const uint32_t *v = G.v;
+      const int *pp = G.p, *rr = G.r;
+      const bool *ok = G.ok;
 #pragma unroll
       for (int u = 0; u < kAccU; u++) {
         if (!SINGLE) {  // batches: one reduction per donor (measured faster there)
