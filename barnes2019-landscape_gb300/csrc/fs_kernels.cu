@@ -38,7 +38,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
 constexpr int kWalkWarps = kWalkThreads / 32;
-constexpr int kPer = 8;   // entries per thread per expansion chunk
+constexpr int kPer = 8;   // entries per thread per expansion chunk (measured best of 4..16)
 constexpr int kChunk = kPer * kWalkThreads;
 constexpr int kNewtonMaxIt = 1000;
 
@@ -822,29 +822,32 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       int32_t *ent = a.ent + d.off;
       const uint8_t *mask = a.mask + d.off;
       const int offk = nbr_off(lane & 7, d.W);  // lane k < 8: offset of direction k
+      // Per pass q: the entry's cell, and its donor mask with the warp's
+      // inclusive donor prefix (relative to the warp's first donor, below
+      // 32 * 8 * kPer) packed as (prefix << 8) | mask, to keep the chunk's
+      // state in registers across its barriers.
       int cs[kPer];
-      unsigned ms[kPer];
-      int incl[kPer];
+      unsigned mi[kPer];
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
         const int i = wbase + 32 * q + lane;
         cs[q] = 0;
-        ms[q] = 0;
+        mi[q] = 0;
         if (i < hi) {
           cs[q] = __ldcg(&ent[i]);
-          ms[q] = mask[cs[q]];
+          mi[q] = mask[cs[q]];
         }
       }
       int wtot = 0;
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
-        int v = __popc(ms[q]);
+        int v = __popc(mi[q]);
 #pragma unroll
         for (int dd = 1; dd < 32; dd <<= 1) {
           const int x = __shfl_up_sync(kFull, v, dd);
           if (lane >= dd) v += x;
         }
-        incl[q] = wtot + v;  // inclusive, relative to the warp's first donor
+        mi[q] |= (unsigned)(wtot + v) << 8;  // inclusive prefix
         wtot += __shfl_sync(kFull, v, 31);
       }
       // Place the chunk: prefix of the warp totals and one atomic, with two
@@ -870,7 +873,9 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
 #pragma unroll
       for (int q = 0; q < kPer; q++) {
         const int i = wbase + 32 * q + lane;
-        const int n_d = __popc(ms[q]);
+        const unsigned msk = mi[q] & 0xFFu;
+        const int incl = (int)(mi[q] >> 8);
+        const int n_d = __popc(msk);
         if (i < hi) {
           a.acc[d.off + i] = 1u;  // the cell itself; donors add theirs below
         }
@@ -878,11 +883,11 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         // entry order. Each lane records (its lane, direction) for the slots
         // of its donors in the warp's shared bytes; then lane t writes slot t
         // of every 32, coalesced.
-        const int q_lo = __shfl_sync(kFull, incl[q] - n_d, 0);
-        const int q_n = __shfl_sync(kFull, incl[q], 31) - q_lo;  // <= 32 * 8
+        const int q_lo = __shfl_sync(kFull, incl - n_d, 0);
+        const int q_n = __shfl_sync(kFull, incl, 31) - q_lo;  // <= 32 * 8
         {
-          unsigned m = ms[q];
-          int slot = incl[q] - n_d - q_lo;
+          unsigned m = msk;
+          int slot = incl - n_d - q_lo;
           while (m) {
             s_own[wid][slot++] = (uint8_t)((lane << 3) | (__ffs(m) - 1));
             m &= m - 1;
