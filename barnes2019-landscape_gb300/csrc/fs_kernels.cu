@@ -654,17 +654,6 @@ __device__ __forceinline__ void powers(double x, double neq, double &pn, double 
   }
 }
 
-// Erosion of one cell for n = 1 (fastscape_RB.cpp:315-326) on bit
-// patterns: h0 the uplifted elevation, hn the receiver's final elevation,
-// Tb the table record of the cell's drainage count and direction class
-// (fact, D = 1 + fact, R = 1/D).
-//
-// First iterate: hnew - h0 = +0, pow(x,1) = x and pow(x,0) = 1, so
-// hnew = RN(h0 - RN(RN(fact*RN(h0-hn)) / D)). With ISUB the two
-// subtractions run in integer arithmetic: that relieves the FP64 pipe but
-// lengthens the cell's dependency chain after the receiver's elevation
-// arrives, which pays where the pipe, not latency, limits the erosion (the
-// autotuner decides per workload).
 // The fields of a table record the n = 1 erosion reads up front.
 struct TabN1 {
   uint64_t fact, D, Rn;
@@ -674,35 +663,88 @@ __device__ __forceinline__ TabN1 load_tab_n1(const unsigned long long *Tb) {
   return TabN1{__ldg(Tb + 0), __ldg(Tb + 1), __ldg(Tb + 3)};
 }
 
+// True when |RN(x - y)| <= tol is proven for x = RN(y - q), y the previous
+// iterate and qn = -q: |RN(x - y)| <= (|q| + 2^-51(|y|+|q|))(1+2^-53), and
+// an FP32 test on truncated magnitudes (each within 2^-23 relative, flushed
+// below 2^-126) with 2^-21 of slack proves it for almost every cell without
+// the subtraction.
+__device__ __forceinline__ bool step_below_tol(uint64_t qn, uint64_t y, const RealDesc &d) {
+  const float qf = fabsf(trunc_bits_to_float(qn));
+  const float yf = fabsf(trunc_bits_to_float(y));
+  return qf * (1.f + 0x1p-21f) + yf * 0x1p-48f <= d.tol_lo_f;
+}
+
+// RN(x - y) for any two elevations: the exact integer difference when both
+// are positive normal and within a factor 2 of each other (Sterbenz), else
+// in FP64.
+__device__ __forceinline__ uint64_t sub_sterbenz(uint64_t x, uint64_t y) {
+  if (add_pos_operand(x) && add_pos_operand(y) && x != y) {
+    const bool gt = x > y;
+    const uint64_t r = sub_near_bits(gt ? x : y, gt ? y : x);
+    if (r) return gt ? r : (r ^ kSignBit);
+  }
+  return fadd_bits_volatile(x, y ^ kSignBit);
+}
+
+// RN(x + y), y = -q with |q| far below x > 0 (a Newton correction): in
+// integer arithmetic when the operands allow, else in FP64.
+__device__ __forceinline__ uint64_t add_correction(uint64_t x, uint64_t y) {
+  return (y & kSignBit) ? sub_far(x, y ^ kSignBit) : uplift_bits(x, y);
+}
+
+// Erosion of one cell for n = 1 (fastscape_RB.cpp:315-326) on bit
+// patterns: h0 the uplifted elevation, hn the receiver's final elevation,
+// t the table record of the cell's drainage count and direction class
+// (fact, D = 1 + fact, -1/D; Tb the record itself for 1/D).
+//
+// The reference's loop for n = 1 (pow(x,1) = x, pow(x,0) = 1):
+//   x' = RN(x - RN(RN(RN(x - h0) + RN(fact*RN(x - hn))) / D)),
+//   stop when |RN(x' - x)| <= tol.
+// First iterate (x = h0): RN(h0 - h0) = +0, so x1 = RN(h0 - RN(RN(fact*
+// RN(h0-hn)) / D)). Cells whose erosion exceeds tol take a second iterate,
+// unrolled here too; its residual num2 is often exactly 0 (then x2 = x1).
+// Rarer third iterates follow the generic loop. With ISUB the subtractions
+// of elevations run in integer arithmetic: that relieves the FP64 pipe but
+// lengthens the cell's dependency chain after the receiver's elevation
+// arrives, which pays where the pipe, not latency, limits the erosion (the
+// autotuner decides per workload).
 template <bool ISUB>
 __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
                                                   const unsigned long long *Tb, TabN1 t,
                                                   uint64_t h0, uint64_t hn) {
   const uint64_t factb = t.fact;
-  const double D = __longlong_as_double(t.D);
+  const double D = __longlong_as_double(t.D), Rn = __longlong_as_double(t.Rn);
   const uint64_t dh = ISUB ? sub_near(h0, hn) : fadd_bits(h0, hn ^ kSignBit);
   const uint64_t num = fmul_bits(factb, dh);
-  const uint64_t qn = neg_div_rn_bits(num, D, __longlong_as_double(t.Rn));  // -q
-  const uint64_t hnew = ISUB ? sub_far(h0, qn ^ kSignBit) : fadd_bits(h0, qn);
-  // The loop stops after this iterate iff |RN(hnew - h0)| <= tol. Since
-  // |RN(hnew-h0)| <= (|q| + 2^-51(|h0|+|q|))(1+2^-53), an FP32 test on
-  // truncated magnitudes (each within 2^-23 relative, flushed below
-  // 2^-126) with 2^-21 of slack proves it for almost every cell without
-  // the subtraction; the rest evaluate diff and follow the loop in FP64.
-  const float qf = fabsf(trunc_bits_to_float(qn));
-  const float hf = fabsf(trunc_bits_to_float(h0));
-  if (qf * (1.f + 0x1p-21f) + hf * 0x1p-48f <= d.tol_lo_f) return hnew;
+  const uint64_t qn = neg_div_rn_bits(num, D, Rn);  // -q
+  const uint64_t x1 = ISUB ? sub_far(h0, qn ^ kSignBit) : fadd_bits(h0, qn);
+  if (step_below_tol(qn, h0, d)) return x1;
+  // diff = RN(x1 - h0); |diff| > tol as an integer compare of the
+  // magnitudes' bits (a NaN diff stops the loop, as fabs(NaN) > tol is false)
+  const uint64_t a = ISUB ? sub_sterbenz(x1, h0) : fadd_bits(x1, h0 ^ kSignBit);
+  auto more = [&](uint64_t df) {
+    const long long m = (long long)(df & ~kSignBit);
+    return m > d.tol_bits && m <= 0x7FF0000000000000ll;
+  };
+  if (!more(a)) return x1;
+  // second iterate: num2 = RN(a + RN(fact * RN(x1 - hn)))
+  const uint64_t b = ISUB ? sub_sterbenz(x1, hn) : fadd_bits(x1, hn ^ kSignBit);
+  const uint64_t c = fmul_bits(factb, b);
+  const uint64_t num2 = ISUB ? sub_sterbenz(c, a ^ kSignBit) : fadd_bits(a, c);
+  if ((num2 << 1) == 0) return x1;  // RN(0/D) = +0 and x1 - 0 = x1: diff = 0
+  const uint64_t q2n = neg_div_rn_bits(num2, D, Rn);
+  const uint64_t x2 = ISUB ? add_correction(x1, q2n) : fadd_bits(x1, q2n);
+  if (step_below_tol(q2n, x1, d)) return x2;
+  // third and later iterates: the reference's loop in FP64
   const double R = __longlong_as_double(__ldg(Tb + 2));
   const double fact = __longlong_as_double(factb), h0d = __longlong_as_double(h0),
                hnd = __longlong_as_double(hn);
-  double x = __longlong_as_double(hnew);
-  double diff = x - h0d, hp = x;
-  int it = 1;
-  // fabs(diff) > tol as an integer compare of the magnitudes' bits (both
-  // non-negative; a NaN diff stops the loop, as fabs(NaN) > tol is false)
-  while (abs_bits(diff) > d.tol_bits && abs_bits(diff) <= 0x7FF0000000000000ll) {
-    const double num2 = (x - h0d) + fact * (x - hnd);
-    x -= div_rn(num2, D, R);
+  double x = __longlong_as_double(x2);
+  double diff = x - __longlong_as_double(x1), hp = x;
+  int it = 2;
+  while (more((uint64_t)__double_as_longlong(diff))) {
+    const double n3 = (x - h0d) + fact * (x - hnd);
+    x -= div_rn(n3, D, R);
     diff = x - hp;
     hp = x;
     if (++it >= kNewtonMaxIt) {

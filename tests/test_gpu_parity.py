@@ -140,6 +140,28 @@ def test_oracle_trajectory_integer_subtractions(pkg, oracle, W, H, steps, seed):
             assert_step_equal(m, W, H, ref, f"step {s}")
 
 
+@pytest.mark.parametrize("int_sub", [False, True])
+def test_second_newton_iterate(pkg, oracle, int_sub):
+    """Strong erosion (K 5e-5, U 5e-3, 500 m of relief): most cells erode by
+    more than tol per timestep and take the unrolled second Newton iterate
+    (its zero-residual shortcut included); bit-identical to the oracle at
+    every timestep, with FP64 or integer subtractions."""
+    W, H, steps = 200, 150, 8
+    rng = np.random.default_rng(17)
+    p = pkg.workload_params(keq=5e-5, ueq=5e-3, meq=0.5)
+    op = Params(*p.as_tuple())
+    h = rng.uniform(0, 500, W * H)
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+        m.use_int_sub(int_sub)
+        m.setH(h)
+        for s in range(steps):
+            m.step(1)
+            ref = oracle.phases(h, W, H, op)
+            assert_step_equal(m, W, H, ref, f"step {s}")
+
+
 def test_workload_1000_integer_subtractions(pkg, oracle):
     """run(120) of the 1000x1000 workload with the integer subtractions:
     bit-identical to the oracle, like the default erosion."""
