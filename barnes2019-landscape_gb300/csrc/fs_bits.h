@@ -15,6 +15,29 @@
 
 namespace fs {
 
+FS_BITS_FN float float_from_bits(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  __builtin_memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+// Truncation of a double (as bits) to FP32 with integer operations only:
+// rebias the exponent, keep the top 23 fraction bits. Values below 2^-126
+// flush to signed zero; |x| >= 2^128, Inf and NaN give NaN.
+FS_BITS_FN float trunc_bits_to_float(uint64_t b) {
+  const uint32_t hi = (uint32_t)(b >> 32);
+  const uint32_t sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  const uint32_t frac = (uint32_t)(b >> 29) & 0x7FFFFFu;
+  if (e <= 0) return float_from_bits(sign);
+  if (e >= 255) return float_from_bits(0x7FC00000u);
+  return float_from_bits(sign | ((uint32_t)e << 23) | frac);
+}
+
 // True when x is positive, normal and at most 2^1023 (biased exponent in
 // [1, 2045]): the operands add_pos_rn_bits accepts.
 FS_BITS_FN bool add_pos_operand(uint64_t x) {
@@ -100,6 +123,38 @@ FS_BITS_FN uint64_t sub_far_bits(uint64_t x, uint64_t y) {
   s <<= lz;
   const uint64_t r = (s + 0x1FF + ((s >> 10) & 1)) >> 10;  // [2^52, 2^53]
   return ((uint64_t)(ex - lz - 1) << 52) + r;
+}
+
+// A Newton correction far below its iterate: x2 = RN(x - q), q = RN(num/D),
+// with x > 0, 1 <= D < 2^100 (bits D) and |q| within about one spacing of x. x2 is x or one of its
+// neighbours (bits x - 1 or x + 1): x when |q| is below half the spacing
+// on q's side, the neighbour when |q| lies between a half and 1.2 spacings
+// (the next spacing beyond a power of two at least halves, which 1.2 keeps
+// clear of). qe is an FP32 estimate of |num/D| within 2^-18 relative (plus
+// an absolute error far below the spacing: x >= 2^-23 and D < 2^100); q's
+// own rounding is below 2^-52 relative. With a margin of 2^-16 around the
+// half-spacing threshold the estimate decides like the exact quotient;
+// nearer the threshold, or for x or D out of range, false is returned and
+// the caller computes q exactly. On true, *step is -1, 0 or +1 and
+// x2 = x + *step as bits. `ulp` returns the spacing above x as FP32.
+FS_BITS_FN bool newton_step_in_spacing(uint64_t num, uint64_t D, uint64_t x, float qe,
+                                       int *step, float *ulp) {
+  const int ex = (int)(x >> 52);  // x > 0: no sign bit
+  if (ex < 1000 || ex > 1160 || (D >> 52) >= 1123) return false;
+  *ulp = float_from_bits((uint32_t)(ex - 948) << 23);             // 2^(ex-1075)
+  const bool down = (num >> 63) == 0;                              // q > 0: below x
+  const bool half = down && (x << 12) == 0;                        // x a power of 2
+  const float inv = float_from_bits((uint32_t)(1202 - ex + (half ? 1 : 0)) << 23);
+  const float r = qe * inv;  // |q| in spacings on its side (a power-of-2 scaling)
+  if (r < 0.5f * (1.f - 0x1p-16f)) {
+    *step = 0;
+    return true;
+  }
+  if (r > 0.5f * (1.f + 0x1p-16f) && r < 1.2f) {
+    *step = down ? -1 : 1;
+    return true;
+  }
+  return false;
 }
 
 }  // namespace fs

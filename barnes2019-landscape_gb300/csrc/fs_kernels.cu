@@ -299,19 +299,8 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 //   best < -E                         => every q_n < 0 (NO_FLOW);
 // otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
 
-// Truncation of a double to FP32 with integer operations only (no FP64
-// pipe): rebias the exponent, keep the top 23 fraction bits. Values below
-// 2^-126 flush to signed zero; |x| >= 2^128, Inf and NaN give NaN.
-__device__ __forceinline__ float trunc_bits_to_float(unsigned long long b) {
-  const unsigned hi = (unsigned)(b >> 32);
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
-  const unsigned frac = (unsigned)(b >> 29) & 0x7FFFFFu;
-  if (e <= 0) return __uint_as_float(sign);
-  if (e >= 255) return __uint_as_float(0x7FC00000u);
-  return __uint_as_float(sign | ((unsigned)e << 23) | frac);
-}
-
+// trunc_bits_to_float (fs_bits.h): truncation of a double to FP32 with
+// integer operations only (no FP64 pipe).
 __device__ __forceinline__ float trunc_to_float(double x) {
   return trunc_bits_to_float((unsigned long long)__double_as_longlong(x));
 }
@@ -732,6 +721,16 @@ __device__ __forceinline__ uint64_t erode_cell_n1(const RealDesc &d, Ctl *ctl,
   const uint64_t c = fmul_bits(factb, b);
   const uint64_t num2 = ISUB ? sub_sterbenz(c, a ^ kSignBit) : fadd_bits(a, c);
   if ((num2 << 1) == 0) return x1;  // RN(0/D) = +0 and x1 - 0 = x1: diff = 0
+  // The correction is a residual of x1's rounding: x2 is x1 or a neighbour,
+  // decided from an FP32 estimate of the quotient (newton_step_in_spacing),
+  // and a step of at most one spacing <= tol ends the loop.
+  if (add_pos_operand(x1)) {
+    const float qe = __fdividef(fabsf(trunc_bits_to_float(num2)), trunc_bits_to_float(t.D));
+    int step;
+    float ulp;
+    if (newton_step_in_spacing(num2, t.D, x1, qe, &step, &ulp) && ulp <= d.tol_lo_f)
+      return x1 + (uint64_t)(int64_t)step;
+  }
   const uint64_t q2n = neg_div_rn_bits(num2, D, Rn);
   const uint64_t x2 = ISUB ? add_correction(x1, q2n) : fadd_bits(x1, q2n);
   if (step_below_tol(q2n, x1, d)) return x2;

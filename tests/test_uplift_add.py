@@ -1,9 +1,8 @@
-"""The erosion kernel's integer uplift addition (fs::add_pos_rn_bits in
-csrc/fs_bits.h, the same source the kernel compiles) checked on the host
-against the hardware's RN addition: random operands at every exponent
-difference, sums next to rounding ties, carries through the rounding,
-overflow to +Inf, and the operand filter. The GPU parity tests check the
-device results bit for bit against the oracle."""
+"""The erosion kernel's integer-arithmetic operations (csrc/fs_bits.h, the
+same source the kernel compiles) checked on the host: the additions and
+subtractions of elevations against the hardware's RN operations, and the
+second Newton iterate's FP32 step decision against the exact iterate. The
+GPU parity tests check the device results bit for bit against the oracle."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -24,3 +23,18 @@ def test_integer_uplift_add_matches_hardware(tmp_path):
         out = subprocess.run([str(exe), "5000000", str(seed)], capture_output=True, text=True)
         assert out.returncode == 0, out.stdout + out.stderr
         assert "all equal to the hardware operation" in out.stdout
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_second_iterate_step_decision(tmp_path):
+    """fs::newton_step_in_spacing: the second Newton iterate decided from an
+    FP32 quotient (perturbed by +-2^-20) equals the exact double iterate."""
+    exe = tmp_path / "newton_step_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(ROOT / "barnes2019-landscape_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "newton_step_check.cpp"), "-o", str(exe)],
+                   check=True)
+    for seed in (1, 2):
+        out = subprocess.run([str(exe), "3000000", str(seed)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "all decisions equal to the exact iterate" in out.stdout
