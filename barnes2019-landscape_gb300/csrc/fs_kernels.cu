@@ -267,6 +267,39 @@ __device__ __forceinline__ int receiver_fp64(const double *h, int c, int W, doub
   return max_n == FS_NO_FLOW ? kPit : max_n;
 }
 
+// The same formula for the cells the FP32 filter leaves open -- mostly
+// flat ground, where neighbours are equal or differ by less than the
+// filter's bound. Only a strictly lower neighbour can have a slope above the
+// running maximum (which starts at 0), so the others are skipped by an
+// integer comparison of order-preserving keys of the bit patterns: a flat
+// cell costs no FP64 operation. (Keys order -0 below +0 where FP64 calls
+// them equal; that lets through a slope of +0, which never wins. A NaN
+// neighbour is skipped or yields a NaN slope, which never wins either.)
+__device__ __forceinline__ uint64_t order_key(uint64_t x) {
+  return (x >> 63) ? ~x : (x | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ int receiver_fp64_lower(const double *h, int c, int W, double dr_orth,
+                                                   double dr_diag) {
+  const unsigned long long *hb = reinterpret_cast<const unsigned long long *>(h);
+  const uint64_t hcb = hb[c];
+  const uint64_t kc = order_key(hcb);
+  const double hc = __longlong_as_double(hcb);
+  double max_slope = 0;
+  int max_n = FS_NO_FLOW;
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const uint64_t hnb = hb[c + nbr_off(n, W)];
+    if (order_key(hnb) >= kc) continue;
+    const double slope = (hc - __longlong_as_double(hnb)) / ((n & 1) ? dr_diag : dr_orth);
+    if (slope > max_slope) {
+      max_slope = slope;
+      max_n = n;
+    }
+  }
+  return max_n == FS_NO_FLOW ? kPit : max_n;
+}
+
 __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
   if (stopped(a.ctl)) return;
   const Tile t = a.rtiles[blockIdx.x];
@@ -430,7 +463,7 @@ __global__ void __launch_bounds__(256) k_receivers_fixup(StepArgs a) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_amb; i += gridDim.x * blockDim.x) {
     const RealDesc &d = a.desc[a.amb_r[i]];
     const int c = a.amb[i] - d.off;
-    a.rec[d.off + c] = (int8_t)receiver_fp64(a.h + d.off, c, d.W, d.dr_orth, d.dr_diag);
+    a.rec[d.off + c] = (int8_t)receiver_fp64_lower(a.h + d.off, c, d.W, d.dr_orth, d.dr_diag);
   }
 }
 

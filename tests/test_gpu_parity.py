@@ -306,6 +306,38 @@ def test_receiver_filter_equals_fp64_formula(pkg):
         assert 0 < n.value < W * H // 100
 
 
+def test_receiver_fixup_on_flat_ground(pkg):
+    """Flat-heavy terrain -- integer terraces (exact ties and zero slopes),
+    +0 and -0, negative heights, neighbours one ulp apart -- sends most cells
+    to the FP64 fix-up; its lower-neighbour shortcut must give the verbatim
+    formula's receivers."""
+    import ctypes as C
+    W, H = 700, 500
+    rng = np.random.default_rng(23)
+    h = rng.integers(0, 4, W * H).astype(np.float64)
+    k = rng.integers(0, 6, W * H)
+    h[k == 1] = np.nextafter(h[k == 1], np.inf)        # one ulp above a terrace
+    h[k == 2] = -h[k == 2]                             # -0 and negative terraces
+    h[k == 3] = 1e-300 * rng.integers(0, 3, (k == 3).sum())
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    p = pkg.workload_params()
+    L = pkg.library()
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as a, \
+            pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as b:
+        L.fs_test_set_receiver_path(b.handle, 1)
+        a.setH(h)
+        b.setH(h)
+        for s in range(3):
+            a.step(1)
+            b.step(1)
+            assert np.array_equal(a.receivers(), b.receivers()), f"step {s}"
+            assert np.array_equal(a.getH(), b.getH()), f"step {s}"
+        n = C.c_int32(0)
+        pkg.check(L.fs_test_receiver_fixups(a.handle, C.byref(n)))
+        assert n.value > W * H // 10
+
+
 def valley(W, H):
     """V-shaped valley whose axis runs down to the base-level ring at y = 1:
     nearly every cell drains into the axis, so the axis cell next to base
