@@ -61,6 +61,8 @@ struct RealDesc {
   float tol_lo_f;          // an FP32 value <= tol*(1-2^-20)
   float g_orth, g_diag, gmax;  // FP32 1/dr for the receiver filter
   double dr_orth, dr_diag;
+  double rdr_orth_n, rdr_diag_n;  // -RN(1/dr) for the tabled receiver
+                                  // slope division; 0: divide in IEEE FP64
   const double *tab;       // erosion table, kTabStride doubles per count
   int tab_cap;             // counts k < tab_cap are in the table
   int pad;
@@ -200,6 +202,8 @@ cudaError_t launch_dfs_order(const DfsArgs &d, const int32_t *lvl_host, int nlev
 
 // Host helpers shared by the entry points.
 float tol_lower_float(double tol);
+// -RN(1/dr) when the tabled division covers dr (1 <= dr <= 2^60), else 0.
+double neg_recip_dr(double dr);
 int ring_cells(int W, int H);
 // Appends the receiver (kind 0) or donor (kind 1) tiles of realization r to
 // out (capacity cap); returns the number appended, or -1 if out is full.

@@ -243,6 +243,60 @@ __device__ __forceinline__ uint64_t sub_far(uint64_t x, uint64_t y) {
   return fadd_bits_volatile(x, y ^ kSignBit);
 }
 
+// RN(x - y) for any two elevations: the exact integer difference when both
+// are positive normal and within a factor 2 of each other (Sterbenz), else
+// in FP64.
+__device__ __forceinline__ uint64_t sub_sterbenz(uint64_t x, uint64_t y) {
+  if (add_pos_operand(x) && add_pos_operand(y) && x != y) {
+    const bool gt = x > y;
+    const uint64_t r = sub_near_bits(gt ? x : y, gt ? y : x);
+    if (r) return gt ? r : (r ^ kSignBit);
+  }
+  return fadd_bits_volatile(x, y ^ kSignBit);
+}
+
+// -RN(num/D) on bit patterns, given Rn = -R, R = RN(1/D), in three FP64
+// operations. q0 = RN(num*R) and r0 = num - q0*D by a fused multiply-add;
+// when q0 is not a power of two, its exponent is far from the range limits,
+// D is positive and normal with D*ulp(q0) normal too (the threshold below
+// is built by adding exponents) and |r0| < D*ulp(q0), q0 lies within one
+// ulp of num/D, r0 is
+// exact, and by Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1),
+// 1990) q1 = RN(q0 + r0*R) is the correctly rounded quotient
+// (tests/native/division_check.cpp replays this on the host against the
+// IEEE division, near rounding midpoints included). (A q0 more
+// than an ulp away makes |num - q0*D| >= D*ulp(q0), which its rounding
+// keeps, so the test is never passed wrongly.) Every quotient is carried
+// negated -- RN is symmetric; q0n = RN(num*Rn) = -q0 -- which puts the
+// negations into the operands; the caller adds the result to h0. Anything
+// else takes the IEEE division, volatile PTX in a branch; the numerator and
+// result stay in integer registers.
+__device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double Rn) {
+  const double num = __longlong_as_double(numb);
+  const double q0n = num * Rn;
+  const double r0 = fma(q0n, D, num);
+  // Magnitudes are compared with the sign shifted out (x << 1) rather than
+  // masked: the compiler turns a sign mask of a double into an FP64
+  // absolute value.
+  const uint64_t q0b = (uint64_t)__double_as_longlong(q0n);
+  const int e = (int)((q0b << 1) >> 53);
+  const int ed = (int)((uint64_t)__double_as_longlong(D) >> 52);  // sign and exponent of D
+  const int et = ed + e - 1075;                                    // exponent of D*ulp(q0)
+  if (e >= 64 && e <= 1980 && ed >= 1 && ed <= 2046 && et >= 1 && et <= 2046 &&
+      (q0b << 12) != 0) {
+    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1075) << 52));
+    if (((uint64_t)__double_as_longlong(r0) << 1) < (thr << 1))
+      return (uint64_t)__double_as_longlong(fma(r0, Rn, q0n));
+  }
+  uint64_t r;
+  asm volatile(
+      "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(numb), "l"((uint64_t)__double_as_longlong(D)));
+  return r ^ kSignBit;
+}
+
 // ---------------------------------------------------------------------------
 // 1. Receivers: fastscape_RB.cpp:160-182. slope = (h[c]-h[n])/dr[n], strict
 // '>' against a running maximum that starts at 0, so the first maximum in
@@ -279,19 +333,26 @@ __device__ __forceinline__ uint64_t order_key(uint64_t x) {
   return (x >> 63) ? ~x : (x | 0x8000000000000000ull);
 }
 
-__device__ __forceinline__ int receiver_fp64_lower(const double *h, int c, int W, double dr_orth,
-                                                   double dr_diag) {
+__device__ __forceinline__ int receiver_fp64_lower(const double *h, int c, const RealDesc &d) {
   const unsigned long long *hb = reinterpret_cast<const unsigned long long *>(h);
   const uint64_t hcb = hb[c];
+  if ((hcb & ~kSignBit) > 0x7FF0000000000000ull) return kPit;  // NaN: every slope NaN
   const uint64_t kc = order_key(hcb);
-  const double hc = __longlong_as_double(hcb);
-  double max_slope = 0;
+  uint64_t max_slope = 0;  // bits of +0; slopes compared as non-negative bit patterns
   int max_n = FS_NO_FLOW;
 #pragma unroll
   for (int n = 0; n < 8; n++) {
-    const uint64_t hnb = hb[c + nbr_off(n, W)];
-    if (order_key(hnb) >= kc) continue;
-    const double slope = (hc - __longlong_as_double(hnb)) / ((n & 1) ? dr_diag : dr_orth);
+    const uint64_t hnb = hb[c + nbr_off(n, d.W)];
+    if (order_key(hnb) >= kc || (hnb & ~kSignBit) > 0x7FF0000000000000ull) continue;
+    const uint64_t db = sub_sterbenz(hcb, hnb);  // RN(hc - hn) > 0 (or +0)
+    const double dr = (n & 1) ? d.dr_diag : d.dr_orth;
+    const double rn = (n & 1) ? d.rdr_diag_n : d.rdr_orth_n;
+    uint64_t slope;
+    if (__double_as_longlong(rn) != 0) {
+      slope = neg_div_rn_bits(db, dr, rn) ^ kSignBit;  // RN(d / dr)
+    } else {
+      slope = (uint64_t)__double_as_longlong(__longlong_as_double(db) / dr);
+    }
     if (slope > max_slope) {
       max_slope = slope;
       max_n = n;
@@ -463,7 +524,7 @@ __global__ void __launch_bounds__(256) k_receivers_fixup(StepArgs a) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_amb; i += gridDim.x * blockDim.x) {
     const RealDesc &d = a.desc[a.amb_r[i]];
     const int c = a.amb[i] - d.off;
-    a.rec[d.off + c] = (int8_t)receiver_fp64_lower(a.h + d.off, c, d.W, d.dr_orth, d.dr_diag);
+    a.rec[d.off + c] = (int8_t)receiver_fp64_lower(a.h + d.off, c, d);
   }
 }
 
@@ -624,43 +685,6 @@ __device__ __forceinline__ double div_rn(double num, double D, double R) {
   return num / D;
 }
 
-// -RN(num/D) on bit patterns, given D >= 1 and Rn = -R, R = RN(1/D), in
-// three FP64 operations. q0 = RN(num*R) and r0 = num - q0*D by a fused
-// multiply-add; when q0 is not a power of two, its exponent is far from the
-// range limits and |r0| < D*ulp(q0), q0 lies within one ulp of num/D, r0 is
-// exact, and by Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1),
-// 1990) q1 = RN(q0 + r0*R) is the correctly rounded quotient
-// (tests/native/division_check.cpp replays this on the host against the
-// IEEE division, near rounding midpoints included). (A q0 more
-// than an ulp away makes |num - q0*D| >= D*ulp(q0), which its rounding
-// keeps, so the test is never passed wrongly.) Every quotient is carried
-// negated -- RN is symmetric; q0n = RN(num*Rn) = -q0 -- which puts the
-// negations into the operands; the caller adds the result to h0. Anything
-// else takes the IEEE division, volatile PTX in a branch; the numerator and
-// result stay in integer registers.
-__device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double Rn) {
-  const double num = __longlong_as_double(numb);
-  const double q0n = num * Rn;
-  const double r0 = fma(q0n, D, num);
-  // Magnitudes are compared with the sign shifted out (x << 1) rather than
-  // masked: the compiler turns a sign mask of a double into an FP64
-  // absolute value.
-  const uint64_t q0b = (uint64_t)__double_as_longlong(q0n);
-  const int e = (int)((q0b << 1) >> 53);
-  if (e >= 64 && e <= 1980 && (q0b << 12) != 0) {
-    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1075) << 52));
-    if (((uint64_t)__double_as_longlong(r0) << 1) < (thr << 1))
-      return (uint64_t)__double_as_longlong(fma(r0, Rn, q0n));
-  }
-  uint64_t r;
-  asm volatile(
-      "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
-      "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
-      : "=l"(r)
-      : "l"(numb), "l"((uint64_t)__double_as_longlong(D)));
-  return r ^ kSignBit;
-}
-
 // pow(x, n) and pow(x, n-1) for the Newton update of fastscape_RB.cpp:322.
 template <int NMODE>
 __device__ __forceinline__ void powers(double x, double neq, double &pn, double &pn1) {
@@ -694,18 +718,6 @@ __device__ __forceinline__ bool step_below_tol(uint64_t qn, uint64_t y, const Re
   const float qf = fabsf(trunc_bits_to_float(qn));
   const float yf = fabsf(trunc_bits_to_float(y));
   return qf * (1.f + 0x1p-21f) + yf * 0x1p-48f <= d.tol_lo_f;
-}
-
-// RN(x - y) for any two elevations: the exact integer difference when both
-// are positive normal and within a factor 2 of each other (Sterbenz), else
-// in FP64.
-__device__ __forceinline__ uint64_t sub_sterbenz(uint64_t x, uint64_t y) {
-  if (add_pos_operand(x) && add_pos_operand(y) && x != y) {
-    const bool gt = x > y;
-    const uint64_t r = sub_near_bits(gt ? x : y, gt ? y : x);
-    if (r) return gt ? r : (r ^ kSignBit);
-  }
-  return fadd_bits_volatile(x, y ^ kSignBit);
 }
 
 // RN(x + y), y = -q with |q| far below x > 0 (a Newton correction): in
@@ -1584,6 +1596,10 @@ cudaError_t prepare_walk_kernels() {
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+double neg_recip_dr(double dr) {
+  return dr >= 1.0 && dr <= 0x1p60 ? -(1.0 / dr) : 0.0;
 }
 
 float tol_lower_float(double tol) {

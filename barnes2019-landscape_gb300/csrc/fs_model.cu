@@ -538,6 +538,8 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
     d.gmax = std::max(d.g_orth, d.g_diag);
     d.dr_orth = p.dr_orth;
     d.dr_diag = p.dr_diag;
+    d.rdr_orth_n = fs::neg_recip_dr(p.dr_orth);
+    d.rdr_diag_n = fs::neg_recip_dr(p.dr_diag);
   }
   if (!cu(cudaMemcpyAsync(b->d_desc, b->desc.data(), n * sizeof(fs::RealDesc),
                           cudaMemcpyHostToDevice, b->stream),

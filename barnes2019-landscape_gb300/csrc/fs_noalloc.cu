@@ -214,6 +214,8 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   rd.gmax = rd.g_orth > rd.g_diag ? rd.g_orth : rd.g_diag;
   rd.dr_orth = p.dr_orth;
   rd.dr_diag = p.dr_diag;
+  rd.rdr_orth_n = fs::neg_recip_dr(p.dr_orth);
+  rd.rdr_diag_n = fs::neg_recip_dr(p.dr_diag);
   rd.tab = tab;
   rd.tab_cap = static_cast<int>(kTabRecords);
 

@@ -1,12 +1,14 @@
 // Host restatement of the erosion kernel's quotient (neg_div_rn_bits in
 // fs_kernels.cu): q0 = RN(num * R) with R = RN(1/D), r0 = num - q0*D by a
 // fused multiply-add, q1 = RN(q0 + r0*R), accepted when q0 is not a power of
-// two, its exponent is far from the range limits and |r0| < D*ulp(q0) --
+// two, its exponent is far from the range limits, D and D*ulp(q0) are
+// positive normal numbers and |r0| < D*ulp(q0) --
 // then q0 is within one ulp of num/D, r0 is exact, and by Markstein's theorem
 // (P. Markstein, IBM J. Res. Dev. 34(1), 1990) q1 = RN(num/D). The check
 // compares every accepted q1 with the IEEE quotient on random operands and
 // on operands built next to rounding midpoints (num = RN(D * midpoint)),
-// D of all significand shapes, and reports the acceptance rate.
+// D of all significand shapes and exponents (below 1, huge, negative, the
+// receiver slopes' divisors), and reports the acceptance rate.
 // Usage: division_check <cases> <seed>; exit 1 on the first mismatch.
 #include <cinttypes>
 #include <cmath>
@@ -25,7 +27,10 @@ static bool fast_quotient(double num, double D, double R, double *q) {
   const double r0 = std::fma(q0n, D, num);
   const uint64_t q0b = bits(q0n);
   const int e = (int)((q0b << 1) >> 53);
-  if (e >= 64 && e <= 1980 && (q0b << 12) != 0) {
+  const int ed = (int)(bits(D) >> 52);
+  const int et = ed + e - 1075;
+  if (e >= 64 && e <= 1980 && ed >= 1 && ed <= 2046 && et >= 1 && et <= 2046 &&
+      (q0b << 12) != 0) {
     const uint64_t thr = (uint64_t)((int64_t)bits(D) + ((int64_t)(e - 1075) << 52));
     if ((bits(r0) << 1) < (thr << 1)) {
       *q = -std::fma(r0, Rn, q0n);
@@ -40,15 +45,20 @@ int main(int argc, char **argv) {
   std::mt19937_64 g(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
   long accepted = 0;
   for (long i = 0; i < n; i++) {
-    // D = 1 + F, F from tiny to huge; significands of every shape
+    // D = 1 + F, F from tiny to huge; significands of every shape; also the
+    // receiver slopes' divisors (dx, dx*sqrt(2)), D below 1, huge D (where
+    // the threshold's exponent leaves the range) and negative D
     double D;
-    switch (i % 4) {
+    switch (i % 7) {
       case 0: D = 1.0 + std::ldexp((double)(g() >> 11), -53 + (int)(g() % 80) - 40); break;
       case 1: D = dbl((uint64_t)(1023 + g() % 40) << 52 | (g() & ((1ull << 52) - 1))); break;
       case 2: D = dbl((uint64_t)(1023 + g() % 40) << 52 | (((1ull << 52) - 1) ^ ((1ull << (g() % 52)) - 1))); break;
-      default: D = dbl((uint64_t)(1023 + g() % 40) << 52 | ((1ull << (g() % 52)) | (g() & 0xFF))); break;
+      case 3: D = dbl((uint64_t)(1023 + g() % 40) << 52 | ((1ull << (g() % 52)) | (g() & 0xFF))); break;
+      case 4: D = (g() & 1) ? 100.0 : 100.0 * 1.4142135623730951; break;
+      case 5: D = dbl((uint64_t)(1 + g() % 2046) << 52 | (g() & ((1ull << 52) - 1))); break;
+      default: D = -dbl((uint64_t)(1023 + g() % 40) << 52 | (g() & ((1ull << 52) - 1))); break;
     }
-    if (!(D >= 1.0) || !std::isfinite(D)) continue;
+    if (D == 0 || !std::isfinite(D)) continue;
     const double R = 1.0 / D;
     double num;
     if (i & 1) {
@@ -57,6 +67,8 @@ int main(int argc, char **argv) {
       int e; std::frexp(m, &e);
       num = std::fma(D, m, D * std::ldexp(1.0, e - 54));
       if (i % 3 == 0) num = dbl(bits(num) + (int)(g() % 5) - 2);
+    } else if (i % 5 == 0) {
+      num = dbl((uint64_t)(1 + g() % 2046) << 52 | (g() & ((1ull << 52) - 1)));  // any exponent
     } else {
       num = dbl((uint64_t)(1023 + (int)(g() % 400) - 200) << 52 | (g() & ((1ull << 52) - 1)));
     }
