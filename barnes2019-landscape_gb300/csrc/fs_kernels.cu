@@ -39,6 +39,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWalkThreads = 512;
 constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kPer = 8;   // entries per thread per expansion chunk (measured best of 4..16)
+constexpr int kLevelCache = 2048;  // level offsets a single grid's walk keeps in shared memory
 constexpr int kChunk = kPer * kWalkThreads;
 constexpr int kNewtonMaxIt = 1000;
 
@@ -395,9 +396,6 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 
 // trunc_bits_to_float (fs_bits.h): truncation of a double to FP32 with
 // integer operations only (no FP64 pipe).
-__device__ __forceinline__ float trunc_to_float(double x) {
-  return trunc_bits_to_float((unsigned long long)__double_as_longlong(x));
-}
 
 __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   if (stopped(a.ctl)) return;
@@ -858,9 +856,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
   auto desc = [&](int r) -> const RealDesc & { return SINGLE ? d0 : a.desc[r]; };
   auto real_of = [&](int g) -> int { return SINGLE ? 0 : find_real(s_pre, nreal, g); };
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nthreads = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int warp_global = tid >> 5, nwarps = nthreads >> 5;
   const bool stamp = a.stamp && tid == 0;
   unsigned long long t_prev = stamp ? globaltimer_ns() : 0;
   auto lap = [&](int slot) {
@@ -1001,7 +997,11 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       }
     }
     if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
-    int any = 0;
+    // Thread r alone reads realization r's size (one load per block, not a
+    // load of one word by every thread). Every block sees the same sizes:
+    // an overflow ends the walk in all of them; other errors reach them at
+    // the next barrier's spin.
+    int any = 0, ovf = 0;
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
       const int added = ld_volatile_i32(&a.rctl[r].lvlcnt[j]);
       s_lo[r] = s_hi[r];
@@ -1009,16 +1009,18 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         s_hi[r] += added;
         s_nlev[r] = L + 2;
         any = 1;
-        if (s_hi[r] > desc(r).size) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
-        if (blockIdx.x == 0 && s_hi[r] <= desc(r).size)
+        if (s_hi[r] > desc(r).size) {
+          if (blockIdx.x == 0) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+          ovf = 1;
+        } else if (blockIdx.x == 0) {
           a.lvl_off[desc(r).lvl_base + L + 2] = s_hi[r];
+        }
       }
     }
+    if (__syncthreads_or(ovf)) return;
     if (!__syncthreads_or(any)) break;
-    if (ld_volatile_i32(&ctl->err) != 0) return;
     ++L;
   }
-  const int maxlev = L + 1;  // levels of the deepest realization
   // s_hi[r] is the realization's total; anything short of its size means
   // cells that never reached base level: the receivers contain a cycle.
   {
@@ -1073,9 +1075,38 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
   __syncthreads();
   const int maxlev = s_maxlev;
 
-  // Level Lv of every realization as [s_lo[r], s_hi[r]) (empty past its
-  // depth), and the prefix of its 32-entry groups over the batch.
+  // Level Lv of every realization as [lo_of(r), hi_of(r)) (empty past its
+  // depth), and the prefix of its 32-entry groups over the batch. A batch
+  // of one copies its level table into shared memory once (one load per
+  // entry and block) and takes each level's range from there into
+  // registers: no block barrier, scan or global load per level.
+  __shared__ int s_off[kLevelCache + 1];
+  if (SINGLE) {
+    const int n = min(maxlev, kLevelCache) + 1;
+    for (int k = threadIdx.x; k < n; k += kWalkThreads) s_off[k] = __ldcg(&a.lvl_off[d0.lvl_base + k]);
+    __syncthreads();
+  }
+  int lv_lo = 0, lv_hi = 0;
+  auto lo_of = [&](int r) -> int { return SINGLE ? lv_lo : s_lo[r]; };
+  auto hi_of = [&](int r) -> int { return SINGLE ? lv_hi : s_hi[r]; };
+  auto pre_of = [&](int r) -> int { return SINGLE ? 0 : s_pre[r]; };
   auto level_groups = [&](int Lv) -> int {
+    if (SINGLE) {
+      if (Lv < kLevelCache) {
+        lv_lo = s_off[Lv];
+        lv_hi = s_off[Lv + 1];
+      } else {  // deeper than the cache: one load per block
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          s_lo[0] = __ldcg(&a.lvl_off[d0.lvl_base + Lv]);
+          s_hi[0] = __ldcg(&a.lvl_off[d0.lvl_base + Lv + 1]);
+        }
+        __syncthreads();
+        lv_lo = s_lo[0];
+        lv_hi = s_hi[0];
+      }
+      return (lv_hi - lv_lo + 31) >> 5;
+    }
     __syncthreads();  // every warp is done with the previous ranges
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
       if (Lv < s_nlev[r]) {
@@ -1122,9 +1153,9 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
         G.r[u] = 0;
         if (g < ngroups) {
           const int r = real_of(g);
-          const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
+          const int i = lo_of(r) + 32 * (g - pre_of(r)) + lane;
           G.r[u] = r;
-          if (i < s_hi[r]) {
+          if (i < hi_of(r)) {
             const int off = desc(r).off;
             G.ok[u] = true;
             G.v[u] = __ldcg(&a.acc[off + i]);
@@ -1246,9 +1277,38 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   __syncthreads();
   const int maxlev = s_maxlev;
 
-  // Level Lv of every realization as [s_lo[r], s_hi[r]) (empty past its
-  // depth), and the prefix of its 32-entry groups over the batch.
+  // Level Lv of every realization as [lo_of(r), hi_of(r)) (empty past its
+  // depth), and the prefix of its 32-entry groups over the batch. A batch
+  // of one copies its level table into shared memory once (one load per
+  // entry and block) and takes each level's range from there into
+  // registers: no block barrier, scan or global load per level.
+  __shared__ int s_off[kLevelCache + 1];
+  if (SINGLE) {
+    const int n = min(maxlev, kLevelCache) + 1;
+    for (int k = threadIdx.x; k < n; k += kWalkThreads) s_off[k] = __ldcg(&a.lvl_off[d0.lvl_base + k]);
+    __syncthreads();
+  }
+  int lv_lo = 0, lv_hi = 0;
+  auto lo_of = [&](int r) -> int { return SINGLE ? lv_lo : s_lo[r]; };
+  auto hi_of = [&](int r) -> int { return SINGLE ? lv_hi : s_hi[r]; };
+  auto pre_of = [&](int r) -> int { return SINGLE ? 0 : s_pre[r]; };
   auto level_groups = [&](int Lv) -> int {
+    if (SINGLE) {
+      if (Lv < kLevelCache) {
+        lv_lo = s_off[Lv];
+        lv_hi = s_off[Lv + 1];
+      } else {  // deeper than the cache: one load per block
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          s_lo[0] = __ldcg(&a.lvl_off[d0.lvl_base + Lv]);
+          s_hi[0] = __ldcg(&a.lvl_off[d0.lvl_base + Lv + 1]);
+        }
+        __syncthreads();
+        lv_lo = s_lo[0];
+        lv_hi = s_hi[0];
+      }
+      return (lv_hi - lv_lo + 31) >> 5;
+    }
     __syncthreads();  // every warp is done with the previous ranges
     for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
       if (Lv < s_nlev[r]) {
@@ -1287,9 +1347,9 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
       Entry e{0, 0, 0, 0u, false};
       if (g < ngroups) {
         const int r = real_of(g);
-        const int i = s_lo[r] + 32 * (g - s_pre[r]) + lane;
+        const int i = lo_of(r) + 32 * (g - pre_of(r)) + lane;
         e.r = r;
-        if (i < s_hi[r]) {
+        if (i < hi_of(r)) {
           const int off = desc(r).off;
           e.ok = true;
           e.c = __ldcg(&a.ent[off + i]);
