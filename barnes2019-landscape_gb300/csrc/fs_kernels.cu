@@ -67,11 +67,20 @@ __device__ __forceinline__ bool stopped(const Ctl *ctl) {
   return (ld_volatile_i32(&ctl->err) | ld_volatile_i32(&ctl->abort_k)) != 0;
 }
 
-// Grid-wide barrier for a cooperative launch. Arrival counter only grows
+__device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch. The arrival counter only grows
 // during a launch (reset by the host before it), so barrier number `epoch`
-// completes when bar reaches epoch*gridDim.x. Every wait is bounded by
-// `timeout_ns` of wall time; on timeout, or when another block has already
-// raised an error, it returns false and the caller leaves the kernel.
+// completes when bar reaches epoch*gridDim.x. Arrival: the block barrier
+// orders the block's writes before thread 0's release reduction; wait:
+// thread 0's acquire loads see every block's release, and the closing block
+// barrier orders the rest of the block after them (the release/acquire
+// pattern of the CUTLASS grid barrier). Every wait is bounded by
+// `timeout_ns` of wall time; on timeout, or when another block has raised
+// an error (the error word is polled every 16 spins), it returns false and
+// the caller leaves the kernel.
 __device__ bool grid_barrier(Ctl *ctl, unsigned *bar, unsigned &epoch,
                              unsigned long long timeout_ns) {
   __shared__ int s_ok;
@@ -79,21 +88,20 @@ __device__ bool grid_barrier(Ctl *ctl, unsigned *bar, unsigned &epoch,
   if (threadIdx.x == 0) {
     ++epoch;
     const unsigned target = epoch * gridDim.x;
-    __threadfence();
-    atomicAdd(bar, 1u);
+    red_release_add_u32(bar, 1u);
     int ok = 1;
     const unsigned long long t0 = globaltimer_ns();
     unsigned spins = 0;
     while (ld_acquire_u32(bar) < target) {
-      if (ld_volatile_i32(&ctl->err) != 0) { ok = 0; break; }
-      if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
+      ++spins;
+      if ((spins & 15u) == 0 && ld_volatile_i32(&ctl->err) != 0) { ok = 0; break; }
+      if ((spins & 255u) == 0 && globaltimer_ns() - t0 > timeout_ns) {
         raise_err(ctl, FS_ERR_TIMEOUT, kPhaseBarrier);
         ok = 0;
         break;
       }
       __nanosleep(64);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
