@@ -26,6 +26,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "fastscape_gb300.h"
 #include "fs_bits.h"
@@ -901,14 +902,21 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
     const int j = L % 3;
     if (blockIdx.x == 0)
       for (int r = threadIdx.x; r < nreal; r += kWalkThreads) a.rctl[r].lvlcnt[(L + 1) % 3] = 0;
+    // Passes per warp in this level's chunks: kPer, or one for a single
+    // grid's level that fits one round of one-pass chunks over the grid, so
+    // that its chunks spread over more blocks (two compiled forms: a
+    // run-time pass count slows the big levels' expansion).
+    const bool one_pass = SINGLE && s_hi[0] - s_lo[0] <= (int)gridDim.x * kWalkThreads;
+    const int chunk = (one_pass ? 1 : kPer) * kWalkThreads;
     const int nchunks = block_prefix(
-        nreal, [&](int r) { return (s_hi[r] - s_lo[r] + kChunk - 1) / kChunk; }, s_pre);
-    for (int g = blockIdx.x; g < nchunks; g += gridDim.x) {
+        nreal, [&](int r) { return (s_hi[r] - s_lo[r] + chunk - 1) / chunk; }, s_pre);
+    auto expand = [&](auto passes, int g) {
+      constexpr int NP = decltype(passes)::value;
       const int r = real_of(g);
       const RealDesc &d = desc(r);
       const int hi = s_hi[r];
-      const int base = s_lo[r] + (g - s_pre[r]) * kChunk;
-      const int wbase = base + wid * (32 * kPer);
+      const int base = s_lo[r] + (g - s_pre[r]) * (NP * kWalkThreads);
+      const int wbase = base + wid * (32 * NP);
       int32_t *ent = a.ent + d.off;
       const uint8_t *mask = a.mask + d.off;
       const int offk = nbr_off(lane & 7, d.W);  // lane k < 8: offset of direction k
@@ -916,10 +924,10 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       // inclusive donor prefix (relative to the warp's first donor, below
       // 32 * 8 * kPer) packed as (prefix << 8) | mask, to keep the chunk's
       // state in registers across its barriers.
-      int cs[kPer];
-      unsigned mi[kPer];
+      int cs[NP];
+      unsigned mi[NP];
 #pragma unroll
-      for (int q = 0; q < kPer; q++) {
+      for (int q = 0; q < NP; q++) {
         const int i = wbase + 32 * q + lane;
         cs[q] = 0;
         mi[q] = 0;
@@ -930,7 +938,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       }
       int wtot = 0;
 #pragma unroll
-      for (int q = 0; q < kPer; q++) {
+      for (int q = 0; q < NP; q++) {
         int v = __popc(mi[q]);
 #pragma unroll
         for (int dd = 1; dd < 32; dd <<= 1) {
@@ -961,7 +969,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       const int cbase = hi + s_cbase[cbuf] + (wid ? s_cw[cbuf][wid - 1] : 0);
       cbuf ^= 1;
 #pragma unroll
-      for (int q = 0; q < kPer; q++) {
+      for (int q = 0; q < NP; q++) {
         const int i = wbase + 32 * q + lane;
         const unsigned msk = mi[q] & 0xFFu;
         const int incl = (int)(mi[q] >> 8);
@@ -1003,6 +1011,10 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         }
         __syncwarp();  // s_own is refilled by the next pass
       }
+        };
+    for (int g = blockIdx.x; g < nchunks; g += gridDim.x) {
+      if (one_pass) expand(std::integral_constant<int, 1>{}, g);
+      else expand(std::integral_constant<int, kPer>{}, g);
     }
     if (!grid_barrier(ctl, &ctl->bar, epoch, a.timeout_ns)) return;
     // Thread r alone reads realization r's size (one load per block, not a
