@@ -233,6 +233,40 @@ def cpu_sample(side: int, nsteps: int, prefer_reference: bool):
             f"{side}^2, {nsteps} timesteps after 1 warm-up")
 
 
+def cpu_steps_from(h: np.ndarray, side: int, params, nsteps: int):
+    """Times the oracle's restatement of fastscape_RB+P for nsteps timesteps
+    from the elevation h (copied) with the given oracle Params. Returns
+    (cell-steps/s, threads)."""
+    import ctypes
+
+    from oracle.pyoracle import FsoParams, Oracle
+    o = Oracle()
+    lib = o.lib
+
+    class Work(ctypes.Structure):
+        _fields_ = [("W", ctypes.c_int), ("H", ctypes.c_int)] + \
+                   [(n, ctypes.c_void_p) for n in ("rec", "ndon", "donor", "stack", "levels", "accum")] + \
+                   [("nlevel", ctypes.c_int)]
+    lib.fso_work_init.argtypes = [ctypes.POINTER(Work), ctypes.c_int, ctypes.c_int]
+    lib.fso_work_free.argtypes = [ctypes.POINTER(Work)]
+    lib.fso_step.argtypes = [ctypes.POINTER(Work), ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(FsoParams), ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_double)]
+    w = Work()
+    if lib.fso_work_init(ctypes.byref(w), side, side) != 0:
+        raise MemoryError("oracle work arrays")
+    hh = np.array(h, dtype=np.float64, copy=True)
+    pc = params.c()
+    hp = hh.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    lib.fso_step(ctypes.byref(w), hp, ctypes.byref(pc), 1, None)   # warm-up
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        lib.fso_step(ctypes.byref(w), hp, ctypes.byref(pc), 1, None)
+    dt = time.perf_counter() - t0
+    lib.fso_work_free(ctypes.byref(w))
+    return side * side * nsteps / dt, o.threads()
+
+
 def run_reference_arm(args, dist, rank, ws):
     if rank != 0:
         return
@@ -443,6 +477,76 @@ def run_sweep(args, dist, rank, ws, local):
         dist.destroy_process_group()
 
 
+DEEP_SIDE = 512
+DEEP_SPINUP = 2000
+DEEP_PARAMS = {"keq": 1e-5, "meq": 0.6, "ueq": 5e-3}
+
+
+def run_deep(args, dist, rank, ws, local):
+    """Long-run regime: a 512^2 grid after 2000 timesteps of strong uplift and
+    erosion (K 1e-5, m 0.6, U 5e-3: ~290 levels of at most a few thousand
+    cells each), where a timestep is dominated by the per-level latency of
+    the three level walks rather than by bandwidth or FP64 throughput.
+    Device cell-steps/s over 10 x --steps timesteps of that state (CUDA
+    events; the spin-up is untimed), with the CPU restatement of
+    fastscape_RB+P timed from the same elevations."""
+    import __graft_entry__ as ge
+    import torch  # noqa: F401
+    from oracle.pyoracle import workload_params as oracle_params
+    pkg = ge.load()
+    if ws > 1:
+        torch.cuda.set_device(local)
+    side = DEEP_SIDE
+    p = pkg.workload_params(**DEEP_PARAMS)
+    m = pkg.FastScape_RBP(side, side, params=p, init=pkg.INIT_PHILOX, seed=7 + rank)
+    m.step(DEEP_SPINUP)
+    tune = m.autotune(probe_steps=2)
+    m.step(args.warmup)
+    nsteps = 10 * args.steps
+    m.set_timing(True)
+    m.phase_times(reset=True)
+    m.synchronize()
+    barrier(dist)
+    with Clocks(local) as clk:
+        m.step(nsteps)
+    t = m.phase_times(reset=True)
+    dev_s = max_over_ranks(dist, float(t[3]) * 1e-3)
+    levels = int(m.levels()[1])
+    h = m.getH()
+    m.close()
+    if rank == 0:
+        value = ws * side * side * nsteps / dev_s
+        cpu = None
+        if ws == 1 and not args.no_cpu_baseline:
+            nst = 20
+            v, thr = cpu_steps_from(h, side, oracle_params(**DEEP_PARAMS), nst)
+            cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                   "sample": f"oracle restatement of fastscape_RB+P (OpenMP) from the same "
+                             f"{side}^2 state, {nst} timesteps after 1 warm-up"}
+        print(json.dumps({
+            "metric": f"cell-steps/s, {side}^2 after {DEEP_SPINUP} timesteps "
+                      "(K 1e-5 m 0.6 U 5e-3)",
+            "value": value, "unit": UNIT, "n_gpus": ws, "steps": nsteps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{side}x{side} FP64, Philox initial field, K 1e-5 m 0.6 "
+                                   f"n 1 U 5e-3 dt 1000 dx 100, after {DEEP_SPINUP} "
+                                   "untimed timesteps", "levels": levels, "launch": tune},
+            "kernel_ms": {"receivers": t[0] / nsteps, "donors_level0": t[1] / nsteps,
+                          "order": t[7] / nsteps, "accum": t[9] / nsteps,
+                          "erode": t[8] / nsteps},
+            "per_level_us": {"order": 1e3 * t[7] / nsteps / levels,
+                             "accum": 1e3 * t[9] / nsteps / levels,
+                             "erode": 1e3 * t[8] / nsteps / levels},
+            "gpu_launches": 6 * nsteps,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,9 +557,10 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep"],
+    ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep", "deep"],
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
-                         "256-realization batch; sweep: grid sizes 100..20000")
+                         "256-realization batch; sweep: grid sizes 100..20000; deep: a "
+                         "512^2 grid after 2000 timesteps of strong erosion (~290 levels)")
     ap.add_argument("--realizations", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=ENSEMBLE_STEPS,
                     help="ensemble: timesteps of the timed run (the metric's run length)")
@@ -473,6 +578,9 @@ def main():
         return
     if args.workload == "sweep":
         run_sweep(args, dist, rank, ws, local)
+        return
+    if args.workload == "deep":
+        run_deep(args, dist, rank, ws, local)
         return
 
     import __graft_entry__ as ge
