@@ -306,6 +306,61 @@ def test_receiver_filter_equals_fp64_formula(pkg):
         assert 0 < n.value < W * H // 100
 
 
+def serpentine(W, H):
+    """A channel snaking along every other row between walls 1000 m high,
+    descending 1 cm per cell to a single outlet next to the base-level
+    ring: one drainage path of thousands of cells, so thousands of levels
+    (2489 at 120x50)."""
+    h = np.full((H, W), 1000.0)
+    rows = list(range(3, H - 3, 2))
+    p = 0
+    for k, y in enumerate(rows):
+        xs = range(3, W - 3) if k % 2 == 0 else range(W - 4, 2, -1)
+        for x in xs:
+            p += 1
+            h[y, x] = p * 0.01
+        if k + 1 < len(rows):
+            p += 1
+            h[y + 1, W - 4 if k % 2 == 0 else 3] = p * 0.01
+    h[2, 3] = 0.005
+    h = h.reshape(-1).copy()
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    return h
+
+
+def test_thousands_of_levels(pkg, oracle):
+    """More levels than the walk kernels keep in shared memory (2048): every
+    level of a 2489-level drainage path, one-pass ordering chunks, the
+    level-table fallback of accumulation and erosion -- bit-identical to the
+    oracle at every timestep, alone and inside a batch."""
+    W, H = 120, 50
+    h = serpentine(W, H)
+    p = pkg.workload_params()
+    op = Params(*p.as_tuple())
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+        m.setH(h)
+        ho = h.copy()
+        for s in range(3):
+            m.step(1)
+            ref = oracle.phases(ho, W, H, op)
+            assert len(ref["levels"]) - 2 > 2048
+            assert_step_equal(m, W, H, ref, f"step {s}")
+    ws, hs = [W, 40, 90], [H, 30, 70]
+    with pkg.FastScapeBatch(ws, hs, [p] * 3, init=pkg.INIT_PHILOX, seeds=[1, 2, 3]) as b:
+        b.setH(0, h)
+        singles = []
+        for r in range(3):
+            mm = pkg.FastScape_RBP(ws[r], hs[r], params=p, init=pkg.INIT_ZERO)
+            mm.setH(b.getH(r))
+            singles.append(mm)
+        b.step(2)
+        for r, mm in enumerate(singles):
+            mm.step(2)
+            assert np.array_equal(b.getH(r), mm.getH()), f"batch r={r}"
+            mm.close()
+
+
 def test_receiver_fixup_on_flat_ground(pkg):
     """Flat-heavy terrain -- integer terraces (exact ties and zero slopes),
     +0 and -0, negative heights, neighbours one ulp apart -- sends most cells
