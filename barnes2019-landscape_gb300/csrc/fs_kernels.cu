@@ -886,11 +886,17 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
   // level keeps this level's order. Each realization's append counter
   // rotates over three words so a block that reads the size of level k after
   // the barrier never races with the reset for level k+2.
+  // s_tot[L & 1]: entries of level L over the batch (double-buffered: the
+  // next level's count is summed while this one's may still be read)
+  __shared__ int s_tot[2];
+  if (threadIdx.x == 0) s_tot[0] = s_tot[1] = 0;
+  __syncthreads();
   for (int r = threadIdx.x; r < nreal; r += kWalkThreads) {
     const RealDesc &d = desc(r);
     s_lo[r] = 0;
     s_hi[r] = d.nring + ld_volatile_i32(&a.rctl[r].top);
     s_nlev[r] = 1;
+    atomicAdd(&s_tot[0], s_hi[r]);
     if (blockIdx.x == 0) {
       a.lvl_off[d.lvl_base + 0] = 0;
       a.lvl_off[d.lvl_base + 1] = s_hi[r];
@@ -902,11 +908,12 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
     const int j = L % 3;
     if (blockIdx.x == 0)
       for (int r = threadIdx.x; r < nreal; r += kWalkThreads) a.rctl[r].lvlcnt[(L + 1) % 3] = 0;
-    // Passes per warp in this level's chunks: kPer, or one for a single
-    // grid's level that fits one round of one-pass chunks over the grid, so
-    // that its chunks spread over more blocks (two compiled forms: a
-    // run-time pass count slows the big levels' expansion).
-    const bool one_pass = SINGLE && s_hi[0] - s_lo[0] <= (int)gridDim.x * kWalkThreads;
+    // Passes per warp in this level's chunks: kPer, or one for a level that
+    // fits one round of one-pass chunks over the grid, so that its chunks
+    // spread over more blocks (two compiled forms: a run-time pass count
+    // slows the big levels' expansion).
+    const bool one_pass = s_tot[L & 1] <= (int)gridDim.x * kWalkThreads;
+    if (threadIdx.x == 0) s_tot[(L + 1) & 1] = 0;  // summed after this level's barrier
     const int chunk = (one_pass ? 1 : kPer) * kWalkThreads;
     const int nchunks = block_prefix(
         nreal, [&](int r) { return (s_hi[r] - s_lo[r] + chunk - 1) / chunk; }, s_pre);
@@ -1026,6 +1033,7 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
       const int added = ld_volatile_i32(&a.rctl[r].lvlcnt[j]);
       s_lo[r] = s_hi[r];
       if (added) {
+        atomicAdd(&s_tot[(L + 1) & 1], added);
         s_hi[r] += added;
         s_nlev[r] = L + 2;
         any = 1;
