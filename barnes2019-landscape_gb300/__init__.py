@@ -51,7 +51,7 @@ ABI_SYMBOLS = [
     "fs_autotune", "fs_launch_config",
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
-    "fs_test_set_receiver_path", "fs_test_receiver_fixups",
+    "fs_test_set_receiver_path", "fs_test_set_erosion_path", "fs_test_receiver_fixups",
     "fs_test_table_capacity",
 ]
 
@@ -156,6 +156,7 @@ def library() -> C.CDLL:
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
     L.fs_test_barrier_timeout.argtypes = [vp, C.c_double]
     L.fs_test_set_receiver_path.argtypes = [vp, C.c_int]
+    L.fs_test_set_erosion_path.argtypes = [vp, C.c_int]
     L.fs_test_receiver_fixups.argtypes = [vp, i32p]
     L.fs_test_table_capacity.argtypes = [vp, i32p]
     _lib = L
@@ -298,8 +299,8 @@ class FastScape_RBP:
         return self.launch_config()
 
     def use_int_sub(self, on: bool = True) -> None:
-        """n = 1: the erosion's elevation subtractions in integer arithmetic
-        (same results; fs_autotune chooses by speed)."""
+        """n = 1 or 2: the erosion's elevation subtractions in integer
+        arithmetic (same results; fs_autotune chooses by speed)."""
         check(library().fs_use_int_sub(self._m, int(bool(on))))
 
     def launch_config(self):

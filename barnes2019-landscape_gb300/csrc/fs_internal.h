@@ -149,8 +149,11 @@ struct StepArgs {
   int nmode;
   double neq;
   int do_erode;            // 0: ordering + accumulation only
-  int erode_isub;          // 1: the n = 1 erosion subtracts elevations in
-                           // integer arithmetic (host-side launch choice)
+  int erode_isub;          // 1: the n = 1 / n = 2 erosion subtracts
+                           // elevations in integer arithmetic (host-side
+                           // launch choice)
+  int erode_generic;       // 1: the reference's Newton loop literally, for
+                           // every n (a test of the fast paths)
   int stamp;               // 1: accumulate phase times into ctl->walk_ns
   unsigned long long timeout_ns;
 };
@@ -173,7 +176,9 @@ cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s);  
 cudaError_t launch_accum(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_accum
 cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s);  // k_erode
 int walk_threads();
-const void *walk_kernel_ptr(int nmode, bool single, bool isub = false);  // k_erode
+// k_erode: var 0 FP64 subtractions, 1 integer subtractions (n = 1, 2), 2 the
+// reference's loop literally
+const void *walk_kernel_ptr(int nmode, bool single, int var = 0);
 const void *order_kernel_ptr(bool single, int bps);     // k_order for bps 2 or 3
 const void *accum_kernel_ptr(bool single);              // k_accum
 constexpr int kAccumMaxBps = 4;                         // k_accum's register budget

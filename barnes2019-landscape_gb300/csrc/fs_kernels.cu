@@ -733,6 +733,78 @@ __device__ __forceinline__ uint64_t add_correction(uint64_t x, uint64_t y) {
   return (y & kSignBit) ? sub_far(x, y ^ kSignBit) : uplift_bits(x, y);
 }
 
+// RN(x / y) of bit patterns on the FP64 pipe.
+__device__ __forceinline__ uint64_t fdiv_bits(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+      "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(b));
+  return r;
+}
+
+// RN(x - y) for any operands: in integer arithmetic when both are positive
+// normal (sub_near_bits within a factor 2, sub_far_bits from an exponent gap
+// of 2) or x is positive and y negative (add_pos_rn_bits), else in FP64.
+__device__ __forceinline__ uint64_t sub_gen(uint64_t x, uint64_t y) {
+  if (add_pos_operand(x)) {
+    if (add_pos_operand(y)) {
+      if (x != y) {
+        const bool gt = x > y;
+        const uint64_t hi = gt ? x : y, lo = gt ? y : x;
+        const uint64_t r = ((int)(hi >> 52) - (int)(lo >> 52) >= 2) ? sub_far_bits(hi, lo)
+                                                                     : sub_near_bits(hi, lo);
+        if (r) return gt ? r : (r ^ kSignBit);
+      }
+    } else if (add_pos_operand(y ^ kSignBit)) {
+      return add_pos_rn_bits(x, y ^ kSignBit);
+    }
+  }
+  return fadd_bits_volatile(x, y ^ kSignBit);
+}
+
+// Erosion of one cell for n = 2 (fastscape_RB.cpp:315-326; pow(x,2) as x*x,
+// pow(x,1) = x) on bit patterns, iterate by iterate in the reference's
+// operation order: x' = RN(x - RN(num/den)) with
+//   num = RN(RN(x - h0) + RN(fact*RN(RN(x-hn)^2))),
+//   den = RN(1 + RN(RN(fact*n)*RN(x-hn))),
+// RN(fact*n) hoisted (the reference's grouping), the first iterate's
+// x - h0 = +0 dropped, and |x' - x| <= tol proven in FP32 for most
+// iterates without the subtraction. With ISUB the subtractions run in
+// integer arithmetic.
+template <bool ISUB>
+__device__ __forceinline__ uint64_t erode_cell_n2(const RealDesc &d, double neq, Ctl *ctl,
+                                                  uint64_t factb, uint64_t h0, uint64_t hn) {
+  auto sub = [](uint64_t x, uint64_t y) { return ISUB ? sub_gen(x, y) : fadd_bits(x, y ^ kSignBit); };
+  constexpr uint64_t kOne = 0x3FF0000000000000ull;
+  const uint64_t fact2 = fmul_bits(factb, (uint64_t)__double_as_longlong(neq));
+  uint64_t x = h0;
+  for (int it = 1;; ++it) {
+    const uint64_t dx = sub(x, hn);
+    const uint64_t fpn = fmul_bits(factb, fmul_bits(dx, dx));
+    uint64_t num;
+    if (it == 1) {
+      num = (fpn << 1) == 0 ? 0 : fpn;  // RN(+0 + fpn)
+    } else {
+      const uint64_t a = sub(x, h0);
+      num = ISUB ? sub_gen(fpn, a ^ kSignBit) : fadd_bits(a, fpn);
+    }
+    const uint64_t den = fadd_bits(kOne, fmul_bits(fact2, dx));
+    const uint64_t q = fdiv_bits(num, den);
+    const uint64_t xn = sub(x, q);
+    if (step_below_tol(q ^ kSignBit, x, d)) return xn;
+    const uint64_t df = sub(xn, x);
+    x = xn;
+    // fabs(diff) > tol as an integer compare (a NaN diff stops the loop)
+    const long long m = (long long)(df & ~kSignBit);
+    if (!(m > d.tol_bits && m <= 0x7FF0000000000000ll)) return x;
+    if (it >= kNewtonMaxIt) {
+      raise_err(ctl, FS_ERR_NEWTON, kPhaseErode);
+      return x;
+    }
+  }
+}
+
 // Erosion of one cell for n = 1 (fastscape_RB.cpp:315-326) on bit
 // patterns: h0 the uplifted elevation, hn the receiver's final elevation,
 // t the table record of the cell's drainage count and direction class
@@ -1274,8 +1346,12 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
 // counts (and uplifted the pits). A kernel of its own: the ordering and
 // accumulation run with more resident threads than the register-hungry FP64
 // erosion allows.
-template <int NMODE, bool SINGLE, bool ISUB>
+// VAR 0: subtractions of elevations on the FP64 pipe; 1: in integer
+// arithmetic (n = 1, 2); 2: the reference's Newton loop literally, for every
+// n (a test of the fast paths).
+template <int NMODE, bool SINGLE, int VAR>
 __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
+  constexpr bool ISUB = VAR == 1, GENERIC = VAR == 2;
   extern __shared__ int smem[];
   const int nreal = a.nreal;
   int *s_lo = smem;
@@ -1416,9 +1492,13 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
         const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
         const uint64_t h0 = uplift_bits(hg.hc, udt);
         uint64_t hnew;
-        if (NMODE == kNOne) {
+        if (NMODE == kNOne && !GENERIC) {
           const unsigned long long *Tb = reinterpret_cast<const unsigned long long *>(d.tab) + rec_at;
           hnew = erode_cell_n1<ISUB>(d, ctl, Tb, load_tab_n1(Tb), h0, hg.hn);
+        } else if (NMODE == kNTwo && !GENERIC) {
+          hnew = erode_cell_n2<ISUB>(d, a.neq, ctl,
+                                     __ldg(reinterpret_cast<const unsigned long long *>(d.tab) + rec_at),
+                                     h0, hg.hn);
         } else {
           hnew = (uint64_t)__double_as_longlong(
               erode_cell<NMODE>(d, a.neq, ctl, d.tab + rec_at, __longlong_as_double(h0),
@@ -1636,19 +1716,23 @@ size_t walk_smem_bytes(int nreal) { return sizeof(int) * (4 * (size_t)nreal + 1)
 
 int walk_threads() { return kWalkThreads; }
 
-const void *walk_kernel_ptr(int nmode, bool single, bool isub) {
+template <int NMODE, bool SINGLE>
+const void *erode_ptr(int var) {
+  if (var == 1) return reinterpret_cast<const void *>(&k_erode<NMODE, SINGLE, 1>);
+  if (var == 2) return reinterpret_cast<const void *>(&k_erode<NMODE, SINGLE, 2>);
+  return reinterpret_cast<const void *>(&k_erode<NMODE, SINGLE, 0>);
+}
+
+const void *walk_kernel_ptr(int nmode, bool single, int var) {
+  if (nmode == kNGeneral) var = var == 2 ? 2 : 0;  // no integer variant
   if (single) {
-    if (nmode == kNOne)
-      return isub ? reinterpret_cast<const void *>(&k_erode<kNOne, true, true>)
-                  : reinterpret_cast<const void *>(&k_erode<kNOne, true, false>);
-    if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, true, false>);
-    return reinterpret_cast<const void *>(&k_erode<kNGeneral, true, false>);
+    if (nmode == kNOne) return erode_ptr<kNOne, true>(var);
+    if (nmode == kNTwo) return erode_ptr<kNTwo, true>(var);
+    return erode_ptr<kNGeneral, true>(var);
   }
-  if (nmode == kNOne)
-    return isub ? reinterpret_cast<const void *>(&k_erode<kNOne, false, true>)
-                : reinterpret_cast<const void *>(&k_erode<kNOne, false, false>);
-  if (nmode == kNTwo) return reinterpret_cast<const void *>(&k_erode<kNTwo, false, false>);
-  return reinterpret_cast<const void *>(&k_erode<kNGeneral, false, false>);
+  if (nmode == kNOne) return erode_ptr<kNOne, false>(var);
+  if (nmode == kNTwo) return erode_ptr<kNTwo, false>(var);
+  return erode_ptr<kNGeneral, false>(var);
 }
 
 const void *order_kernel_ptr(bool single, int bps) {
@@ -1668,8 +1752,8 @@ cudaError_t prepare_walk_kernels() {
   const int bytes = (int)walk_smem_bytes(kMaxReal);
   for (int single = 0; single < 2; single++) {
     for (int nm = 0; nm < 3; nm++) {
-      for (int isub = 0; isub < 2; isub++) {
-        cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0, isub != 0),
+      for (int var = 0; var < 3; var++) {
+        cudaError_t e = cudaFuncSetAttribute(walk_kernel_ptr(nm, single != 0, var),
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
       }
@@ -1769,7 +1853,8 @@ cudaError_t launch_order(const StepArgs &a, int sms, int bps, cudaStream_t s) {
 cudaError_t launch_erode(const StepArgs &a, int sms, int bps, cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
-  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1, a.erode_isub != 0),
+  return cudaLaunchCooperativeKernel(walk_kernel_ptr(a.nmode, a.nreal == 1,
+                                                     a.erode_generic ? 2 : a.erode_isub ? 1 : 0),
                                      dim3(sms * bps),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
 }

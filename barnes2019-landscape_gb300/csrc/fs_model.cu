@@ -129,6 +129,7 @@ struct fs_batch {
   bool have_step = false;
   bool timing = false;
   bool exact_receivers = false;
+  bool erode_generic = false;                    // test: the reference's Newton loop literally
   bool use_graph = false;
   cudaGraphExec_t graph = nullptr;
   bool graph_dirty = true;
@@ -258,6 +259,7 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.neq = b->neq;
   a.do_erode = do_erode;
   a.erode_isub = b->erode_isub;
+  a.erode_generic = b->erode_generic ? 1 : 0;
   a.stamp = b->timing ? 1 : 0;
   a.timeout_ns = b->timeout_ns;
   return a;
@@ -851,7 +853,7 @@ int autotune(fs_batch *b, int probe, int *chosen) {
       }
     }
   }
-  if (st == FS_OK && b->nmode == fs::kNOne) {
+  if (st == FS_OK && b->nmode != fs::kNGeneral) {
     float ms = 0;
     st = time_config(best_obps, best_bps, best_graph, 1, &ms);
     if (st == FS_OK && ms < best) {
@@ -1132,7 +1134,7 @@ int fs_batch_use_graph(fs_batch *b, int enable) {
 
 int fs_batch_use_int_sub(fs_batch *b, int enable) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
-  b->erode_isub = enable != 0 && b->nmode == fs::kNOne ? 1 : 0;
+  b->erode_isub = enable != 0 && b->nmode != fs::kNGeneral ? 1 : 0;
   b->graph_dirty = true;
   return FS_OK;
 }
@@ -1212,6 +1214,13 @@ int fs_test_order_from_receivers(fs_model *m, const int32_t *dir) {
 int fs_test_set_receiver_path(fs_model *m, int exact) {
   FS_MODEL(m);
   m->b->exact_receivers = exact != 0;
+  m->b->graph_dirty = true;
+  return FS_OK;
+}
+
+int fs_test_set_erosion_path(fs_model *m, int generic) {
+  FS_MODEL(m);
+  m->b->erode_generic = generic != 0;
   m->b->graph_dirty = true;
   return FS_OK;
 }

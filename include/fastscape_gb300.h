@@ -219,12 +219,12 @@ int fs_batch_get_phase_times(const fs_batch *b, double *ms, int reset);
 /* Replays each timestep from a captured CUDA graph (1) or launches it
  * directly (0, default). */
 int fs_batch_use_graph(fs_batch *b, int enable);
-/* With n = 1, the erosion subtracts elevations in integer arithmetic (1) or
- * on the FP64 pipe (0, default); identical results, different speed
- * (fs_batch_autotune picks). Ignored for n != 1. */
+/* With n = 1 or 2, the erosion subtracts elevations in integer arithmetic
+ * (1) or on the FP64 pipe (0, default); identical results, different speed
+ * (fs_batch_autotune picks). Ignored for other n. */
 int fs_batch_use_int_sub(fs_batch *b, int enable);
 /* Times every launch configuration (blocks per SM of the ordering and
- * erosion kernels, graph or direct; for n = 1 then the best of these with
+ * erosion kernels, graph or direct; for n = 1 or 2 then the best of these with
  * the erosion's elevation subtractions in integer arithmetic) over
  * probe_steps timesteps of the batch's own state, restores the state and
  * keeps the fastest; chosen[0] = erosion kernel blocks per SM, chosen[1] =

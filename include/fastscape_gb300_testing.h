@@ -27,6 +27,12 @@ int fs_test_barrier_timeout(fs_model *m, double ms);
  * Both produce identical receivers. */
 int fs_test_set_receiver_path(fs_model *m, int exact);
 
+/* generic = 1: erode with the reference's Newton loop literally (FP64
+ * division every iterate, pow(x,1) = x, pow(x,2) = x*x) instead of the
+ * unrolled bit-pattern iterates, so that tests can compare the two paths
+ * bit for bit. */
+int fs_test_set_erosion_path(fs_model *m, int generic);
+
 /* Cells queued for the FP64 fix-up by the receiver filter in the last
  * timestep. */
 int fs_test_receiver_fixups(const fs_model *m, int32_t *count);

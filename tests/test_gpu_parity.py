@@ -162,6 +162,35 @@ def test_second_newton_iterate(pkg, oracle, int_sub):
             assert_step_equal(m, W, H, ref, f"step {s}")
 
 
+@pytest.mark.parametrize("n,int_sub", [(1, False), (1, True), (2, False), (2, True)])
+def test_erosion_equals_literal_newton_loop(pkg, n, int_sub):
+    """The unrolled bit-pattern erosion -- n = 1: the first and second
+    iterates; n = 2: every iterate -- with FP64 or integer subtractions gives
+    bit for bit the elevations of the reference's Newton loop evaluated
+    literally (FP64 division every iterate, pow(x,1) = x, pow(x,2) = x*x),
+    on terrain whose cells take several iterates. (n = 2 cannot be compared
+    bit for bit with the oracle, whose glibc pow(x, 2) is not always x*x.)"""
+    L = pkg.library()
+    W, H = 300, 200
+    rng = np.random.default_rng(31 + n)
+    p = pkg.workload_params(keq=5e-5, ueq=5e-3, meq=0.5) if n == 1 else pkg.reference_params()
+    h = rng.uniform(0, 300, W * H)
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as a, \
+            pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as b:
+        a.use_int_sub(int_sub)
+        assert a.launch_config()["erode_int_sub"] == int_sub
+        pkg.check(L.fs_test_set_erosion_path(b.handle, 1))
+        a.setH(h)
+        b.setH(h)
+        for s in range(6):
+            a.step(1)
+            b.step(1)
+            assert np.array_equal(a.receivers(), b.receivers()), f"step {s}"
+            assert np.array_equal(a.getH(), b.getH()), f"step {s}"
+
+
 def test_workload_1000_integer_subtractions(pkg, oracle):
     """run(120) of the 1000x1000 workload with the integer subtractions:
     bit-identical to the oracle, like the default erosion."""
@@ -177,7 +206,8 @@ def test_workload_1000_integer_subtractions(pkg, oracle):
 
 
 def test_integer_subtractions_ignored_for_general_n(pkg):
-    with pkg.FastScape_RBP(64, 64, params=pkg.reference_params(), init=pkg.INIT_PHILOX) as m:
+    p = pkg.workload_params(neq=1.5)
+    with pkg.FastScape_RBP(64, 64, params=p, init=pkg.INIT_PHILOX) as m:
         m.use_int_sub(True)
         assert not m.launch_config()["erode_int_sub"]
 
