@@ -477,6 +477,63 @@ def run_sweep(args, dist, rank, ws, local):
         dist.destroy_process_group()
 
 
+def run_refconst(args, dist, rank, ws, local):
+    """The reference's own constants (fastscape_RB.cpp:58-65: K 2e-6, n 2,
+    m 0.8, U 2e-3, dt 1000, dr {1, sqrt 2}, cell area 40000) on the 10000^2
+    reference field: n = 2 runs the multi-iterate Newton erosion. Device
+    cell-steps/s over --steps timesteps (CUDA events, after --warmup and the
+    autotuner), with the CPU restatement of fastscape_RB+P on a bounded
+    sample (2000^2, 2 timesteps) with the same constants."""
+    import __graft_entry__ as ge
+    import torch  # noqa: F401
+    from oracle.pyoracle import Oracle, Params as OParams
+    pkg = ge.load()
+    if ws > 1:
+        torch.cuda.set_device(local)
+    side = args.side
+    p = pkg.reference_params()
+    m = pkg.FastScape_RBP(side, side, params=p, init=pkg.INIT_REFERENCE, seed=123)
+    m.step(args.warmup)
+    tune = m.autotune(probe_steps=2)
+    m.set_timing(True)
+    m.phase_times(reset=True)
+    m.synchronize()
+    barrier(dist)
+    with Clocks(local) as clk:
+        m.step(args.steps)
+    t = m.phase_times(reset=True)
+    dev_s = max_over_ranks(dist, float(t[3]) * 1e-3)
+    levels = int(m.levels()[1])
+    m.close()
+    if rank == 0:
+        cpu = None
+        if ws == 1 and not args.no_cpu_baseline:
+            cs, nst = 2000, 2
+            h = Oracle().terrain(cs, cs, 0)
+            v, thr = cpu_steps_from(h, cs, OParams(*p.as_tuple()), nst)
+            cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+                   "sample": f"oracle restatement of fastscape_RB+P (OpenMP) with the same "
+                             f"constants, {cs}^2 reference field, {nst} timesteps after 1 warm-up"}
+        print(json.dumps({
+            "metric": f"cell-steps/s at {side}^2 FP64, reference constants (n 2)",
+            "value": ws * side * side * args.steps / dev_s, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"FastScape timestep, {side}x{side} FP64, reference initial "
+                                   "field, K 2e-6 n 2 m 0.8 U 2e-3 dt 1000 dr {1, sqrt 2}",
+                       "levels": levels, "launch": tune},
+            "kernel_ms": {"receivers": t[0] / args.steps, "donors_level0": t[1] / args.steps,
+                          "order": t[7] / args.steps, "accum": t[9] / args.steps,
+                          "erode": t[8] / args.steps},
+            "gpu_launches": 6 * args.steps,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 DEEP_SIDE = 512
 DEEP_SPINUP = 2000
 DEEP_PARAMS = {"keq": 1e-5, "meq": 0.6, "ueq": 5e-3}
@@ -557,10 +614,13 @@ def main():
     ap.add_argument("--e2e-calls", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="grid", choices=["grid", "ensemble", "sweep", "deep"],
+    ap.add_argument("--workload", default="grid",
+                    choices=["grid", "ensemble", "sweep", "deep", "refconst"],
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
                          "256-realization batch; sweep: grid sizes 100..20000; deep: a "
-                         "512^2 grid after 2000 timesteps of strong erosion (~290 levels)")
+                         "512^2 grid after 2000 timesteps of strong erosion (~290 levels); "
+                         "refconst: the 10000^2 timestep with the reference's own "
+                         "constants (n 2)")
     ap.add_argument("--realizations", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=ENSEMBLE_STEPS,
                     help="ensemble: timesteps of the timed run (the metric's run length)")
@@ -581,6 +641,9 @@ def main():
         return
     if args.workload == "deep":
         run_deep(args, dist, rank, ws, local)
+        return
+    if args.workload == "refconst":
+        run_refconst(args, dist, rank, ws, local)
         return
 
     import __graft_entry__ as ge
