@@ -16,12 +16,13 @@
 //                          and the implicit erosion solved upward from base
 //                          level (:306-328, in the level order of
 //                          fastscape_RB+P.cpp:319-350).
-//   In both, all realizations walk their levels in lock step, so one grid
-//   barrier per level serves the whole batch.
+//   In the three walk kernels all realizations walk their levels in lock
+//   step, so one grid barrier per level serves the whole batch.
 //
 // Floating point follows the reference's operation order exactly; the whole
-// file is compiled with -fmad=false so no multiply-add is contracted, and
-// every FP64 division is correctly rounded.
+// file is compiled with -fmad=false so no multiply-add is contracted, every
+// FP64 division is correctly rounded, and the additions and subtractions
+// done in integer arithmetic (fs_bits.h) give the bits of the FP64 ones.
 #include <cuda_runtime.h>
 
 #include <cmath>
