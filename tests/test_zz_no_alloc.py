@@ -34,11 +34,11 @@ def _field(W, H, seed):
     return h
 
 
-@pytest.mark.parametrize("W,H", [(300, 200), (512, 512)])
-def test_noalloc_matches_allocating_entry_point(pkg, W, H):
+@pytest.mark.parametrize("W,H,n", [(300, 200, 1), (512, 512, 1), (300, 200, 2)])
+def test_noalloc_matches_allocating_entry_point(pkg, W, H, n):
     torch = pytest.importorskip("torch")
     step_noalloc = _noalloc(pkg)
-    p = pkg.workload_params()
+    p = pkg.workload_params() if n == 1 else pkg.reference_params()
     h0 = _field(W, H, W + H)
     d_h = torch.from_numpy(h0.copy()).cuda()
     with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
