@@ -1433,60 +1433,70 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   // their first read (uplift of every interior cell precedes erosion in the
   // reference; a cell's h is read first by its own erosion, its receiver's
   // h is final).
+  // A warp erodes one 32-entry group per iteration, in a software pipeline:
+  // the entries (cell, receiver direction, drainage count) of the group two
+  // iterations ahead and the elevations of the next group are loaded before
+  // this group's erosion, so the chain entry -> elevation -> erosion of one
+  // group overlaps the erosion of the groups before it. A single grid also
+  // loads its first groups of the next level -- entries and the cells' own
+  // elevations, which this level does not change -- before the level's
+  // barrier; after it only the receivers' elevations remain to be gathered.
+  int ngroups = 0;  // groups of the level being eroded
+  struct Entry {
+    int c, dir, r;
+    uint32_t k;
+    bool ok;
+  };
+  struct Heights {
+    uint64_t hc, hn;  // bit patterns in integer registers (see fadd_bits)
+  };
+  auto load_entry = [&](int g) -> Entry {
+    Entry e{0, 0, 0, 0u, false};
+    if (g < ngroups) {
+      const int r = real_of(g);
+      const int i = lo_of(r) + 32 * (g - pre_of(r)) + lane;
+      e.r = r;
+      if (i < hi_of(r)) {
+        const int off = desc(r).off;
+        e.ok = true;
+        e.c = __ldcg(&a.ent[off + i]);
+        e.dir = __ldcg(&a.pdir[off + i]);
+        e.k = __ldcg(&a.acc[off + i]);
+      }
+    }
+    return e;
+  };
+  auto gather_hc = [&](const Entry &e) -> uint64_t {
+    return e.ok ? __ldcg(reinterpret_cast<const unsigned long long *>(a.h + desc(e.r).off) + e.c)
+                : 0ull;
+  };
+  auto gather_hn = [&](const Entry &e) -> uint64_t {
+    // a group lies in one realization: lane k < 8 holds direction k's offset
+    const int offk = SINGLE ? offk0 : nbr_off(lane & 7, desc(e.r).W);
+    const int ro = __shfl_sync(kFull, offk, e.dir & 7);
+    return e.ok ? __ldcg(reinterpret_cast<const unsigned long long *>(a.h + desc(e.r).off) +
+                         e.c + ro)
+                : 0ull;
+  };
+  const int gstride = nwarps;
+  Entry e1{}, e2{};
+  Heights h1{0, 0};
+  bool ahead = false;  // e1, e2 and h1.hc already hold this level's first groups
   for (int Lv = 1; Lv < maxlev; ++Lv) {
-    const int ngroups = level_groups(Lv);
-    // A warp erodes one 32-entry group per iteration, in a software
-    // pipeline: the entries (cell, receiver direction, drainage count) of the
-    // group two iterations ahead and the elevations of the next group are
-    // loaded before this group's erosion, so the chain entry -> elevation ->
-    // erosion of one group overlaps the erosion of the groups before it.
-    struct Entry {
-      int c, dir, r;
-      uint32_t k;
-      bool ok;
-    };
-    struct Heights {
-      uint64_t hc, hn;  // bit patterns in integer registers (see fadd_bits)
-    };
-    auto load_entry = [&](int g) -> Entry {
-      Entry e{0, 0, 0, 0u, false};
-      if (g < ngroups) {
-        const int r = real_of(g);
-        const int i = lo_of(r) + 32 * (g - pre_of(r)) + lane;
-        e.r = r;
-        if (i < hi_of(r)) {
-          const int off = desc(r).off;
-          e.ok = true;
-          e.c = __ldcg(&a.ent[off + i]);
-          e.dir = __ldcg(&a.pdir[off + i]);
-          e.k = __ldcg(&a.acc[off + i]);
-        }
-      }
-      return e;
-    };
-    auto gather = [&](const Entry &e) -> Heights {
-      Heights g{0, 0};
-      // a group lies in one realization: lane k < 8 holds direction k's offset
-      const int offk = SINGLE ? offk0 : nbr_off(lane & 7, desc(e.r).W);
-      const int ro = __shfl_sync(kFull, offk, e.dir & 7);
-      if (e.ok) {
-        const unsigned long long *hh =
-            reinterpret_cast<const unsigned long long *>(a.h + desc(e.r).off);
-        g.hc = __ldcg(&hh[e.c]);
-        g.hn = __ldcg(&hh[e.c + ro]);
-      }
-      return g;
-    };
-    const int gstride = nwarps;
-    Entry e1 = load_entry(warp_global);
-    Entry e2 = load_entry(warp_global + gstride);
-    Heights h1 = gather(e1);
+    ngroups = level_groups(Lv);
+    if (!ahead) {
+      e1 = load_entry(warp_global);
+      e2 = load_entry(warp_global + gstride);
+      h1.hc = gather_hc(e1);
+    }
+    h1.hn = gather_hn(e1);
     for (int g = warp_global; g < ngroups; g += gstride) {
       const Entry e = e1;
       const Heights hg = h1;
       e1 = e2;
       e2 = load_entry(g + 2 * gstride);
-      h1 = gather(e1);
+      h1.hc = gather_hc(e1);
+      h1.hn = gather_hn(e1);
       if (e.ok) {
         const RealDesc &d = desc(e.r);
         const size_t rec_at = (size_t)e.k * kTabStride + 4 * (e.dir & 1);
@@ -1510,8 +1520,14 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
         reinterpret_cast<unsigned long long *>(a.h + d.off)[e.c] = hnew;
       }
     }
-    if (Lv + 1 < maxlev && !grid_barrier(ctl, &ctl->bar2, epoch, a.timeout_ns)) return;
-  }
+    ahead = SINGLE && Lv + 1 < maxlev && Lv + 1 < kLevelCache;
+    if (ahead) {
+      ngroups = level_groups(Lv + 1);  // from the shared level table: no barrier
+      e1 = load_entry(warp_global);
+      e2 = load_entry(warp_global + gstride);
+      h1.hc = gather_hc(e1);
+    }
+    if (Lv + 1 < maxlev && !grid_barrier(ctl, &ctl->bar2, epoch, a.timeout_ns)) return;  }
   if (stamp) atomicAdd(&ctl->walk_ns[2], globaltimer_ns() - t_start);
   if (tid == 0) atomicAdd(&ctl->steps_done, 1);
 }
