@@ -1231,8 +1231,10 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
   // reduction. Integer sums are exact in any order. A count at level >= 1
   // beyond its realization's erosion table stops the timestep before any
   // elevation changes; the host grows the table and repeats it.
+  // Each level's ranges come from the finished level table, so the next
+  // level's are set up before this level's barrier.
+  int ngroups = maxlev > 1 ? level_groups(maxlev - 1) : 0;
   for (int Lv = maxlev - 1; Lv >= 1; --Lv) {
-    const int ngroups = level_groups(Lv);
     // 32-entry groups per warp per iteration. A single grid sums runs of
     // donors in the warp (more work per group) and loads the next groups
     // before reducing these; a batch reduces per donor and keeps more groups'
@@ -1318,6 +1320,7 @@ __global__ void __launch_bounds__(kWalkThreads, 4) k_accum(StepArgs a) {
         }
       }
     }
+    if (Lv > 1) ngroups = level_groups(Lv - 1);
     if (!grid_barrier(ctl, &ctl->bar3, epoch, a.timeout_ns)) return;
   }
   // Level 0: counts final. With no table exceeded, uplift the pits (level 0
@@ -1437,10 +1440,10 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   // the entries (cell, receiver direction, drainage count) of the group two
   // iterations ahead and the elevations of the next group are loaded before
   // this group's erosion, so the chain entry -> elevation -> erosion of one
-  // group overlaps the erosion of the groups before it. A single grid also
-  // loads its first groups of the next level -- entries and the cells' own
-  // elevations, which this level does not change -- before the level's
-  // barrier; after it only the receivers' elevations remain to be gathered.
+  // group overlaps the erosion of the groups before it. The next level's
+  // ranges and first groups -- entries and the cells' own elevations, which
+  // this level does not change -- are loaded before the level's barrier;
+  // after it only the receivers' elevations remain to be gathered.
   int ngroups = 0;  // groups of the level being eroded
   struct Entry {
     int c, dir, r;
@@ -1483,8 +1486,8 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   Heights h1{0, 0};
   bool ahead = false;  // e1, e2 and h1.hc already hold this level's first groups
   for (int Lv = 1; Lv < maxlev; ++Lv) {
-    ngroups = level_groups(Lv);
     if (!ahead) {
+      ngroups = level_groups(Lv);
       e1 = load_entry(warp_global);
       e2 = load_entry(warp_global + gstride);
       h1.hc = gather_hc(e1);
@@ -1520,9 +1523,9 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
         reinterpret_cast<unsigned long long *>(a.h + d.off)[e.c] = hnew;
       }
     }
-    ahead = SINGLE && Lv + 1 < maxlev && Lv + 1 < kLevelCache;
+    ahead = Lv + 1 < maxlev;
     if (ahead) {
-      ngroups = level_groups(Lv + 1);  // from the shared level table: no barrier
+      ngroups = level_groups(Lv + 1);  // reads only the finished level table
       e1 = load_entry(warp_global);
       e2 = load_entry(warp_global + gstride);
       h1.hc = gather_hc(e1);
