@@ -1064,11 +1064,12 @@ __global__ void __launch_bounds__(kWalkThreads, MINB) k_order(StepArgs a) {
         const int q_lo = __shfl_sync(kFull, incl - n_d, 0);
         const int q_n = __shfl_sync(kFull, incl, 31) - q_lo;  // <= 32 * 8
         {
-          unsigned m = msk;
           int slot = incl - n_d - q_lo;
-          while (m) {
-            s_own[wid][slot++] = (uint8_t)((lane << 3) | (__ffs(m) - 1));
-            m &= m - 1;
+          // every direction, predicated: no divergence across the warp (a
+          // loop over the set bits runs as long as the lane with most donors)
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            if (msk >> k & 1u) s_own[wid][slot++] = (uint8_t)((lane << 3) | k);
           }
         }
         __syncwarp();
