@@ -72,7 +72,7 @@ def erode_fp64_per_cell(int_sub: bool) -> int:
 
 
 FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12
-STEP_ALG_BYTES = 79        # survey accounting per cell-step (int32 receivers)
+STEP_ALG_BYTES = 79        # compulsory streaming bytes per cell-step with int32 receivers
 
 
 def load_peaks():
@@ -339,12 +339,16 @@ def run_reference_arm(args, dist, rank, ws):
 ENSEMBLE_STEPS = 200      # timesteps of one ensemble run
 
 
-def ensemble_spec(pkg, n: int, seed: int = 2019):
+def ensemble_spec(pkg, n: int, seed: int = 2019, side: int = 0):
     """The ragged ensemble: square sides log-uniform in [256, 2048], K
     log-uniform in [1e-6, 1e-5], m uniform in [0.3, 0.6], U log-uniform in
-    [1e-4, 5e-3] m/yr, n 1, dt 1000 yr, dx 100 m, seeded."""
+    [1e-4, 5e-3] m/yr, n 1, dt 1000 yr, dx 100 m, seeded. With `side` > 0
+    every realization is side x side (the parameters are drawn the same
+    way)."""
     rng = np.random.default_rng(seed)
     sides = np.exp(rng.uniform(np.log(256), np.log(2048), n)).astype(int)
+    if side > 0:
+        sides = np.full(n, side)
     params = [pkg.workload_params(keq=float(10 ** rng.uniform(-6, -5)),
                                   meq=float(rng.uniform(0.3, 0.6)),
                                   ueq=float(10 ** rng.uniform(-4, np.log10(5e-3))))
@@ -361,7 +365,8 @@ def run_ensemble(args, dist, rank, ws, local):
     pkg = ge.load()
     if ws > 1:
         torch.cuda.set_device(local)
-    sides, params = ensemble_spec(pkg, args.realizations, seed=2019 + rank)
+    sides, params = ensemble_spec(pkg, args.realizations, seed=2019 + rank,
+                                  side=args.ensemble_side)
     b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX,
                            seeds=list(range(1000 * rank, 1000 * rank + len(sides))))
     cells = b.cells()
@@ -384,6 +389,9 @@ def run_ensemble(args, dist, rank, ws, local):
     per_step = dt / nsteps
     value = ws * len(sides) / (nsteps * per_step)
     if rank == 0:
+        shape = "equal-size" if args.ensemble_side > 0 else "ragged"
+        side_desc = (f"{args.ensemble_side}" if args.ensemble_side > 0
+                     else "log-U[256,2048]")
         peak, peak_kind = load_peaks()
         kern = {"receivers": t[0] / 2, "donors_level0": t[1] / 2, "order": t[7] / 2,
                 "accum": t[9] / 2, "erode": t[8] / 2}
@@ -394,8 +402,8 @@ def run_ensemble(args, dist, rank, ws, local):
             "unit": "realizations/s", "n_gpus": ws, "steps": nsteps, "warmup": warm,
             "ms_per_step": 1e3 * per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"ragged ensemble of {len(sides)} realizations, sides "
-                                   "log-U[256,2048], K log-U[1e-6,1e-5], m U[0.3,0.6], "
+            "config": {"workload": f"{shape} ensemble of {len(sides)} realizations, sides "
+                                   f"{side_desc}, K log-U[1e-6,1e-5], m U[0.3,0.6], "
                                    "U log-U[1e-4,5e-3], n 1, dt 1000, dx 100",
                        "cells_per_step": cells, "cell_steps_per_s": cells / per_step,
                        "autotune": tune, "l2": "inputs larger than L2",
@@ -624,6 +632,10 @@ def main():
     ap.add_argument("--realizations", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=ENSEMBLE_STEPS,
                     help="ensemble: timesteps of the timed run (the metric's run length)")
+    ap.add_argument("--ensemble-side", type=int, default=0,
+                    help="ensemble: give every realization this edge instead of the ragged "
+                         "draw (1024 x 512 with 2000 timesteps is the plain batched method "
+                         "at the surrogate ensemble's shape)")
     ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
     args = ap.parse_args()
     if args.warmup < 3:
