@@ -38,6 +38,19 @@ FS_BITS_FN float trunc_bits_to_float(uint64_t b) {
   return float_from_bits(sign | ((uint32_t)e << 23) | frac);
 }
 
+// Fixed-point value of a double (bits b) in units of 2^(et - 1084), et a
+// biased exponent at least b's: the significand with 9 guard bits, shifted
+// right by et - e (bits below the unit truncated toward zero), signed.
+// |result| < 2^62, so the difference of two such values fits an int64.
+// Zeros, subnormals and values 63 or more binades below 2^(et-1023) give 0.
+FS_BITS_FN long long fixed_in_binade(uint64_t b, int et) {
+  const int e = (int)((b >> 52) & 0x7FF);
+  const int d = et - e;
+  if (e == 0 || d > 62) return 0;
+  const uint64_t mag = (((b & ((1ull << 52) - 1)) | (1ull << 52)) << 9) >> d;
+  return (b >> 63) ? -(long long)mag : (long long)mag;
+}
+
 // True when x is positive, normal and at most 2^1023 (biased exponent in
 // [1, 2045]): the operands add_pos_rn_bits accepts.
 FS_BITS_FN bool add_pos_operand(uint64_t x) {

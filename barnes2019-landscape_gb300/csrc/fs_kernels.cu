@@ -403,9 +403,25 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 //   best - second > 2E  and best > E  => q_best is the unique maximum > 0;
 //   best < -E                         => every q_n < 0 (NO_FLOW);
 // otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
+//
+// High ground: the bound grows with the elevations themselves, so on a tile
+// whose largest |h| reaches 2^(kRelEmin-1023) the values are staged relative
+// to the tile's first one instead: X = fixed_in_binade(h, et) (fs_bits.h;
+// et the tile's largest biased exponent, unit u = 2^(et-1084), truncation
+// error below u), f = RN32(X - X_ref) * u. Then
+// |f - (h - X_ref*u)| <= 2^-24 |h - X_ref*u| + 1.01 u, a common offset that
+// cancels in every difference h_c - h_n, so the same bound holds with M the
+// largest |f| of the relative values -- the tile's relief rather than its
+// height -- plus 2^22 u for the truncation:
+//   E/2 = 2^-20 * gmax * (M + 2^22 u).
+// Tiles up to 2^(kRelEmax-1022) qualify (f and u stay normal FP32); others,
+// and tiles below 2^(kRelEmin-1023), where truncation is already tight, keep
+// the truncated values.
 
 // trunc_bits_to_float (fs_bits.h): truncation of a double to FP32 with
 // integer operations only (no FP64 pipe).
+constexpr int kRelEmin = 1030;  // |h| >= 128
+constexpr int kRelEmax = 1123;  // |h| < 2^101
 
 __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   if (stopped(a.ctl)) return;
@@ -424,86 +440,155 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   constexpr int kSw = kRxTile + 2, kSn = (kRyTile + 2) * kSw;
   constexpr int kSPer = (kSn + 255) / 256;  // staged values per thread
   // all of a thread's loads in flight before the first is used
-  unsigned long long hv[kSPer];
   const int t0 = threadIdx.y * 32 + threadIdx.x;
-#pragma unroll
-  for (int k = 0; k < kSPer; k++) {
-    const int i = t0 + 256 * k;
+  auto load_value = [&](int tb, int k) -> unsigned long long {  // staged value tb + 256k
+    const int i = tb + 256 * k;
     const int ly = i / kSw, lx = i - ly * kSw;
     const int gx = x0 + lx, gy = y0 + ly;
-    hv[k] = 0;  // bits of +0.0
     if (i < kSn && gx < W && gy < H)
-      hv[k] = __ldg(reinterpret_cast<const unsigned long long *>(h) + (gy * W + gx));
-  }
+      return __ldg(reinterpret_cast<const unsigned long long *>(h) + (gy * W + gx));
+    return 0;  // bits of +0.0
+  };
+  // Truncated values first, with the tile's largest biased exponent, which
+  // decides whether the tile is staged again relative to its first cell.
+  __shared__ int s_wexp[8];
+  int ew = 0;
+  {
+    unsigned long long hv[kSPer];
 #pragma unroll
-  for (int k = 0; k < kSPer; k++) {
-    const int i = t0 + 256 * k;
-    if (i < kSn) {
-      const int ly = i / kSw, lx = i - ly * kSw;
-      const float f = trunc_bits_to_float(hv[k]);
-      s[ly][lx] = f;
-      m = fmaxf(m, fabsf(f));
-      bad |= !(f == f);
+    for (int k = 0; k < kSPer; k++) hv[k] = load_value(t0, k);
+#pragma unroll
+    for (int k = 0; k < kSPer; k++) {
+      const int i = t0 + 256 * k;
+      if (i < kSn) {
+        const int ly = i / kSw, lx = i - ly * kSw;
+        const float f = trunc_bits_to_float(hv[k]);
+        s[ly][lx] = f;
+        m = fmaxf(m, fabsf(f));
+        bad |= !(f == f);
+        ew = max(ew, (int)(hv[k] >> 52) & 0x7FF);
+      }
     }
   }
   const unsigned wm = __reduce_max_sync(kFull, __float_as_uint(m));  // m >= 0: bits order
-  if (threadIdx.x == 0) s_wmax[threadIdx.y] = wm;
+  ew = __reduce_max_sync(kFull, ew);
+  if (threadIdx.x == 0) {
+    s_wmax[threadIdx.y] = wm;
+    s_wexp[threadIdx.y] = ew;
+  }
   const bool tile_bad = __syncthreads_or(bad) != 0;
   float M = 0.f;
+  int et = 0;
 #pragma unroll
-  for (int w = 0; w < 8; w++) M = fmaxf(M, __uint_as_float(s_wmax[w]));
+  for (int w = 0; w < 8; w++) {
+    M = fmaxf(M, __uint_as_float(s_wmax[w]));
+    et = max(et, s_wexp[w]);
+  }
+  float absterm = 0x1p-100f;
+  const bool rel = et >= kRelEmin && et <= kRelEmax;  // block-uniform; no NaN then
+  if (rel) {
+    // Staged again relative to the tile's first cell (interior: tiles start
+    // at x, y >= 2), from a second read of the tile (cached). No thread
+    // reads s before the barrier below.
+    const long long xr = fixed_in_binade(
+        __ldg(reinterpret_cast<const unsigned long long *>(h) + (t.y0 * W + t.x0)), et);
+    const float unit = float_from_bits((uint32_t)(et - 1084 + 127) << 23);  // u
+    absterm = float_from_bits((uint32_t)(et - 1062 + 127) << 23);           // 2^22 u
+    // an opaque copy of t0: the indices are recomputed here instead of
+    // being kept in registers across the first pass
+    int tb;
+    asm volatile("mov.u32 %0, %1;" : "=r"(tb) : "r"(t0));
+    // two batches of loads in flight (one loop body: fewer registers)
+    constexpr int kHalf = (kSPer + 1) / 2;
+#pragma unroll 1
+    for (int k0 = 0; k0 < kSPer; k0 += kHalf) {
+      unsigned long long hv[kHalf];
+#pragma unroll
+      for (int k = 0; k < kHalf; k++) hv[k] = k0 + k < kSPer ? load_value(tb, k0 + k) : 0;
+#pragma unroll
+      for (int k = 0; k < kHalf; k++) {
+        const int i = tb + 256 * (k0 + k);
+        if (k0 + k < kSPer && i < kSn) {
+          const int ly = i / kSw, lx = i - ly * kSw;
+          s[ly][lx] = (float)(fixed_in_binade(hv[k], et) - xr) * unit;
+        }
+      }
+    }
+    __syncthreads();
+  }
   const float g_orth = d.g_orth, g_diag = d.g_diag;
-  const float E = 0x1p-19f * d.gmax * (M + 0x1p-100f);
+  const float cE = 0x1p-19f * d.gmax;
   const int lx = threadIdx.x + 1;
   const int gx = x0 + lx;
   unsigned qbits = 0;  // bit r: the cell of row lyb + r is queued
-  // Each thread takes 4 consecutive rows of its column, sliding a 3x3
-  // window down: 3 new shared loads per row.
+  // Each thread takes kRows consecutive rows of its column, sliding a 3x3
+  // window down: 3 new shared loads per row. LOCAL (relative tiles): M is
+  // the largest |f| of each cell's own window instead of the tile's, so a
+  // jump inside the tile (base level next to high ground) widens the bound
+  // only where it is.
   constexpr int kRows = kRyTile / 8;
   const int lyb = kRows * threadIdx.y + 1;
-  float u0 = s[lyb - 1][lx - 1], u1 = s[lyb - 1][lx], u2 = s[lyb - 1][lx + 1];
-  float m0 = s[lyb][lx - 1], m1 = s[lyb][lx], m2 = s[lyb][lx + 1];
-#pragma unroll
-  for (int r = 0; r < kRows; r++) {
-    const int ly = lyb + r;
-    const float d0 = s[ly + 1][lx - 1], d1 = s[ly + 1][lx], d2 = s[ly + 1][lx + 1];
-    const int gy = y0 + ly;
-    if (gx < W - 2 && gy < H - 2) {
-      const float fc = m1;
-      // Largest and second largest approximate slope. Within a direction
-      // class (orthogonal W N E S = codes 0 2 4 6, diagonal NW NE SE SW =
-      // 1 3 5 7) a_n = fl(fl(fc - f_n) * g) does not increase with f_n
-      // (rounding is monotone), so the class's largest and second largest
-      // slopes are those of its smallest and second smallest f -- the same
-      // values as over all eight slopes. bn is the direction of the largest;
-      // it is used only when the largest exceeds every other slope, when its
-      // f is the unique minimum of its class (a tie leaves best == second,
-      // which queues the cell). Without NaN in the tile no slope is NaN (an
-      // overflowing difference is +-Inf, and Inf - Inf below only queues).
-      const float lo1 = fminf(m0, m2), hi1 = fmaxf(m0, m2);  // W, E
-      const float lo2 = fminf(u1, d1), hi2 = fmaxf(u1, d1);  // N, S
-      const float lo3 = fminf(u0, u2), hi3 = fmaxf(u0, u2);  // NW, NE
-      const float lo4 = fminf(d2, d0), hi4 = fmaxf(d2, d0);  // SE, SW
-      const float omin = fminf(lo1, lo2), osec = fminf(fmaxf(lo1, lo2), fminf(hi1, hi2));
-      const float dmin = fminf(lo3, lo4), dsec = fminf(fmaxf(lo3, lo4), fminf(hi3, hi4));
-      const int oi = lo2 < lo1 ? (d1 < u1 ? 6 : 2) : (m2 < m0 ? 4 : 0);
-      const int di = lo4 < lo3 ? (d0 < d2 ? 7 : 5) : (u2 < u0 ? 3 : 1);
-      const float bo = (fc - omin) * g_orth, so = (fc - osec) * g_orth;
-      const float bd = (fc - dmin) * g_diag, sd = (fc - dsec) * g_diag;
-      const float best = fmaxf(bo, bd);
-      const float second = fmaxf(fminf(bo, bd), fmaxf(so, sd));
-      const int bn = bo > bd ? oi : di;
-      int code = -1;
-      if (!tile_bad) {
-        if (best - second > 2.f * E && best > E) code = bn;
-        else if (best < -E) code = kPit;
-      }
-      if (code != -1) rec[gy * W + gx] = (int8_t)code;
-      else qbits |= 1u << r;
+  auto rows = [&](auto local) {
+    constexpr bool LOCAL = decltype(local)::value;
+    float u0 = s[lyb - 1][lx - 1], u1 = s[lyb - 1][lx], u2 = s[lyb - 1][lx + 1];
+    float m0 = s[lyb][lx - 1], m1 = s[lyb][lx], m2 = s[lyb][lx + 1];
+    float E = cE * (M + absterm);
+    float cu = 0.f, cm = 0.f;  // LOCAL: largest |f| of the window's upper and middle rows
+    if (LOCAL) {
+      cu = fmaxf(fabsf(u0), fmaxf(fabsf(u1), fabsf(u2)));
+      cm = fmaxf(fabsf(m0), fmaxf(fabsf(m1), fabsf(m2)));
     }
-    u0 = m0; u1 = m1; u2 = m2;
-    m0 = d0; m1 = d1; m2 = d2;
-  }
+#pragma unroll
+    for (int r = 0; r < kRows; r++) {
+      const int ly = lyb + r;
+      const float d0 = s[ly + 1][lx - 1], d1 = s[ly + 1][lx], d2 = s[ly + 1][lx + 1];
+      if (LOCAL) {
+        const float cd = fmaxf(fabsf(d0), fmaxf(fabsf(d1), fabsf(d2)));
+        E = cE * (fmaxf(cu, fmaxf(cm, cd)) + absterm);
+        cu = cm;
+        cm = cd;
+      }
+      const int gy = y0 + ly;
+      if (gx < W - 2 && gy < H - 2) {
+        const float fc = m1;
+        // Largest and second largest approximate slope. Within a direction
+        // class (orthogonal W N E S = codes 0 2 4 6, diagonal NW NE SE SW =
+        // 1 3 5 7) a_n = fl(fl(fc - f_n) * g) does not increase with f_n
+        // (rounding is monotone), so the class's largest and second largest
+        // slopes are those of its smallest and second smallest f -- the same
+        // values as over all eight slopes. bn is the direction of the
+        // largest; it is used only when the largest exceeds every other
+        // slope, when its f is the unique minimum of its class (a tie leaves
+        // best == second, which queues the cell). Without NaN in the tile no
+        // slope is NaN (an overflowing difference is +-Inf, and Inf - Inf
+        // below only queues).
+        const float lo1 = fminf(m0, m2), hi1 = fmaxf(m0, m2);  // W, E
+        const float lo2 = fminf(u1, d1), hi2 = fmaxf(u1, d1);  // N, S
+        const float lo3 = fminf(u0, u2), hi3 = fmaxf(u0, u2);  // NW, NE
+        const float lo4 = fminf(d2, d0), hi4 = fmaxf(d2, d0);  // SE, SW
+        const float omin = fminf(lo1, lo2), osec = fminf(fmaxf(lo1, lo2), fminf(hi1, hi2));
+        const float dmin = fminf(lo3, lo4), dsec = fminf(fmaxf(lo3, lo4), fminf(hi3, hi4));
+        const int oi = lo2 < lo1 ? (d1 < u1 ? 6 : 2) : (m2 < m0 ? 4 : 0);
+        const int di = lo4 < lo3 ? (d0 < d2 ? 7 : 5) : (u2 < u0 ? 3 : 1);
+        const float bo = (fc - omin) * g_orth, so = (fc - osec) * g_orth;
+        const float bd = (fc - dmin) * g_diag, sd = (fc - dsec) * g_diag;
+        const float best = fmaxf(bo, bd);
+        const float second = fmaxf(fminf(bo, bd), fmaxf(so, sd));
+        const int bn = bo > bd ? oi : di;
+        int code = -1;
+        if (!tile_bad) {
+          if (best - second > 2.f * E && best > E) code = bn;
+          else if (best < -E) code = kPit;
+        }
+        if (code != -1) rec[gy * W + gx] = (int8_t)code;
+        else qbits |= 1u << r;
+      }
+      u0 = m0; u1 = m1; u2 = m2;
+      m0 = d0; m1 = d1; m2 = d2;
+    }
+  };
+  if (rel) rows(std::true_type{});
+  else rows(std::false_type{});
   // The queued cells of the tile, placed with one atomic per tile (a
   // counter shared by the whole grid would serialise on one address).
   int total;

@@ -423,6 +423,64 @@ def test_receiver_fixup_on_flat_ground(pkg):
         assert n.value > W * H // 10
 
 
+def relief(W, H, base, scale):
+    """A smooth tilted surface with gentle bumps, `base` metres up, rings at 0."""
+    yy, xx = np.divmod(np.arange(W * H), W)
+    h = base + scale * (0.05 * xx + 0.03 * yy + 4.0 * np.sin(xx / 53.0) * np.sin(yy / 41.0))
+    h[(xx <= 1) | (yy <= 1) | (xx >= W - 2) | (yy >= H - 2)] = 0
+    return h
+
+
+def test_receiver_filter_high_ground(pkg):
+    """Tiles whose heights reach 128 m are staged relative to their first
+    value, so the filter's error bound follows the tile's relief rather than
+    its height: the same relief 4000 m up sends no more cells to the FP64
+    fix-up than near sea level (staged by truncation), and the receivers
+    equal the FP64 formula's -- also on tiles mixing negative ground, zeros
+    and subnormals with high ground, values across a binade boundary, exact
+    flats, and heights beyond the relative range (1e35; with K = 0 there,
+    since no Newton iteration meets a 1e-3 m tolerance at 1e35 m)."""
+    import ctypes as C
+    W, H = 900, 700
+    p = pkg.workload_params()
+    L = pkg.library()
+    counts = []
+    for base in (1.0, 4000.0):
+        with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+            m.setH(relief(W, H, base, 1.0))
+            m.step(1)
+            n = C.c_int32(0)
+            pkg.check(L.fs_test_receiver_fixups(m.handle, C.byref(n)))
+            counts.append(n.value)
+    assert counts[1] <= counts[0] + 100, counts
+
+    rng = np.random.default_rng(31)
+    h = relief(W, H, 4000.0, 1.0)
+    yy, xx = np.divmod(np.arange(W * H), W)
+    interior = (xx > 1) & (yy > 1) & (xx < W - 2) & (yy < H - 2)
+    a_neg = interior & (xx < 150) & (yy < 200)
+    h[a_neg] = -3000.0 + rng.uniform(0, 50, a_neg.sum())
+    a_tiny = interior & (xx >= 200) & (xx < 300) & (yy < 300) & (np.arange(W * H) % 7 == 0)
+    h[a_tiny] = rng.choice([0.0, -0.0, 1e-300, 5e-324], a_tiny.sum())
+    a_huge = interior & (xx >= 400) & (xx < 440) & (yy >= 100) & (yy < 200)
+    h[a_huge] = 1e35 * rng.uniform(1, 2, a_huge.sum())
+    a_flat = interior & (xx >= 500) & (xx < 700) & (yy >= 300) & (yy < 400)
+    h[a_flat] = 5000.0
+    a_binade = interior & (xx >= 100) & (xx < 400) & (yy >= 450)
+    h[a_binade] = 4096.0 + rng.uniform(-1e-3, 1e-3, a_binade.sum())
+    p0 = pkg.workload_params(keq=0.0)
+    with pkg.FastScape_RBP(W, H, params=p0, init=pkg.INIT_ZERO) as a, \
+            pkg.FastScape_RBP(W, H, params=p0, init=pkg.INIT_ZERO) as b:
+        L.fs_test_set_receiver_path(b.handle, 1)
+        a.setH(h)
+        b.setH(h)
+        for s in range(3):
+            a.step(1)
+            b.step(1)
+            assert np.array_equal(a.receivers(), b.receivers()), f"step {s}"
+            assert np.array_equal(a.getH(), b.getH()), f"step {s}"
+
+
 def valley(W, H):
     """V-shaped valley whose axis runs down to the base-level ring at y = 1:
     nearly every cell drains into the axis, so the axis cell next to base

@@ -1,8 +1,10 @@
-"""The erosion kernel's integer-arithmetic operations (csrc/fs_bits.h, the
-same source the kernel compiles) checked on the host: the additions and
-subtractions of elevations against the hardware's RN operations, and the
-second Newton iterate's FP32 step decision against the exact iterate. The
-GPU parity tests check the device results bit for bit against the oracle."""
+"""The kernels' integer-arithmetic operations (csrc/fs_bits.h, the same
+source the kernels compile) checked on the host: the erosion's additions and
+subtractions of elevations against the hardware's RN operations, the second
+Newton iterate's FP32 step decision against the exact iterate, and the
+receiver filter's fixed-point staging of high ground against its error
+bound. The GPU parity tests check the device results bit for bit against the
+oracle."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -38,3 +40,19 @@ def test_second_iterate_step_decision(tmp_path):
         out = subprocess.run([str(exe), "3000000", str(seed)], capture_output=True, text=True)
         assert out.returncode == 0, out.stdout + out.stderr
         assert "all decisions equal to the exact iterate" in out.stdout
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_high_ground_staging_bound(tmp_path):
+    """fs::fixed_in_binade: a tile of high ground staged relative to its
+    first value, f = RN32(X - X_ref) * u, is within 2^-24 |h - X_ref u| + 1.01 u
+    of the exact relative height (checked in 128-bit integers)."""
+    exe = tmp_path / "tile_fixed_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(ROOT / "barnes2019-landscape_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "tile_fixed_check.cpp"), "-o", str(exe)],
+                   check=True)
+    for seed in (1, 2, 3):
+        out = subprocess.run([str(exe), "2000000", str(seed)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "all within the staging bound" in out.stdout
