@@ -404,19 +404,22 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 //   best < -E                         => every q_n < 0 (NO_FLOW);
 // otherwise (near-ties, zero slopes, NaN, |h| >= 2^128) the cell is queued.
 //
-// High ground: the bound grows with the elevations themselves, so on a tile
-// whose largest |h| reaches 2^(kRelEmin-1023) the values are staged relative
-// to the tile's first one instead: X = fixed_in_binade(h, et) (fs_bits.h;
-// et the tile's largest biased exponent, unit u = 2^(et-1084), truncation
-// error below u), f = RN32(X - X_ref) * u. Then
+// High ground: the bound grows with the elevations themselves, so a tile
+// whose largest |h| reaches 2^(kRelEmin-1023) is staged a second time,
+// relative to its first cell: X = fixed_in_binade(h, et) (fs_bits.h; et the
+// tile's largest biased exponent, unit u = 2^(et-1084), truncation error
+// below u), f = RN32(X - X_ref) * u. Then
 // |f - (h - X_ref*u)| <= 2^-24 |h - X_ref*u| + 1.01 u, a common offset that
 // cancels in every difference h_c - h_n, so the same bound holds with M the
-// largest |f| of the relative values -- the tile's relief rather than its
-// height -- plus 2^22 u for the truncation:
-//   E/2 = 2^-20 * gmax * (M + 2^22 u).
-// Tiles up to 2^(kRelEmax-1022) qualify (f and u stay normal FP32); others,
-// and tiles below 2^(kRelEmin-1023), where truncation is already tight, keep
-// the truncated values.
+// largest |f| of the relative values plus 2^22 u for the truncation:
+//   E/2 = 2^-20 * gmax * (M + 2^22 u),
+// and M is taken per cell over its own 3x3 window (the proof needs no
+// more), so a jump inside the tile -- base level beside high ground --
+// widens the bound only next to it. Tiles below 2^(kRelEmax-1022) qualify
+// (f and u stay normal FP32); others, and tiles below 2^(kRelEmin-1023),
+// where truncation is already tight, keep the truncated values and the
+// tile's M. tests/native/filter_bound_check.cpp restates these decisions on
+// the host and checks them against the FP64 formula.
 
 // trunc_bits_to_float (fs_bits.h): truncation of a double to FP32 with
 // integer operations only (no FP64 pipe).

@@ -1,10 +1,11 @@
 """The kernels' integer-arithmetic operations (csrc/fs_bits.h, the same
 source the kernels compile) checked on the host: the erosion's additions and
 subtractions of elevations against the hardware's RN operations, the second
-Newton iterate's FP32 step decision against the exact iterate, and the
+Newton iterate's FP32 step decision against the exact iterate, the
 receiver filter's fixed-point staging of high ground against its error
-bound. The GPU parity tests check the device results bit for bit against the
-oracle."""
+bound, and the filter's decisions (restated in FP32 on the host) against the
+FP64 reference formula. The GPU parity tests check the device results bit
+for bit against the oracle."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -56,3 +57,21 @@ def test_high_ground_staging_bound(tmp_path):
         out = subprocess.run([str(exe), "2000000", str(seed)], capture_output=True, text=True)
         assert out.returncode == 0, out.stdout + out.stderr
         assert "all within the staging bound" in out.stdout
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_receiver_filter_decisions(tmp_path):
+    """The receiver filter's FP32 decisions, restated operation for operation
+    on the host with both stagings (truncated; relative to the tile's first
+    cell with a per-cell bound), never differ from the FP64 reference formula
+    on cells they settle -- over random terrain with planted near-ties,
+    ties, jumps to base level and special values."""
+    exe = tmp_path / "filter_bound_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", str(ROOT / "barnes2019-landscape_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "filter_bound_check.cpp"), "-o", str(exe)],
+                   check=True)
+    for seed in (1, 2):
+        out = subprocess.run([str(exe), "30000", str(seed)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "all decisions exact" in out.stdout
