@@ -32,6 +32,9 @@ STATUS = {
     -7: "FS_ERR_NEWTON", -8: "FS_ERR_NOMEM", -9: "FS_ERR_STATE",
 }
 INIT_ZERO, INIT_REFERENCE, INIT_MT19937, INIT_PHILOX = 0, 1, 2, 3
+# fs_set_timing modes: per-kernel events (direct launches) or whole calls
+# (the launch path in use, CUDA-graph replay included)
+TIMING_OFF, TIMING_KERNELS, TIMING_CALL = 0, 1, 2
 
 # Exported C symbols, in header order (include/fastscape_gb300.h and
 # include/fastscape_gb300_testing.h).
@@ -278,8 +281,11 @@ class FastScape_RBP:
     def steps_executed(self) -> int:
         return int(library().fs_steps_executed(self._m))
 
-    def set_timing(self, on: bool = True) -> None:
-        check(library().fs_set_timing(self._m, int(bool(on))))
+    def set_timing(self, on=True) -> None:
+        """True / TIMING_KERNELS: per-kernel events (direct launches);
+        TIMING_CALL: events around whole calls only (graph replay kept);
+        False: off."""
+        check(library().fs_set_timing(self._m, int(on)))
 
     TIMERS = ("receivers", "donors_level0", "walk", "total",
               "walk_order", "walk_accumulation", "walk_erosion",
@@ -411,8 +417,9 @@ class FastScapeBatch:
         check(library().fs_batch_get_levels(self._b, int(r), _p(out, C.c_int32), C.byref(n)))
         return out, n.value
 
-    def set_timing(self, on: bool = True) -> None:
-        check(library().fs_batch_set_timing(self._b, int(bool(on))))
+    def set_timing(self, on=True) -> None:
+        """As FastScape_RBP.set_timing."""
+        check(library().fs_batch_set_timing(self._b, int(on)))
 
     def phase_times(self, reset: bool = False):
         out = np.zeros(len(FastScape_RBP.TIMERS), np.float64)

@@ -127,7 +127,7 @@ struct fs_batch {
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
-  bool timing = false;
+  int timing = 0;          // 0 off, 1 per kernel (direct launches), 2 whole calls
   bool exact_receivers = false;
   bool erode_generic = false;                    // test: the reference's Newton loop literally
   bool use_graph = false;
@@ -260,7 +260,7 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.do_erode = do_erode;
   a.erode_isub = b->erode_isub;
   a.erode_generic = b->erode_generic ? 1 : 0;
-  a.stamp = b->timing ? 1 : 0;
+  a.stamp = b->timing == 1 ? 1 : 0;
   a.timeout_ns = b->timeout_ns;
   return a;
 }
@@ -385,7 +385,7 @@ int batch_step(fs_batch *b, int k) {
     const int batch = k - done;
     const fs::StepArgs a = step_args(b, 1);
     FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, fs::kCtlCallResetBytes, b->stream));
-    if (b->timing) {
+    if (b->timing == 1) {
       if (int st = ensure_events(b, kEvPerStep * static_cast<size_t>(batch) + 1)) return st;
       for (int i = 0; i < batch; i++)
         if (int st = timed_step(b, a, i)) return st;
@@ -394,11 +394,24 @@ int batch_step(fs_batch *b, int k) {
     } else {
       if (b->use_graph && b->graph_dirty)
         if (int st = build_graph(b)) return st;
+      if (b->timing == 2) {
+        if (int st = ensure_events(b, 2)) return st;
+        FS_CUDA(cudaEventRecord(b->ev[0], b->stream));
+      }
       for (int i = 0; i < batch; i++) {
         if (b->use_graph && b->graph)
           FS_CUDA(cudaGraphLaunch(b->graph, b->stream));
         else
           FS_CUDA(launch_step(b, a));
+      }
+      if (b->timing == 2) {
+        // the whole call only: the launch path (graph replay or direct) is
+        // the one in use, with no event between its kernels
+        FS_CUDA(cudaEventRecord(b->ev[1], b->stream));
+        FS_CUDA(cudaEventSynchronize(b->ev[1]));
+        float tot = 0;
+        FS_CUDA(cudaEventElapsedTime(&tot, b->ev[0], b->ev[1]));
+        b->phase_ms[3] += tot;
       }
     }
     if (int st = collect_status(b)) return st;
@@ -810,9 +823,9 @@ int autotune(fs_batch *b, int probe, int *chosen) {
     release();
     return cuda_error(e, "autotune save");
   }
-  const bool timing = b->timing;
+  const int timing = b->timing;
   const long long steps = b->steps;
-  b->timing = false;
+  b->timing = 0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1034,8 +1047,7 @@ int64_t fs_steps_executed(const fs_model *m) { return m && m->b ? m->b->steps : 
 
 int fs_set_timing(fs_model *m, int enable) {
   FS_MODEL(m);
-  m->b->timing = enable != 0;
-  return FS_OK;
+  return fs_batch_set_timing(m->b, enable);
 }
 
 int fs_get_phase_times(const fs_model *m, double *ms, int reset) {
@@ -1116,7 +1128,10 @@ int fs_batch_info(const fs_batch *b, int *n, int64_t *cells) {
 
 int fs_batch_set_timing(fs_batch *b, int enable) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
-  b->timing = enable != 0;
+  if (enable < 0 || enable > FS_TIMING_CALL)
+    return set_error(FS_ERR_ARG, "timing mode must be 0, 1 or 2 (got %d)", enable);
+  if (b->timing != enable) b->graph_dirty = true;  // the walk's clock stamps change
+  b->timing = enable;
   return FS_OK;
 }
 

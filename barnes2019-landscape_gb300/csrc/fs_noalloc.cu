@@ -21,11 +21,18 @@
 //     image, so every GPU that loads the library holds it until the process
 //     exits;
 //   * every call on a device uses the same array and it keeps the last
-//     call's contents; calls that overlap on the GPU (two host threads, or
-//     two streams) race on it and must be serialized by the caller;
+//     call's contents; calls that overlap on the GPU race on it. The library
+//     serializes its own calls (a host mutex, and each call waits for its
+//     stream before returning), so two calls of this entry point do not
+//     overlap; what the caller must still order against the call's stream is
+//     its own work on d_h (kernels or copies in flight on other streams);
+//   * the input is checked for NaN/Inf first, as fs_set_elevation does
+//     (FS_ERR_NONFINITE, d_h untouched);
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) and the walk kernel's occupancy; make that first
-//     call before any stream capture.
+//     call before any stream capture. Later calls look the address up again
+//     and start over when it moved (after a cudaDeviceReset the module is
+//     loaded afresh and the array comes back zeroed).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -104,10 +111,13 @@ bool same_params(const fs_params &a, const fs_params &b) {
 }
 
 int setup_device(int dev, DeviceState &d) {
-  if (d.ready) return FS_OK;
   void *ptr = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&ptr, g_scratch);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+  if (d.ready && d.base == ptr) return FS_OK;
+  // first call on this device, or the module was reloaded (the array is
+  // zeroed and may sit elsewhere): nothing cached about it holds any more
+  d = DeviceState{};
   e = fs::prepare_walk_kernels();
   if (e != cudaSuccess) return cuda_fail(e, "walk smem attribute");
   int sms = 0;
@@ -256,9 +266,17 @@ extern "C" int fs_step_noalloc(double *d_h, int width, int height, const fs_para
   if (e == cudaSuccess) e = cudaMemsetAsync(a.rec, 0xff, size, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.mask, 0, size, s);
   if (e == cudaSuccess) e = fs::launch_place_rings(a.ent, width, height, s);
+  // NaN/Inf in the caller's field is refused before any timestep, like
+  // fs_set_elevation refuses it
+  if (e == cudaSuccess) e = fs::launch_check_finite(d_h, size, ctl, s);
+  int in_err = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&in_err, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, s);
   // the host copies above read static buffers this call rewrites next time
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(e, "scratch reset");
+  if (in_err == FS_ERR_NONFINITE) return fail(FS_ERR_NONFINITE, "input holds NaN or Inf");
+  if (in_err != 0) return fail(in_err, "input check failed on the device");
 
   for (int i = 0; i < nsteps; i++) {
     e = cudaMemsetAsync(reinterpret_cast<char *>(ctl) + fs::kCtlResetOffset, 0,

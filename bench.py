@@ -36,6 +36,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -75,6 +76,14 @@ FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12
 STEP_ALG_BYTES = 79        # compulsory streaming bytes per cell-step with int32 receivers
 
 
+def grid_config(side: int) -> dict:
+    """The workload description both arms print (identical dictionaries)."""
+    return {"workload": f"FastScape timestep, {side}x{side} FP64, reference initial field, "
+                        "K 2e-6 m 0.4 n 1 U 2e-3 dt 1000 dx 100",
+            "grid": [side, side], "step": "one timestep over the whole grid",
+            "l2": "inputs larger than L2 (h is 800 MB at 10000^2)"}
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -89,7 +98,7 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"fs_bench_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
@@ -115,13 +124,18 @@ class Clocks:
             self.proc.terminate()
             self.proc.wait()
             self.f.close()
+            self._text = self.path.read_text() if self.path.exists() else ""
+            try:
+                self.path.unlink()
+            except OSError:
+                pass
 
     def summary(self):
-        if self.proc is None or not self.path.exists():
+        if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.path.read_text().splitlines():
+        for line in getattr(self, "_text", "").splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -326,9 +340,7 @@ def run_reference_arm(args, dist, rank, ws):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"FastScape timestep, {side}x{side} FP64, K 2e-6 m 0.4 n 1 "
-                               f"U 2e-3 dt 1000 dx 100", "grid": [side, side],
-                   "step": "one timestep over the whole grid", "parallelism": "host cores"},
+        "config": grid_config(side), "parallelism": "host cores",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": kind,
                          "sample": f"{desc}, {args.steps} timesteps after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -673,16 +685,25 @@ def main():
     m.step(args.warmup)
     tune = m.autotune(probe_steps=2)      # launch shape; restores the state
     m.step(1)
-    m.set_timing(True)
+    # the timed region: the launch path the autotuner chose (graph replay or
+    # direct launches), CUDA events around the whole call on the model's
+    # stream and none between its kernels
+    m.set_timing(pkg.TIMING_CALL)
     m.phase_times(reset=True)
     barrier(dist)
     m.synchronize()
     with Clocks(local) as clk:
         m.step(args.steps)
     barrier(dist)
+    total_ms = max_over_ranks(dist, float(m.phase_times(reset=True)[3]))
+    # the same number of timesteps again, launched directly with an event
+    # between kernels, for the per-kernel split and the roofline
+    m.set_timing(pkg.TIMING_KERNELS)
+    m.phase_times(reset=True)
+    m.step(args.steps)
     t = m.phase_times(reset=True)
-    m.set_timing(False)
-    total_ms = max_over_ranks(dist, float(t[3]))
+    m.set_timing(pkg.TIMING_OFF)
+    split_total_ms = float(t[3])
     cells = side * side
     value = ws * cells * args.steps / (total_ms * 1e-3)
     # receivers filter + fix-up, donors/level 0, ordering, accumulation,
@@ -720,7 +741,7 @@ def main():
     if prof.exists():
         try:
             tr = json.loads(prof.read_text())
-            if dom in tr:   # ncu bytes per cell (profiles/kernels_step_4000.md) x cells
+            if dom in tr:   # ncu DRAM bytes per cell of the 4000^2 capture x cells
                 roofline["traffic"] = tr[dom]["bytes_per_cell"] * cells
         except (ValueError, KeyError):
             pass
@@ -760,19 +781,23 @@ def main():
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"FastScape timestep, {side}x{side} FP64, reference initial "
-                                   f"field, K 2e-6 m 0.4 n 1 U 2e-3 dt 1000 dx 100",
-                       "grid": [side, side], "step": "one timestep over the whole grid",
-                       "e2e_step": f"fs_set_elevation + fs_run({RUN_NSTEP}) "
-                                   f"({RUN_NSTEP + 1} timesteps) + fs_get_elevation",
-                       "l2": "inputs larger than L2 (h is 800 MB)",
-                       "launch": tune,
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": grid_config(side),
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "launch": dict(tune, timed_region="graph replay" if tune.get("graph")
+                           else "direct launches",
+                           kernel_split="direct launches with events between kernels, "
+                                        f"{args.steps} more timesteps",
+                           kernel_split_ms_per_step=split_total_ms / args.steps),
             "roofline": roofline,
             "step_roofline": {"alg_bytes_per_cell_step": STEP_ALG_BYTES,
                               "achieved_gbs": step_rf, "frac": step_rf / peak},
             "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": 8 * cells, "d2h_bytes_per_step": 8 * cells,
+                    "h2d_bytes_per_step": 8 * cells / (RUN_NSTEP + 1),
+                    "d2h_bytes_per_step": 8 * cells / (RUN_NSTEP + 1),
+                    "step": "one timestep; a call is fs_set_elevation + "
+                            f"fs_run({RUN_NSTEP}) ({RUN_NSTEP + 1} timesteps) + "
+                            "fs_get_elevation",
+                    "h2d_bytes_per_call": 8 * cells, "d2h_bytes_per_call": 8 * cells,
                     "calls": args.e2e_calls, "call_ms": [1e3 * x for x in call_s],
                     "statistic": "median call", "checksum": checksum},
             "gpu_launches": launches,

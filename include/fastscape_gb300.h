@@ -155,13 +155,21 @@ int64_t fs_steps_executed(const fs_model *m);
 
 /* Device time in milliseconds accumulated over timed fs_step/fs_run calls
  * since the last reset, measured with CUDA events on the model's stream
- * (enabled by fs_set_timing(m, 1)). ms[] holds FS_NUM_TIMERS values:
+ * (enabled by fs_set_timing(m, FS_TIMING_KERNELS)). ms[] holds FS_NUM_TIMERS
+ * values:
  *   0 receiver kernels, 1 donor/level-0 kernel, 2 level walk (both of
  *   its kernels), 3 whole timed calls (first event to last),
  *   4..6 split of the level walk measured inside it by the GPU clock
  *        (ordering, accumulation, uplift+erosion),
  *   7 ordering kernel, 8 erosion kernel, 9 accumulation kernel (events). */
 #define FS_NUM_TIMERS 10
+/* Timing modes: FS_TIMING_KERNELS launches each timestep's kernels directly
+ * with events between them (fills every timer); FS_TIMING_CALL keeps the
+ * launch path in use (CUDA-graph replay when chosen) and records events only
+ * around each call's launches (fills timer 3 alone). */
+#define FS_TIMING_OFF 0
+#define FS_TIMING_KERNELS 1
+#define FS_TIMING_CALL 2
 int fs_set_timing(fs_model *m, int enable);
 int fs_get_phase_times(const fs_model *m, double *ms, int reset);
 
@@ -245,6 +253,8 @@ int fs_batch_synchronize(const fs_batch *b);
  * row-major, the layout of fs_get_elevation) by exactly nsteps timesteps on
  * `stream` (a cudaStream_t; NULL for the default stream), with results
  * identical to fs_create + fs_set_elevation + fs_step, and waits for them.
+ * Like fs_set_elevation it refuses a field holding NaN or Inf
+ * (FS_ERR_NONFINITE, d_h left as it was).
  * No counterpart in the reference. It allocates nothing: for callers that
  * may not allocate device memory while running (a host application that
  * owns all device memory through its own pool, a latency-critical loop where
@@ -252,7 +262,9 @@ int fs_batch_synchronize(const fs_batch *b);
  * footprint). All scratch (~24 MB) is one static device array in the
  * library, held on every GPU that loads it until the process exits, shared
  * by all calls and keeping the last call's contents: calls that overlap on
- * the GPU race and must be serialized by the caller. Grids larger than
+ * the GPU race. The library itself serializes its calls (a lock, and each
+ * call waits for its stream), so the caller's part is to order its own
+ * other work on d_h against `stream`. Grids larger than
  * FS_NOALLOC_MAX_CELLS return FS_ERR_ARG. The first call on a device looks
  * up the array's device address; make it before any stream capture. */
 int fs_step_noalloc(double *d_h, int width, int height, const fs_params *params,

@@ -1,6 +1,6 @@
 // ref_harness.cpp -- C API around the reference's own FastScape_RB and
 // FastScape_RBP classes, used to PIN the oracle restatement. Test
-// infrastructure only: oracle/build_ref.py compiles this file together with
+// infrastructure only: oracle/build.py (--ref) compiles this file together with
 // the reference sources read from where they lie (never copied), and writes
 // the result only to oracle/_ref/. Nothing in the product path loads it.
 //

@@ -32,6 +32,19 @@ def test_cli_dem_matches_reference(tmp_path, golden, args):
     steps = [int(ln.split("=")[1]) for ln in lines if ln.startswith("p Step")]
     nstep = int(args[1])
     assert steps == list(range(0, nstep + 1, 20))
+    # the reference's timer columns, as its tests/d.make_tabular names them
+    # (tag, then the name with ':' dropped and spaces as '_')
+    cols = {}
+    for ln in lines:
+        if ln.startswith("t ") and "=" in ln:
+            name, val = ln[2:].split("=", 1)
+            cols[name.strip().replace(":", "").replace(" ", "_")] = val.split()[0]
+    want = ["Step1_Initialize", "Step2_DetermineReceivers", "Step3_DetermineDonors",
+            "Step4_GenerateOrder", "Step5_FlowAcc", "Step6_Uplift", "Step7_Erosion",
+            "Overall"]
+    assert all(c in cols for c in want), sorted(cols)
+    assert all(int(cols[c]) >= 0 for c in want)
+    assert int(cols["Step7_Erosion"]) > 0 and int(cols["Step6_Uplift"]) == 0
 
 
 def test_cli_usage_error():

@@ -60,3 +60,28 @@ def test_noalloc_rejects_grids_over_the_limit(pkg):
     st = step_noalloc(C.c_void_p(d_h.data_ptr()), 1024, 1024, C.byref(p), 1, None)
     assert st == -1
     assert "FS_NOALLOC_MAX_CELLS" in pkg.last_error()
+
+
+def test_noalloc_refuses_nonfinite_input(pkg):
+    """Like fs_set_elevation, the entry point refuses NaN/Inf in the caller's
+    field and leaves the buffer as it was; the next call still works."""
+    torch = pytest.importorskip("torch")
+    step_noalloc = _noalloc(pkg)
+    p = pkg.workload_params()
+    W, H = 64, 48
+    h0 = _field(W, H, 5)
+    bad = h0.copy()
+    bad[10 * W + 20] = np.nan
+    d_h = torch.from_numpy(bad.copy()).cuda()
+    st = step_noalloc(C.c_void_p(d_h.data_ptr()), W, H, C.byref(p), 2, None)
+    assert st == -5, pkg.last_error()
+    got = d_h.cpu().numpy()
+    assert np.array_equal(np.isnan(got), np.isnan(bad))
+    assert np.array_equal(got[~np.isnan(got)], bad[~np.isnan(bad)])
+    d_h = torch.from_numpy(h0.copy()).cuda()
+    assert step_noalloc(C.c_void_p(d_h.data_ptr()), W, H, C.byref(p), 2, None) == 0
+    with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_ZERO) as m:
+        m.setH(h0)
+        m.step(2)
+        torch.cuda.synchronize()
+        assert np.array_equal(d_h.cpu().numpy(), m.getH())
