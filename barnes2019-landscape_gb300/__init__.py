@@ -55,7 +55,7 @@ ABI_SYMBOLS = [
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_set_erosion_path", "fs_test_receiver_fixups",
-    "fs_test_table_capacity",
+    "fs_test_table_capacity", "fs_test_sg_conv",
 ]
 
 
@@ -162,6 +162,9 @@ def library() -> C.CDLL:
     L.fs_test_set_erosion_path.argtypes = [vp, C.c_int]
     L.fs_test_receiver_fixups.argtypes = [vp, i32p]
     L.fs_test_table_capacity.argtypes = [vp, i32p]
+    u16p = C.POINTER(C.c_uint16)
+    L.fs_test_sg_conv.argtypes = [C.c_int] * 7 + [u16p, u16p, C.POINTER(C.c_float), C.c_int,
+                                                  u16p, vp]
     _lib = L
     return L
 
@@ -455,3 +458,36 @@ class FastScapeBatch:
 
 def version() -> str:
     return library().fs_version().decode()
+
+
+def sg_conv(mode: int, x_bits: np.ndarray, w_bits: np.ndarray, taps: int = 9, bias=None,
+            relu: bool = False, mask_bits=None) -> np.ndarray:
+    """One convolution of the surrogate's tensor-core kernels on host arrays
+    (fs_test_sg_conv). mode 0: forward, x [B,H,W,cin], w [cout,taps,cin] ->
+    BF16 bits [B,H,W,cout]; mode 1: data gradient, x = dy [B,H,W,cout], w as
+    above, mask [B,H,W,cin] or None -> BF16 bits [B,H,W,cin]; mode 2: weight
+    gradient, x [B,H,W,cin], w = dy [B,H,W,cout] -> FP32 [cout,taps,cin]."""
+    x_bits = np.ascontiguousarray(x_bits, np.uint16)
+    w_bits = np.ascontiguousarray(w_bits, np.uint16)
+    B, H, W = x_bits.shape[:3]
+    if mode == 2:
+        cin, cout = x_bits.shape[3], w_bits.shape[3]
+        out = np.empty((cout, taps, cin), np.float32)
+    else:
+        cout, t, cin = w_bits.shape
+        if t != taps:
+            raise ValueError("weights do not match taps")
+        out = np.empty((B, H, W, cout if mode == 0 else cin), np.uint16)
+    u16 = C.POINTER(C.c_uint16)
+    bp = None
+    if bias is not None:
+        bias = np.ascontiguousarray(bias, np.float32)
+        bp = bias.ctypes.data_as(C.POINTER(C.c_float))
+    mp = None
+    if mask_bits is not None:
+        mask_bits = np.ascontiguousarray(mask_bits, np.uint16)
+        mp = mask_bits.ctypes.data_as(u16)
+    check(library().fs_test_sg_conv(int(mode), B, H, W, cin, cout, int(taps),
+                                    x_bits.ctypes.data_as(u16), w_bits.ctypes.data_as(u16), bp,
+                                    int(bool(relu)), mp, out.ctypes.data_as(C.c_void_p)))
+    return out

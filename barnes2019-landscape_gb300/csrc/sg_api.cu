@@ -1,0 +1,120 @@
+// sg_api.cu -- C ABI of the learned surrogate's kernels: the test entry
+// point for single convolutions (include/fastscape_gb300_testing.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "fastscape_gb300.h"
+#include "fastscape_gb300_testing.h"
+#include "fs_internal.h"
+#include "sg_internal.h"
+
+namespace {
+
+int sg_fail(int status, const char *fmt, const char *what) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), fmt, what ? what : "");
+  return fs::record_error(status, buf);
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  return fs::record_error(FS_ERR_CUDA, buf);
+}
+
+// Device buffers of one test call, released on every path.
+struct Bufs {
+  void *p[8] = {};
+  int n = 0;
+  ~Bufs() {
+    for (int i = 0; i < n; i++) cudaFree(p[i]);
+  }
+  template <class T>
+  cudaError_t alloc(T **out, size_t bytes) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes < 16 ? 16 : bytes);
+    if (e == cudaSuccess) p[n++] = q;
+    *out = static_cast<T *>(q);
+    return e;
+  }
+};
+
+}  // namespace
+
+extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout, int taps,
+                               const uint16_t *x, const uint16_t *w, const float *bias, int relu,
+                               const uint16_t *mask, void *out) {
+  if (mode < 0 || mode > 2) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: mode must be 0, 1 or 2%s", "");
+  if (B < 1 || H < 1 || W < 1 || cin < 16 || cout < 16 || cin % 16 || cout % 16 ||
+      (taps != 1 && taps != 9) || !x || !w || !out)
+    return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: bad shape or NULL buffer%s", "");
+  const long long pix = static_cast<long long>(B) * H * W;
+  const size_t nw = static_cast<size_t>(cout) * taps * cin;
+  Bufs bufs;
+  sg::bf16 *dx = nullptr, *dw = nullptr, *dwd = nullptr, *dmask = nullptr, *dout = nullptr;
+  float *dbias = nullptr, *dgw = nullptr;
+  int *derr = nullptr;
+  cudaStream_t s = nullptr;
+  cudaError_t e = bufs.alloc(&derr, sizeof(int));
+  const char *why = nullptr;
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  if (mode == 0) {
+    if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cin * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dw, nw * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dout, pix * cout * 2);
+    if (e == cudaSuccess && bias) e = bufs.alloc(&dbias, cout * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dw, w, nw * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bias) e = cudaMemcpy(dbias, bias, cout * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
+    sg::Act src{dx, B, H, W, cin};
+    sg::ConvPlan plan;
+    e = sg::plan_conv(plan, src, dw, taps, cout, dbias, relu, nullptr, 0, dout, cout, &why);
+    if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
+    e = sg::launch_conv(plan, derr, s);
+  } else if (mode == 1) {
+    if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cout * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dw, nw * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dwd, nw * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dout, pix * cin * 2);
+    if (e == cudaSuccess && mask) e = bufs.alloc(&dmask, pix * cin * 2);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cout * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dw, w, nw * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && mask) e = cudaMemcpy(dmask, mask, pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = sg::launch_flip_weights(dw, dwd, cout, cin, taps, s);
+    if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
+    sg::Act src{dx, B, H, W, cout};
+    sg::ConvPlan plan;
+    e = sg::plan_conv(plan, src, dwd, taps, cin, nullptr, 0, dmask, cin, dout, cin, &why);
+    if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
+    e = sg::launch_conv(plan, derr, s);
+  } else {
+    if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cin * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dw, pix * cout * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dgw, nw * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dw, w, pix * cout * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(dgw, 0, nw * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
+    sg::Act xa{dx, B, H, W, cin}, ya{dw, B, H, W, cout};
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    sg::WgradPlan plan;
+    e = sg::plan_wgrad(plan, xa, ya, taps, dgw, sms > 0 ? sms : 1, &why);
+    if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
+    e = sg::launch_wgrad(plan, derr, s);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: launch");
+  int herr = 0;
+  e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: status");
+  if (herr) return sg_fail(FS_ERR_TIMEOUT, "fs_test_sg_conv: a pipeline wait ran out%s", "");
+  if (mode == 0) e = cudaMemcpy(out, dout, pix * cout * 2, cudaMemcpyDeviceToHost);
+  else if (mode == 1) e = cudaMemcpy(out, dout, pix * cin * 2, cudaMemcpyDeviceToHost);
+  else e = cudaMemcpy(out, dgw, nw * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: copy back");
+  return FS_OK;
+}

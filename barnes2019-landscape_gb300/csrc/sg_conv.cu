@@ -1,0 +1,825 @@
+// sg_conv.cu -- the surrogate's dense contraction: 3x3 (and 1x1)
+// convolutions over NHWC BF16 tensors as implicit GEMMs on the 5th-generation
+// tensor cores (tcgen05.mma kind::f16, BF16 x BF16 -> FP32), operands staged
+// in shared memory by TMA (cp.async.bulk.tensor), accumulators in tensor
+// memory (TMEM), read back with tcgen05.ld for a fused epilogue. No library
+// GEMM, no cluster multicast: every tensor map covers this GPU's own memory.
+//
+// Forward / data gradient (k_conv): D[p][n] = sum over taps and input
+// channels of A[p + off(tap)][ci] * Bw[n][tap*cin + ci].
+//   M = 128 pixels of one image (BW x BH, BW = min(W,128)), N = output
+//   channels of the tile (<= 256), K = taps * cin in blocks of cb channels.
+//   A block is one TMA load of a {cb, BW, BH, 1} box at the tap's offset:
+//   coordinates outside the image read zeros, which is the convolution's
+//   zero padding. Both operands are K-major with the box's swizzle (32-, 64-
+//   or 128-byte rows). The data gradient is the same kernel on the output
+//   gradient with flipped, transposed weights (launch_flip_weights).
+// Weight gradient (k_wgrad): dW^T[(tap,ci)][co] = sum over pixels p of
+//   X[p + off(tap)][ci] * dY[p][co]. K = pixels (128 per step), both operands
+//   MN-major (channels contiguous in the NHWC boxes). The 128 M rows are
+//   chunks of (tap, channel block) stacked in shared memory at a fixed
+//   stride, so a 32-channel layer fills a tile with four taps. The pixel
+//   range is split across CTAs; each adds its FP32 partial sums with
+//   reductions into dW.
+//
+// Warp roles (128 threads): warp 0 lane 0 issues the TMA loads into a ring
+// of stages (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees
+// each stage with tcgen05.commit, and all four warps run the epilogue, warp w
+// reading TMEM lanes 32w..32w+31 (its pixels, or its (tap, ci) rows). Every
+// mbarrier wait is bounded (1 s of the global timer): on expiry the CTA sets
+// the error word, stops issuing, waits (again bounded) for its own copies
+// and MMAs in flight, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "sg_internal.h"
+
+namespace sg {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kM = 128;                             // rows of every MMA tile
+constexpr int kKPix = 128;                          // pixels per weight-gradient step
+constexpr int kMaxStages = 8;
+constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
+constexpr unsigned long long kWaitNs = 1000000000ull;
+
+// ---------------------------------------------------------------- PTX ----
+
+__device__ __forceinline__ uint32_t su32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the phase of `parity` to complete; false after kWaitNs, or as
+// soon as *abort is set when watch_abort.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                          bool watch_abort) {
+  if (mbar_test(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  for (int it = 1;; it++) {
+    if (mbar_test(bar, parity)) return true;
+    if ((it & 15) == 0) {
+      if (watch_abort && *abort) return false;
+      if (gtimer() - t0 > kWaitNs) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch(const CUtensorMap *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   su32(slot)),
+               "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, BF16 inputs, FP32 accumulation.
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// The mbarrier receives one arrival once every MMA this thread issued before
+// has completed.
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          su32(bar))
+      : "memory");
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void red_add_f32(float *p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+// Swizzle-mode code of the shared-memory descriptor for rows of `row_bytes`
+// (the TMA box's swizzle span): 128 B -> 2, 64 B -> 4, 32 B -> 6.
+__host__ __device__ constexpr uint64_t swizzle_code(int row_bytes) {
+  return row_bytes == 128 ? 2 : row_bytes == 64 ? 4 : 6;
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading and
+// stride byte offsets (16-byte units), descriptor version 1, swizzle mode.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo,
+                                              uint64_t swz) {
+  uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFF) >> 4);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;
+  d |= static_cast<uint64_t>(1) << 46;
+  d |= swz << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B,
+// A/B K-major (0) or MN-major (1), N = n, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n, int a_mn, int b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(a_mn) << 15) |
+         (static_cast<uint32_t>(b_mn) << 16) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void sg_raise(int *err, volatile int *abort, int code) {
+  *abort = 1;
+  atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+struct ConvArgs {
+  int H, W, BW, BH, tiles_x, tiles_y;
+  int cin, taps, bn, stages;
+  const float *bias;
+  int relu;
+  const bf16 *mask;
+  int ldm;
+  bf16 *out;
+  int ldo;
+  int *err;
+};
+
+// ------------------------------------------------------ forward / dgrad ----
+template <int CB>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_conv(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
+           const ConvArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], accf;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kRow = CB * 2;  // bytes per operand row (the swizzle span)
+  const int a_bytes = kM * kRow;
+  const int b_bytes = a.bn * kRow;
+  const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
+  const int S = a.stages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&accf, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma_prefetch(&tma);
+    tma_prefetch(&tmb);
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, ncols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  const int tiles_img = a.tiles_x * a.tiles_y;
+  const int b = blockIdx.x / tiles_img;
+  const int t = blockIdx.x - b * tiles_img;
+  const int y0 = (t / a.tiles_x) * a.BH, x0 = (t % a.tiles_x) * a.BW;
+  const int n0 = blockIdx.y * a.bn;
+  const int kch = a.cin / CB;
+  const int nkb = a.taps * kch;
+
+  if (warp == 0 && lane == 0) {
+    // producer
+    int issued = 0;
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % S;
+      const uint32_t ph = (kb / S) & 1;
+      if (!mbar_wait(&empty[s], ph ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      const int tap = kb / kch, cc = kb - tap * kch;
+      const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+      unsigned char *sa = smem + s * stage_bytes;
+      mbar_expect_tx(&full[s], a_bytes + b_bytes);
+      tma_load_4d(sa, &tma, &full[s], cc * CB, x0 + dx, y0 + dy, b);
+      tma_load_2d(sa + a_bytes, &tmb, &full[s], tap * a.cin + cc * CB, n0);
+      issued = kb + 1;
+    }
+    // leave no copy in flight into this CTA's shared memory
+    for (int kb = issued > S ? issued - S : 0; kb < issued; kb++)
+      if (!mbar_wait(&full[kb % S], (kb / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % S;
+      if (!mbar_wait(&full[s], (kb / S) & 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sa = su32(smem + s * stage_bytes);
+      const uint64_t da = smem_desc(sa, 16, 8 * kRow, swizzle_code(kRow));
+      const uint64_t db = smem_desc(sa + a_bytes, 16, 8 * kRow, swizzle_code(kRow));
+#pragma unroll
+      for (int k = 0; k < CB / 16; k++)  // K = 16 per MMA: 32 bytes along the row
+        umma_bf16(tmem, da + 2 * k, db + 2 * k, idesc, (kb | k) != 0);
+      umma_commit(&empty[s]);
+    }
+    umma_commit(&accf);
+  }
+  __syncwarp();
+
+  // epilogue: TMEM lane = tile row = pixel
+  const bool ok = mbar_wait(&accf, 0, &abort_flag, false);
+  if (!ok) sg_raise(a.err, &abort_flag, kSgTimeout);
+  tc_fence_after();
+  if (ok && !abort_flag) {
+    const int r = warp * 32 + lane;
+    const int py = y0 + r / a.BW, px = x0 + r % a.BW;
+    const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
+    bf16 *out = a.out + pix * a.ldo + n0;
+    const bf16 *msk = a.mask ? a.mask + pix * a.ldm + n0 : nullptr;
+    for (int c = 0; c < a.bn; c += 16) {
+      uint32_t v[16];
+      tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c, v);
+      tmem_ld_wait();
+      float f[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
+      if (a.bias) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) f[j] += a.bias[n0 + c + j];
+      }
+      if (a.relu) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
+      }
+      if (msk) {
+        const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
+        const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
+        const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
+        const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
+          if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
+        }
+      }
+      uint4 o0, o1;
+      o0.x = pack_bf16(f[0], f[1]);
+      o0.y = pack_bf16(f[2], f[3]);
+      o0.z = pack_bf16(f[4], f[5]);
+      o0.w = pack_bf16(f[6], f[7]);
+      o1.x = pack_bf16(f[8], f[9]);
+      o1.y = pack_bf16(f[10], f[11]);
+      o1.z = pack_bf16(f[12], f[13]);
+      o1.w = pack_bf16(f[14], f[15]);
+      *reinterpret_cast<uint4 *>(out + c) = o0;
+      *reinterpret_cast<uint4 *>(out + c + 8) = o1;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
+struct WgradArgs {
+  int H, W, BW, BH, tiles_x, tiles_y;
+  int cin, cout, taps, nchunk, stages, ksteps, kper;
+  float *dw;
+  int *err;
+};
+
+// --------------------------------------------------------- weight grad ----
+// CWA: channels per chunk of X (M side), CWB: per chunk of dY (N side).
+template <int CWA, int CWB>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_wgrad(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmy,
+            const WgradArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], accf;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kRowA = CWA * 2, kRowB = CWB * 2;
+  constexpr int kChunkA = kKPix * kRowA;  // one (tap, channel block) chunk: 128 pixel rows
+  constexpr int kChunkB = kKPix * kRowB;
+  constexpr int kPerTile = kM / CWA;      // chunks stacked in one M tile
+  const int a_bytes = kPerTile * kChunkA;  // = 128 * 256 bytes
+  const int b_bytes = (a.cout / CWB) * kChunkB;
+  const int stage_bytes = a_bytes + b_bytes;  // multiples of 1024
+  const int S = a.stages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = a.cout <= 32 ? 32 : a.cout <= 64 ? 64 : a.cout <= 128 ? 128 : 256;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&accf, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma_prefetch(&tmx);
+    tma_prefetch(&tmy);
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, ncols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  const int q0 = blockIdx.x * kPerTile;  // first chunk of this M tile
+  const int nq = min(kPerTile, a.nchunk - q0);
+  const int kchx = a.cin / CWA;
+  const int k_lo = blockIdx.y * a.kper;
+  const int k_hi = min(a.ksteps, k_lo + a.kper);
+  const int nk = k_hi - k_lo;
+  const int tiles_img = a.tiles_x * a.tiles_y;
+
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    const uint32_t tx = nq * kChunkA + b_bytes;
+    for (int i = 0; i < nk; i++) {
+      const int s = i % S;
+      if (!mbar_wait(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      const int kt = k_lo + i;
+      const int b = kt / tiles_img, t = kt - b * tiles_img;
+      const int y0 = (t / a.tiles_x) * a.BH, x0 = (t % a.tiles_x) * a.BW;
+      unsigned char *sa = smem + s * stage_bytes;
+      unsigned char *sb = sa + a_bytes;
+      mbar_expect_tx(&full[s], tx);
+      for (int j = 0; j < nq; j++) {
+        const int q = q0 + j;
+        const int tap = q / kchx, cc = q - tap * kchx;
+        const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+        tma_load_4d(sa + j * kChunkA, &tmx, &full[s], cc * CWA, x0 + dx, y0 + dy, b);
+      }
+      for (int j = 0; j < a.cout / CWB; j++)
+        tma_load_4d(sb + j * kChunkB, &tmy, &full[s], j * CWB, x0, y0, b);
+      issued = i + 1;
+    }
+    for (int i = issued > S ? issued - S : 0; i < issued; i++)
+      if (!mbar_wait(&full[i % S], (i / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+  } else if (warp == 1 && lane == 0) {
+    const uint32_t idesc = idesc_bf16(a.cout, 1, 1);
+    for (int i = 0; i < nk; i++) {
+      const int s = i % S;
+      if (!mbar_wait(&full[s], (i / S) & 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sa = su32(smem + s * stage_bytes);
+      // MN-major: LBO = stride between channel chunks, SBO = 8 pixel rows
+      const uint64_t da = smem_desc(sa, kChunkA, 8 * kRowA, swizzle_code(kRowA));
+      const uint64_t db = smem_desc(sa + a_bytes, kChunkB, 8 * kRowB, swizzle_code(kRowB));
+#pragma unroll
+      for (int k = 0; k < kKPix / 16; k++)  // 16 pixel rows per MMA
+        umma_bf16(tmem, da + ((16 * kRowA * k) >> 4), db + ((16 * kRowB * k) >> 4), idesc,
+                  (i | k) != 0);
+      umma_commit(&empty[s]);
+    }
+    umma_commit(&accf);
+  }
+  __syncwarp();
+
+  const bool ok = mbar_wait(&accf, 0, &abort_flag, false);
+  if (!ok) sg_raise(a.err, &abort_flag, kSgTimeout);
+  tc_fence_after();
+  if (ok && !abort_flag && nk > 0) {
+    const int r = warp * 32 + lane;
+    const int j = r / CWA;
+    const bool valid = j < nq;
+    const int q = q0 + j;
+    const int tap = q / kchx;
+    const int ci = (q - tap * kchx) * CWA + (r % CWA);
+    const long long kdim = static_cast<long long>(a.taps) * a.cin;
+    float *dst = a.dw + tap * a.cin + ci;
+    for (int c = 0; c < a.cout; c += 16) {
+      uint32_t v[16];
+      tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c, v);
+      tmem_ld_wait();
+      if (valid) {
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) red_add_f32(dst + (c + jj) * kdim, __uint_as_float(v[jj]));
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
+__global__ void k_flip_weights(const bf16 *__restrict__ w, bf16 *__restrict__ wd, int cout,
+                               int cin, int taps) {
+  const long long n = static_cast<long long>(cout) * taps * cin;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int ci = static_cast<int>(i % cin);
+    const int tap = static_cast<int>((i / cin) % taps);
+    const int co = static_cast<int>(i / (static_cast<long long>(cin) * taps));
+    wd[(static_cast<long long>(ci) * taps + (taps - 1 - tap)) * cout + co] = w[i];
+  }
+}
+
+// ------------------------------------------------------------- host ----
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+CUtensorMapSwizzle swizzle_of(int row_bytes) {
+  return row_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+         : row_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                           : CU_TENSOR_MAP_SWIZZLE_32B;
+}
+
+// {cb, BW, BH, 1} boxes of an NHWC tensor.
+cudaError_t map_act(CUtensorMap *m, const Act &t, int cb, const PixTile &pt) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
+                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
+  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
+  const cuuint32_t box[4] = {static_cast<cuuint32_t>(cb), static_cast<cuuint32_t>(pt.BW),
+                             static_cast<cuuint32_t>(pt.BH), 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_of(cb * 2),
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// {cb, bn} boxes of a [rows][cols] BF16 matrix.
+cudaError_t map_mat(CUtensorMap *m, const bf16 *p, int rows, int cols, int cb, int bn) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(cols) * 2};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(cb), static_cast<cuuint32_t>(bn)};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(p), dims,
+                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_of(cb * 2),
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+
+PixTile pixel_tile(int H, int W) {
+  PixTile pt;
+  if (W <= 0 || H <= 0) return pt;
+  if (W >= kM) {
+    if (W % kM) return pt;
+    pt.BW = kM;
+    pt.BH = 1;
+  } else {
+    if (kM % W) return pt;
+    pt.BW = W;
+    pt.BH = kM / W;
+    if (H % pt.BH) return pt;
+  }
+  pt.tiles_x = W / pt.BW;
+  pt.tiles_y = H / pt.BH;
+  pt.ok = true;
+  return pt;
+}
+
+cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
+                      const float *bias, int relu, const bf16 *mask, int ldm, bf16 *out, int ldo,
+                      const char **why) {
+  const char *dummy;
+  if (!why) why = &dummy;
+  p = ConvPlan{};
+  p.pt = pixel_tile(src.H, src.W);
+  if (!p.pt.ok) return *why = "image width must divide or be a multiple of 128", cudaErrorInvalidValue;
+  if (src.C % 16 || src.C <= 0) return *why = "source channels must be a multiple of 16", cudaErrorInvalidValue;
+  if (taps != 1 && taps != 9) return *why = "taps must be 1 or 9", cudaErrorInvalidValue;
+  if (ntot % 16 || ntot <= 0) return *why = "output channels must be a multiple of 16", cudaErrorInvalidValue;
+  if (ldo % 8 || ldo < ntot || (mask && (ldm % 8 || ldm < ntot)))
+    return *why = "output/mask row strides must be multiples of 8 covering the channels", cudaErrorInvalidValue;
+  if (!aligned16(src.p) || !aligned16(w) || !aligned16(out) || (mask && !aligned16(mask)))
+    return *why = "tensors must be 16-byte aligned", cudaErrorInvalidValue;
+  // N tile: the whole output when it fits one accumulator, else the largest
+  // divisor <= 256 that is a multiple of 16
+  int bn = ntot;
+  if (bn > 256) {
+    bn = 0;
+    for (int c = 256; c >= 16; c -= 16)
+      if (ntot % c == 0) {
+        bn = c;
+        break;
+      }
+  }
+  p.B = src.B;
+  p.H = src.H;
+  p.W = src.W;
+  p.cin = src.C;
+  p.taps = taps;
+  p.ntot = ntot;
+  p.bn = bn;
+  p.cb = channel_block(src.C);
+  const size_t stage = (static_cast<size_t>(kM) * p.cb * 2 + static_cast<size_t>(bn) * p.cb * 2 + 1023) &
+                       ~static_cast<size_t>(1023);
+  int S = static_cast<int>(kSmemBudget / stage);
+  if (S > kMaxStages) S = kMaxStages;
+  const int nkb = taps * (src.C / p.cb);
+  if (S > nkb) S = nkb < 2 ? 2 : nkb;
+  if (S < 2) return *why = "stage does not fit shared memory", cudaErrorInvalidValue;
+  p.stages = S;
+  p.smem = S * stage + 1024;
+  p.bias = bias;
+  p.relu = relu;
+  p.mask = mask;
+  p.ldm = ldm;
+  p.out = out;
+  p.ldo = ldo;
+  p.grid_x = static_cast<int>(src.pixels() / kM);
+  p.grid_y = ntot / bn;
+  cudaError_t e = map_act(&p.tma, src, p.cb, p.pt);
+  if (e != cudaSuccess) return *why = "tensor map (source)", e;
+  e = map_mat(&p.tmb, w, ntot, taps * src.C, p.cb, bn);
+  if (e != cudaSuccess) return *why = "tensor map (weights)", e;
+  return cudaSuccess;
+}
+
+cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
+                       const char **why) {
+  const char *dummy;
+  if (!why) why = &dummy;
+  p = WgradPlan{};
+  if (x.B != dy.B || x.H != dy.H || x.W != dy.W)
+    return *why = "X and dY must have the same pixel grid", cudaErrorInvalidValue;
+  p.pt = pixel_tile(x.H, x.W);
+  if (!p.pt.ok) return *why = "image width must divide or be a multiple of 128", cudaErrorInvalidValue;
+  if (x.C % 16 || dy.C % 16 || dy.C > 256 || x.C <= 0 || dy.C <= 0)
+    return *why = "channels must be multiples of 16, at most 256 output channels", cudaErrorInvalidValue;
+  if (taps != 1 && taps != 9) return *why = "taps must be 1 or 9", cudaErrorInvalidValue;
+  if (!aligned16(x.p) || !aligned16(dy.p) || !aligned16(dw))
+    return *why = "tensors must be 16-byte aligned", cudaErrorInvalidValue;
+  p.B = x.B;
+  p.H = x.H;
+  p.W = x.W;
+  p.cin = x.C;
+  p.cout = dy.C;
+  p.taps = taps;
+  p.cwa = channel_block(x.C);
+  p.cwb = channel_block(dy.C);
+  const size_t a_bytes = static_cast<size_t>(kM) * kKPix * 2;
+  const size_t b_bytes = static_cast<size_t>(dy.C) * kKPix * 2;
+  int S = static_cast<int>(kSmemBudget / (a_bytes + b_bytes));
+  if (S > kMaxStages) S = kMaxStages;
+  if (S < 2) return *why = "stage does not fit shared memory", cudaErrorInvalidValue;
+  p.stages = S;
+  p.smem = S * (a_bytes + b_bytes) + 1024;
+  const int nchunk = taps * (x.C / p.cwa);
+  p.mtiles = (nchunk + (kM / p.cwa) - 1) / (kM / p.cwa);
+  p.ksteps = static_cast<int>(x.pixels() / kKPix);
+  // split the pixels so about three CTAs per SM run, each over >= 8 steps
+  int splits = (3 * sms + p.mtiles - 1) / p.mtiles;
+  if (splits > p.ksteps / 8) splits = p.ksteps / 8;
+  if (splits < 1) splits = 1;
+  p.kper = (p.ksteps + splits - 1) / splits;
+  p.splits = (p.ksteps + p.kper - 1) / p.kper;
+  p.dw = dw;
+  cudaError_t e = map_act(&p.tmx, x, p.cwa, p.pt);
+  if (e != cudaSuccess) return *why = "tensor map (X)", e;
+  e = map_act(&p.tmy, dy, p.cwb, p.pt);
+  if (e != cudaSuccess) return *why = "tensor map (dY)", e;
+  return cudaSuccess;
+}
+
+namespace {
+
+template <int CB>
+cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kSmemBudget + 1024));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  ConvArgs a{};
+  a.H = p.H;
+  a.W = p.W;
+  a.BW = p.pt.BW;
+  a.BH = p.pt.BH;
+  a.tiles_x = p.pt.tiles_x;
+  a.tiles_y = p.pt.tiles_y;
+  a.cin = p.cin;
+  a.taps = p.taps;
+  a.bn = p.bn;
+  a.stages = p.stages;
+  a.bias = p.bias;
+  a.relu = p.relu;
+  a.mask = p.mask;
+  a.ldm = p.ldm;
+  a.out = p.out;
+  a.ldo = p.ldo;
+  a.err = err;
+  k_conv<CB><<<dim3(p.grid_x, p.grid_y), kThreads, p.smem, s>>>(p.tma, p.tmb, a);
+  return cudaGetLastError();
+}
+
+template <int CWA, int CWB>
+cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_wgrad<CWA, CWB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kSmemBudget + 1024));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  WgradArgs a{};
+  a.H = p.H;
+  a.W = p.W;
+  a.BW = p.pt.BW;
+  a.BH = p.pt.BH;
+  a.tiles_x = p.pt.tiles_x;
+  a.tiles_y = p.pt.tiles_y;
+  a.cin = p.cin;
+  a.cout = p.cout;
+  a.taps = p.taps;
+  a.nchunk = p.taps * (p.cin / p.cwa);
+  a.stages = p.stages;
+  a.ksteps = p.ksteps;
+  a.kper = p.kper;
+  a.dw = p.dw;
+  a.err = err;
+  k_wgrad<CWA, CWB><<<dim3(p.mtiles, p.splits), kThreads, p.smem, s>>>(p.tmx, p.tmy, a);
+  return cudaGetLastError();
+}
+
+template <int CWA>
+cudaError_t launch_wgrad_a(const WgradPlan &p, int *err, cudaStream_t s) {
+  switch (p.cwb) {
+    case 64: return launch_wgrad_cw<CWA, 64>(p, err, s);
+    case 32: return launch_wgrad_cw<CWA, 32>(p, err, s);
+    default: return launch_wgrad_cw<CWA, 16>(p, err, s);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s) {
+  if (p.grid_x <= 0) return cudaErrorInvalidValue;
+  switch (p.cb) {
+    case 64: return launch_conv_cb<64>(p, err, s);
+    case 32: return launch_conv_cb<32>(p, err, s);
+    default: return launch_conv_cb<16>(p, err, s);
+  }
+}
+
+cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s) {
+  if (p.mtiles <= 0) return cudaErrorInvalidValue;
+  switch (p.cwa) {
+    case 64: return launch_wgrad_a<64>(p, err, s);
+    case 32: return launch_wgrad_a<32>(p, err, s);
+    default: return launch_wgrad_a<16>(p, err, s);
+  }
+}
+
+cudaError_t launch_flip_weights(const bf16 *w, bf16 *wd, int cout, int cin, int taps,
+                                cudaStream_t s) {
+  const long long n = static_cast<long long>(cout) * taps * cin;
+  int blocks = static_cast<int>((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  k_flip_weights<<<blocks, 256, 0, s>>>(w, wd, cout, cin, taps);
+  return cudaGetLastError();
+}
+
+}  // namespace sg

@@ -1,0 +1,93 @@
+// sg_internal.h -- the learned surrogate's device building blocks, shared by
+// the convolution kernels (sg_conv.cu), the network (sg_net.cu) and the
+// judged ensemble (sg_ensemble.cu). Not part of the public ABI.
+//
+// Activations are NHWC BF16 tensors (channels innermost, a multiple of 16);
+// weights of a 3x3 (or 1x1) convolution are BF16 [cout][tap][cin] with
+// tap = 3*dy + dx (the GEMM's K dimension tap*cin + ci contiguous), kept
+// with an FP32 master copy; weight gradients are FP32 in the same layout.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace sg {
+
+using bf16 = __nv_bfloat16;
+
+// Error codes written to the device error word (0 = none).
+enum SgErr : int {
+  kSgOk = 0,
+  kSgTimeout = 1,  // an mbarrier wait ran out (producer, MMA or epilogue)
+};
+
+// An NHWC activation tensor on the device.
+struct Act {
+  bf16 *p = nullptr;
+  int B = 0, H = 0, W = 0, C = 0;
+  long long pixels() const { return static_cast<long long>(B) * H * W; }
+  size_t bytes() const { return static_cast<size_t>(pixels()) * C * sizeof(bf16); }
+};
+
+// Channels one K-block (and one TMA box) of a tensor with C channels spans:
+// 64 when C is a multiple of 64, else 32, else 16 (128-, 64- or 32-byte rows,
+// the swizzle span of the box).
+inline int channel_block(int C) { return C % 64 == 0 ? 64 : C % 32 == 0 ? 32 : 16; }
+
+// Pixel tile of 128 pixels of one image: BW x BH with BW = min(W, 128).
+struct PixTile {
+  int BW = 0, BH = 0, tiles_x = 0, tiles_y = 0;
+  bool ok = false;
+};
+PixTile pixel_tile(int H, int W);
+
+// A forward (or data-gradient) convolution prepared for launches: the tensor
+// maps of its source and weights, the tile shape and the epilogue.
+struct ConvPlan {
+  CUtensorMap tma;  // source activations, box {cb, BW, BH, 1}
+  CUtensorMap tmb;  // weights [ntot][taps*cin], box {cb, bn}
+  int B = 0, H = 0, W = 0, cin = 0, taps = 9, ntot = 0, bn = 0, cb = 0, stages = 0;
+  PixTile pt;
+  const float *bias = nullptr;  // [ntot] or null
+  int relu = 0;
+  const bf16 *mask = nullptr;   // output zeroed where mask <= 0 (or null)
+  int ldm = 0;
+  bf16 *out = nullptr;
+  int ldo = 0;
+  size_t smem = 0;
+  int grid_x = 0, grid_y = 0;
+};
+
+// A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=
+// sum over pixels of dY[p][co] * X[p + off(tap)][ci].
+struct WgradPlan {
+  CUtensorMap tmx;  // X, box {cwa, BW, BH, 1}
+  CUtensorMap tmy;  // dY, box {cwb, BW, BH, 1}
+  int B = 0, H = 0, W = 0, cin = 0, cout = 0, taps = 9, cwa = 0, cwb = 0, stages = 0;
+  PixTile pt;
+  int mtiles = 0, splits = 0, ksteps = 0, kper = 0;
+  float *dw = nullptr;
+  size_t smem = 0;
+};
+
+// Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for
+// shapes the kernels do not take. Source and output tensors must stay
+// allocated for the plan's lifetime.
+cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
+                      const float *bias, int relu, const bf16 *mask, int ldm, bf16 *out,
+                      int ldo, const char **why);
+cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
+                       const char **why);
+cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s);
+cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s);
+
+// Flipped, transposed weights for the data gradient:
+// wd[ci][8 - tap][co] = w[co][tap][ci] (taps = 9), wd[ci][0][co] = w[co][0][ci] (taps = 1).
+cudaError_t launch_flip_weights(const bf16 *w, bf16 *wd, int cout, int cin, int taps,
+                                cudaStream_t s);
+
+}  // namespace sg

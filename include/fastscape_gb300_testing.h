@@ -42,6 +42,25 @@ int fs_test_receiver_fixups(const fs_model *m, int32_t *count);
  * a timestep meets a larger count (that timestep is redone, bit-exactly). */
 int fs_test_table_capacity(const fs_model *m, int32_t *cap);
 
+/* One convolution of the learned surrogate's kernels on host buffers (the
+ * library allocates, copies, runs on the current device and copies back),
+ * for checking the tensor-core kernels against a CPU convolution. Tensors
+ * are NHWC BF16 (uint16 bit patterns), B images of H x W pixels; weights
+ * are BF16 [cout][taps][cin] with tap = 3*dy + dx (taps 9: 3x3 with zero
+ * padding; taps 1: 1x1); cin and cout multiples of 16.
+ *   mode 0 (forward):  out[p][co] = act(bias[co] + sum x[p+off][ci] w[co][tap][ci])
+ *                      x: [B,H,W,cin], out: [B,H,W,cout] BF16; act = ReLU when
+ *                      relu, bias may be NULL; mask NULL.
+ *   mode 1 (data gradient): out[p][ci] = sum dy[p-off][co] w[co][tap][ci],
+ *                      zeroed where mask[p][ci] <= 0 (mask may be NULL);
+ *                      x holds dy [B,H,W,cout], out: [B,H,W,cin] BF16.
+ *   mode 2 (weight gradient): out[co][tap][ci] = sum_p dy[p][co] x[p+off][ci]
+ *                      (FP32); x: [B,H,W,cin], w holds dy [B,H,W,cout].
+ * No counterpart in the reference (it has no learned part). */
+int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout, int taps,
+                    const uint16_t *x, const uint16_t *w, const float *bias, int relu,
+                    const uint16_t *mask, void *out);
+
 #ifdef __cplusplus
 }
 #endif
