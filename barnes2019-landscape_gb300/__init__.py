@@ -52,10 +52,18 @@ ABI_SYMBOLS = [
     "fs_batch_use_int_sub", "fs_use_int_sub",
     "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
     "fs_autotune", "fs_launch_config",
+    "fs_batch_set_active", "fs_batch_device_elevation", "fs_batch_stream",
+    "fs_batch_get_params", "fs_batch_get_shape",
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
     "fs_test_set_receiver_path", "fs_test_set_erosion_path", "fs_test_receiver_fixups",
     "fs_test_table_capacity", "fs_test_sg_conv",
+    "fs_sg_config_default", "fs_sg_create", "fs_sg_destroy", "fs_sg_get_config",
+    "fs_sg_param_count", "fs_sg_get_params", "fs_sg_set_params", "fs_sg_get_grads",
+    "fs_sg_save", "fs_sg_load", "fs_sg_reserve", "fs_sg_add_samples", "fs_sg_generate",
+    "fs_sg_set_holdout", "fs_sg_dataset_info", "fs_sg_get_sample", "fs_sg_train", "fs_sg_eval",
+    "fs_sg_eval_baselines", "fs_sg_grad", "fs_sg_train_stats", "fs_sg_predict_host", "fs_sg_predict_batch",
+    "fs_sg_infer_flops", "fs_sg_ensemble_defaults", "fs_sg_compare_host", "fs_sg_ensemble_run",
 ]
 
 
@@ -90,6 +98,29 @@ def workload_params(dx: float = 100.0, keq: float = 2e-6, meq: float = 0.4,
     """K 2e-6, n 1, m 0.4, U 2e-3, dt 1000, dr {dx, dx*SQRT2}, tol 1e-3,
     cell_area dx*dx (the 1000^2 and 10000^2 workloads, dx = 100 m)."""
     return Params(keq, neq, meq, ueq, 1000.0, dx, dx * SQRT2, 1e-3, dx * dx)
+
+
+class SgConfig(C.Structure):
+    """fs_sg_config (include/fastscape_surrogate.h)."""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("base_channels", C.c_int),
+                ("batch", C.c_int), ("jump", C.c_int), ("dt", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class EnsembleOpts(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("plain_steps", C.c_int), ("judge_fraction", C.c_double),
+                ("max_rel_rms", C.c_double), ("min_agreement", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class EnsembleStats(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("cycles", "jumps", "judged", "fallbacks")] + \
+               [(n, C.c_double) for n in ("rel_rms_mean", "rel_rms_max", "agreement_mean",
+                                          "agreement_min", "ms_total", "ms_infer", "ms_exact",
+                                          "ms_plain", "ms_judge")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 _lib = None
@@ -155,6 +186,11 @@ def library() -> C.CDLL:
     L.fs_autotune.argtypes = [vp, C.c_int, ip]
     L.fs_launch_config.argtypes = [vp, ip, ip, ip, ip]
     L.fs_batch_synchronize.argtypes = [vp]
+    L.fs_batch_set_active.argtypes = [vp, C.c_int, ip]
+    L.fs_batch_device_elevation.argtypes = [vp, C.c_int, C.POINTER(C.c_void_p)]
+    L.fs_batch_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
+    L.fs_batch_get_params.argtypes = [vp, C.c_int, pp]
+    L.fs_batch_get_shape.argtypes = [vp, C.c_int, ip, ip]
     L.fs_step_noalloc.argtypes = [vp, C.c_int, C.c_int, pp, C.c_int, vp]
     L.fs_test_order_from_receivers.argtypes = [vp, i32p]
     L.fs_test_barrier_timeout.argtypes = [vp, C.c_double]
@@ -162,6 +198,40 @@ def library() -> C.CDLL:
     L.fs_test_set_erosion_path.argtypes = [vp, C.c_int]
     L.fs_test_receiver_fixups.argtypes = [vp, i32p]
     L.fs_test_table_capacity.argtypes = [vp, i32p]
+    sgc = C.POINTER(SgConfig)
+    L.fs_sg_config_default.argtypes = [sgc]
+    L.fs_sg_config_default.restype = None
+    L.fs_sg_create.argtypes = [sgc, ip]
+    L.fs_sg_create.restype = vp
+    L.fs_sg_destroy.argtypes = [vp]
+    L.fs_sg_destroy.restype = None
+    L.fs_sg_get_config.argtypes = [vp, sgc]
+    L.fs_sg_param_count.argtypes = [vp, C.POINTER(C.c_int64)]
+    fp = C.POINTER(C.c_float)
+    L.fs_sg_get_params.argtypes = [vp, fp]
+    L.fs_sg_set_params.argtypes = [vp, fp]
+    L.fs_sg_get_grads.argtypes = [vp, fp]
+    L.fs_sg_save.argtypes = [vp, C.c_char_p]
+    L.fs_sg_load.argtypes = [vp, C.c_char_p]
+    L.fs_sg_reserve.argtypes = [vp, C.c_int]
+    L.fs_sg_add_samples.argtypes = [vp, C.c_int, dp, dp, pp]
+    L.fs_sg_generate.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_uint64, ip]
+    L.fs_sg_set_holdout.argtypes = [vp, C.c_int]
+    L.fs_sg_dataset_info.argtypes = [vp, ip, ip]
+    L.fs_sg_get_sample.argtypes = [vp, C.c_int, fp, fp]
+    L.fs_sg_train.argtypes = [vp, C.c_int, C.c_float, dp]
+    L.fs_sg_eval.argtypes = [vp, dp]
+    L.fs_sg_eval_baselines.argtypes = [vp, dp, dp]
+    L.fs_sg_grad.argtypes = [vp, C.c_int, ip, dp]
+    L.fs_sg_train_stats.argtypes = [vp, dp, dp]
+    L.fs_sg_predict_host.argtypes = [vp, C.c_int, dp, pp, dp]
+    L.fs_sg_predict_batch.argtypes = [vp, vp, C.c_int, ip, C.POINTER(C.c_void_p)]
+    L.fs_sg_infer_flops.argtypes = [vp, dp]
+    L.fs_sg_ensemble_defaults.argtypes = [C.POINTER(EnsembleOpts)]
+    L.fs_sg_ensemble_defaults.restype = None
+    L.fs_sg_compare_host.argtypes = [C.c_int, C.c_int, pp, C.c_int, dp, dp, dp, dp]
+    L.fs_sg_ensemble_run.argtypes = [vp, vp, C.POINTER(EnsembleOpts), C.POINTER(EnsembleStats),
+                                     ip]
     u16p = C.POINTER(C.c_uint16)
     L.fs_test_sg_conv.argtypes = [C.c_int] * 7 + [u16p, u16p, C.POINTER(C.c_float), C.c_int,
                                                   u16p, vp]
@@ -451,6 +521,20 @@ class FastScapeBatch:
     def synchronize(self) -> None:
         check(library().fs_batch_synchronize(self._b))
 
+    def set_active(self, idx=None) -> None:
+        """Advance only the realizations in idx from now on (None: all)."""
+        if idx is None or len(idx) == 0:
+            check(library().fs_batch_set_active(self._b, 0, None))
+            return
+        a = (C.c_int * len(idx))(*[int(i) for i in idx])
+        check(library().fs_batch_set_active(self._b, len(idx), a))
+
+    def device_elevation(self, r: int) -> int:
+        """Device address of realization r's elevation field."""
+        p = C.c_void_p()
+        check(library().fs_batch_device_elevation(self._b, int(r), C.byref(p)))
+        return int(p.value)
+
     @property
     def handle(self):
         return self._b
@@ -491,3 +575,171 @@ def sg_conv(mode: int, x_bits: np.ndarray, w_bits: np.ndarray, taps: int = 9, bi
                                     x_bits.ctypes.data_as(u16), w_bits.ctypes.data_as(u16), bp,
                                     int(bool(relu)), mp, out.ctypes.data_as(C.c_void_p)))
     return out
+
+
+class Surrogate:
+    """The learned surrogate (include/fastscape_surrogate.h): a BF16
+    encoder-decoder trained on the GPU on data the plain method generates,
+    jumping realizations `jump` timesteps ahead."""
+
+    def __init__(self, width=512, height=512, base_channels=32, batch=32, jump=50, dt=1000.0,
+                 seed=1):
+        L = library()
+        self.cfg = SgConfig(int(width), int(height), int(base_channels), int(batch), int(jump),
+                            float(dt), int(seed))
+        st = C.c_int(0)
+        self._s = L.fs_sg_create(C.byref(self.cfg), C.byref(st))
+        if not self._s:
+            raise FastScapeError(st.value, last_error())
+        self.size = self.cfg.width * self.cfg.height
+
+    def close(self):
+        if getattr(self, "_s", None):
+            library().fs_sg_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def param_count(self) -> int:
+        n = C.c_int64(0)
+        check(library().fs_sg_param_count(self._s, C.byref(n)))
+        return n.value
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.param_count(), np.float32)
+        check(library().fs_sg_get_params(self._s, _p(out, C.c_float)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.param_count():
+            raise ValueError("wrong parameter count")
+        check(library().fs_sg_set_params(self._s, _p(p, C.c_float)))
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(self.param_count(), np.float32)
+        check(library().fs_sg_get_grads(self._s, _p(out, C.c_float)))
+        return out
+
+    def save(self, path) -> None:
+        check(library().fs_sg_save(self._s, str(path).encode()))
+
+    def load(self, path) -> None:
+        check(library().fs_sg_load(self._s, str(path).encode()))
+
+    def reserve(self, n: int) -> None:
+        check(library().fs_sg_reserve(self._s, int(n)))
+
+    def add_samples(self, h_t, h_next, params) -> None:
+        h_t = np.ascontiguousarray(h_t, np.float64).reshape(-1, self.size)
+        h_next = np.ascontiguousarray(h_next, np.float64).reshape(-1, self.size)
+        n = h_t.shape[0]
+        pa = (Params * n)(*params)
+        check(library().fs_sg_add_samples(self._s, n, _p(h_t, C.c_double),
+                                          _p(h_next, C.c_double), pa))
+
+    def generate(self, ntraj: int, per_traj: int, max_spinup: int, seed: int = 0) -> int:
+        got = C.c_int(0)
+        check(library().fs_sg_generate(self._s, int(ntraj), int(per_traj), int(max_spinup),
+                                       int(seed) & 0xFFFFFFFFFFFFFFFF, C.byref(got)))
+        return got.value
+
+    def set_holdout(self, n: int) -> None:
+        check(library().fs_sg_set_holdout(self._s, int(n)))
+
+    def dataset_info(self):
+        n, h = C.c_int(0), C.c_int(0)
+        check(library().fs_sg_dataset_info(self._s, C.byref(n), C.byref(h)))
+        return n.value, h.value
+
+    def sample(self, k: int):
+        h = np.empty(self.size, np.float32)
+        y = np.empty(self.size, np.float32)
+        check(library().fs_sg_get_sample(self._s, int(k), _p(h, C.c_float), _p(y, C.c_float)))
+        return h, y
+
+    def train(self, steps: int, lr: float = 1e-3) -> float:
+        loss = C.c_double(0)
+        check(library().fs_sg_train(self._s, int(steps), float(lr), C.byref(loss)))
+        return loss.value
+
+    def eval(self) -> float:
+        loss = C.c_double(0)
+        check(library().fs_sg_eval(self._s, C.byref(loss)))
+        return loss.value
+
+    def eval_baselines(self):
+        """(uplift-only loss, no-change loss) over the held-out split."""
+        a, b = C.c_double(0), C.c_double(0)
+        check(library().fs_sg_eval_baselines(self._s, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def grad(self, idx) -> float:
+        a = (C.c_int * len(idx))(*[int(i) for i in idx])
+        loss = C.c_double(0)
+        check(library().fs_sg_grad(self._s, len(idx), a, C.byref(loss)))
+        return loss.value
+
+    def train_stats(self):
+        ms, fl = C.c_double(0), C.c_double(0)
+        check(library().fs_sg_train_stats(self._s, C.byref(ms), C.byref(fl)))
+        return ms.value, fl.value
+
+    def infer_flops(self) -> float:
+        f = C.c_double(0)
+        check(library().fs_sg_infer_flops(self._s, C.byref(f)))
+        return f.value
+
+    def predict(self, h, params) -> np.ndarray:
+        h = np.ascontiguousarray(h, np.float64).reshape(-1, self.size)
+        n = h.shape[0]
+        out = np.empty_like(h)
+        pa = (Params * n)(*params)
+        check(library().fs_sg_predict_host(self._s, n, _p(h, C.c_double), pa,
+                                           _p(out, C.c_double)))
+        return out
+
+    def predict_batch(self, batch: "FastScapeBatch", idx) -> None:
+        a = (C.c_int * len(idx))(*[int(i) for i in idx])
+        check(library().fs_sg_predict_batch(self._s, batch.handle, len(idx), a, None))
+
+    def ensemble(self, batch: "FastScapeBatch", nsteps: int, judge_fraction: float = 0.05,
+                 max_rel_rms: float = 0.01, min_agreement: float = 0.99, plain_steps: int = 1,
+                 seed: int = 2019):
+        """Judged surrogate-accelerated run of every realization of `batch`
+        (fs_sg_ensemble_run); returns (stats dict, fallen flags)."""
+        o = EnsembleOpts()
+        library().fs_sg_ensemble_defaults(C.byref(o))
+        o.nsteps, o.plain_steps = int(nsteps), int(plain_steps)
+        o.judge_fraction, o.max_rel_rms = float(judge_fraction), float(max_rel_rms)
+        o.min_agreement, o.seed = float(min_agreement), int(seed)
+        st = EnsembleStats()
+        fallen = (C.c_int * batch.n)()
+        check(library().fs_sg_ensemble_run(batch.handle, self._s, C.byref(o), C.byref(st),
+                                           fallen))
+        return st.as_dict(), np.array(fallen[:], dtype=np.int32)
+
+
+def compare_fields(width: int, height: int, params, a, b):
+    """The ensemble judge's measures for host field pairs: (relief-normalised
+    RMS error, receiver agreement) per pair (fs_sg_compare_host)."""
+    a = np.ascontiguousarray(a, np.float64).reshape(-1, width * height)
+    b = np.ascontiguousarray(b, np.float64).reshape(-1, width * height)
+    n = a.shape[0]
+    rel = np.empty(n, np.float64)
+    ag = np.empty(n, np.float64)
+    pa = (Params * n)(*params)
+    check(library().fs_sg_compare_host(width, height, pa, n, _p(a, C.c_double),
+                                       _p(b, C.c_double), _p(rel, C.c_double),
+                                       _p(ag, C.c_double)))
+    return rel, ag

@@ -135,6 +135,17 @@ struct fs_batch {
   bool graph_dirty = true;
   std::vector<cudaEvent_t> ev;
   double phase_ms[FS_NUM_TIMERS] = {};  // event timers (indices 0-3, 7, 8)
+  // Active subset (fs_batch_set_active): act_n > 0 steps only the
+  // realizations act_idx through their own descriptor, counter and tile
+  // arrays (the per-cell arrays are shared); act_n == 0 steps all.
+  int act_n = 0;
+  std::vector<int> act_idx;
+  fs::RealDesc *d_desc_act = nullptr;
+  fs::RealCtl *d_rctl_act = nullptr;
+  int *d_act_idx = nullptr;
+  fs::Tile *d_rtiles_act = nullptr, *d_dtiles_act = nullptr;
+  int nrt_act = 0, ndt_act = 0, act_cap = 0, act_tiles_cap[2] = {0, 0};
+  int act_walk_bps = 0, act_order_bps = 0, act_accum_bps = 0;
 };
 
 struct fs_model {
@@ -160,7 +171,9 @@ void free_batch(fs_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   void *bufs[] = {b->h, b->rec_alloc, b->mask, b->pdir, b->ent, b->par, b->amb, b->amb_r,
-                  b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles};
+                  b->lvl, b->acc, b->d_desc, b->d_rctl, b->d_ctl, b->d_rtiles, b->d_dtiles,
+                  b->d_desc_act, b->d_rctl_act, b->d_act_idx, b->d_rtiles_act,
+                  b->d_dtiles_act};
   for (void *x : bufs) cudaFree(x);
   for (double *t : b->tab) cudaFree(t);
   if (b->h_ctl) cudaFreeHost(b->h_ctl);
@@ -255,6 +268,15 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   a.nrtiles = b->nrtiles;
   a.dtiles = b->d_dtiles;
   a.ndtiles = b->ndtiles;
+  if (b->act_n > 0) {
+    a.desc = b->d_desc_act;
+    a.rctl = b->d_rctl_act;
+    a.nreal = b->act_n;
+    a.rtiles = b->d_rtiles_act;
+    a.nrtiles = b->nrt_act;
+    a.dtiles = b->d_dtiles_act;
+    a.ndtiles = b->ndt_act;
+  }
   a.nmode = b->nmode;
   a.neq = b->neq;
   a.do_erode = do_erode;
@@ -270,12 +292,18 @@ cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
   cudaError_t e = cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
                                   fs::kCtlResetBytes, b->stream);
   if (e == cudaSuccess)
-    e = cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream);
+    e = cudaMemsetAsync(a.rctl, 0, sizeof(fs::RealCtl) * a.nreal, b->stream);
   if (e == cudaSuccess)
     e = b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
                            : fs::launch_receivers_fast(a, b->stream);
   if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
-  if (e == cudaSuccess) e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->accum_bps, b->walk_bps, b->stream);
+  if (e == cudaSuccess) {
+    if (b->act_n > 0)
+      e = fs::launch_walk(a, b->walk_sms, b->act_order_bps, b->act_accum_bps, b->act_walk_bps,
+                          b->stream);
+    else
+      e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->accum_bps, b->walk_bps, b->stream);
+  }
   return e;
 }
 
@@ -299,17 +327,18 @@ int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
   FS_CUDA(cudaEventRecord(ev[0], b->stream));
   FS_CUDA(cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
                           fs::kCtlResetBytes, b->stream));
-  FS_CUDA(cudaMemsetAsync(b->d_rctl, 0, sizeof(fs::RealCtl) * b->n, b->stream));
+  FS_CUDA(cudaMemsetAsync(a.rctl, 0, sizeof(fs::RealCtl) * a.nreal, b->stream));
   FS_CUDA(b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
                              : fs::launch_receivers_fast(a, b->stream));
   FS_CUDA(cudaEventRecord(ev[1], b->stream));
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
   FS_CUDA(cudaEventRecord(ev[2], b->stream));
-  FS_CUDA(fs::launch_order(a, b->walk_sms, b->order_bps, b->stream));
+  const bool act = b->act_n > 0;
+  FS_CUDA(fs::launch_order(a, b->walk_sms, act ? b->act_order_bps : b->order_bps, b->stream));
   FS_CUDA(cudaEventRecord(ev[3], b->stream));
-  FS_CUDA(fs::launch_accum(a, b->walk_sms, b->accum_bps, b->stream));
+  FS_CUDA(fs::launch_accum(a, b->walk_sms, act ? b->act_accum_bps : b->accum_bps, b->stream));
   FS_CUDA(cudaEventRecord(ev[4], b->stream));
-  FS_CUDA(fs::launch_erode(a, b->walk_sms, b->walk_bps, b->stream));
+  FS_CUDA(fs::launch_erode(a, b->walk_sms, act ? b->act_walk_bps : b->walk_bps, b->stream));
   return FS_OK;
 }
 
@@ -373,6 +402,170 @@ int read_rctl(const fs_batch *b) {
   return FS_OK;
 }
 
+// Copies the active subset's per-realization counters (levels found,
+// cells placed) back to the realizations' own entries.
+__global__ void k_scatter_rctl(const fs::RealCtl *__restrict__ src, const int *__restrict__ idx,
+                               int n, fs::RealCtl *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[idx[i]] = src[i];
+}
+
+cudaError_t launch_scatter_rctl(fs_batch *b) {
+  k_scatter_rctl<<<(b->act_n + 127) / 128, 128, 0, b->stream>>>(b->d_rctl_act, b->d_act_idx,
+                                                                b->act_n, b->d_rctl);
+  return cudaGetLastError();
+}
+
+// Initial erosion tables of every realization (counts below min(65536,
+// size+1)), evaluated on host threads in parallel over realizations -- the
+// same records grow_table writes -- then uploaded.
+int init_tables(fs_batch *b) {
+  const int n = b->n;
+  std::vector<std::vector<double>> host(n);
+  std::vector<long long> cap(n);
+  for (int r = 0; r < n; r++) {
+    long long c = 1;
+    while (c <= std::min<long long>(b->size[r], 65535)) c *= 2;
+    cap[r] = std::min<long long>(c, static_cast<long long>(b->size[r]) + 1);
+  }
+  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(nt, 64);
+  nt = std::min<unsigned>(nt, static_cast<unsigned>(n));
+  auto work = [&](unsigned t) {
+    for (int r = static_cast<int>(t); r < n; r += static_cast<int>(nt)) {
+      const fs_params &p = b->p[r];
+      host[r].resize(static_cast<size_t>(cap[r]) * fs::kTabStride);
+      fs::fill_table_range(p.keq, p.neq, p.meq, p.dt, p.dr_orth, p.dr_diag, p.cell_area, 0,
+                           cap[r], host[r].data());
+    }
+  };
+  if (nt <= 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++) th.emplace_back(work, t);
+    for (auto &x : th) x.join();
+  }
+  for (int r = 0; r < n; r++) {
+    double *d = nullptr;
+    FS_CUDA(cudaMalloc(&d, host[r].size() * sizeof(double)));
+    b->tab[r] = d;
+    b->tab_cap[r] = static_cast<int>(cap[r]);
+    b->desc[r].tab = d;
+    b->desc[r].tab_cap = static_cast<int>(cap[r]);
+    FS_CUDA(cudaMemcpyAsync(d, host[r].data(), host[r].size() * sizeof(double),
+                            cudaMemcpyHostToDevice, b->stream));
+    FS_CUDA(cudaStreamSynchronize(b->stream));  // host[r] may be released next
+    std::vector<double>().swap(host[r]);
+  }
+  FS_CUDA(cudaMemcpyAsync(b->d_desc, b->desc.data(), n * sizeof(fs::RealDesc),
+                          cudaMemcpyHostToDevice, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  b->graph_dirty = true;
+  return FS_OK;
+}
+
+// Blocks per SM of a cooperative walk kernel: `want`, or fewer when fewer are
+// resident with `smem` bytes of shared memory.
+int resident_bps(const void *kernel, size_t smem, int want, int *out) {
+  int occ = 0;
+  FS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, fs::walk_threads(), smem));
+  if (occ < 1) return set_error(FS_ERR_CUDA, "walk kernel cannot be resident");
+  *out = std::min(occ, want);
+  return FS_OK;
+}
+
+// Selects the realizations the next timesteps advance (n = 0: all).
+int set_active(fs_batch *b, int n, const int *idx) {
+  if (n < 0 || n > b->n) return set_error(FS_ERR_ARG, "active count %d out of [0, %d]", n, b->n);
+  if (n > 0 && !idx) return set_error(FS_ERR_ARG, "idx is NULL");
+  DeviceGuard dg(b->device);
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  b->graph_dirty = true;
+  if (n == 0) {
+    b->act_n = 0;
+    b->act_idx.clear();
+    return FS_OK;
+  }
+  std::vector<char> seen(b->n, 0);
+  for (int i = 0; i < n; i++) {
+    if (idx[i] < 0 || idx[i] >= b->n)
+      return set_error(FS_ERR_ARG, "realization %d out of range [0, %d)", idx[i], b->n);
+    if (seen[idx[i]]) return set_error(FS_ERR_ARG, "realization %d listed twice", idx[i]);
+    seen[idx[i]] = 1;
+  }
+  std::vector<fs::RealDesc> desc(n);
+  std::vector<fs::Tile> rt, dt;
+  for (int i = 0; i < n; i++) {
+    const int r = idx[i];
+    desc[i] = b->desc[r];
+    for (int kind = 0; kind < 2; kind++) {
+      std::vector<fs::Tile> &v = kind == 0 ? rt : dt;
+      const size_t at = v.size();
+      v.resize(at + static_cast<size_t>(b->W[r] / 32 + 2) * (b->H[r] / 32 + 2));
+      const int got = fs::append_tiles(kind, i, b->W[r], b->H[r], v.data() + at,
+                                       static_cast<int>(v.size() - at));
+      v.resize(at + std::max(got, 0));
+    }
+  }
+  if (n > b->act_cap) {
+    cudaFree(b->d_desc_act);
+    cudaFree(b->d_rctl_act);
+    cudaFree(b->d_act_idx);
+    b->d_desc_act = nullptr;
+    b->d_rctl_act = nullptr;
+    b->d_act_idx = nullptr;
+    b->act_cap = 0;
+    FS_CUDA(cudaMalloc(&b->d_desc_act, n * sizeof(fs::RealDesc)));
+    FS_CUDA(cudaMalloc(&b->d_rctl_act, n * sizeof(fs::RealCtl)));
+    FS_CUDA(cudaMalloc(&b->d_act_idx, n * sizeof(int)));
+    b->act_cap = n;
+  }
+  fs::Tile **tiles[2] = {&b->d_rtiles_act, &b->d_dtiles_act};
+  const size_t ntile[2] = {rt.size(), dt.size()};
+  for (int k = 0; k < 2; k++)
+    if (static_cast<int>(ntile[k]) > b->act_tiles_cap[k]) {
+      cudaFree(*tiles[k]);
+      *tiles[k] = nullptr;
+      b->act_tiles_cap[k] = 0;
+      FS_CUDA(cudaMalloc(tiles[k], std::max<size_t>(1, ntile[k]) * sizeof(fs::Tile)));
+      b->act_tiles_cap[k] = static_cast<int>(ntile[k]);
+    }
+  FS_CUDA(cudaMemcpyAsync(b->d_desc_act, desc.data(), n * sizeof(fs::RealDesc),
+                          cudaMemcpyHostToDevice, b->stream));
+  FS_CUDA(cudaMemcpyAsync(b->d_act_idx, idx, n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  if (!rt.empty())
+    FS_CUDA(cudaMemcpyAsync(b->d_rtiles_act, rt.data(), rt.size() * sizeof(fs::Tile),
+                            cudaMemcpyHostToDevice, b->stream));
+  if (!dt.empty())
+    FS_CUDA(cudaMemcpyAsync(b->d_dtiles_act, dt.data(), dt.size() * sizeof(fs::Tile),
+                            cudaMemcpyHostToDevice, b->stream));
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  // a subset of one runs the single-grid kernels, which may hold fewer
+  // blocks per SM than the batch kernels the launch shape was tuned for
+  const bool single = n == 1;
+  const size_t smem = fs::walk_smem_bytes(n);
+  if (int st = resident_bps(fs::walk_kernel_ptr(b->nmode, single, b->erode_isub ? 1 : 0), smem,
+                           b->walk_bps, &b->act_walk_bps))
+    return st;
+  if (int st = resident_bps(fs::order_kernel_ptr(single, b->order_bps), smem, b->order_bps,
+                           &b->act_order_bps))
+    return st;
+  if (b->act_order_bps < b->order_bps) {
+    // the 3-block ordering form is compiled for exactly 3 blocks per SM
+    if (int st = resident_bps(fs::order_kernel_ptr(single, 2), smem, 2, &b->act_order_bps))
+      return st;
+  }
+  if (int st = resident_bps(fs::accum_kernel_ptr(single), smem, b->accum_bps,
+                           &b->act_accum_bps))
+    return st;
+  b->nrt_act = static_cast<int>(rt.size());
+  b->ndt_act = static_cast<int>(dt.size());
+  b->act_idx.assign(idx, idx + n);
+  b->act_n = n;
+  return FS_OK;
+}
+
 // k timesteps of every realization; a timestep that outgrew an erosion table
 // stopped before changing h and the rest of the batch did nothing: grow the
 // table and carry on from there.
@@ -414,13 +607,20 @@ int batch_step(fs_batch *b, int k) {
         b->phase_ms[3] += tot;
       }
     }
+    if (b->act_n > 0) FS_CUDA(launch_scatter_rctl(b));
     if (int st = collect_status(b)) return st;
     const int completed = b->h_ctl->steps_done;
     done += completed;
     b->steps += completed;
     if (completed > 0) b->have_step = true;
     if (b->h_ctl->abort_k > 0) {
-      if (int st = grow_table(b, b->h_ctl->abort_r, b->h_ctl->abort_k)) return st;
+      const int ar = b->act_n > 0 ? b->act_idx[b->h_ctl->abort_r] : b->h_ctl->abort_r;
+      if (int st = grow_table(b, ar, b->h_ctl->abort_k)) return st;
+      if (b->act_n > 0)
+        for (int i = 0; i < b->act_n; i++)
+          if (b->act_idx[i] == ar)
+            FS_CUDA(cudaMemcpyAsync(b->d_desc_act + i, &b->desc[ar], sizeof(fs::RealDesc),
+                                    cudaMemcpyHostToDevice, b->stream));
     } else if (completed != batch) {
       return set_error(FS_ERR_CUDA, "%d of %d timesteps completed without a status", completed,
                        batch);
@@ -560,8 +760,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
                           cudaMemcpyHostToDevice, b->stream),
           "upload(desc)"))
     return fail(*status);
-  for (int r = 0; r < n; r++)
-    if (int st = grow_table(b, r, std::min<long long>(b->size[r], 65535))) return fail(st);
+  if (int st = init_tables(b)) return fail(st);
   // Stencil tiles of every realization.
   {
     std::vector<fs::Tile> rt, dt;
@@ -1185,6 +1384,39 @@ int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *gra
                      int *erode_int_sub) {
   FS_MODEL(m);
   return fs_batch_launch_config(m->b, order_bps, erode_bps, graph, erode_int_sub);
+}
+
+int fs_batch_set_active(fs_batch *b, int n, const int *idx) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  return set_active(b, n, idx);
+}
+
+int fs_batch_device_elevation(const fs_batch *b, int r, double **d_h) {
+  if (int st = check_r(b, r)) return st;
+  if (!d_h) return set_error(FS_ERR_ARG, "d_h is NULL");
+  *d_h = b->h + b->off[r];
+  return FS_OK;
+}
+
+int fs_batch_get_params(const fs_batch *b, int r, fs_params *out) {
+  if (int st = check_r(b, r)) return st;
+  if (!out) return set_error(FS_ERR_ARG, "out is NULL");
+  *out = b->p[r];
+  return FS_OK;
+}
+
+int fs_batch_get_shape(const fs_batch *b, int r, int *width, int *height) {
+  if (int st = check_r(b, r)) return st;
+  if (width) *width = b->W[r];
+  if (height) *height = b->H[r];
+  return FS_OK;
+}
+
+int fs_batch_stream(const fs_batch *b, void **stream) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (!stream) return set_error(FS_ERR_ARG, "stream is NULL");
+  *stream = b->stream;
+  return FS_OK;
 }
 
 int fs_batch_synchronize(const fs_batch *b) {

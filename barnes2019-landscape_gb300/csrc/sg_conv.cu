@@ -675,6 +675,16 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   return cudaSuccess;
 }
 
+// Splits `ksteps` pixel steps so that about three CTAs per SM run, each
+// over at least 8 steps.
+void split_pixels(WgradPlan &p, int ksteps) {
+  int splits = (3 * p.sms + p.mtiles - 1) / p.mtiles;
+  if (splits > ksteps / 8) splits = ksteps / 8;
+  if (splits < 1) splits = 1;
+  p.kper = (ksteps + splits - 1) / splits;
+  p.splits = (ksteps + p.kper - 1) / p.kper;
+}
+
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
                        const char **why) {
   const char *dummy;
@@ -707,12 +717,8 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
   const int nchunk = taps * (x.C / p.cwa);
   p.mtiles = (nchunk + (kM / p.cwa) - 1) / (kM / p.cwa);
   p.ksteps = static_cast<int>(x.pixels() / kKPix);
-  // split the pixels so about three CTAs per SM run, each over >= 8 steps
-  int splits = (3 * sms + p.mtiles - 1) / p.mtiles;
-  if (splits > p.ksteps / 8) splits = p.ksteps / 8;
-  if (splits < 1) splits = 1;
-  p.kper = (p.ksteps + splits - 1) / splits;
-  p.splits = (p.ksteps + p.kper - 1) / p.kper;
+  p.sms = sms;
+  split_pixels(p, p.ksteps);
   p.dw = dw;
   cudaError_t e = map_act(&p.tmx, x, p.cwa, p.pt);
   if (e != cudaSuccess) return *why = "tensor map (X)", e;
@@ -724,7 +730,7 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
 namespace {
 
 template <int CB>
-cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s) {
+cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_conv<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -750,12 +756,13 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s) {
   a.out = p.out;
   a.ldo = p.ldo;
   a.err = err;
-  k_conv<CB><<<dim3(p.grid_x, p.grid_y), kThreads, p.smem, s>>>(p.tma, p.tmb, a);
+  const int gx = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
+  k_conv<CB><<<dim3(gx, p.grid_y), kThreads, p.smem, s>>>(p.tma, p.tmb, a);
   return cudaGetLastError();
 }
 
 template <int CWA, int CWB>
-cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s) {
+cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_wgrad<CWA, CWB>,
@@ -776,40 +783,42 @@ cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s) {
   a.taps = p.taps;
   a.nchunk = p.taps * (p.cin / p.cwa);
   a.stages = p.stages;
-  a.ksteps = p.ksteps;
-  a.kper = p.kper;
+  WgradPlan q = p;
+  if (nimg > 0) split_pixels(q, nimg * p.pt.tiles_x * p.pt.tiles_y);
+  a.ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
+  a.kper = q.kper;
   a.dw = p.dw;
   a.err = err;
-  k_wgrad<CWA, CWB><<<dim3(p.mtiles, p.splits), kThreads, p.smem, s>>>(p.tmx, p.tmy, a);
+  k_wgrad<CWA, CWB><<<dim3(p.mtiles, q.splits), kThreads, p.smem, s>>>(p.tmx, p.tmy, a);
   return cudaGetLastError();
 }
 
 template <int CWA>
-cudaError_t launch_wgrad_a(const WgradPlan &p, int *err, cudaStream_t s) {
+cudaError_t launch_wgrad_a(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
   switch (p.cwb) {
-    case 64: return launch_wgrad_cw<CWA, 64>(p, err, s);
-    case 32: return launch_wgrad_cw<CWA, 32>(p, err, s);
-    default: return launch_wgrad_cw<CWA, 16>(p, err, s);
+    case 64: return launch_wgrad_cw<CWA, 64>(p, err, s, nimg);
+    case 32: return launch_wgrad_cw<CWA, 32>(p, err, s, nimg);
+    default: return launch_wgrad_cw<CWA, 16>(p, err, s, nimg);
   }
 }
 
 }  // namespace
 
-cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s) {
-  if (p.grid_x <= 0) return cudaErrorInvalidValue;
+cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s, int nimg) {
+  if (p.grid_x <= 0 || nimg < 0 || nimg > p.B) return cudaErrorInvalidValue;
   switch (p.cb) {
-    case 64: return launch_conv_cb<64>(p, err, s);
-    case 32: return launch_conv_cb<32>(p, err, s);
-    default: return launch_conv_cb<16>(p, err, s);
+    case 64: return launch_conv_cb<64>(p, err, s, nimg);
+    case 32: return launch_conv_cb<32>(p, err, s, nimg);
+    default: return launch_conv_cb<16>(p, err, s, nimg);
   }
 }
 
-cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s) {
-  if (p.mtiles <= 0) return cudaErrorInvalidValue;
+cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
+  if (p.mtiles <= 0 || nimg < 0 || nimg > p.B) return cudaErrorInvalidValue;
   switch (p.cwa) {
-    case 64: return launch_wgrad_a<64>(p, err, s);
-    case 32: return launch_wgrad_a<32>(p, err, s);
-    default: return launch_wgrad_a<16>(p, err, s);
+    case 64: return launch_wgrad_a<64>(p, err, s, nimg);
+    case 32: return launch_wgrad_a<32>(p, err, s, nimg);
+    default: return launch_wgrad_a<16>(p, err, s, nimg);
   }
 }
 

@@ -69,7 +69,7 @@ struct WgradPlan {
   CUtensorMap tmy;  // dY, box {cwb, BW, BH, 1}
   int B = 0, H = 0, W = 0, cin = 0, cout = 0, taps = 9, cwa = 0, cwb = 0, stages = 0;
   PixTile pt;
-  int mtiles = 0, splits = 0, ksteps = 0, kper = 0;
+  int mtiles = 0, splits = 0, ksteps = 0, kper = 0, sms = 1;
   float *dw = nullptr;
   size_t smem = 0;
 };
@@ -82,8 +82,10 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
                       int ldo, const char **why);
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
                        const char **why);
-cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s);
-cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s);
+// nimg > 0 runs the plan over the first nimg images only (the tensor maps
+// cover the plan's full batch).
+cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s, int nimg = 0);
+cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s, int nimg = 0);
 
 // Flipped, transposed weights for the data gradient:
 // wd[ci][8 - tap][co] = w[co][tap][ci] (taps = 9), wd[ci][0][co] = w[co][0][ci] (taps = 1).

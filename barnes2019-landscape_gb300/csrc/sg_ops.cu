@@ -1,0 +1,568 @@
+// sg_ops.cu -- the surrogate network's memory-bound kernels: input planes,
+// 2x2 pooling and its adjoint, upsample-and-concatenate and its adjoint, the
+// 1x1 output head with the loss and its gradient, bias gradients, Adam, and
+// the jump that applies a prediction to an FP64 elevation field. All NHWC
+// BF16 tensors move 8 channels (16 bytes) per access.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sg_ops.h"
+
+namespace sg {
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ void load8(const bf16 *p, float (&f)[8]) {
+  const uint4 v = *reinterpret_cast<const uint4 *>(p);
+  const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 t = __bfloat1622float2(h[i]);
+    f[2 * i] = t.x;
+    f[2 * i + 1] = t.y;
+  }
+}
+
+__device__ __forceinline__ void store8(bf16 *p, const float (&f)[8]) {
+  uint4 v;
+  __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+  for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+  *reinterpret_cast<uint4 *>(p) = v;
+}
+
+int blocks_for(long long n) {
+  long long b = (n + kBlock - 1) / kBlock;
+  if (b > 152 * 16) b = 152 * 16;
+  return b < 1 ? 1 : static_cast<int>(b);
+}
+
+// ring cells (the halo and the base-level ring) never change
+__device__ __forceinline__ bool interior(int x, int y, int W, int H) {
+  return x >= 2 && y >= 2 && x < W - 2 && y < H - 2;
+}
+
+__global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__restrict__ yt, int W,
+                        int H) {
+  const long long hw = static_cast<long long>(W) * H;
+  const long long n = hw * v.n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int b = static_cast<int>(i / hw);
+    const long long pix = i - b * hw;
+    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+    const int src = v.idx ? v.idx[b] : b;
+    const SampleMeta m = v.meta[src];
+    double h;
+    if (v.h64)
+      h = v.h64[src][pix];
+    else
+      h = v.h32[static_cast<long long>(src) * hw + pix];
+    float f[16];
+    f[0] = static_cast<float>(h / m.s);
+    f[1] = m.log_su;
+    f[2] = m.k_n;
+    f[3] = m.m_n;
+    f[4] = m.u_n;
+    f[5] = interior(x, y, W, H) ? 0.0f : 1.0f;
+#pragma unroll
+    for (int j = 6; j < 16; j++) f[j] = 0.0f;
+    float lo[8], hi[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      lo[j] = f[j];
+      hi[j] = f[8 + j];
+    }
+    bf16 *o = in + i * kInputChannels;
+    store8(o, lo);
+    store8(o + 8, hi);
+    if (yt) yt[i] = v.y ? v.y[static_cast<long long>(src) * hw + pix] : 0.0f;
+  }
+}
+
+__global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, int B, int Ho,
+                           int Wo, int C) {
+  const int c8n = C / 8;
+  const long long n = static_cast<long long>(B) * Ho * Wo * c8n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int c8 = static_cast<int>(i % c8n);
+    const long long pix = i / c8n;
+    const int x = static_cast<int>(pix % Wo);
+    const long long r = pix / Wo;
+    const int y = static_cast<int>(r % Ho);
+    const int b = static_cast<int>(r / Ho);
+    const long long Wi = 2ll * Wo;
+    const bf16 *p = in + ((static_cast<long long>(b) * 2 * Ho + 2 * y) * Wi + 2 * x) * C + c8 * 8;
+    float a[8], t[8];
+    load8(p, a);
+    load8(p + C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += t[j];
+    load8(p + Wi * C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += t[j];
+    load8(p + Wi * C + C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = 0.25f * (a[j] + t[j]);
+    store8(out + pix * C + c8 * 8, a);
+  }
+}
+
+// cat[b,y,x,0:Cd] = d[b,y/2,x/2,:], cat[b,y,x,Cd:Cd+Cs] = s[b,y,x,:]
+__global__ void k_upcat(const bf16 *__restrict__ d, const bf16 *__restrict__ s,
+                        bf16 *__restrict__ cat, int B, int H, int W, int Cd, int Cs) {
+  const int C = Cd + Cs, c8n = C / 8;
+  const long long n = static_cast<long long>(B) * H * W * c8n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int c = static_cast<int>(i % c8n) * 8;
+    const long long pix = i / c8n;
+    uint4 v;
+    if (c < Cd) {
+      const int x = static_cast<int>(pix % W);
+      const long long r = pix / W;
+      const int y = static_cast<int>(r % H);
+      const int b = static_cast<int>(r / H);
+      const long long lp = (static_cast<long long>(b) * (H / 2) + y / 2) * (W / 2) + x / 2;
+      v = *reinterpret_cast<const uint4 *>(d + lp * Cd + c);
+    } else {
+      v = *reinterpret_cast<const uint4 *>(s + pix * Cs + (c - Cd));
+    }
+    *reinterpret_cast<uint4 *>(cat + pix * C + c) = v;
+  }
+}
+
+// gd[b,y,x,:] = sum over the 2x2 block of g[b,2y+i,2x+j,0:Cd] (g has C
+// channels at twice the resolution): the adjoint of nearest upsampling
+__global__ void k_sumpool2(const bf16 *__restrict__ g, int C, bf16 *__restrict__ gd, int B,
+                           int Ho, int Wo, int Cd) {
+  const int c8n = Cd / 8;
+  const long long n = static_cast<long long>(B) * Ho * Wo * c8n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int c8 = static_cast<int>(i % c8n);
+    const long long pix = i / c8n;
+    const int x = static_cast<int>(pix % Wo);
+    const long long r = pix / Wo;
+    const int y = static_cast<int>(r % Ho);
+    const int b = static_cast<int>(r / Ho);
+    const long long Wi = 2ll * Wo;
+    const bf16 *p = g + ((static_cast<long long>(b) * 2 * Ho + 2 * y) * Wi + 2 * x) * C + c8 * 8;
+    float a[8], t[8];
+    load8(p, a);
+    load8(p + C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += t[j];
+    load8(p + Wi * C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += t[j];
+    load8(p + Wi * C + C, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] += t[j];
+    store8(gd + pix * Cd + c8 * 8, a);
+  }
+}
+
+// gs = gcat[..., Cd:Cd+Cs] + (s > 0) * gp(up) / 4: the skip tensor's gradient
+// from the decoder (already masked) plus the pooling path's, masked by ReLU
+__global__ void k_skipgrad(const bf16 *__restrict__ gcat, int C, int Cd,
+                           const bf16 *__restrict__ s, const bf16 *__restrict__ gp,
+                           bf16 *__restrict__ gs, int B, int H, int W, int Cs) {
+  const int c8n = Cs / 8;
+  const long long n = static_cast<long long>(B) * H * W * c8n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int c = static_cast<int>(i % c8n) * 8;
+    const long long pix = i / c8n;
+    const int x = static_cast<int>(pix % W);
+    const long long r = pix / W;
+    const int y = static_cast<int>(r % H);
+    const int b = static_cast<int>(r / H);
+    const long long lp = (static_cast<long long>(b) * (H / 2) + y / 2) * (W / 2) + x / 2;
+    float a[8], sv[8], pv[8];
+    load8(gcat + pix * C + Cd + c, a);
+    load8(s + pix * Cs + c, sv);
+    load8(gp + lp * Cs + c, pv);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (sv[j] > 0.0f) a[j] += 0.25f * pv[j];
+    store8(gs + pix * Cs + c, a);
+  }
+}
+
+// 1x1 head on the last decoder activation x (C channels): z = b + w.x;
+// training: err = z - y on interior cells, the loss
+//   L = (1/n) sum_s wgt_s * mean_interior(err^2),
+// dz = dL/dz, gx = dz * w * (x > 0) (the ReLU of x), dw += dz * x, db += dz.
+template <int C>
+__global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ x,
+                                                       const float *__restrict__ hw_,
+                                                       const float *__restrict__ yt,
+                                                       const SampleView v, int W, int H,
+                                                       bf16 *__restrict__ gx,
+                                                       float *__restrict__ dwb,
+                                                       double *__restrict__ loss) {
+  __shared__ float s_w[C + 1];
+  __shared__ float s_red[kBlock / 32][C + 2];
+  if (threadIdx.x <= C) s_w[threadIdx.x] = hw_[threadIdx.x];
+  __syncthreads();
+  const long long hwn = static_cast<long long>(W) * H;
+  const long long n = hwn * v.n;
+  const double inv_int = 1.0 / (static_cast<double>(W - 4) * (H - 4) * v.n);
+  float acc[C + 1];
+#pragma unroll
+  for (int j = 0; j <= C; j++) acc[j] = 0.0f;
+  double lsum = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int b = static_cast<int>(i / hwn);
+    const long long pix = i - b * hwn;
+    const int px = static_cast<int>(pix % W), py = static_cast<int>(pix / W);
+    float xv[C];
+#pragma unroll
+    for (int j = 0; j < C; j += 8) {
+      float t[8];
+      load8(x + i * C + j, t);
+#pragma unroll
+      for (int k = 0; k < 8; k++) xv[j + k] = t[k];
+    }
+    float z = s_w[C];
+#pragma unroll
+    for (int j = 0; j < C; j++) z += s_w[j] * xv[j];
+    float dz = 0.0f;
+    if (interior(px, py, W, H)) {
+      const int src = v.idx ? v.idx[b] : b;
+      const float wgt = v.meta[src].weight;
+      const float err = z - yt[i];
+      lsum += static_cast<double>(wgt) * err * err * inv_int;
+      dz = static_cast<float>(2.0 * wgt * err * inv_int);
+    }
+#pragma unroll
+    for (int j = 0; j < C; j += 8) {
+      float t[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) t[k] = xv[j + k] > 0.0f ? dz * s_w[j + k] : 0.0f;
+      store8(gx + i * C + j, t);
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++) acc[j] += dz * xv[j];
+    acc[C] += dz;
+  }
+  // block reduction: warp shuffles, then one row per warp in shared memory
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j <= C; j++) {
+    float t = acc[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) s_red[warp][j] = t;
+  }
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if (lane == 0) s_red[warp][C + 1] = static_cast<float>(lsum);
+  __syncthreads();
+  if (threadIdx.x <= C) {
+    float t = 0.0f;
+    for (int k = 0; k < kBlock / 32; k++) t += s_red[k][threadIdx.x];
+    atomicAdd(dwb + threadIdx.x, t);
+  }
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < kBlock / 32; k++) t += s_red[k][C + 1];
+    atomicAdd(loss, t);
+  }
+}
+
+// inference: h_out = h_in + u * z on interior cells (FP64), rings unchanged
+template <int C>
+__global__ void __launch_bounds__(kBlock) k_head_apply(const bf16 *__restrict__ x,
+                                                       const float *__restrict__ hw_,
+                                                       const SampleView v, int W, int H,
+                                                       double *const *__restrict__ hout) {
+  __shared__ float s_w[C + 1];
+  if (threadIdx.x <= C) s_w[threadIdx.x] = hw_[threadIdx.x];
+  __syncthreads();
+  const long long hwn = static_cast<long long>(W) * H;
+  const long long n = hwn * v.n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int b = static_cast<int>(i / hwn);
+    const long long pix = i - b * hwn;
+    const int px = static_cast<int>(pix % W), py = static_cast<int>(pix / W);
+    const int src = v.idx ? v.idx[b] : b;
+    const double h = v.h64[src][pix];
+    double out = h;
+    if (interior(px, py, W, H)) {
+      float z = s_w[C];
+#pragma unroll
+      for (int j = 0; j < C; j += 8) {
+        float t[8];
+        load8(x + i * C + j, t);
+#pragma unroll
+        for (int k = 0; k < 8; k++) z += s_w[j + k] * t[k];
+      }
+      out = h + static_cast<double>(v.meta[src].u) * z;
+    }
+    hout[b][pix] = out;
+  }
+}
+
+// db[c] += sum over pixels of g[p][c]
+__global__ void __launch_bounds__(kBlock) k_bias_grad(const bf16 *__restrict__ g, long long pixels,
+                                                      int C, float *__restrict__ db) {
+  __shared__ float s_acc[kBlock][8];
+  const int c8n = C / 8;
+  const int per = kBlock / c8n;  // pixels per block row
+  const int c8 = threadIdx.x % c8n, row = threadIdx.x / c8n;
+  float a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (row < per) {
+    for (long long p = blockIdx.x * static_cast<long long>(per) + row; p < pixels;
+         p += static_cast<long long>(gridDim.x) * per) {
+      float t[8];
+      load8(g + p * C + c8 * 8, t);
+#pragma unroll
+      for (int j = 0; j < 8; j++) a[j] += t[j];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; j++) s_acc[threadIdx.x][j] = a[j];
+  __syncthreads();
+  if (threadIdx.x < C) {
+    const int cg = threadIdx.x / 8, j = threadIdx.x % 8;
+    float t = 0.0f;
+    for (int r = 0; r < per; r++) t += s_acc[r * c8n + cg][j];
+    atomicAdd(db + threadIdx.x, t);
+  }
+}
+
+// Adam (bias-corrected) on FP32 masters; conv weights also refresh their BF16
+// copies: forward layout [cout][tap][cin] and the data-gradient layout
+// [cin][taps-1-tap][cout]
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, long long n, float lr_t, float b1, float b2,
+                       float eps_t, bf16 *__restrict__ wf, bf16 *__restrict__ wd, int cout,
+                       int cin, int taps) {
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float pi = p[i] - lr_t * mi / (sqrtf(vi) + eps_t);
+    p[i] = pi;
+    if (wf) {
+      const bf16 q = __float2bfloat16_rn(pi);
+      wf[i] = q;
+      const int ci = static_cast<int>(i % cin);
+      const int tap = static_cast<int>((i / cin) % taps);
+      const int co = static_cast<int>(i / (static_cast<long long>(cin) * taps));
+      wd[(static_cast<long long>(ci) * taps + (taps - 1 - tap)) * cout + co] = q;
+    }
+  }
+}
+
+__global__ void k_to_bf16(const float *__restrict__ p, long long n, bf16 *__restrict__ wf,
+                          bf16 *__restrict__ wd, int cout, int cin, int taps) {
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const bf16 q = __float2bfloat16_rn(p[i]);
+    wf[i] = q;
+    const int ci = static_cast<int>(i % cin);
+    const int tap = static_cast<int>((i / cin) % taps);
+    const int co = static_cast<int>(i / (static_cast<long long>(cin) * taps));
+    wd[(static_cast<long long>(ci) * taps + (taps - 1 - tap)) * cout + co] = q;
+  }
+}
+
+// per-field maximum (one block per field; every field has hw cells)
+__global__ void __launch_bounds__(kBlock) k_field_max(double *const *__restrict__ h64,
+                                                      const float *__restrict__ h32,
+                                                      long long hw, double *__restrict__ out) {
+  const int f = blockIdx.x;
+  double mx = -1e300;
+  for (long long i = threadIdx.x; i < hw; i += kBlock) {
+    const double t = h64 ? h64[f][i] : static_cast<double>(h32[f * hw + i]);
+    mx = t > mx ? t : mx;
+  }
+  __shared__ double s[kBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mx = s[0];
+    for (int k = 1; k < kBlock / 32; k++) mx = fmax(mx, s[k]);
+    out[f] = mx;
+  }
+}
+
+// dataset record: h_t as FP32 and the target y = (h_next - h_t)/u (0 on the rings)
+__global__ void k_record(double *const *__restrict__ ht, double *const *__restrict__ hn,
+                         const int *__restrict__ slot, const float *__restrict__ u, int n, int W,
+                         int H, float *__restrict__ dh, float *__restrict__ dy) {
+  const long long hw = static_cast<long long>(W) * H;
+  const long long tot = hw * n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < tot;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int k = static_cast<int>(i / hw);
+    const long long pix = i - k * hw;
+    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+    const long long o = static_cast<long long>(slot[k]) * hw + pix;
+    const double a = ht[k][pix];
+    if (dh) dh[o] = static_cast<float>(a);
+    if (dy) dy[o] = interior(x, y, W, H) ? static_cast<float>((hn[k][pix] - a) / u[k]) : 0.0f;
+  }
+}
+
+// losses of the two jumps that need no network, with the training loss's
+// weighting: uplift only (y_pred = 1) into out[0], no change (y_pred = 0)
+// into out[1]
+__global__ void __launch_bounds__(kBlock) k_baseline_loss(const SampleView v, int W, int H,
+                                                          double *__restrict__ out) {
+  const long long hw = static_cast<long long>(W) * H;
+  const long long n = hw * v.n;
+  const double inv_int = 1.0 / (static_cast<double>(W - 4) * (H - 4) * v.n);
+  double a = 0.0, b = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int k = static_cast<int>(i / hw);
+    const long long pix = i - k * hw;
+    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+    if (!interior(x, y, W, H)) continue;
+    const int src = v.idx ? v.idx[k] : k;
+    const double w = v.meta[src].weight;
+    const double t = v.y[static_cast<long long>(src) * hw + pix];
+    a += w * (1.0 - t) * (1.0 - t) * inv_int;
+    b += w * t * t * inv_int;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, a);
+    atomicAdd(out + 1, b);
+  }
+}
+
+// copies FP64 fields (gather by pointer)
+__global__ void k_copy_fields(double *const *__restrict__ src, double *const *__restrict__ dst,
+                              int n, long long hw) {
+  const long long tot = hw * n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < tot;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int k = static_cast<int>(i / hw);
+    const long long pix = i - k * hw;
+    dst[k][pix] = src[k][pix];
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H, cudaStream_t s) {
+  k_input<<<blocks_for(static_cast<long long>(W) * H * v.n), kBlock, 0, s>>>(v, in, yt, W, H);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_avgpool2(const Act &in, const Act &out, cudaStream_t s) {
+  k_avgpool2<<<blocks_for(out.pixels() * out.C / 8), kBlock, 0, s>>>(in.p, out.p, out.B, out.H,
+                                                                      out.W, out.C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_upcat(const Act &d, const Act &skip, const Act &cat, cudaStream_t s) {
+  k_upcat<<<blocks_for(cat.pixels() * cat.C / 8), kBlock, 0, s>>>(d.p, skip.p, cat.p, cat.B,
+                                                                   cat.H, cat.W, d.C, skip.C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s) {
+  k_sumpool2<<<blocks_for(gd.pixels() * gd.C / 8), kBlock, 0, s>>>(gcat.p, gcat.C, gd.p, gd.B,
+                                                                   gd.H, gd.W, gd.C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act &gp,
+                            const Act &gs, cudaStream_t s) {
+  k_skipgrad<<<blocks_for(gs.pixels() * gs.C / 8), kBlock, 0, s>>>(
+      gcat.p, gcat.C, cd, skip.p, gp.p, gs.p, gs.B, gs.H, gs.W, gs.C);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_head_train(const Act &x, const float *head, const float *yt,
+                              const SampleView &v, const Act &gx, float *dhead, double *loss,
+                              cudaStream_t s) {
+  const int blocks = blocks_for(x.pixels());
+  switch (x.C) {
+    case 16:
+      k_head_train<16><<<blocks, kBlock, 0, s>>>(x.p, head, yt, v, x.W, x.H, gx.p, dhead, loss);
+      break;
+    case 32:
+      k_head_train<32><<<blocks, kBlock, 0, s>>>(x.p, head, yt, v, x.W, x.H, gx.p, dhead, loss);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView &v,
+                              double *const *hout, cudaStream_t s) {
+  const int blocks = blocks_for(x.pixels());
+  switch (x.C) {
+    case 16: k_head_apply<16><<<blocks, kBlock, 0, s>>>(x.p, head, v, x.W, x.H, hout); break;
+    case 32: k_head_apply<32><<<blocks, kBlock, 0, s>>>(x.p, head, v, x.W, x.H, hout); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s) {
+  if (g.C % 8 || g.C > 256) return cudaErrorInvalidValue;
+  int blocks = static_cast<int>((g.pixels() + 4095) / 4096);
+  if (blocks > 152 * 4) blocks = 152 * 4;
+  if (blocks < 1) blocks = 1;
+  k_bias_grad<<<blocks, kBlock, 0, s>>>(g.p, g.pixels(), g.C, db);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float *p, const float *g, float *m, float *v, long long n, float lr_t,
+                        float b1, float b2, float eps_t, bf16 *wf, bf16 *wd, int cout, int cin,
+                        int taps, cudaStream_t s) {
+  k_adam<<<blocks_for(n), kBlock, 0, s>>>(p, g, m, v, n, lr_t, b1, b2, eps_t, wf, wd, cout, cin,
+                                          taps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float *p, long long n, bf16 *wf, bf16 *wd, int cout, int cin,
+                           int taps, cudaStream_t s) {
+  k_to_bf16<<<blocks_for(n), kBlock, 0, s>>>(p, n, wf, wd, cout, cin, taps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_field_max(double *const *h64, const float *h32, int nfields, long long hw,
+                             double *out, cudaStream_t s) {
+  k_field_max<<<nfields, kBlock, 0, s>>>(h64, h32, hw, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record(double *const *ht, double *const *hn, const int *slot, const float *u,
+                          int n, int W, int H, float *dh, float *dy, cudaStream_t s) {
+  k_record<<<blocks_for(static_cast<long long>(W) * H * n), kBlock, 0, s>>>(ht, hn, slot, u, n, W,
+                                                                            H, dh, dy);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_baseline_loss(const SampleView &v, int W, int H, double *out, cudaStream_t s) {
+  k_baseline_loss<<<blocks_for(static_cast<long long>(W) * H * v.n), kBlock, 0, s>>>(v, W, H, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_fields(double *const *src, double *const *dst, int n, long long hw,
+                               cudaStream_t s) {
+  k_copy_fields<<<blocks_for(hw * n), kBlock, 0, s>>>(src, dst, n, hw);
+  return cudaGetLastError();
+}
+
+}  // namespace sg

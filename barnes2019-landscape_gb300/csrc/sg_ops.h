@@ -1,0 +1,61 @@
+// sg_ops.h -- launchers of the surrogate network's memory-bound kernels
+// (sg_ops.cu). Not part of the public ABI.
+#pragma once
+
+#include "sg_internal.h"
+
+namespace sg {
+
+// Input planes of the network: 0 h/s, 1 log(s/u)/4, 2..4 K, m, U mapped to
+// about [-1, 1], 5 ring mask (1 on the two outer rings), 6..15 zero.
+constexpr int kInputChannels = 16;
+
+// Per-sample constants of one jump. s = max(max h, u) scales the heights,
+// u = jump * U * dt is the jump's uplift (the target is (h_next - h)/u).
+struct SampleMeta {
+  float s, u, log_su, k_n, m_n, u_n, weight, pad;
+};
+
+// The samples of one network pass: sample b reads field src = idx[b] (or b
+// when idx is null) from h64[src] (FP64 device fields) or h32 + src*W*H,
+// target y + src*W*H (training), constants meta[src].
+struct SampleView {
+  int n = 0;
+  const int *idx = nullptr;
+  const SampleMeta *meta = nullptr;
+  double *const *h64 = nullptr;
+  const float *h32 = nullptr;
+  const float *y = nullptr;
+};
+
+cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H, cudaStream_t s);
+cudaError_t launch_avgpool2(const Act &in, const Act &out, cudaStream_t s);
+cudaError_t launch_upcat(const Act &d, const Act &skip, const Act &cat, cudaStream_t s);
+cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s);
+cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act &gp,
+                            const Act &gs, cudaStream_t s);
+// head = [w_0 .. w_{C-1}, b] (FP32); dhead accumulates the same layout
+cudaError_t launch_head_train(const Act &x, const float *head, const float *yt,
+                              const SampleView &v, const Act &gx, float *dhead, double *loss,
+                              cudaStream_t s);
+cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView &v,
+                              double *const *hout, cudaStream_t s);
+cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s);
+// lr_t, eps_t: Adam's bias-corrected step size and epsilon; wf/wd (may be
+// null): BF16 copies in the forward and data-gradient layouts
+cudaError_t launch_adam(float *p, const float *g, float *m, float *v, long long n, float lr_t,
+                        float b1, float b2, float eps_t, bf16 *wf, bf16 *wd, int cout, int cin,
+                        int taps, cudaStream_t s);
+cudaError_t launch_to_bf16(const float *p, long long n, bf16 *wf, bf16 *wd, int cout, int cin,
+                           int taps, cudaStream_t s);
+cudaError_t launch_field_max(double *const *h64, const float *h32, int nfields, long long hw,
+                             double *out, cudaStream_t s);
+cudaError_t launch_record(double *const *ht, double *const *hn, const int *slot, const float *u,
+                          int n, int W, int H, float *dh, float *dy, cudaStream_t s);
+// the training loss of y_pred = 1 (uplift only) and y_pred = 0 (no change),
+// added into out[0] and out[1]
+cudaError_t launch_baseline_loss(const SampleView &v, int W, int H, double *out, cudaStream_t s);
+cudaError_t launch_copy_fields(double *const *src, double *const *dst, int n, long long hw,
+                               cudaStream_t s);
+
+}  // namespace sg

@@ -246,6 +246,29 @@ int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps,
                            int *graph, int *erode_int_sub);
 int fs_batch_synchronize(const fs_batch *b);
 
+/* Restricts the following fs_batch_step / fs_batch_run calls to the n
+ * realizations listed in idx (distinct, in [0, number of realizations));
+ * n = 0 (idx may be NULL) makes every realization active again. Inactive
+ * realizations keep their fields; the active ones advance exactly as in a
+ * full-batch timestep (same results bit for bit). Read-backs of receivers,
+ * levels and accumulation reflect the last timestep that included the
+ * realization. No reference counterpart: it lets a caller advance only some
+ * members of an ensemble (the surrogate's judged and fallen-back
+ * realizations). */
+int fs_batch_set_active(fs_batch *b, int n, const int *idx);
+
+/* Device address of realization r's elevation (width*height doubles,
+ * row-major), valid until fs_batch_destroy: for callers that process the
+ * fields on the GPU without a host round trip. Work on it must be ordered
+ * against the batch's stream (fs_batch_stream; every fs_batch_* call that
+ * launches work waits for it before returning). */
+int fs_batch_device_elevation(const fs_batch *b, int r, double **d_h);
+/* The batch's CUDA stream (a cudaStream_t). */
+int fs_batch_stream(const fs_batch *b, void **stream);
+/* Constants and grid size of realization r. */
+int fs_batch_get_params(const fs_batch *b, int r, fs_params *out);
+int fs_batch_get_shape(const fs_batch *b, int r, int *width, int *height);
+
 /* Largest grid (width*height cells) fs_step_noalloc accepts. */
 #define FS_NOALLOC_MAX_CELLS 262144
 
