@@ -52,7 +52,8 @@ ABI_SYMBOLS = [
     "fs_batch_use_int_sub", "fs_use_int_sub",
     "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
     "fs_autotune", "fs_launch_config",
-    "fs_batch_set_active", "fs_batch_device_elevation", "fs_batch_stream",
+    "fs_batch_set_active", "fs_batch_analyze", "fs_batch_drainage_counts",
+    "fs_batch_device_elevation", "fs_batch_stream",
     "fs_batch_get_params", "fs_batch_get_shape",
     "fs_step_noalloc",
     "fs_test_order_from_receivers", "fs_test_barrier_timeout",
@@ -63,7 +64,7 @@ ABI_SYMBOLS = [
     "fs_sg_save", "fs_sg_load", "fs_sg_reserve", "fs_sg_add_samples", "fs_sg_generate",
     "fs_sg_set_holdout", "fs_sg_dataset_info", "fs_sg_get_sample", "fs_sg_train", "fs_sg_eval",
     "fs_sg_eval_baselines", "fs_sg_grad", "fs_sg_train_stats", "fs_sg_predict_host", "fs_sg_predict_batch",
-    "fs_sg_infer_flops", "fs_sg_ensemble_defaults", "fs_sg_compare_host", "fs_sg_ensemble_run",
+    "fs_sg_time_forward", "fs_sg_infer_flops", "fs_sg_ensemble_defaults", "fs_sg_compare_host", "fs_sg_ensemble_run",
 ]
 
 
@@ -187,6 +188,8 @@ def library() -> C.CDLL:
     L.fs_launch_config.argtypes = [vp, ip, ip, ip, ip]
     L.fs_batch_synchronize.argtypes = [vp]
     L.fs_batch_set_active.argtypes = [vp, C.c_int, ip]
+    L.fs_batch_analyze.argtypes = [vp]
+    L.fs_batch_drainage_counts.argtypes = [vp, C.c_int, vp]
     L.fs_batch_device_elevation.argtypes = [vp, C.c_int, C.POINTER(C.c_void_p)]
     L.fs_batch_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
     L.fs_batch_get_params.argtypes = [vp, C.c_int, pp]
@@ -226,6 +229,7 @@ def library() -> C.CDLL:
     L.fs_sg_train_stats.argtypes = [vp, dp, dp]
     L.fs_sg_predict_host.argtypes = [vp, C.c_int, dp, pp, dp]
     L.fs_sg_predict_batch.argtypes = [vp, vp, C.c_int, ip, C.POINTER(C.c_void_p)]
+    L.fs_sg_time_forward.argtypes = [vp, C.c_int, dp, dp]
     L.fs_sg_infer_flops.argtypes = [vp, dp]
     L.fs_sg_ensemble_defaults.argtypes = [C.POINTER(EnsembleOpts)]
     L.fs_sg_ensemble_defaults.restype = None
@@ -529,6 +533,11 @@ class FastScapeBatch:
         a = (C.c_int * len(idx))(*[int(i) for i in idx])
         check(library().fs_batch_set_active(self._b, len(idx), a))
 
+    def analyze(self) -> None:
+        """Receivers, levels and accumulation of the current fields, without
+        uplift or erosion (fs_batch_analyze)."""
+        check(library().fs_batch_analyze(self._b))
+
     def device_elevation(self, r: int) -> int:
         """Device address of realization r's elevation field."""
         p = C.c_void_p()
@@ -693,6 +702,12 @@ class Surrogate:
     def train_stats(self):
         ms, fl = C.c_double(0), C.c_double(0)
         check(library().fs_sg_train_stats(self._s, C.byref(ms), C.byref(fl)))
+        return ms.value, fl.value
+
+    def time_forward(self, reps: int = 5):
+        """(ms per forward pass over a full batch, conv FLOPs of that pass)."""
+        ms, fl = C.c_double(0), C.c_double(0)
+        check(library().fs_sg_time_forward(self._s, int(reps), C.byref(ms), C.byref(fl)))
         return ms.value, fl.value
 
     def infer_flops(self) -> float:

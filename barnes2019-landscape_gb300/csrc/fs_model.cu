@@ -416,6 +416,14 @@ cudaError_t launch_scatter_rctl(fs_batch *b) {
   return cudaGetLastError();
 }
 
+// Per-cell drainage counts of one realization from the walk's
+// position-indexed arrays: counts[ent[i]] = acc[i].
+__global__ void k_drainage_counts(const int32_t *__restrict__ ent, const uint32_t *__restrict__ acc,
+                                  int size, uint32_t *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x)
+    out[ent[i]] = acc[i];
+}
+
 // Initial erosion tables of every realization (counts below min(65536,
 // size+1)), evaluated on host threads in parallel over realizations -- the
 // same records grow_table writes -- then uploaded.
@@ -1389,6 +1397,31 @@ int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *gra
 int fs_batch_set_active(fs_batch *b, int n, const int *idx) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
   return set_active(b, n, idx);
+}
+
+int fs_batch_analyze(fs_batch *b) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  DeviceGuard dg(b->device);
+  const fs::StepArgs a = step_args(b, 0);
+  FS_CUDA(cudaMemsetAsync(b->d_ctl, 0, fs::kCtlCallResetBytes, b->stream));
+  FS_CUDA(launch_step(b, a));
+  if (b->act_n > 0) FS_CUDA(launch_scatter_rctl(b));
+  if (int st = collect_status(b)) return st;
+  b->have_step = true;
+  return FS_OK;
+}
+
+int fs_batch_drainage_counts(const fs_batch *b, int r, uint32_t *d_counts) {
+  if (int st = check_r(b, r)) return st;
+  if (!d_counts) return set_error(FS_ERR_ARG, "d_counts is NULL");
+  if (!b->have_step) return set_error(FS_ERR_STATE, "no timestep executed yet");
+  DeviceGuard dg(b->device);
+  const int n = b->size[r];
+  k_drainage_counts<<<std::min((n + 255) / 256, 1024), 256, 0, b->stream>>>(
+      b->ent + b->off[r], b->acc + b->off[r], n, d_counts);
+  FS_CUDA(cudaGetLastError());
+  FS_CUDA(cudaStreamSynchronize(b->stream));
+  return FS_OK;
 }
 
 int fs_batch_device_elevation(const fs_batch *b, int r, double **d_h) {

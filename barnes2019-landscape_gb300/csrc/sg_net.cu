@@ -61,7 +61,9 @@ SampleMeta make_meta(const fs_params &p, double hmax, double hmax_next, int jump
   m.u_n = static_cast<float>((std::log10(p.ueq) - kLog10UMid) / kLog10UHalf);
   const double r = std::max(hmax_next, u);
   m.weight = static_cast<float>((u / r) * (u / r));
-  m.pad = 0.0f;
+  m.inv_s = 1.0f / m.s;
+  m.inv_u = 1.0f / m.u;
+  m.pad[0] = m.pad[1] = m.pad[2] = 0.0f;
   return m;
 }
 
@@ -103,10 +105,12 @@ struct fs_surrogate {
   sg::SampleMeta *d_meta = nullptr;  // per-pass constants (inference)
   double **d_hptr = nullptr, **d_optr = nullptr;
   double *d_hmax = nullptr;
+  uint32_t *cnt_buf = nullptr;       // drainage counts of one inference pass
+  uint32_t **d_cptr = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double train_ms = 0;
   // dataset
-  float *data_h = nullptr, *data_y = nullptr;
+  float *data_h = nullptr, *data_y = nullptr, *data_a = nullptr;
   sg::SampleMeta *data_meta = nullptr;
   int ds_cap = 0, ds_n = 0, ds_held = 0;
   std::mt19937_64 rng;
@@ -148,6 +152,7 @@ void free_all(fs_surrogate *s) {
   if (s->data_h) cudaFree(s->data_h);
   if (s->data_y) cudaFree(s->data_y);
   if (s->data_meta) cudaFree(s->data_meta);
+  if (s->data_a) cudaFree(s->data_a);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -257,6 +262,8 @@ int build(fs_surrogate *s) {
   SG_CUDA(dalloc(s, &s->d_hptr, s->cap));
   SG_CUDA(dalloc(s, &s->d_optr, s->cap));
   SG_CUDA(dalloc(s, &s->d_hmax, s->cap));
+  SG_CUDA(dalloc(s, &s->cnt_buf, static_cast<size_t>(s->cap) * W * H));
+  SG_CUDA(dalloc(s, &s->d_cptr, s->cap));
   SG_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream));
   for (int l = 0; l < 14; l++) {
     SgLayer &L = s->L[l];
@@ -404,6 +411,7 @@ sg::SampleView data_view(const fs_surrogate *s, int n, const int *d_idx) {
   v.meta = s->data_meta;
   v.h32 = s->data_h;
   v.y = s->data_y;
+  v.a32 = s->data_a;
   return v;
 }
 
@@ -593,7 +601,8 @@ int fs_sg_reserve(fs_surrogate *s, int capacity) {
   cudaFree(s->data_h);
   cudaFree(s->data_y);
   cudaFree(s->data_meta);
-  s->data_h = s->data_y = nullptr;
+  cudaFree(s->data_a);
+  s->data_h = s->data_y = s->data_a = nullptr;
   s->data_meta = nullptr;
   s->ds_cap = s->ds_n = s->ds_held = 0;
   if (capacity == 0) return FS_OK;
@@ -601,6 +610,7 @@ int fs_sg_reserve(fs_surrogate *s, int capacity) {
   SG_CUDA(cudaMalloc(&s->data_h, hw * capacity * sizeof(float)));
   SG_CUDA(cudaMalloc(&s->data_y, hw * capacity * sizeof(float)));
   SG_CUDA(cudaMalloc(&s->data_meta, capacity * sizeof(sg::SampleMeta)));
+  SG_CUDA(cudaMalloc(&s->data_a, hw * capacity * sizeof(float)));
   s->ds_cap = capacity;
   return FS_OK;
 }
@@ -609,48 +619,66 @@ int fs_sg_add_samples(fs_surrogate *s, int n, const double *h_t, const double *h
                       const fs_params *params) {
   if (!s || n < 0 || (n > 0 && (!h_t || !h_next || !params)))
     return fail(FS_ERR_ARG, "surrogate: bad samples");
+  if (n == 0) return FS_OK;
   if (int st = ensure_dataset(s, s->ds_n + n)) return st;
   DeviceGuard dg(s->device);
   const size_t hw = static_cast<size_t>(s->W) * s->H;
-  double *dh = nullptr, *dn = nullptr;
-  SG_CUDA(cudaMalloc(&dh, hw * sizeof(double)));
-  cudaError_t e = cudaMalloc(&dn, hw * sizeof(double));
+  // the drainage counts of every h_t: a temporary batch of these fields,
+  // analysed without erosion
+  std::vector<int> Wv(n, s->W), Hv(n, s->H);
+  int status = FS_OK;
+  fs_batch *b = fs_batch_create(n, Wv.data(), Hv.data(), params, FS_INIT_ZERO, nullptr, &status);
+  if (!b) return status;
+  for (int k = 0; k < n && status == FS_OK; k++) status = fs_batch_set_elevation(b, k, h_t + k * hw);
+  if (status == FS_OK) status = fs_batch_analyze(b);
+  double *dn = nullptr;
+  uint32_t *dc = nullptr;
   double **dp = nullptr;
+  uint32_t **dcp = nullptr;
   int *dslot = nullptr;
   float *du = nullptr;
+  cudaError_t e = cudaMalloc(&dn, hw * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dc, hw * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&dp, 2 * sizeof(double *));
+  if (e == cudaSuccess) e = cudaMalloc(&dcp, sizeof(uint32_t *));
   if (e == cudaSuccess) e = cudaMalloc(&dslot, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&du, sizeof(float));
-  int st = FS_OK;
-  for (int k = 0; k < n && e == cudaSuccess; k++) {
-    const double *a = h_t + k * hw, *b = h_next + k * hw;
+  for (int k = 0; k < n && e == cudaSuccess && status == FS_OK; k++) {
+    const double *a = h_t + k * hw, *nx = h_next + k * hw;
     double hmax = 0, hmax2 = 0;
     for (size_t i = 0; i < hw; i++) {
       hmax = std::max(hmax, a[i]);
-      hmax2 = std::max(hmax2, b[i]);
+      hmax2 = std::max(hmax2, nx[i]);
     }
     const sg::SampleMeta m = sg::make_meta(params[k], hmax, hmax2, s->cfg.jump, s->cfg.dt);
     const int slot = s->ds_n + k;
-    double *ptrs[2] = {dh, dn};
-    e = cudaMemcpyAsync(dh, a, hw * sizeof(double), cudaMemcpyHostToDevice, s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dn, b, hw * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+    double *field = nullptr;
+    status = fs_batch_device_elevation(b, k, &field);
+    if (status == FS_OK) status = fs_batch_drainage_counts(b, k, dc);
+    if (status != FS_OK) break;
+    double *ptrs[2] = {field, dn};
+    e = cudaMemcpyAsync(dn, nx, hw * sizeof(double), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dp, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dcp, &dc, sizeof(dc), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dslot, &slot, sizeof(int), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(du, &m.u, sizeof(float), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess)
       e = sg::launch_record(dp, dp + 1, dslot, du, 1, s->W, s->H, s->data_h, s->data_y, s->stream);
+    if (e == cudaSuccess) e = sg::launch_count_plane(dcp, dslot, 1, hw, s->data_a, s->stream);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s->data_meta + slot, &m, sizeof(m), cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   }
-  if (e != cudaSuccess) st = cuda_fail(e, "add samples");
-  cudaFree(dh);
+  if (e != cudaSuccess && status == FS_OK) status = cuda_fail(e, "add samples");
   cudaFree(dn);
+  cudaFree(dc);
   cudaFree(dp);
+  cudaFree(dcp);
   cudaFree(dslot);
   cudaFree(du);
-  if (st == FS_OK) s->ds_n += n;
-  return st;
+  fs_batch_destroy(b);
+  if (status == FS_OK) s->ds_n += n;
+  return status;
 }
 
 int fs_sg_set_holdout(fs_surrogate *s, int held) {
@@ -727,15 +755,21 @@ int fs_sg_generate(fs_surrogate *s, int ntraj, int per_traj, int max_spinup, uin
   void *bstream = nullptr;
   if (status == FS_OK) status = fs_batch_stream(b, &bstream);
   std::vector<double> hmax_start(ntraj, 0.0);
+  std::vector<int> slot_of(ntraj, -1);
+  uint32_t *cnt = nullptr;
+  uint32_t **d_c = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&cnt, hw * ntraj * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&d_c, ntraj * sizeof(uint32_t *));
   const int jump = s->cfg.jump;
   const int tmax = (per_traj - 1) * gap + (gap - 10) + jump;
   int t = 0, count = 0;
   std::vector<double *> pa, pb;
+  std::vector<uint32_t *> pc;
   std::vector<int> slots, who;
   std::vector<float> us;
   std::vector<double> mx;
   while (e == cudaSuccess && status == FS_OK) {
-    // samples ending now: record (snapshot, current field)
+    // samples ending now: h_t from the snapshot, target from the field
     pa.clear();
     pb.clear();
     slots.clear();
@@ -746,7 +780,7 @@ int fs_sg_generate(fs_surrogate *s, int ntraj, int per_traj, int max_spinup, uin
       if (t - jump >= off[r] && (t - jump - off[r]) % gap == 0 && k < per_traj) {
         pa.push_back(snap + r * hw);
         pb.push_back(field[r]);
-        slots.push_back(s->ds_n + count + static_cast<int>(who.size()));
+        slots.push_back(slot_of[r]);
         us.push_back(static_cast<float>(jump * P[r].ueq * s->cfg.dt));
         who.push_back(r);
       }
@@ -764,31 +798,43 @@ int fs_sg_generate(fs_surrogate *s, int ntraj, int per_traj, int max_spinup, uin
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(mx.data(), d_mx, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-      std::vector<sg::SampleMeta> meta(m);
-      for (int i = 0; i < m && e == cudaSuccess; i++)
-        meta[i] = sg::make_meta(P[who[i]], hmax_start[who[i]], mx[i], jump, s->cfg.dt);
-      if (e == cudaSuccess)
-        e = cudaMemcpy(s->data_meta + s->ds_n + count, meta.data(), m * sizeof(sg::SampleMeta),
-                       cudaMemcpyHostToDevice);
-      count += m;
+      for (int i = 0; i < m && e == cudaSuccess; i++) {
+        const sg::SampleMeta meta =
+            sg::make_meta(P[who[i]], hmax_start[who[i]], mx[i], jump, s->cfg.dt);
+        e = cudaMemcpy(s->data_meta + slots[i], &meta, sizeof(meta), cudaMemcpyHostToDevice);
+      }
     }
     if (t >= tmax) break;
-    // samples starting now: snapshot
+    // samples starting now: snapshot, maximum, drainage counts of h_t
     pa.clear();
     pb.clear();
+    pc.clear();
+    slots.clear();
     who.clear();
     for (int r = 0; r < ntraj; r++)
       if (t >= off[r] && (t - off[r]) % gap == 0 && (t - off[r]) / gap < per_traj) {
+        slot_of[r] = s->ds_n + count++;
         pa.push_back(field[r]);
         pb.push_back(snap + r * hw);
+        pc.push_back(cnt + r * hw);
+        slots.push_back(slot_of[r]);
         who.push_back(r);
       }
     if (!who.empty() && e == cudaSuccess) {
       const int m = static_cast<int>(who.size());
+      status = fs_batch_set_active(b, m, who.data());
+      if (status == FS_OK) status = fs_batch_analyze(b);
+      for (int i = 0; i < m && status == FS_OK; i++)
+        status = fs_batch_drainage_counts(b, who[i], pc[i]);
+      if (status == FS_OK) status = fs_batch_set_active(b, 0, nullptr);
+      if (status != FS_OK) break;
       mx.assign(m, 0.0);
       e = cudaMemcpy(d_a, pa.data(), m * sizeof(double *), cudaMemcpyHostToDevice);
       if (e == cudaSuccess) e = cudaMemcpy(d_b, pb.data(), m * sizeof(double *), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(d_c, pc.data(), m * sizeof(uint32_t *), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(d_slot, slots.data(), m * sizeof(int), cudaMemcpyHostToDevice);
       if (e == cudaSuccess) e = sg::launch_copy_fields(d_a, d_b, m, hw, s->stream);
+      if (e == cudaSuccess) e = sg::launch_count_plane(d_c, d_slot, m, hw, s->data_a, s->stream);
       if (e == cudaSuccess) e = sg::launch_field_max(d_a, nullptr, m, hw, d_mx, s->stream);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(mx.data(), d_mx, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
@@ -804,9 +850,11 @@ int fs_sg_generate(fs_surrogate *s, int ntraj, int per_traj, int max_spinup, uin
         if (te > t && te < next) next = te;
       }
     }
-    if (e == cudaSuccess) status = fs_batch_step(b, next - t);
+    if (e == cudaSuccess && status == FS_OK) status = fs_batch_step(b, next - t);
     t = next;
   }
+  cudaFree(cnt);
+  cudaFree(d_c);
   if (e != cudaSuccess && status == FS_OK) status = cuda_fail(e, "generate");
   cudaStreamSynchronize(s->stream);
   cudaFree(snap);
@@ -964,6 +1012,29 @@ int fs_sg_train_stats(const fs_surrogate *s, double *ms, double *conv_flops_per_
   return FS_OK;
 }
 
+int fs_sg_time_forward(fs_surrogate *s, int reps, double *ms_per_pass, double *flops_per_pass) {
+  if (!s || reps < 1) return fail(FS_ERR_ARG, "surrogate: bad timing call");
+  if (s->ds_n < 1) return fail(FS_ERR_STATE, "surrogate: no samples");
+  DeviceGuard dg(s->device);
+  const int n = std::min(s->cap, s->ds_n);
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  SG_CUDA(cudaMemcpyAsync(s->d_idx, idx.data(), n * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  const sg::SampleView v = data_view(s, n, s->d_idx);
+  if (int st = forward(s, v, false)) return st;  // warm-up
+  SG_CUDA(cudaEventRecord(s->ev0, s->stream));
+  for (int k = 0; k < reps; k++)
+    if (int st = forward(s, v, false)) return st;
+  SG_CUDA(cudaEventRecord(s->ev1, s->stream));
+  SG_CUDA(cudaEventSynchronize(s->ev1));
+  if (int st = check_err(s)) return st;
+  float ms = 0;
+  SG_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+  if (ms_per_pass) *ms_per_pass = ms / reps;
+  if (flops_per_pass) *flops_per_pass = conv_flops(s, 0) * n;
+  return FS_OK;
+}
+
 int fs_sg_infer_flops(const fs_surrogate *s, double *flops) {
   if (!s || !flops) return fail(FS_ERR_ARG, "surrogate: NULL argument");
   *flops = conv_flops(s, 0);
@@ -975,7 +1046,7 @@ int fs_sg_infer_flops(const fs_surrogate *s, double *flops) {
 // Jumps n device fields hin[k] (params p[k]) into hout[k] (hout may equal
 // hin), in chunks of the network's batch.
 int sg_predict_fields(fs_surrogate *s, int n, double *const *hin, double *const *hout,
-                      const fs_params *p) {
+                      const fs_params *p, uint32_t *const *cnt) {
   DeviceGuard dg(s->device);
   const size_t hw = static_cast<size_t>(s->W) * s->H;
   std::vector<double> mx(s->cap);
@@ -985,6 +1056,8 @@ int sg_predict_fields(fs_surrogate *s, int n, double *const *hin, double *const 
     SG_CUDA(cudaMemcpyAsync(s->d_hptr, hin + a, m * sizeof(double *), cudaMemcpyHostToDevice,
                             s->stream));
     SG_CUDA(cudaMemcpyAsync(s->d_optr, hout + a, m * sizeof(double *), cudaMemcpyHostToDevice,
+                            s->stream));
+    SG_CUDA(cudaMemcpyAsync(s->d_cptr, cnt + a, m * sizeof(uint32_t *), cudaMemcpyHostToDevice,
                             s->stream));
     SG_CUDA(sg::launch_field_max(s->d_hptr, nullptr, m, hw, s->d_hmax, s->stream));
     SG_CUDA(cudaMemcpyAsync(mx.data(), s->d_hmax, m * sizeof(double), cudaMemcpyDeviceToHost,
@@ -997,6 +1070,7 @@ int sg_predict_fields(fs_surrogate *s, int n, double *const *hin, double *const 
     v.n = m;
     v.meta = s->d_meta;
     v.h64 = s->d_hptr;
+    v.cnt = s->d_cptr;
     if (int st = forward(s, v, false)) return st;
     SG_CUDA(sg::launch_head_apply(view(s->d0b, m), s->p + s->head_off, v, s->d_optr, s->stream));
     SG_CUDA(cudaStreamSynchronize(s->stream));  // the host arrays above are reused
@@ -1004,31 +1078,10 @@ int sg_predict_fields(fs_surrogate *s, int n, double *const *hin, double *const 
   return check_err(s);
 }
 
-extern "C" int fs_sg_predict_host(fs_surrogate *s, int n, const double *h_in,
-                                  const fs_params *params, double *h_out) {
-  if (!s || n < 0 || (n > 0 && (!h_in || !params || !h_out)))
-    return fail(FS_ERR_ARG, "surrogate: bad predict call");
-  if (n == 0) return FS_OK;
-  DeviceGuard dg(s->device);
-  const size_t hw = static_cast<size_t>(s->W) * s->H;
-  double *d = nullptr;
-  SG_CUDA(cudaMalloc(&d, hw * n * sizeof(double)));
-  cudaError_t e = cudaMemcpy(d, h_in, hw * n * sizeof(double), cudaMemcpyHostToDevice);
-  int st = e == cudaSuccess ? FS_OK : cuda_fail(e, "predict upload");
-  std::vector<double *> ptr(n);
-  for (int k = 0; k < n; k++) ptr[k] = d + k * hw;
-  if (st == FS_OK) st = sg_predict_fields(s, n, ptr.data(), ptr.data(), params);
-  if (st == FS_OK) {
-    e = cudaMemcpy(h_out, d, hw * n * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) st = cuda_fail(e, "predict download");
-  }
-  cudaFree(d);
-  return st;
-}
-
 extern "C" int fs_sg_predict_batch(fs_surrogate *s, fs_batch *b, int n, const int *idx,
                                    double *const *d_out) {
   if (!s || !b || n < 0 || (n > 0 && !idx)) return fail(FS_ERR_ARG, "surrogate: bad predict call");
+  const size_t hw = static_cast<size_t>(s->W) * s->H;
   std::vector<double *> in(n), out(n);
   std::vector<fs_params> p(n);
   for (int k = 0; k < n; k++) {
@@ -1041,6 +1094,38 @@ extern "C" int fs_sg_predict_batch(fs_surrogate *s, fs_batch *b, int n, const in
     if (int st = fs_batch_get_params(b, idx[k], &p[k])) return st;
     out[k] = d_out ? d_out[k] : in[k];
   }
-  if (int st = fs_batch_synchronize(b)) return st;
-  return sg_predict_fields(s, n, in.data(), out.data(), p.data());
+  std::vector<uint32_t *> cp(s->cap);
+  for (int i = 0; i < s->cap; i++) cp[i] = s->cnt_buf + i * hw;
+  int st = FS_OK;
+  for (int a = 0; a < n && st == FS_OK; a += s->cap) {
+    const int m = std::min(s->cap, n - a);
+    // drainage counts of the fields about to jump
+    st = fs_batch_set_active(b, m, idx + a);
+    if (st == FS_OK) st = fs_batch_analyze(b);
+    for (int i = 0; i < m && st == FS_OK; i++) st = fs_batch_drainage_counts(b, idx[a + i], cp[i]);
+    if (st == FS_OK) st = sg_predict_fields(s, m, in.data() + a, out.data() + a, p.data() + a, cp.data());
+  }
+  const int st2 = fs_batch_set_active(b, 0, nullptr);
+  return st != FS_OK ? st : st2;
+}
+
+extern "C" int fs_sg_predict_host(fs_surrogate *s, int n, const double *h_in,
+                                  const fs_params *params, double *h_out) {
+  if (!s || n < 0 || (n > 0 && (!h_in || !params || !h_out)))
+    return fail(FS_ERR_ARG, "surrogate: bad predict call");
+  if (n == 0) return FS_OK;
+  const size_t hw = static_cast<size_t>(s->W) * s->H;
+  std::vector<int> Wv(n, s->W), Hv(n, s->H), idx(n);
+  int status = FS_OK;
+  fs_batch *b = fs_batch_create(n, Wv.data(), Hv.data(), params, FS_INIT_ZERO, nullptr, &status);
+  if (!b) return status;
+  for (int k = 0; k < n && status == FS_OK; k++) {
+    idx[k] = k;
+    status = fs_batch_set_elevation(b, k, h_in + k * hw);
+  }
+  if (status == FS_OK) status = fs_sg_predict_batch(s, b, n, idx.data(), nullptr);
+  for (int k = 0; k < n && status == FS_OK; k++)
+    status = fs_batch_get_elevation(b, k, h_out + k * hw);
+  fs_batch_destroy(b);
+  return status;
 }

@@ -15,7 +15,7 @@ SampleMeta make_meta(const fs_params &p, double hmax, double hmax_next, int jump
 
 }  // namespace sg
 
-// Jumps n device fields hin[k] with constants p[k] into hout[k] (hout[k] may
-// be hin[k]); returns when they are written.
+// Jumps n device fields hin[k] with constants p[k] and drainage counts
+// cnt[k] into hout[k] (hout[k] may be hin[k]); returns when they are written.
 int sg_predict_fields(fs_surrogate *s, int n, double *const *hin, double *const *hout,
-                      const fs_params *p);
+                      const fs_params *p, uint32_t *const *cnt);

@@ -45,6 +45,17 @@ __device__ __forceinline__ bool interior(int x, int y, int W, int H) {
   return x >= 2 && y >= 2 && x < W - 2 && y < H - 2;
 }
 
+__device__ __forceinline__ float field_at(const SampleView &v, int src, long long hw,
+                                          long long pix) {
+  return v.h64 ? static_cast<float>(v.h64[src][pix]) : v.h32[src * hw + pix];
+}
+
+__device__ __forceinline__ float count_plane(uint32_t c) {
+  return log2f(static_cast<float>(c > 0u ? c : 1u)) * 0.0625f;
+}
+
+// All plane arithmetic is FP32 on FP32 heights (no FP64 on the narrow FP64
+// pipe; -fmad=false keeps every operation separately rounded).
 __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__restrict__ yt, int W,
                         int H) {
   const long long hw = static_cast<long long>(W) * H;
@@ -56,20 +67,39 @@ __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__rest
     const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
     const int src = v.idx ? v.idx[b] : b;
     const SampleMeta m = v.meta[src];
-    double h;
-    if (v.h64)
-      h = v.h64[src][pix];
-    else
-      h = v.h32[static_cast<long long>(src) * hw + pix];
+    const float h = field_at(v, src, hw, pix);
     float f[16];
-    f[0] = static_cast<float>(h / m.s);
+    f[0] = h * m.inv_s;
     f[1] = m.log_su;
     f[2] = m.k_n;
     f[3] = m.m_n;
     f[4] = m.u_n;
     f[5] = interior(x, y, W, H) ? 0.0f : 1.0f;
+    f[6] = v.a32 ? v.a32[src * hw + pix] : (v.cnt ? count_plane(v.cnt[b][pix]) : 0.0f);
 #pragma unroll
-    for (int j = 6; j < 16; j++) f[j] = 0.0f;
+    for (int j = 7; j < 16; j++) f[j] = 0.0f;
+    if (x >= 1 && y >= 1 && x < W - 1 && y < H - 1) {
+      // neighbours in the reference's order W, NW, N, NE, E, SE, S, SW
+      const long long off[8] = {-1, -W - 1, -W, -W + 1, 1, W + 1, W, W - 1};
+      float nb[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) nb[k] = field_at(v, src, hw, pix + off[k]);
+      float best = 0.0f, drop = 0.0f, sum = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const float d = h - nb[k];
+        const float slope = (k & 1) ? d / 1.41421356f : d;
+        if (slope > best) {
+          best = slope;
+          drop = d;
+        }
+        sum += nb[k];
+      }
+      f[7] = drop * m.inv_u;
+      f[8] = (nb[4] - nb[0]) * 0.5f * m.inv_u;
+      f[9] = (nb[6] - nb[2]) * 0.5f * m.inv_u;
+      f[10] = (h - 0.125f * sum) * m.inv_u;
+    }
     float lo[8], hi[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
@@ -447,6 +477,17 @@ __global__ void __launch_bounds__(kBlock) k_baseline_loss(const SampleView v, in
   }
 }
 
+__global__ void k_count_plane(const uint32_t *const *__restrict__ cnt, const int *__restrict__ slot,
+                              int n, long long hw, float *__restrict__ da) {
+  const long long tot = hw * n;
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < tot;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int k = static_cast<int>(i / hw);
+    const long long pix = i - k * hw;
+    da[static_cast<long long>(slot[k]) * hw + pix] = count_plane(cnt[k][pix]);
+  }
+}
+
 // copies FP64 fields (gather by pointer)
 __global__ void k_copy_fields(double *const *__restrict__ src, double *const *__restrict__ dst,
                               int n, long long hw) {
@@ -556,6 +597,12 @@ cudaError_t launch_record(double *const *ht, double *const *hn, const int *slot,
 
 cudaError_t launch_baseline_loss(const SampleView &v, int W, int H, double *out, cudaStream_t s) {
   k_baseline_loss<<<blocks_for(static_cast<long long>(W) * H * v.n), kBlock, 0, s>>>(v, W, H, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_plane(const uint32_t *const *cnt, const int *slot, int n, long long hw,
+                               float *da, cudaStream_t s) {
+  k_count_plane<<<blocks_for(hw * n), kBlock, 0, s>>>(cnt, slot, n, hw, da);
   return cudaGetLastError();
 }
 

@@ -7,13 +7,21 @@
 namespace sg {
 
 // Input planes of the network: 0 h/s, 1 log(s/u)/4, 2..4 K, m, U mapped to
-// about [-1, 1], 5 ring mask (1 on the two outer rings), 6..15 zero.
+// about [-1, 1], 5 ring mask (1 on the two outer rings), 6 log2(drainage
+// count)/16, 7 drop to the D8 receiver / u, 8 and 9 central differences
+// along x and y / (2u), 10 (h - mean of the 8 neighbours) / u, 11..15 zero.
+// Planes 7..10 are 0 on ring 0 (no full neighbourhood). They are formed in
+// FP32 from FP32 heights before the BF16 rounding, so slopes keep their
+// precision however high the ground stands (h/s alone would quantise them
+// to 2^-8 of s).
 constexpr int kInputChannels = 16;
 
 // Per-sample constants of one jump. s = max(max h, u) scales the heights,
 // u = jump * U * dt is the jump's uplift (the target is (h_next - h)/u).
 struct SampleMeta {
-  float s, u, log_su, k_n, m_n, u_n, weight, pad;
+  float s, u, log_su, k_n, m_n, u_n, weight;
+  float inv_s, inv_u;  // FP32 reciprocals of s and u
+  float pad[3];
 };
 
 // The samples of one network pass: sample b reads field src = idx[b] (or b
@@ -26,6 +34,8 @@ struct SampleView {
   double *const *h64 = nullptr;
   const float *h32 = nullptr;
   const float *y = nullptr;
+  const float *a32 = nullptr;              // dataset: plane 6 per cell
+  const uint32_t *const *cnt = nullptr;    // fields: drainage counts
 };
 
 cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H, cudaStream_t s);
@@ -52,6 +62,9 @@ cudaError_t launch_field_max(double *const *h64, const float *h32, int nfields, 
                              double *out, cudaStream_t s);
 cudaError_t launch_record(double *const *ht, double *const *hn, const int *slot, const float *u,
                           int n, int W, int H, float *dh, float *dy, cudaStream_t s);
+// plane 6 of fields k (drainage counts cnt[k]) into da + slot[k]*W*H
+cudaError_t launch_count_plane(const uint32_t *const *cnt, const int *slot, int n, long long hw,
+                               float *da, cudaStream_t s);
 // the training loss of y_pred = 1 (uplift only) and y_pred = 0 (no change),
 // added into out[0] and out[1]
 cudaError_t launch_baseline_loss(const SampleView &v, int W, int H, double *out, cudaStream_t s);

@@ -432,6 +432,168 @@ def run_ensemble(args, dist, rank, ws, local):
         dist.destroy_process_group()
 
 
+SG_WEIGHTS = ROOT / "barnes2019-landscape_gb300" / "weights" / "surrogate_512_c32_j50.bin"
+
+
+def load_bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), \
+            "measured"
+    return 1900.0, 1700.0, "fallback"
+
+
+def surrogate_ensemble(pkg, net, n, side, nsteps, judge, seed, clk_index):
+    """The judged surrogate ensemble and the plain batched method on the
+    same n realizations (parameters and initial fields as the ragged
+    ensemble's, all side x side); returns a dict of both."""
+    import torch  # noqa: F401
+    sides, params = ensemble_spec(pkg, n, seed=seed, side=side)
+    seeds = list(range(5000, 5000 + n))
+    out = {}
+    # plain batched method (the yardstick), its launch shape autotuned
+    plain = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX, seeds=seeds)
+    tune = plain.autotune(probe_steps=2)
+    plain.synchronize()
+    with Clocks(clk_index) as clk:
+        t0 = time.perf_counter()
+        plain.step(nsteps)
+        plain.synchronize()
+        t_plain = time.perf_counter() - t0
+    out["plain"] = {"seconds": t_plain, "realizations_per_s": n / t_plain, "launch": tune,
+                    "levels_at_end": max(plain.levels(r)[1] for r in range(n)),
+                    "clocks": clk.summary()}
+    h_plain = [plain.getH(r) for r in range(min(n, 16))]
+    plain.close()
+    b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX, seeds=seeds)
+    b.autotune(probe_steps=2)
+    b.use_graph(False)
+    b.synchronize()
+    with Clocks(clk_index) as clk:
+        t0 = time.perf_counter()
+        stats, fallen = net.ensemble(b, nsteps, judge_fraction=judge, seed=seed)
+        b.synchronize()
+        t_sg = time.perf_counter() - t0
+    # end state against the plain run (realizations that never fell back
+    # carry the surrogate's errors; the others are exact from their fallback)
+    rel = []
+    for r in range(len(h_plain)):
+        h = b.getH(r)
+        relief = h_plain[r].max() - h_plain[r].min()
+        rel.append(float(np.sqrt(np.mean((h - h_plain[r]) ** 2)) / relief))
+    b.close()
+    out["surrogate"] = {"seconds": t_sg, "realizations_per_s": n / t_sg, "stats": stats,
+                        "fallen": int(np.sum(fallen)),
+                        "end_rel_rms_vs_plain_first16": {"mean": float(np.mean(rel)),
+                                                         "max": float(np.max(rel))},
+                        "clocks": clk.summary()}
+    out["ratio"] = out["surrogate"]["realizations_per_s"] / out["plain"]["realizations_per_s"]
+    return out
+
+
+def run_surrogate(args, dist, rank, ws, local):
+    """Configs 3 and 4: the surrogate trained on data the plain method
+    generates on the device (config 3: --sg-traj x --sg-per samples of
+    512^2 spun up 0..--sg-spinup timesteps, --sg-train-steps Adam steps at
+    batch 32), then the judged surrogate ensemble (config 4: --realizations
+    x 512^2, --ensemble-steps timesteps, --sg-judge of the jumps re-run
+    exactly) against the plain batched method on the same realizations.
+    --sg-load skips generation and training and uses saved parameters."""
+    import __graft_entry__ as ge
+    import torch  # noqa: F401
+    pkg = ge.load()
+    if ws > 1:
+        torch.cuda.set_device(local)
+    side = 512
+    peak_b, peak_s, peak_kind = load_bf16_peak()
+    line = {"metric": "ensemble realizations/s, surrogate vs plain (512^2, judged)",
+            "unit": "realizations/s", "n_gpus": ws, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 network, f64 timestep", "data": "synthetic"}
+    net = pkg.Surrogate(side, side, base_channels=32, batch=32, jump=50, seed=1 + rank)
+    train = None
+    nsamp = args.sg_traj * args.sg_per
+    if args.sg_load:
+        net.load(args.sg_load)
+        net.reserve(64)
+        net.generate(16, 4, 400, seed=99 + rank)        # samples for the timing pass
+    else:
+        net.reserve(nsamp)
+        t0 = time.perf_counter()
+        got = net.generate(args.sg_traj, args.sg_per, args.sg_spinup, seed=2019 + rank)
+        t_gen = time.perf_counter() - t0
+        held = max(32, nsamp // 20)
+        net.set_holdout(held)
+        before = net.eval()
+        curve = []
+        t0 = time.perf_counter()
+        done = 0
+        steps_total = 0.0
+        ms_total = 0.0
+        chunk = max(1, args.sg_train_steps // 10)
+        while done < args.sg_train_steps:
+            k = min(chunk, args.sg_train_steps - done)
+            frac = done / max(1, args.sg_train_steps)
+            lr = args.sg_lr * (0.5 * (1 + np.cos(np.pi * frac)))  # cosine decay
+            lr = max(lr, args.sg_lr * 0.02)
+            loss = net.train(k, lr=float(lr))
+            ms, flops = net.train_stats()
+            ms_total += ms
+            steps_total += k
+            done += k
+            curve.append({"step": done, "train_loss": loss, "heldout_loss": net.eval()})
+        t_train = time.perf_counter() - t0
+        uplift_only, no_change = net.eval_baselines()
+        after = curve[-1]["heldout_loss"] if curve else before
+        _, flops_step = net.train_stats()
+        achieved = flops_step * steps_total / (ms_total * 1e-3) / 1e12
+        train = {"samples": got, "heldout": held, "generate_s": t_gen, "train_s": t_train,
+                 "steps": args.sg_train_steps, "batch": 32,
+                 "samples_per_s": 32 * steps_total / (ms_total * 1e-3),
+                 "ms_per_step": ms_total / steps_total,
+                 "conv_tflops": achieved, "conv_frac_of_bf16_sustained": achieved / peak_s,
+                 "heldout_loss_before": before, "heldout_loss_after": after,
+                 "heldout_loss_uplift_only": uplift_only, "heldout_loss_no_change": no_change,
+                 "curve": curve}
+        if args.sg_save:
+            net.save(args.sg_save)
+    fwd_ms, fwd_flops = net.time_forward(reps=5)
+    fwd_tf = fwd_flops / (fwd_ms * 1e-3) / 1e12
+    ens = surrogate_ensemble(pkg, net, args.realizations, side, args.ensemble_steps, args.sg_judge,
+                             2019 + rank, local)
+    net.close()
+    if rank == 0:
+        line["value"] = ens["surrogate"]["realizations_per_s"]
+        line["steps"] = args.ensemble_steps
+        line["warmup"] = args.warmup
+        line["ms_per_step"] = 1e3 * ens["surrogate"]["seconds"] / args.ensemble_steps
+        line["config"] = {"workload": f"{args.realizations} realizations of {side}x{side}, "
+                                      "K log-U[1e-6,1e-5], m U[0.3,0.6], U log-U[1e-4,5e-3], n 1, "
+                                      f"{args.ensemble_steps} timesteps, 50-step jumps + 1 plain "
+                                      f"timestep per cycle, {args.sg_judge:g} of jumps judged",
+                          "network": "4-level conv encoder-decoder, 32-256 channels, BF16, "
+                                     f"{net_param_count(pkg)} parameters"}
+        line["plain_realizations_per_s"] = ens["plain"]["realizations_per_s"]
+        line["surrogate_vs_plain"] = ens["ratio"]
+        line["ensemble"] = ens
+        line["training"] = train
+        line["roofline"] = {"bound": "tensor", "kernel": "forward pass (14 tcgen05 convolutions "
+                                                         "+ pooling/concat), batch 32",
+                            "achieved": fwd_tf, "peak": peak_b, "unit": "TFLOP/s",
+                            "frac": fwd_tf / peak_b, "ms_per_pass": fwd_ms,
+                            "flops_per_pass": fwd_flops,
+                            "peak_source": f"{peak_kind} bf16_tflops (burst)"}
+        line["clocks"] = ens["surrogate"]["clocks"]
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def net_param_count(pkg):
+    with pkg.Surrogate(512, 512, base_channels=32, batch=1) as s:
+        return s.param_count()
+
+
 SWEEP_SIDES = (100, 200, 400, 700, 1000, 1500, 2000, 3000, 4000, 5000, 7000, 10000,
                14000, 20000)
 SWEEP_NSTEP = 120          # run(120): 121 timesteps, the reference's sweep length
@@ -635,7 +797,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="grid",
-                    choices=["grid", "ensemble", "sweep", "deep", "refconst"],
+                    choices=["grid", "ensemble", "sweep", "deep", "refconst", "surrogate"],
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
                          "256-realization batch; sweep: grid sizes 100..20000; deep: a "
                          "512^2 grid after 2000 timesteps of strong erosion (~290 levels); "
@@ -649,6 +811,17 @@ def main():
                          "draw (1024 x 512 with 2000 timesteps is the plain batched method "
                          "at the surrogate ensemble's shape)")
     ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
+    ap.add_argument("--sg-traj", type=int, default=2000,
+                    help="surrogate: realizations generating training data")
+    ap.add_argument("--sg-per", type=int, default=10, help="surrogate: samples per realization")
+    ap.add_argument("--sg-spinup", type=int, default=2000,
+                    help="surrogate: samples spread over timesteps [0, spinup)")
+    ap.add_argument("--sg-train-steps", type=int, default=2000)
+    ap.add_argument("--sg-lr", type=float, default=1e-3)
+    ap.add_argument("--sg-judge", type=float, default=0.05)
+    ap.add_argument("--sg-save", default="", help="surrogate: write the trained parameters here")
+    ap.add_argument("--sg-load", default="",
+                    help="surrogate: use these parameters (no generation or training)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -668,6 +841,9 @@ def main():
         return
     if args.workload == "refconst":
         run_refconst(args, dist, rank, ws, local)
+        return
+    if args.workload == "surrogate":
+        run_surrogate(args, dist, rank, ws, local)
         return
 
     import __graft_entry__ as ge

@@ -257,6 +257,17 @@ int fs_batch_synchronize(const fs_batch *b);
  * realizations). */
 int fs_batch_set_active(fs_batch *b, int n, const int *idx);
 
+/* Receivers, donor masks, level ordering and flow accumulation of the
+ * active realizations' current fields (fastscape_RB.cpp:160-279) without
+ * uplift or erosion: the fields do not change, and the read-backs
+ * (receivers, levels, accumulation, drainage counts) describe them. */
+int fs_batch_analyze(fs_batch *b);
+/* Drainage count (accumulation / cell_area, an integer number of cells) of
+ * every cell of realization r, from the last timestep or analysis that
+ * included it, into caller-owned device memory (width*height uint32);
+ * waits for the copy. */
+int fs_batch_drainage_counts(const fs_batch *b, int r, uint32_t *d_counts);
+
 /* Device address of realization r's elevation (width*height doubles,
  * row-major), valid until fs_batch_destroy: for callers that process the
  * fields on the GPU without a host round trip. Work on it must be ordered

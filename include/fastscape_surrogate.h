@@ -122,6 +122,11 @@ int fs_sg_predict_host(fs_surrogate *s, int n, const double *h_in, const fs_para
  * stream; returns when the fields are written. */
 int fs_sg_predict_batch(fs_surrogate *s, fs_batch *b, int n, const int *idx,
                         double *const *d_out);
+/* Device time (CUDA events on the network's stream) of one forward pass
+ * over a full batch of dataset samples -- input planes, the fourteen
+ * convolutions, pooling and concatenation -- averaged over `reps` passes
+ * after one warm-up, and the convolutions' FLOPs of that pass. */
+int fs_sg_time_forward(fs_surrogate *s, int reps, double *ms_per_pass, double *flops_per_pass);
 /* FLOPs of the convolutions of one inference pass over one realization. */
 int fs_sg_infer_flops(const fs_surrogate *s, double *flops);
 

@@ -58,7 +58,7 @@ def make_meta(keq, meq, ueq, hmax, hmax_next, jump=50, dt=1000.0):
     return {"s": f(s), "u": f(u), "log_su": f(math.log(s / u) / 4.0),
             "k_n": f((math.log10(keq) + 5.5) / 0.5), "m_n": f((meq - 0.45) / 0.15),
             "u_n": f((math.log10(ueq) - LOG10_U_MID) / LOG10_U_HALF),
-            "weight": f((u / r) * (u / r))}
+            "weight": f((u / r) * (u / r)), "inv_s": f(1) / f(s), "inv_u": f(1) / f(u)}
 
 
 def ring_mask(W: int, H: int) -> np.ndarray:
@@ -66,14 +66,43 @@ def ring_mask(W: int, H: int) -> np.ndarray:
     return (xx < 2) | (yy < 2) | (xx >= W - 2) | (yy >= H - 2)
 
 
-def input_planes(h: np.ndarray, meta: dict, W: int, H: int) -> np.ndarray:
+def input_planes(h: np.ndarray, meta: dict, W: int, H: int, counts=None) -> np.ndarray:
+    """The 16 input planes of one field (before BF16 rounding), in FP32 like
+    the library: h*(1/s), log(s/u)/4, K, m, U, ring mask, log2(drainage
+    count)/16, and on cells with a full neighbourhood the drop to the D8
+    receiver, the central differences along x and y (times 1/2) and h minus
+    0.125 times the sum of its 8 neighbours, each times 1/u."""
+    f32 = np.float32
+    hh = np.asarray(h, np.float64).reshape(H, W).astype(f32)
     x = np.zeros((H, W, INPUT_CHANNELS), np.float64)
-    x[..., 0] = (np.asarray(h, np.float64).reshape(H, W) / float(meta["s"])).astype(np.float32)
+    x[..., 0] = hh * meta["inv_s"]
     x[..., 1] = meta["log_su"]
     x[..., 2] = meta["k_n"]
     x[..., 3] = meta["m_n"]
     x[..., 4] = meta["u_n"]
     x[..., 5] = ring_mask(W, H).astype(np.float64)
+    if counts is not None:
+        c = np.maximum(np.asarray(counts, np.float64).reshape(H, W), 1.0).astype(f32)
+        x[..., 6] = np.log2(c) * f32(0.0625)
+    iu = meta["inv_u"]
+    c0 = hh[1:H - 1, 1:W - 1]
+    # neighbours in the reference's order W, NW, N, NE, E, SE, S, SW
+    sh = [(0, -1), (-1, -1), (-1, 0), (-1, 1), (0, 1), (1, 1), (1, 0), (1, -1)]
+    nb = [hh[1 + dy:H - 1 + dy, 1 + dx:W - 1 + dx] for dy, dx in sh]
+    best = np.zeros_like(c0)
+    drop = np.zeros_like(c0)
+    total = np.zeros_like(c0)
+    for k in range(8):
+        d = c0 - nb[k]
+        slope = d / f32(1.41421356) if k & 1 else d
+        better = slope > best
+        best = np.where(better, slope, best)
+        drop = np.where(better, d, drop)
+        total = total + nb[k]
+    x[1:H - 1, 1:W - 1, 7] = drop * iu
+    x[1:H - 1, 1:W - 1, 8] = (nb[4] - nb[0]) * f32(0.5) * iu
+    x[1:H - 1, 1:W - 1, 9] = (nb[6] - nb[2]) * f32(0.5) * iu
+    x[1:H - 1, 1:W - 1, 10] = (c0 - f32(0.125) * total) * iu
     return x
 
 

@@ -44,13 +44,21 @@ def _params(pkg, rng, n):
             for _ in range(n)]
 
 
+def _counts(h, W, H, p):
+    """Drainage counts of the field h (receivers and accumulation of the
+    oracle's timestep, before its erosion)."""
+    from oracle.pyoracle import Oracle, Params as OParams
+    ph = Oracle().phases(np.array(h, np.float64), W, H, OParams(*p.as_tuple()))
+    return np.rint(ph["accum"] / p.cell_area)
+
+
 def _oracle_inputs(ht, hn, params, W, H):
     xs, ys, ws = [], [], []
     ring = so.ring_mask(W, H)
     for h, nx, p in zip(ht, hn, params):
         h32 = h.astype(np.float32).astype(np.float64)
         meta = so.make_meta(p.keq, p.meq, p.ueq, h.max(), nx.max())
-        xs.append(so.input_planes(h32, meta, W, H))
+        xs.append(so.input_planes(h32, meta, W, H, counts=_counts(h, W, H, p)))
         u = float(meta["u"])
         y = ((nx - h) / u).astype(np.float32).astype(np.float64).reshape(H, W)
         y[ring] = 0
@@ -102,7 +110,7 @@ def test_prediction_matches_oracle_forward(pkg):
     ring = so.ring_mask(W, H).reshape(-1)
     for k, p in enumerate(params):
         meta = so.make_meta(p.keq, p.meq, p.ueq, ht[k].max(), ht[k].max())
-        x = so.input_planes(ht[k], meta, W, H)[None]
+        x = so.input_planes(ht[k], meta, W, H, counts=_counts(ht[k], W, H, p))[None]
         z = net.forward(p0.astype(np.float64), x)["z"][0].reshape(-1)
         ref = ht[k] + float(meta["u"]) * z
         ref[ring] = ht[k][ring]

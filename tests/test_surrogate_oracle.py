@@ -18,7 +18,7 @@ def _case(c=2, W=16, H=16, n=2, seed=0):
         h[so.ring_mask(W, H)] = 0
         meta = so.make_meta(10 ** rng.uniform(-6, -5), rng.uniform(0.3, 0.6),
                             10 ** rng.uniform(-4, -2.3), h.max(), h.max() + 5)
-        xs.append(so.input_planes(h, meta, W, H))
+        xs.append(so.input_planes(h, meta, W, H, counts=rng.integers(1, 50, (H, W))))
         ys.append(rng.normal(0.8, 0.2, (H, W)) * ~so.ring_mask(W, H))
         wts.append(float(meta["weight"]))
     return net, p, np.stack(xs), np.stack(ys), np.array(wts)
@@ -46,9 +46,9 @@ def test_each_layer_gradient_matches_finite_differences():
         for lo, hi in ((wo, bo), (bo, bo + cout)):
             v = np.zeros(p.size)
             v[lo:hi] = rng.normal(size=hi - lo)
-            eps = 1e-6
+            eps = 1e-8   # small enough that no ReLU input changes sign
             fd = (net.loss_grad(p + eps * v, x, y, w)[0] - net.loss_grad(p - eps * v, x, y, w)[0]) / (2 * eps)
-            assert fd == pytest.approx(float(g @ v), rel=1e-5, abs=1e-12)
+            assert fd == pytest.approx(float(g @ v), rel=1e-4, abs=1e-11)
 
 
 def test_parameter_count_of_the_full_network():
