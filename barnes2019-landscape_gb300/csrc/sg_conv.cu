@@ -47,6 +47,7 @@ constexpr int kM = 128;                             // rows of every MMA tile
 constexpr int kKPix = 128;                          // pixels per weight-gradient step
 constexpr int kMaxStages = 8;
 constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
+constexpr size_t kPlanarSmem = 225 * 1024;          // planar form: weights + ring + guard
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
 // ---------------------------------------------------------------- PTX ----
@@ -222,6 +223,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 struct ConvArgs {
   int H, W, BW, BH, tiles_x, tiles_y;
   int cin, taps, bn, stages;
+  int mtiles, ntiles;  // tiles of 128 pixels, and of bn output channels
   const float *bias;
   int relu;
   const bf16 *mask;
@@ -231,13 +233,24 @@ struct ConvArgs {
   int *err;
 };
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+
+constexpr int kConvThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
+
 // ------------------------------------------------------ forward / dgrad ----
+// Persistent: CTA b takes tiles b, b + gridDim.x, ... (pixel tile major, N
+// tile minor). The stage ring runs on across tiles; the accumulator is
+// double-buffered in TMEM (acc_full: MMAs of a tile done; acc_empty: its
+// epilogue has read it), so the epilogue of one tile overlaps the MMAs of the
+// next.
 template <int CB>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kConvThreads, 1)
     k_conv(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
            const ConvArgs a) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], accf;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -248,14 +261,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t ncols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
+  const uint32_t cols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(&accf, 1);
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 128);
+    }
+    mbar_init(&done, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -263,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tma_prefetch(&tmb);
   }
   if (warp == 0) {
-    tmem_alloc(&tmem_slot, ncols);
+    tmem_alloc(&tmem_slot, 2 * cols);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -272,113 +289,363 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = tmem_slot;
 
   const int tiles_img = a.tiles_x * a.tiles_y;
-  const int b = blockIdx.x / tiles_img;
-  const int t = blockIdx.x - b * tiles_img;
-  const int y0 = (t / a.tiles_x) * a.BH, x0 = (t % a.tiles_x) * a.BW;
-  const int n0 = blockIdx.y * a.bn;
   const int kch = a.cin / CB;
   const int nkb = a.taps * kch;
+  const int ntot_tiles = a.mtiles * a.ntiles;
 
-  if (warp == 0 && lane == 0) {
-    // producer
-    int issued = 0;
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % S;
-      const uint32_t ph = (kb / S) & 1;
-      if (!mbar_wait(&empty[s], ph ^ 1, &abort_flag, true)) {
-        sg_raise(a.err, &abort_flag, kSgTimeout);
-        break;
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer
+      int kbg = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
+        const int mt = t / a.ntiles, nt = t - mt * a.ntiles;
+        const int b = mt / tiles_img;
+        const int tt = mt - b * tiles_img;
+        const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
+        const int n0 = nt * a.bn;
+        for (int kb = 0; kb < nkb; kb++, kbg++) {
+          const int s = kbg % S;
+          if (!mbar_wait(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
+            sg_raise(a.err, &abort_flag, kSgTimeout);
+            stop = true;
+            break;
+          }
+          const int tap = kb / kch, cc = kb - tap * kch;
+          const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+          unsigned char *sa = smem + s * stage_bytes;
+          mbar_expect_tx(&full[s], a_bytes + b_bytes);
+          tma_load_4d(sa, &tma, &full[s], cc * CB, x0 + dx, y0 + dy, b);
+          tma_load_2d(sa + a_bytes, &tmb, &full[s], tap * a.cin + cc * CB, n0);
+        }
       }
-      const int tap = kb / kch, cc = kb - tap * kch;
-      const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
-      unsigned char *sa = smem + s * stage_bytes;
-      mbar_expect_tx(&full[s], a_bytes + b_bytes);
-      tma_load_4d(sa, &tma, &full[s], cc * CB, x0 + dx, y0 + dy, b);
-      tma_load_2d(sa + a_bytes, &tmb, &full[s], tap * a.cin + cc * CB, n0);
-      issued = kb + 1;
+      // leave no copy in flight into this CTA's shared memory
+      for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
+        if (!mbar_wait(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
     }
-    // leave no copy in flight into this CTA's shared memory
-    for (int kb = issued > S ? issued - S : 0; kb < issued; kb++)
-      if (!mbar_wait(&full[kb % S], (kb / S) & 1, &abort_flag, false)) {
-        sg_raise(a.err, &abort_flag, kSgTimeout);
-        break;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
+      int kbg = 0, it = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
+        const int buf = it & 1;
+        if (!mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + buf * cols;
+        for (int kb = 0; kb < nkb; kb++, kbg++) {
+          const int s = kbg % S;
+          if (!mbar_wait(&full[s], (kbg / S) & 1, &abort_flag, true)) {
+            sg_raise(a.err, &abort_flag, kSgTimeout);
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = su32(smem + s * stage_bytes);
+          const uint64_t da = smem_desc(sa, 16, 8 * kRow, swizzle_code(kRow));
+          const uint64_t db = smem_desc(sa + a_bytes, 16, 8 * kRow, swizzle_code(kRow));
+#pragma unroll
+          for (int k = 0; k < CB / 16; k++)  // K = 16 per MMA: 32 bytes along the row
+            umma_bf16(d, da + 2 * k, db + 2 * k, idesc, (kb | k) != 0);
+          umma_commit(&empty[s]);
+        }
+        if (!stop) umma_commit(&acc_full[buf]);
       }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % S;
-      if (!mbar_wait(&full[s], (kb / S) & 1, &abort_flag, true)) {
+      // every MMA this thread issued has completed before the teardown
+      umma_commit(&done);
+      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one pixel each
+    const int q = warp & 3;
+    const int r = q * 32 + lane;
+    int it = 0;
+    for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
+      const int buf = it & 1;
+      if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
       tc_fence_after();
-      const uint32_t sa = su32(smem + s * stage_bytes);
-      const uint64_t da = smem_desc(sa, 16, 8 * kRow, swizzle_code(kRow));
-      const uint64_t db = smem_desc(sa + a_bytes, 16, 8 * kRow, swizzle_code(kRow));
+      const int mt = t / a.ntiles, nt = t - mt * a.ntiles;
+      const int b = mt / tiles_img;
+      const int tt = mt - b * tiles_img;
+      const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
+      const int n0 = nt * a.bn;
+      const int py = y0 + r / a.BW, px = x0 + r % a.BW;
+      const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
+      bf16 *out = a.out + pix * a.ldo + n0;
+      const bf16 *msk = a.mask ? a.mask + pix * a.ldm + n0 : nullptr;
+      const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
+      for (int c = 0; c < a.bn; c += 16) {
+        uint32_t v[16];
+        tmem_ld16(d + c, v);
+        tmem_ld_wait();
+        float f[16];
 #pragma unroll
-      for (int k = 0; k < CB / 16; k++)  // K = 16 per MMA: 32 bytes along the row
-        umma_bf16(tmem, da + 2 * k, db + 2 * k, idesc, (kb | k) != 0);
-      umma_commit(&empty[s]);
+        for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
+        if (a.bias) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) f[j] += a.bias[n0 + c + j];
+        }
+        if (a.relu) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
+        }
+        if (msk) {
+          const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
+          const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
+          const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
+          const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
+            if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
+          }
+        }
+        uint4 o0, o1;
+        o0.x = pack_bf16(f[0], f[1]);
+        o0.y = pack_bf16(f[2], f[3]);
+        o0.z = pack_bf16(f[4], f[5]);
+        o0.w = pack_bf16(f[6], f[7]);
+        o1.x = pack_bf16(f[8], f[9]);
+        o1.y = pack_bf16(f[10], f[11]);
+        o1.z = pack_bf16(f[12], f[13]);
+        o1.w = pack_bf16(f[14], f[15]);
+        *reinterpret_cast<uint4 *>(out + c) = o0;
+        *reinterpret_cast<uint4 *>(out + c + 8) = o1;
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
     }
-    umma_commit(&accf);
   }
   __syncwarp();
-
-  // epilogue: TMEM lane = tile row = pixel
-  const bool ok = mbar_wait(&accf, 0, &abort_flag, false);
-  if (!ok) sg_raise(a.err, &abort_flag, kSgTimeout);
-  tc_fence_after();
-  if (ok && !abort_flag) {
-    const int r = warp * 32 + lane;
-    const int py = y0 + r / a.BW, px = x0 + r % a.BW;
-    const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
-    bf16 *out = a.out + pix * a.ldo + n0;
-    const bf16 *msk = a.mask ? a.mask + pix * a.ldm + n0 : nullptr;
-    for (int c = 0; c < a.bn; c += 16) {
-      uint32_t v[16];
-      tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + c, v);
-      tmem_ld_wait();
-      float f[16];
-#pragma unroll
-      for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
-      if (a.bias) {
-#pragma unroll
-        for (int j = 0; j < 16; j++) f[j] += a.bias[n0 + c + j];
-      }
-      if (a.relu) {
-#pragma unroll
-        for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
-      }
-      if (msk) {
-        const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
-        const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
-        const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
-        const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
-          if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
-        }
-      }
-      uint4 o0, o1;
-      o0.x = pack_bf16(f[0], f[1]);
-      o0.y = pack_bf16(f[2], f[3]);
-      o0.z = pack_bf16(f[4], f[5]);
-      o0.w = pack_bf16(f[6], f[7]);
-      o1.x = pack_bf16(f[8], f[9]);
-      o1.y = pack_bf16(f[10], f[11]);
-      o1.z = pack_bf16(f[12], f[13]);
-      o1.w = pack_bf16(f[14], f[15]);
-      *reinterpret_cast<uint4 *>(out + c) = o0;
-      *reinterpret_cast<uint4 *>(out + c + 8) = o1;
-    }
-  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, ncols);
+    tmem_dealloc(tmem, 2 * cols);
+  }
+}
+
+// ------------------------------------------- forward / dgrad, planar A ----
+// For images at least 128 pixels wide with 3x3 taps and weights that fit in
+// shared memory (the narrow layers): each K-block is one image row (dy) of
+// cb channels, staged once as cb/8 planes of 130 pixels x 8 channels (16
+// bytes per pixel, no swizzle: the K-major core-matrix layout with 8-row
+// groups 128 bytes apart and K chunks one plane apart), and the three taps
+// dx of that row are the same planes read from byte offset 16*dx -- a third
+// of the A traffic of one load per tap. The weights of every tap are loaded
+// into shared memory once per CTA and stay there.
+constexpr int kPlanePix = 130;                         // x0-1 .. x0+128
+constexpr int kPlaneBytes = kPlanePix * 16;            // one box: 2080 bytes
+constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;  // 128-byte aligned TMA targets
+constexpr int kGuardBytes = 36 * 1024;  // slack after the ring: no descriptor reads past it
+
+template <int CB>
+__global__ void __launch_bounds__(kConvThreads, 1)
+    k_conv_planar(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmb,
+                  const ConvArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done, wfull;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kRow = CB * 2;
+  constexpr int kPlanes = CB / 8;
+  constexpr int kStageA = (kPlanes * kPlaneStride + 1023) & ~1023;
+  const int kch = a.cin / CB;
+  const int wbox = a.bn * kRow;  // one (tap, channel block) box of weights
+  const int wbytes = 9 * kch * wbox;
+  unsigned char *ring = smem + ((wbytes + 1023) & ~1023);
+  const int S = a.stages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t cols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 128);
+    }
+    mbar_init(&done, 1);
+    mbar_init(&wfull, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma_prefetch(&tmp);
+    tma_prefetch(&tmb);
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, 2 * cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int tiles_img = a.tiles_x * a.tiles_y;
+  const int nkb = 3 * kch;  // (dy, channel block)
+  const int ntot_tiles = a.mtiles;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // weights once: box (tap, cc) at smem + (tap*kch + cc)*wbox
+      mbar_expect_tx(&wfull, wbytes);
+      for (int tap = 0; tap < 9; tap++)
+        for (int cc = 0; cc < kch; cc++)
+          tma_load_2d(smem + (tap * kch + cc) * wbox, &tmb, &wfull, tap * a.cin + cc * CB, 0);
+      int kbg = 0;
+      bool stop = false;
+      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
+        const int b = t / tiles_img;
+        const int tt = t - b * tiles_img;
+        const int y0 = tt / a.tiles_x, x0 = (tt % a.tiles_x) * 128;
+        for (int kb = 0; kb < nkb; kb++, kbg++) {
+          const int s = kbg % S;
+          if (!mbar_wait(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
+            sg_raise(a.err, &abort_flag, kSgTimeout);
+            stop = true;
+            break;
+          }
+          const int dy = kb / kch, cc = kb - dy * kch;
+          unsigned char *sa = ring + s * kStageA;
+          mbar_expect_tx(&full[s], kPlanes * kPlaneBytes);
+#pragma unroll
+          for (int pl = 0; pl < kPlanes; pl++)
+            tma_load_4d(sa + pl * kPlaneStride, &tmp, &full[s], cc * CB + 8 * pl, x0 - 1,
+                        y0 + dy - 1, b);
+        }
+      }
+      for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
+        if (!mbar_wait(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+      if (!mbar_wait(&wfull, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
+      bool stop = !mbar_wait(&wfull, 0, &abort_flag, true);
+      if (stop) sg_raise(a.err, &abort_flag, kSgTimeout);
+      tc_fence_after();
+      const uint32_t wbase = su32(smem);
+      int kbg = 0, it = 0;
+      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
+        const int buf = it & 1;
+        if (!mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + buf * cols;
+        for (int kb = 0; kb < nkb; kb++, kbg++) {
+          const int s = kbg % S;
+          if (!mbar_wait(&full[s], (kbg / S) & 1, &abort_flag, true)) {
+            sg_raise(a.err, &abort_flag, kSgTimeout);
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const int dy = kb / kch, cc = kb - dy * kch;
+          const uint32_t sa = su32(ring + s * kStageA);
+#pragma unroll
+          for (int dx = 0; dx < 3; dx++) {
+            const uint32_t wb = wbase + ((3 * dy + dx) * kch + cc) * wbox;
+            const uint64_t db = smem_desc(wb, 16, 8 * kRow, swizzle_code(kRow));
+#pragma unroll
+            for (int k = 0; k < CB / 16; k++) {
+              // K-major, no swizzle: K chunks (planes) kPlaneStride apart, 8-row
+              // groups 128 bytes apart; 16 channels = two planes per MMA
+              const uint64_t da = smem_desc(sa + 16 * dx + 2 * k * kPlaneStride, kPlaneStride, 128, 0);
+              umma_bf16(d, da, db + 2 * k, idesc, (kb | dx | k) != 0);
+            }
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!stop) umma_commit(&acc_full[buf]);
+      }
+      umma_commit(&done);
+      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+    }
+  } else {
+    const int q = warp & 3;
+    const int r = q * 32 + lane;
+    int it = 0;
+    for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
+      const int buf = it & 1;
+      if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const int b = t / tiles_img;
+      const int tt = t - b * tiles_img;
+      const int py = tt / a.tiles_x, px = (tt % a.tiles_x) * 128 + r;
+      const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
+      bf16 *out = a.out + pix * a.ldo;
+      const bf16 *msk = a.mask ? a.mask + pix * a.ldm : nullptr;
+      const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
+      for (int c = 0; c < a.bn; c += 16) {
+        uint32_t v[16];
+        tmem_ld16(d + c, v);
+        tmem_ld_wait();
+        float f[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
+        if (a.bias) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) f[j] += a.bias[c + j];
+        }
+        if (a.relu) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
+        }
+        if (msk) {
+          const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
+          const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
+          const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
+          const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
+            if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
+          }
+        }
+        uint4 o0, o1;
+        o0.x = pack_bf16(f[0], f[1]);
+        o0.y = pack_bf16(f[2], f[3]);
+        o0.z = pack_bf16(f[4], f[5]);
+        o0.w = pack_bf16(f[6], f[7]);
+        o1.x = pack_bf16(f[8], f[9]);
+        o1.y = pack_bf16(f[10], f[11]);
+        o1.z = pack_bf16(f[12], f[13]);
+        o1.w = pack_bf16(f[14], f[15]);
+        *reinterpret_cast<uint4 *>(out + c) = o0;
+        *reinterpret_cast<uint4 *>(out + c + 8) = o1;
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * cols);
   }
 }
 
@@ -580,6 +847,24 @@ cudaError_t map_act(CUtensorMap *m, const Act &t, int cb, const PixTile &pt) {
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// {8, 130, 1, 1} boxes of an NHWC tensor without swizzle: one plane of 8
+// channels over 130 pixels of one image row.
+cudaError_t map_planes(CUtensorMap *m, const Act &t) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
+                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
+  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
+  const cuuint32_t box[4] = {8, static_cast<cuuint32_t>(kPlanePix), 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // {cb, bn} boxes of a [rows][cols] BF16 matrix.
 cudaError_t map_mat(CUtensorMap *m, const bf16 *p, int rows, int cols, int cb, int bn) {
   EncodeTiledFn enc = encode_fn();
@@ -660,6 +945,20 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   if (S < 2) return *why = "stage does not fit shared memory", cudaErrorInvalidValue;
   p.stages = S;
   p.smem = S * stage + 1024;
+  // the planar form: wide images, 3x3 taps, one N tile whose weights fit
+  // beside a ring of at least two stages and the guard
+  {
+    const size_t wbytes = (static_cast<size_t>(9) * src.C * bn * 2 + 1023) & ~static_cast<size_t>(1023);
+    const size_t stage_a = (static_cast<size_t>(p.cb / 8) * kPlaneStride + 1023) & ~static_cast<size_t>(1023);
+    const size_t room = kPlanarSmem - 1024 - kGuardBytes;
+    if (taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room) {
+      int Sp = static_cast<int>((room - wbytes) / stage_a);
+      if (Sp > kMaxStages) Sp = kMaxStages;
+      p.planar = 1;
+      p.stages = Sp;
+      p.smem = wbytes + Sp * stage_a + kGuardBytes + 1024;
+    }
+  }
   p.bias = bias;
   p.relu = relu;
   p.mask = mask;
@@ -668,7 +967,12 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   p.ldo = ldo;
   p.grid_x = static_cast<int>(src.pixels() / kM);
   p.grid_y = ntot / bn;
-  cudaError_t e = map_act(&p.tma, src, p.cb, p.pt);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  p.sms = 1;
+  cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, dev);
+  if (p.sms < 1) p.sms = 1;
+  cudaError_t e = p.planar ? map_planes(&p.tma, src) : map_act(&p.tma, src, p.cb, p.pt);
   if (e != cudaSuccess) return *why = "tensor map (source)", e;
   e = map_mat(&p.tmb, w, ntot, taps * src.C, p.cb, bn);
   if (e != cudaSuccess) return *why = "tensor map (weights)", e;
@@ -735,6 +1039,9 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_conv<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kSmemBudget + 1024));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_conv_planar<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kPlanarSmem));
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -756,8 +1063,14 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   a.out = p.out;
   a.ldo = p.ldo;
   a.err = err;
-  const int gx = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
-  k_conv<CB><<<dim3(gx, p.grid_y), kThreads, p.smem, s>>>(p.tma, p.tmb, a);
+  a.mtiles = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
+  a.ntiles = p.grid_y;
+  const int tiles = a.mtiles * a.ntiles;
+  const int grid = tiles < p.sms ? tiles : p.sms;
+  if (p.planar)
+    k_conv_planar<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);
+  else
+    k_conv<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);
   return cudaGetLastError();
 }
 

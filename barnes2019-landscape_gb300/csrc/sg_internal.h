@@ -48,7 +48,7 @@ PixTile pixel_tile(int H, int W);
 // A forward (or data-gradient) convolution prepared for launches: the tensor
 // maps of its source and weights, the tile shape and the epilogue.
 struct ConvPlan {
-  CUtensorMap tma;  // source activations, box {cb, BW, BH, 1}
+  CUtensorMap tma;  // source activations, box {cb, BW, BH, 1} (planar: {8, 130, 1, 1})
   CUtensorMap tmb;  // weights [ntot][taps*cin], box {cb, bn}
   int B = 0, H = 0, W = 0, cin = 0, taps = 9, ntot = 0, bn = 0, cb = 0, stages = 0;
   PixTile pt;
@@ -59,7 +59,9 @@ struct ConvPlan {
   bf16 *out = nullptr;
   int ldo = 0;
   size_t smem = 0;
-  int grid_x = 0, grid_y = 0;
+  int grid_x = 0, grid_y = 0;  // pixel tiles and N tiles
+  int sms = 1;                 // persistent CTAs launched (at most one per SM)
+  int planar = 0;              // planar source staging with resident weights
 };
 
 // A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=
