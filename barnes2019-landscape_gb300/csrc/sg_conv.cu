@@ -46,8 +46,9 @@ constexpr int kThreads = 128;
 constexpr int kM = 128;                             // rows of every MMA tile
 constexpr int kKPix = 128;                          // pixels per weight-gradient step
 constexpr int kMaxStages = 8;
+constexpr int kMaxBias = 512;                       // biased outputs of a forward conv
 constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
-constexpr size_t kPlanarSmem = 225 * 1024;          // planar form: weights + ring + guard
+constexpr size_t kPlanarSmem = 222 * 1024;          // planar form: weights + ring + guard (+ static)
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
 // ---------------------------------------------------------------- PTX ----
@@ -237,7 +238,68 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-constexpr int kConvThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
+constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps
+constexpr int kWgradThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
+
+// One 16-column chunk of a tile row: + bias (shared memory), ReLU, zeroed
+// where the mask is not positive, rounded to BF16, stored (32 bytes).
+__device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, int relu,
+                                      const bf16 *msk, bf16 *out) {
+  float f[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
+  if (sb) {
+#pragma unroll
+    for (int j = 0; j < 16; j++) f[j] += sb[j];
+  }
+  if (relu) {
+#pragma unroll
+    for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
+  }
+  if (msk) {
+    const uint4 m0 = *reinterpret_cast<const uint4 *>(msk);
+    const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + 8);
+    const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
+    const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
+      if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
+    }
+  }
+  uint4 o0, o1;
+  o0.x = pack_bf16(f[0], f[1]);
+  o0.y = pack_bf16(f[2], f[3]);
+  o0.z = pack_bf16(f[4], f[5]);
+  o0.w = pack_bf16(f[6], f[7]);
+  o1.x = pack_bf16(f[8], f[9]);
+  o1.y = pack_bf16(f[10], f[11]);
+  o1.z = pack_bf16(f[12], f[13]);
+  o1.w = pack_bf16(f[14], f[15]);
+  *reinterpret_cast<uint4 *>(out) = o0;
+  *reinterpret_cast<uint4 *>(out + 8) = o1;
+}
+
+// Columns [c_lo, c_hi) of this warp's 32 TMEM lanes (d: lane quarter and
+// accumulator base), two 16-column loads in flight per wait.
+__device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, const float *sb,
+                                            int relu, const bf16 *msk, bf16 *out) {
+  int c = c_lo;
+  for (; c + 32 <= c_hi; c += 32) {
+    uint32_t v0[16], v1[16];
+    tmem_ld16(d + c, v0);
+    tmem_ld16(d + c + 16, v1);
+    tmem_ld_wait();
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + c : nullptr, out + c);
+    epi16(v1, sb ? sb + c + 16 : nullptr, relu, msk ? msk + c + 16 : nullptr, out + c + 16);
+  }
+  if (c < c_hi) {
+    uint32_t v0[16];
+    tmem_ld16(d + c, v0);
+    tmem_ld_wait();
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + c : nullptr, out + c);
+  }
+}
 
 // ------------------------------------------------------ forward / dgrad ----
 // Persistent: CTA b takes tiles b, b + gridDim.x, ... (pixel tile major, N
@@ -253,6 +315,9 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
+  __shared__ float s_bias[kMaxBias];
+  if (a.bias)
+    for (int i = threadIdx.x; i < a.bn * a.ntiles; i += blockDim.x) s_bias[i] = a.bias[i];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   constexpr int kRow = CB * 2;  // bytes per operand row (the swizzle span)
@@ -270,7 +335,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
     for (int i = 0; i < 2; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], 128);
+      mbar_init(&acc_empty[i], kConvThreads - 64);
     }
     mbar_init(&done, 1);
     abort_flag = 0;
@@ -363,9 +428,13 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one pixel each
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (one pixel each);
+    // the two warps of a lane quarter split the columns
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int r = q * 32 + lane;
+    const int csplit = a.bn % 32 == 0 ? a.bn / 2 : a.bn;
+    const int c_lo = half ? csplit : 0, c_hi = half ? a.bn : csplit;
     int it = 0;
     for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
       const int buf = it & 1;
@@ -381,47 +450,9 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       const int n0 = nt * a.bn;
       const int py = y0 + r / a.BW, px = x0 + r % a.BW;
       const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
-      bf16 *out = a.out + pix * a.ldo + n0;
-      const bf16 *msk = a.mask ? a.mask + pix * a.ldm + n0 : nullptr;
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
-      for (int c = 0; c < a.bn; c += 16) {
-        uint32_t v[16];
-        tmem_ld16(d + c, v);
-        tmem_ld_wait();
-        float f[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
-        if (a.bias) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) f[j] += a.bias[n0 + c + j];
-        }
-        if (a.relu) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
-        }
-        if (msk) {
-          const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
-          const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
-          const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
-          const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
-            if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
-          }
-        }
-        uint4 o0, o1;
-        o0.x = pack_bf16(f[0], f[1]);
-        o0.y = pack_bf16(f[2], f[3]);
-        o0.z = pack_bf16(f[4], f[5]);
-        o0.w = pack_bf16(f[6], f[7]);
-        o1.x = pack_bf16(f[8], f[9]);
-        o1.y = pack_bf16(f[10], f[11]);
-        o1.z = pack_bf16(f[12], f[13]);
-        o1.w = pack_bf16(f[14], f[15]);
-        *reinterpret_cast<uint4 *>(out + c) = o0;
-        *reinterpret_cast<uint4 *>(out + c + 8) = o1;
-      }
+      epi_columns(d, c_lo, c_hi, a.bias ? s_bias + n0 : nullptr, a.relu,
+                  a.mask ? a.mask + pix * a.ldm + n0 : nullptr, a.out + pix * a.ldo + n0);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -457,6 +488,9 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done, wfull;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
+  __shared__ float s_bias[kMaxBias];
+  if (a.bias)
+    for (int i = threadIdx.x; i < a.bn; i += blockDim.x) s_bias[i] = a.bias[i];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   constexpr int kRow = CB * 2;
@@ -477,7 +511,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
     for (int i = 0; i < 2; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], 128);
+      mbar_init(&acc_empty[i], kConvThreads - 64);
     }
     mbar_init(&done, 1);
     mbar_init(&wfull, 1);
@@ -582,7 +616,10 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
   } else {
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int r = q * 32 + lane;
+    const int csplit = a.bn % 32 == 0 ? a.bn / 2 : a.bn;
+    const int c_lo = half ? csplit : 0, c_hi = half ? a.bn : csplit;
     int it = 0;
     for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
       const int buf = it & 1;
@@ -595,47 +632,9 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       const int tt = t - b * tiles_img;
       const int py = tt / a.tiles_x, px = (tt % a.tiles_x) * 128 + r;
       const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
-      bf16 *out = a.out + pix * a.ldo;
-      const bf16 *msk = a.mask ? a.mask + pix * a.ldm : nullptr;
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
-      for (int c = 0; c < a.bn; c += 16) {
-        uint32_t v[16];
-        tmem_ld16(d + c, v);
-        tmem_ld_wait();
-        float f[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
-        if (a.bias) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) f[j] += a.bias[c + j];
-        }
-        if (a.relu) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) f[j] = fmaxf(f[j], 0.0f);
-        }
-        if (msk) {
-          const uint4 m0 = *reinterpret_cast<const uint4 *>(msk + c);
-          const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + c + 8);
-          const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
-          const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
-#pragma unroll
-          for (int j = 0; j < 8; j++) {
-            if (!(__bfloat162float(mb0[j]) > 0.0f)) f[j] = 0.0f;
-            if (!(__bfloat162float(mb1[j]) > 0.0f)) f[8 + j] = 0.0f;
-          }
-        }
-        uint4 o0, o1;
-        o0.x = pack_bf16(f[0], f[1]);
-        o0.y = pack_bf16(f[2], f[3]);
-        o0.z = pack_bf16(f[4], f[5]);
-        o0.w = pack_bf16(f[6], f[7]);
-        o1.x = pack_bf16(f[8], f[9]);
-        o1.y = pack_bf16(f[10], f[11]);
-        o1.z = pack_bf16(f[12], f[13]);
-        o1.w = pack_bf16(f[14], f[15]);
-        *reinterpret_cast<uint4 *>(out + c) = o0;
-        *reinterpret_cast<uint4 *>(out + c + 8) = o1;
-      }
+      epi_columns(d, c_lo, c_hi, a.bias ? s_bias : nullptr, a.relu,
+                  a.mask ? a.mask + pix * a.ldm : nullptr, a.out + pix * a.ldo);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -791,6 +790,174 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// ------------------------------------------------ weight grad, planar ----
+// For images at least 128 pixels wide, 3x3 taps and at most 128 output
+// channels: M = output channels (dY, zero planes up to 128 rows), N = input
+// channels (X), K = 128 pixels of one image row per step. Both operands are
+// MN-major without swizzle: planes of 8 channels x pixels, 16 bytes per
+// pixel, so 8-pixel K groups are 128 bytes apart and a tap's shift dx is a
+// 16*dx byte offset into X's planes. A step loads dY's row once and the X
+// rows its taps need once (the swizzled form loads X once per tap and
+// chunk); each tap of the CTA's tap group accumulates in its own TMEM
+// columns. The zero planes of dY are cleared once and never loaded.
+constexpr int kYPlaneBytes = 128 * 16;
+
+struct WgradPlanarArgs {
+  int H, W, tiles_x, cin, cout, tap0, ntap, row0, nrows, cpt, stages, ksteps, kper;
+  int stage_bytes;
+  float *dw;
+  int *err;
+};
+
+__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(kWgradThreads, 1)
+    k_wgrad_planar(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmy,
+                   const WgradPlanarArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full, done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int S = a.stages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int yp = a.cout / 8, xp = a.cin / 8;  // loaded planes of dY and of each X row
+  const uint32_t need = static_cast<uint32_t>(a.ntap * a.cpt);
+  const uint32_t cols = need <= 32 ? 32 : need <= 64 ? 64 : need <= 128 ? 128 : need <= 256 ? 256 : 512;
+
+  // dY's planes yp..15 stay zero in every stage (generic-proxy stores made
+  // visible to the tensor cores by the proxy fence below)
+  for (int st = 0; st < S; st++) {
+    uint4 *z = reinterpret_cast<uint4 *>(smem + st * a.stage_bytes + yp * kYPlaneBytes);
+    const int n16 = (16 - yp) * kYPlaneBytes / 16;
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&acc_full, 1);
+    mbar_init(&done, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tma_prefetch(&tmx);
+    tma_prefetch(&tmy);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int tiles_img = a.tiles_x * a.H;
+  const int k_lo = blockIdx.x * a.kper;
+  const int k_hi = min(a.ksteps, k_lo + a.kper);
+  const int nk = k_hi - k_lo;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      const uint32_t tx = yp * kYPlaneBytes + a.nrows * xp * kPlaneBytes;
+      for (int i = 0; i < nk; i++) {
+        const int s = i % S;
+        if (!mbar_wait(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+        const int kt = k_lo + i;
+        const int b = kt / tiles_img, t = kt - b * tiles_img;
+        const int y0 = t / a.tiles_x, x0 = (t % a.tiles_x) * 128;
+        unsigned char *sy = smem + s * a.stage_bytes;
+        unsigned char *sx = sy + 16 * kYPlaneBytes;
+        mbar_expect_tx(&full[s], tx);
+        for (int pl = 0; pl < yp; pl++)
+          tma_load_4d(sy + pl * kYPlaneBytes, &tmy, &full[s], 8 * pl, x0, y0, b);
+        for (int r = 0; r < a.nrows; r++)
+          for (int pl = 0; pl < xp; pl++)
+            tma_load_4d(sx + (r * xp + pl) * kPlaneStride, &tmx, &full[s], 8 * pl, x0 - 1,
+                        y0 + a.row0 + r - 1, b);
+        issued = i + 1;
+      }
+      for (int i = issued > S ? issued - S : 0; i < issued; i++)
+        if (!mbar_wait(&full[i % S], (i / S) & 1, &abort_flag, false)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16(a.cin, 1, 1);
+      for (int i = 0; i < nk; i++) {
+        const int s = i % S;
+        if (!mbar_wait(&full[s], (i / S) & 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t sy = su32(smem + s * a.stage_bytes);
+        const uint32_t sx = sy + 16 * kYPlaneBytes;
+        for (int j = 0; j < a.ntap; j++) {
+          const int tap = a.tap0 + j;
+          const int r = tap / 3 - a.row0, dx = tap % 3;
+          const uint32_t d = tmem + j * a.cpt;
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            // MN-major, no swizzle: MN chunks (planes) at the plane stride,
+            // 8-pixel K groups 128 bytes apart; 16 pixels per MMA
+            const uint64_t da = smem_desc(sy + 256 * k, 128, kYPlaneBytes, 0);
+            const uint64_t db = smem_desc(sx + r * xp * kPlaneStride + 16 * dx + 256 * k, 128,
+                                          kPlaneStride, 0);
+            umma_bf16(d, da, db, idesc, (i | k) != 0);
+          }
+        }
+        umma_commit(&empty[s]);
+      }
+      umma_commit(&acc_full);
+      umma_commit(&done);
+      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+    }
+  } else if (nk > 0) {
+    const int q = warp & 3;
+    const int co = q * 32 + lane;
+    const bool ok = mbar_wait(&acc_full, 0, &abort_flag, true);
+    if (!ok) sg_raise(a.err, &abort_flag, kSgTimeout);
+    tc_fence_after();
+    if (ok && !abort_flag) {
+      const long long kdim = 9ll * a.cin;
+      for (int j = 0; j < a.ntap; j++) {
+        float *dst = a.dw + co * kdim + (a.tap0 + j) * a.cin;
+        for (int c = 0; c < a.cin; c += 16) {
+          uint32_t v[16];
+          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + j * a.cpt + c, v);
+          tmem_ld_wait();
+          if (co < a.cout) {
+#pragma unroll
+            for (int u = 0; u < 16; u += 4)
+              red_add_v4(dst + c + u, __uint_as_float(v[u]), __uint_as_float(v[u + 1]),
+                         __uint_as_float(v[u + 2]), __uint_as_float(v[u + 3]));
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, cols);
+  }
+}
+
 __global__ void k_flip_weights(const bf16 *__restrict__ w, bf16 *__restrict__ wd, int cout,
                                int cin, int taps) {
   const long long n = static_cast<long long>(cout) * taps * cin;
@@ -913,6 +1080,7 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   if (src.C % 16 || src.C <= 0) return *why = "source channels must be a multiple of 16", cudaErrorInvalidValue;
   if (taps != 1 && taps != 9) return *why = "taps must be 1 or 9", cudaErrorInvalidValue;
   if (ntot % 16 || ntot <= 0) return *why = "output channels must be a multiple of 16", cudaErrorInvalidValue;
+  if (bias && ntot > kMaxBias) return *why = "at most 512 biased output channels", cudaErrorInvalidValue;
   if (ldo % 8 || ldo < ntot || (mask && (ldm % 8 || ldm < ntot)))
     return *why = "output/mask row strides must be multiples of 8 covering the channels", cudaErrorInvalidValue;
   if (!aligned16(src.p) || !aligned16(w) || !aligned16(out) || (mask && !aligned16(mask)))
@@ -989,6 +1157,51 @@ void split_pixels(WgradPlan &p, int ksteps) {
   p.splits = (ksteps + p.kper - 1) / p.kper;
 }
 
+// {8, 128, 1, 1} boxes: one plane of 8 channels over 128 pixels of a row.
+cudaError_t map_planes128(CUtensorMap *m, const Act &t) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
+                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
+  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
+                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
+  const cuuint32_t box[4] = {8, 128, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// The planar weight gradient's tap groups: as many taps per CTA as their
+// accumulators fit in 512 TMEM columns and their X rows plus dY's 16 planes
+// fit two stages of shared memory; false when no grouping fits (the MMA's N
+// is the input channel count, at most 256).
+bool plan_planar_groups(WgradPlan &p) {
+  if (p.taps != 9 || p.W < kM || p.cout > kM || p.W % kM || p.cin > 256) return false;
+  const int cpt = (p.cin + 31) / 32 * 32;
+  const int per = 512 / cpt < 9 ? 512 / cpt : 9;
+  if (per < 1) return false;
+  p.ngroups = 0;
+  for (int t0 = 0; t0 < 9; t0 += per) {
+    const int nt = 9 - t0 < per ? 9 - t0 : per;
+    const int r0 = t0 / 3, r1 = (t0 + nt - 1) / 3;
+    const size_t stage = (16 * static_cast<size_t>(kYPlaneBytes) +
+                          static_cast<size_t>(r1 - r0 + 1) * (p.cin / 8) * kPlaneStride + 1023) &
+                         ~static_cast<size_t>(1023);
+    if (2 * stage > kSmemBudget) return false;
+    p.grp_tap0[p.ngroups] = t0;
+    p.grp_ntap[p.ngroups] = nt;
+    p.grp_row0[p.ngroups] = r0;
+    p.grp_nrows[p.ngroups] = r1 - r0 + 1;
+    p.grp_stage[p.ngroups] = static_cast<int>(stage);
+    p.ngroups++;
+  }
+  p.cpt = cpt;
+  return true;
+}
+
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
                        const char **why) {
   const char *dummy;
@@ -1024,9 +1237,10 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
   p.sms = sms;
   split_pixels(p, p.ksteps);
   p.dw = dw;
-  cudaError_t e = map_act(&p.tmx, x, p.cwa, p.pt);
+  p.planar = plan_planar_groups(p) ? 1 : 0;
+  cudaError_t e = p.planar ? map_planes(&p.tmx, x) : map_act(&p.tmx, x, p.cwa, p.pt);
   if (e != cudaSuccess) return *why = "tensor map (X)", e;
-  e = map_act(&p.tmy, dy, p.cwb, p.pt);
+  e = p.planar ? map_planes128(&p.tmy, dy) : map_act(&p.tmy, dy, p.cwb, p.pt);
   if (e != cudaSuccess) return *why = "tensor map (dY)", e;
   return cudaSuccess;
 }
@@ -1126,8 +1340,50 @@ cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s, int nimg) {
   }
 }
 
+cudaError_t launch_wgrad_planar(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_wgrad_planar, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kSmemBudget + 1024));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const int ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
+  for (int g = 0; g < p.ngroups; g++) {
+    WgradPlanarArgs a{};
+    a.H = p.H;
+    a.W = p.W;
+    a.tiles_x = p.pt.tiles_x;
+    a.cin = p.cin;
+    a.cout = p.cout;
+    a.tap0 = p.grp_tap0[g];
+    a.ntap = p.grp_ntap[g];
+    a.row0 = p.grp_row0[g];
+    a.nrows = p.grp_nrows[g];
+    a.cpt = p.cpt;
+    a.stage_bytes = p.grp_stage[g];
+    int S = static_cast<int>(kSmemBudget / a.stage_bytes);
+    a.stages = S > kMaxStages ? kMaxStages : S;
+    a.ksteps = ksteps;
+    // about three CTAs per SM over the groups, each over >= 8 steps
+    int splits = (3 * p.sms + p.ngroups - 1) / p.ngroups;
+    if (splits > ksteps / 8) splits = ksteps / 8;
+    if (splits < 1) splits = 1;
+    a.kper = (ksteps + splits - 1) / splits;
+    splits = (ksteps + a.kper - 1) / a.kper;
+    a.dw = p.dw;
+    a.err = err;
+    const size_t smem = static_cast<size_t>(a.stages) * a.stage_bytes + 1024;
+    k_wgrad_planar<<<splits, kWgradThreads, smem, s>>>(p.tmx, p.tmy, a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
   if (p.mtiles <= 0 || nimg < 0 || nimg > p.B) return cudaErrorInvalidValue;
+  if (p.planar) return launch_wgrad_planar(p, err, s, nimg);
   switch (p.cwa) {
     case 64: return launch_wgrad_a<64>(p, err, s, nimg);
     case 32: return launch_wgrad_a<32>(p, err, s, nimg);

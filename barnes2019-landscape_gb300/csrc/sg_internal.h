@@ -67,13 +67,17 @@ struct ConvPlan {
 // A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=
 // sum over pixels of dY[p][co] * X[p + off(tap)][ci].
 struct WgradPlan {
-  CUtensorMap tmx;  // X, box {cwa, BW, BH, 1}
-  CUtensorMap tmy;  // dY, box {cwb, BW, BH, 1}
+  CUtensorMap tmx;  // X, box {cwa, BW, BH, 1} (planar: {8, 130, 1, 1})
+  CUtensorMap tmy;  // dY, box {cwb, BW, BH, 1} (planar: {8, 128, 1, 1})
   int B = 0, H = 0, W = 0, cin = 0, cout = 0, taps = 9, cwa = 0, cwb = 0, stages = 0;
   PixTile pt;
   int mtiles = 0, splits = 0, ksteps = 0, kper = 0, sms = 1;
   float *dw = nullptr;
   size_t smem = 0;
+  // planar form (wide images, 3x3, <= 128 output channels): tap groups of
+  // one launch each, every group's taps accumulating in cpt TMEM columns
+  int planar = 0, ngroups = 0, cpt = 0;
+  int grp_tap0[9] = {}, grp_ntap[9] = {}, grp_row0[9] = {}, grp_nrows[9] = {}, grp_stage[9] = {};
 };
 
 // Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for

@@ -561,7 +561,9 @@ cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView 
 
 cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s) {
   if (g.C % 8 || g.C > 256) return cudaErrorInvalidValue;
-  int blocks = static_cast<int>((g.pixels() + 4095) / 4096);
+  // at least 64 pixel rows per block, at most four blocks per SM
+  const long long per = kBlock / (g.C / 8);
+  int blocks = static_cast<int>((g.pixels() + 64 * per - 1) / (64 * per));
   if (blocks > 152 * 4) blocks = 152 * 4;
   if (blocks < 1) blocks = 1;
   k_bias_grad<<<blocks, kBlock, 0, s>>>(g.p, g.pixels(), g.C, db);
