@@ -118,7 +118,8 @@ class EnsembleStats(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("cycles", "jumps", "judged", "fallbacks")] + \
                [(n, C.c_double) for n in ("rel_rms_mean", "rel_rms_max", "agreement_mean",
                                           "agreement_min", "ms_total", "ms_infer", "ms_exact",
-                                          "ms_plain", "ms_judge")]
+                                          "ms_plain", "ms_judge", "rel_rms_unchanged_mean",
+                                          "agreement_unchanged_mean")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

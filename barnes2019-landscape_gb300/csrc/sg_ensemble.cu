@@ -289,11 +289,14 @@ int fs_sg_ensemble_run(fs_batch *b, fs_surrogate *s, const fs_sg_ensemble_opts *
   const int rest = o->nsteps - ncycles * cycle;
   const size_t hw = static_cast<size_t>(cfg.width) * cfg.height;
   const int jmax = static_cast<int>(std::ceil(o->judge_fraction * n)) + 1;
+  // side fields of the judged jumps: their predictions, then the fields
+  // before the jump (the no-change reference the judge also measures)
   double *side = nullptr;
   if (jmax > 0 && o->judge_fraction > 0) {
-    cudaError_t e = cudaMalloc(&side, hw * jmax * sizeof(double));
+    cudaError_t e = cudaMalloc(&side, 2 * hw * jmax * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(e, "judge fields");
   }
+  double pers_rel_sum = 0, pers_agree_sum = 0;
   fs_sg_ensemble_stats S{};
   S.rel_rms_max = 0;
   S.agreement_min = 1;
@@ -326,7 +329,17 @@ int fs_sg_ensemble_run(fs_batch *b, fs_surrogate *s, const fs_sg_ensemble_opts *
     if (!free_jump.empty())
       st = fs_sg_predict_batch(s, b, static_cast<int>(free_jump.size()), free_jump.data(), nullptr);
     outs.resize(judged.size());
-    for (size_t k = 0; k < judged.size(); k++) outs[k] = side + k * hw;
+    std::vector<double *> before(judged.size());
+    for (size_t k = 0; k < judged.size(); k++) {
+      outs[k] = side + k * hw;
+      before[k] = side + (jmax + k) * hw;
+      if (st == FS_OK &&
+          cudaMemcpyAsync(before[k], field[judged[k]], hw * sizeof(double),
+                          cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+        st = cuda_fail(cudaGetLastError(), "judge copy");
+    }
+    if (st == FS_OK && cudaStreamSynchronize(stream) != cudaSuccess)
+      st = cuda_fail(cudaGetLastError(), "judge copy");
     if (st == FS_OK && !judged.empty())
       st = fs_sg_predict_batch(s, b, static_cast<int>(judged.size()), judged.data(), outs.data());
     S.ms_infer += ms_since(t0);
@@ -354,6 +367,15 @@ int fs_sg_ensemble_run(fs_batch *b, fs_surrogate *s, const fs_sg_ensemble_opts *
       }
       st = compare_fields(cfg.width, cfg.height, static_cast<int>(judged.size()), outs.data(),
                           ex.data(), dr.data(), rel.data(), ag.data(), stream);
+      std::vector<double> rel_p(judged.size()), ag_p(judged.size());
+      if (st == FS_OK)
+        st = compare_fields(cfg.width, cfg.height, static_cast<int>(judged.size()),
+                            before.data(), ex.data(), dr.data(), rel_p.data(), ag_p.data(),
+                            stream);
+      for (size_t k = 0; k < judged.size() && st == FS_OK; k++) {
+        pers_rel_sum += rel_p[k];
+        pers_agree_sum += ag_p[k];
+      }
       for (size_t k = 0; k < judged.size() && st == FS_OK; k++) {
         S.judged++;
         rel_sum += rel[k];
@@ -388,6 +410,8 @@ int fs_sg_ensemble_run(fs_batch *b, fs_surrogate *s, const fs_sg_ensemble_opts *
   if (S.judged > 0) {
     S.rel_rms_mean = rel_sum / S.judged;
     S.agreement_mean = agree_sum / S.judged;
+    S.rel_rms_unchanged_mean = pers_rel_sum / S.judged;
+    S.agreement_unchanged_mean = pers_agree_sum / S.judged;
   } else {
     S.agreement_min = 0;
   }

@@ -368,6 +368,67 @@ def ensemble_spec(pkg, n: int, seed: int = 2019, side: int = 0):
     return [int(s) for s in sides], params
 
 
+def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local):
+    """Batched ensemble: realizations/s of nsteps-timestep runs from the
+    initial fields (the launch shape the autotuner picks, CUDA events around
+    the whole run on the batch's stream), then the same run once more from
+    the same initial fields with an event between kernels for the split."""
+    sides, params = ensemble_spec(pkg, n, seed=seed, side=side)
+    seeds = list(range(1000 * rank, 1000 * rank + len(sides)))
+    b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX, seeds=seeds)
+    cells = b.cells()
+    # warm-up: the autotuner's probe timesteps (9 launch configurations x 3),
+    # after which it restores the initial fields
+    tune = b.autotune(probe_steps=2)
+    b.set_timing(pkg.TIMING_CALL)
+    b.phase_times(reset=True)
+    b.synchronize()
+    barrier(dist)
+    with Clocks(local) as clk:
+        b.step(nsteps)                       # the whole run from the initial fields
+    barrier(dist)
+    dt = max_over_ranks(dist, float(b.phase_times(reset=True)[3]) * 1e-3)
+    levels = max(b.levels(r)[1] for r in range(len(sides)))
+    b.close()
+    b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX, seeds=seeds)
+    b.set_timing(pkg.TIMING_KERNELS)
+    b.phase_times(reset=True)
+    b.step(nsteps)
+    t = b.phase_times(reset=True) / nsteps
+    b.close()
+    per_step = dt / nsteps
+    shape = "equal-size" if side > 0 else "ragged"
+    side_desc = f"{side}" if side > 0 else "log-U[256,2048]"
+    peak, peak_kind = load_peaks()
+    kern = {"receivers": t[0], "donors_level0": t[1], "order": t[7], "accum": t[9],
+            "erode": t[8]}
+    dom = max(("order", "accum", "erode"), key=kern.get)
+    achieved = ALG_BYTES[dom] * cells / (kern[dom] * 1e-3) / 1e9
+    return {
+        "metric": f"ensemble realizations/s ({nsteps}-timestep runs)",
+        "value": ws * len(sides) / (nsteps * per_step),
+        "unit": "realizations/s", "n_gpus": ws, "steps": nsteps, "warmup": 9 * 3,
+        "ms_per_step": 1e3 * per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{shape} ensemble of {len(sides)} realizations, sides "
+                               f"{side_desc}, K log-U[1e-6,1e-5], m U[0.3,0.6], "
+                               "U log-U[1e-4,5e-3], n 1, dt 1000, dx 100",
+                   "cells_per_step": cells, "cell_steps_per_s": cells / per_step,
+                   "launch": tune, "l2": "inputs larger than L2",
+                   "timed": f"the whole {nsteps}-timestep run from the initial fields "
+                            "(launch path of the autotuner's choice)",
+                   "kernel_split": "a second run from the same fields, direct launches "
+                                   "with events between kernels",
+                   "levels_at_end": levels},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "alg_bytes_per_cell": ALG_BYTES[dom],
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": kern},
+        "gpu_launches": 6 * nsteps,
+        "clocks": clk.summary(),
+    }
+
+
 def run_ensemble(args, dist, rank, ws, local):
     """Batched ragged ensemble: realizations/s of 200-timestep runs, one
     batched launch sequence per timestep (autotuned). The timed region is the
@@ -377,57 +438,10 @@ def run_ensemble(args, dist, rank, ws, local):
     pkg = ge.load()
     if ws > 1:
         torch.cuda.set_device(local)
-    sides, params = ensemble_spec(pkg, args.realizations, seed=2019 + rank,
-                                  side=args.ensemble_side)
-    b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX,
-                           seeds=list(range(1000 * rank, 1000 * rank + len(sides))))
-    cells = b.cells()
-    # warm-up: the autotuner's probe timesteps (9 launch configurations x 3),
-    # after which it restores the initial fields
-    tune = b.autotune(probe_steps=2)
-    warm = 8 * 3
-    nsteps = args.ensemble_steps
-    b.set_timing(True)
-    b.phase_times(reset=True)
-    b.synchronize()
-    barrier(dist)
-    with Clocks(local) as clk:
-        b.step(nsteps)                       # the whole run from the initial fields
-    barrier(dist)
-    t = b.phase_times(reset=True) / nsteps * 2   # per 2 timesteps, like below
-    dt = max_over_ranks(dist, t[3] / 2 * 1e-3 * nsteps)
-    levels = max(b.levels(r)[1] for r in range(len(sides)))
-    b.close()
-    per_step = dt / nsteps
-    value = ws * len(sides) / (nsteps * per_step)
+    res = ensemble_result(pkg, args.realizations, args.ensemble_side, args.ensemble_steps,
+                          2019 + rank, rank, ws, dist, local)
     if rank == 0:
-        shape = "equal-size" if args.ensemble_side > 0 else "ragged"
-        side_desc = (f"{args.ensemble_side}" if args.ensemble_side > 0
-                     else "log-U[256,2048]")
-        peak, peak_kind = load_peaks()
-        kern = {"receivers": t[0] / 2, "donors_level0": t[1] / 2, "order": t[7] / 2,
-                "accum": t[9] / 2, "erode": t[8] / 2}
-        dom = max(("order", "accum", "erode"), key=kern.get)
-        achieved = ALG_BYTES[dom] * cells / (kern[dom] * 1e-3) / 1e9
-        print(json.dumps({
-            "metric": f"ensemble realizations/s ({nsteps}-timestep runs)", "value": value,
-            "unit": "realizations/s", "n_gpus": ws, "steps": nsteps, "warmup": warm,
-            "ms_per_step": 1e3 * per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{shape} ensemble of {len(sides)} realizations, sides "
-                                   f"{side_desc}, K log-U[1e-6,1e-5], m U[0.3,0.6], "
-                                   "U log-U[1e-4,5e-3], n 1, dt 1000, dx 100",
-                       "cells_per_step": cells, "cell_steps_per_s": cells / per_step,
-                       "autotune": tune, "l2": "inputs larger than L2",
-                       "timed": f"the whole {nsteps}-timestep run from the initial fields",
-                       "levels_at_end": levels},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "alg_bytes_per_cell": ALG_BYTES[dom],
-                         "peak_source": f"{peak_kind} hbm_gbs", "kernel_ms": kern},
-            "gpu_launches": 6 * nsteps,
-            "clocks": clk.summary(),
-        }), flush=True)
+        print(json.dumps(res), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
@@ -587,6 +601,56 @@ def run_surrogate(args, dist, rank, ws, local):
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def surrogate_extras(pkg, args, local):
+    """Configs 3 and 4 for the default run: the surrogate's training
+    throughput (512^2, batch 32, Adam, on samples the plain method generates
+    on the device; short, timed with CUDA events on the network's stream)
+    and the judged surrogate ensemble against the plain batched method with
+    the committed trained parameters (SG_WEIGHTS)."""
+    peak_b, peak_s, peak_kind = load_bf16_peak()
+    out = {}
+    net = pkg.Surrogate(512, 512, base_channels=32, batch=32, jump=50, seed=1)
+    net.reserve(64)
+    net.generate(32, 2, 200, seed=7)
+    net.train(3, lr=1e-4)                      # warm-up steps
+    steps = args.sg_bench_steps
+    with Clocks(local) as clk:
+        net.train(steps, lr=1e-4)
+    ms, flops = net.train_stats()
+    tf = flops * steps / (ms * 1e-3) / 1e12
+    fwd_ms, fwd_flops = net.time_forward(reps=5)
+    fwd_tf = fwd_flops / (fwd_ms * 1e-3) / 1e12
+    out["training"] = {
+        "metric": "surrogate training samples/s (512^2, batch 32, BF16 tcgen05, Adam)",
+        "value": 32 * steps / (ms * 1e-3), "unit": "samples/s", "steps": steps, "warmup": 3,
+        "ms_per_step": ms / steps, "conv_tflops_per_step": flops / 1e12,
+        "roofline": {"bound": "tensor", "kernel": "training step (14 convolutions forward, "
+                                                   "data and weight gradients, and the rest)",
+                     "achieved": tf, "peak": peak_s, "unit": "TFLOP/s", "frac": tf / peak_s,
+                     "peak_source": f"{peak_kind} bf16_tflops_sustained"},
+        "forward_pass": {"ms": fwd_ms, "achieved_tflops": fwd_tf, "peak": peak_b,
+                         "frac": fwd_tf / peak_b,
+                         "peak_source": f"{peak_kind} bf16_tflops (burst)"},
+        "data": "64 samples of 512^2 the plain method generated on the device "
+                "(0..200 timesteps); the full 20000-sample run is --workload surrogate",
+        "clocks": clk.summary()}
+    if SG_WEIGHTS.exists():
+        net.load(SG_WEIGHTS)
+        ens = surrogate_ensemble(pkg, net, args.sg_realizations, 512, args.sg_ensemble_steps,
+                                 0.05, 2019, local)
+        out["ensemble"] = {
+            "metric": "ensemble realizations/s, surrogate vs plain (512^2, judged)",
+            "value": ens["surrogate"]["realizations_per_s"], "unit": "realizations/s",
+            "plain_realizations_per_s": ens["plain"]["realizations_per_s"],
+            "surrogate_vs_plain": ens["ratio"], "steps": args.sg_ensemble_steps,
+            "realizations": args.sg_realizations, "parameters": SG_WEIGHTS.name,
+            "detail": ens}
+    else:
+        out["ensemble"] = {"unavailable": f"no trained parameters at {SG_WEIGHTS.name}"}
+    net.close()
+    return out
 
 
 def net_param_count(pkg):
@@ -820,6 +884,15 @@ def main():
     ap.add_argument("--sg-lr", type=float, default=1e-3)
     ap.add_argument("--sg-judge", type=float, default=0.05)
     ap.add_argument("--sg-save", default="", help="surrogate: write the trained parameters here")
+    ap.add_argument("--sg-bench-steps", type=int, default=20,
+                    help="default run: timed surrogate training steps")
+    ap.add_argument("--sg-realizations", type=int, default=1024,
+                    help="default run: realizations of the surrogate ensemble")
+    ap.add_argument("--sg-ensemble-steps", type=int, default=2000,
+                    help="default run: timesteps of the surrogate ensemble")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default run: only the 10000^2 timestep (no ensemble or surrogate "
+                         "keys)")
     ap.add_argument("--sg-load", default="",
                     help="surrogate: use these parameters (no generation or training)")
     args = ap.parse_args()
@@ -980,6 +1053,13 @@ def main():
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
+        if ws == 1 and not args.no_extras:
+            # the ensemble half of the metric: the 256-realization ragged
+            # ensemble (200 timesteps) and the surrogate against the plain
+            # batched method, each with its own clock record
+            line["ensemble_ragged"] = ensemble_result(pkg, 256, 0, ENSEMBLE_STEPS, 2019, 0, 1,
+                                                      None, local)
+            line["surrogate"] = surrogate_extras(pkg, args, local)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -155,6 +155,10 @@ typedef struct fs_sg_ensemble_stats {
   int cycles, jumps, judged, fallbacks;
   double rel_rms_mean, rel_rms_max, agreement_mean, agreement_min;
   double ms_total, ms_infer, ms_exact, ms_plain, ms_judge;  /* host clock  */
+  /* the judge's measures for the field before the jump (no change) against
+   * the exact run, over the same judged jumps: how far the landscape and
+   * its receivers move in one jump */
+  double rel_rms_unchanged_mean, agreement_unchanged_mean;
 } fs_sg_ensemble_stats;
 
 void fs_sg_ensemble_defaults(fs_sg_ensemble_opts *o);

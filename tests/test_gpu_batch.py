@@ -175,3 +175,38 @@ def test_batch_table_growth_in_one_realization(pkg):
         assert b.accumulation(1).max() / p.cell_area > 65536
         for m in singles:
             m.close()
+
+
+def test_ragged_ensemble_at_its_own_scale(pkg, oracle):
+    """The 256-realization ragged ensemble's own draws (bench.ensemble_spec:
+    sides log-uniform in [256, 2048], K, m, U as drawn there), 200 timesteps:
+    the largest, the smallest and two more realizations of that draw, run as
+    one batch with the launch shape the autotuner picks, each bit-identical to
+    a model of its own (receivers, level ids, accumulation, elevation) after
+    the deep level structures of 200 timesteps, and the smallest bit-identical
+    to the oracle's restatement of the reference as well."""
+    import bench
+    sides, params = bench.ensemble_spec(pkg, 256, seed=2019)
+    order = np.argsort(sides)
+    pick = [int(order[-1]), int(order[0]), int(order[len(order) // 3]),
+            int(order[2 * len(order) // 3])]
+    ws = [sides[i] for i in pick]
+    ps = [params[i] for i in pick]
+    seeds = [1000 + i for i in pick]
+    assert max(ws) > 1800 and min(ws) < 300
+    nsteps = 200
+    with pkg.FastScapeBatch(ws, ws, ps, init=pkg.INIT_PHILOX, seeds=seeds) as b:
+        h_small = b.getH(1)
+        b.autotune(probe_steps=2)
+        b.step(nsteps)
+        singles = [pkg.FastScape_RBP(w, w, params=p, init=pkg.INIT_PHILOX, seed=s)
+                   for w, p, s in zip(ws, ps, seeds)]
+        for m in singles:
+            m.step(nsteps)
+        compare_with_singles(pkg, b, ws, ws, ps, singles, f"{nsteps} timesteps")
+        assert max(b.levels(r)[1] for r in range(len(ws))) > 20
+        p = ps[1]
+        ref = oracle.steps(h_small.copy(), ws[1], ws[1], Params(*p.as_tuple()), nsteps)
+        assert np.array_equal(b.getH(1), ref)
+        for m in singles:
+            m.close()
