@@ -52,6 +52,7 @@ ABI_SYMBOLS = [
     "fs_batch_use_int_sub", "fs_use_int_sub",
     "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
     "fs_autotune", "fs_launch_config",
+    "fs_batch_use_cta_walk", "fs_batch_walk_mode",
     "fs_batch_set_active", "fs_batch_analyze", "fs_batch_drainage_counts",
     "fs_batch_device_elevation", "fs_batch_stream",
     "fs_batch_get_params", "fs_batch_get_shape",
@@ -188,6 +189,8 @@ def library() -> C.CDLL:
     L.fs_autotune.argtypes = [vp, C.c_int, ip]
     L.fs_launch_config.argtypes = [vp, ip, ip, ip, ip]
     L.fs_batch_synchronize.argtypes = [vp]
+    L.fs_batch_use_cta_walk.argtypes = [vp, C.c_int]
+    L.fs_batch_walk_mode.argtypes = [vp, ip]
     L.fs_batch_set_active.argtypes = [vp, C.c_int, ip]
     L.fs_batch_analyze.argtypes = [vp]
     L.fs_batch_drainage_counts.argtypes = [vp, C.c_int, vp]
@@ -517,11 +520,18 @@ class FastScapeBatch:
         return self.launch_config()
 
     def launch_config(self):
-        o, e, g, i = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        o, e, g, i, w = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(library().fs_batch_launch_config(self._b, C.byref(o), C.byref(e), C.byref(g),
                                                C.byref(i)))
+        check(library().fs_batch_walk_mode(self._b, C.byref(w)))
         return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
-                "graph": bool(g.value), "erode_int_sub": bool(i.value)}
+                "graph": bool(g.value), "erode_int_sub": bool(i.value),
+                "cta_walk": bool(w.value)}
+
+    def use_cta_walk(self, on: bool = True) -> None:
+        """One CTA per realization walks its levels (block barriers only)
+        instead of the grid-wide lock step; identical results."""
+        check(library().fs_batch_use_cta_walk(self._b, int(bool(on))))
 
     def synchronize(self) -> None:
         check(library().fs_batch_synchronize(self._b))

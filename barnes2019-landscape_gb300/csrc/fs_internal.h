@@ -183,6 +183,15 @@ const void *order_kernel_ptr(bool single, int bps);     // k_order for bps 2 or 
 const void *accum_kernel_ptr(bool single);              // k_accum
 constexpr int kAccumMaxBps = 4;                         // k_accum's register budget
 cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
+// The per-realization walk (batches of many small realizations): one CTA of
+// cta_threads() threads per realization (blocks CTAs in all, looping over
+// the realizations); launch_cta_order orders and accumulates,
+// launch_cta_erode uplifts and erodes (skipped on an abort or error).
+int cta_threads();
+const void *cta_order_ptr();
+const void *cta_erode_ptr(int nmode, int var);
+cudaError_t launch_cta_order(const StepArgs &a, int blocks, cudaStream_t s);
+cudaError_t launch_cta_erode(const StepArgs &a, int blocks, cudaStream_t s);
 cudaError_t launch_check_finite(const double *h, long long n, Ctl *ctl, cudaStream_t s);
 cudaError_t launch_philox_field(double *h, int W, int H, uint64_t seed, cudaStream_t s);
 cudaError_t launch_place_rings(int32_t *ent, int W, int H, cudaStream_t s);

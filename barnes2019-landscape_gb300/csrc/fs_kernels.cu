@@ -1624,6 +1624,164 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
   if (tid == 0) atomicAdd(&ctl->steps_done, 1);
 }
 
+// ---------------------------------------------------------------------------
+// Per-realization level walk for batches of many small realizations. The
+// grid-wide walk above pays a grid barrier per level for the whole batch,
+// and long runs grow hundreds of levels of a few thousand cells each; here
+// one CTA walks one realization's levels with block barriers only (several
+// realizations per SM), with the same arrays, the same per-cell arithmetic
+// and the same level ids, counts and elevations bit for bit (the order of
+// entries within a level may differ from the grid walk's, which its atomics
+// leave free as well).
+//   k_cta_order_accum: level ordering (fastscape_RB.cpp:213-254: level k+1 =
+//     the donors of level k, each entry's donors contiguous in direction
+//     order) and the accumulation back down the levels (fastscape_RB.cpp:
+//     262-279, counts pushed into the receivers' positions); a count beyond
+//     the realization's erosion table raises the batch-wide abort, so the
+//     next kernel leaves every elevation unchanged and the timestep is redone.
+//   k_cta_erode: uplift of the pits, then uplift + erosion level by level
+//     (fastscape_RB.cpp:285-328 in the level order of fastscape_RB+P.cpp:
+//     319-350), exactly as k_accum's tail and k_erode do.
+// ---------------------------------------------------------------------------
+constexpr int kCtaThreads = 256;
+
+__global__ void __launch_bounds__(kCtaThreads) k_cta_order_accum(StepArgs a) {
+  Ctl *ctl = a.ctl;
+  if (stopped(ctl)) return;
+  const int t = threadIdx.x;
+  __shared__ int s_lvl[kLevelCache + 1];
+  for (int r = blockIdx.x; r < a.nreal; r += gridDim.x) {
+    const RealDesc d = a.desc[r];
+    int32_t *ent = a.ent + d.off;
+    uint8_t *pdir = a.pdir + d.off;
+    uint32_t *acc = a.acc + d.off;
+    int32_t *par = a.par + d.off;
+    const uint8_t *mask = a.mask + d.off;
+    int *lvl = a.lvl_off + d.lvl_base;
+    int lo = 0, hi = d.nring + ld_volatile_i32(&a.rctl[r].top);
+    if (t == 0) {
+      lvl[0] = 0;
+      lvl[1] = hi;
+      s_lvl[0] = 0;
+      s_lvl[1] = hi;
+    }
+    int nlev = 1;
+    bool ovf = false;
+    for (;;) {
+      int next = hi;
+      for (int cs = lo; cs < hi; cs += kCtaThreads) {
+        const int i = cs + t;
+        int cell = 0;
+        unsigned m = 0;
+        if (i < hi) {
+          cell = __ldcg(&ent[i]);
+          m = mask[cell];
+          acc[i] = 1u;  // the cell itself; donors add theirs below
+        }
+        int total;
+        const int excl = block_excl_scan(__popc(m), total, t, kCtaThreads);
+        if (next + total > d.size) {  // block-uniform
+          ovf = true;
+          break;
+        }
+        int pos = next + excl;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          if (m >> k & 1u) {
+            ent[pos] = cell + nbr_off(k, d.W);
+            pdir[pos] = (uint8_t)((k + 4) & 7);
+            par[pos] = i;  // the receiver's position
+            ++pos;
+          }
+        }
+        next += total;
+      }
+      __syncthreads();  // the next level's entries are written
+      if (ovf || next == hi) break;
+      lo = hi;
+      hi = next;
+      ++nlev;
+      if (t == 0) {
+        lvl[nlev] = hi;
+        if (nlev <= kLevelCache) s_lvl[nlev] = hi;
+      }
+    }
+    if (t == 0) {
+      a.rctl[r].nlevels = nlev;
+      a.rctl[r].total = hi;
+      if (ovf) raise_err(ctl, FS_ERR_LEVEL_OVERFLOW, kPhaseOrder);
+      else if (hi != d.size) raise_err(ctl, FS_ERR_ORDER, kPhaseOrder);  // a cycle
+    }
+    __syncthreads();
+    if (ovf || hi != d.size) continue;
+    for (int Lv = nlev - 1; Lv >= 1; --Lv) {
+      const int l0 = Lv <= kLevelCache ? s_lvl[Lv] : __ldcg(&lvl[Lv]);
+      const int l1 = Lv + 1 <= kLevelCache ? s_lvl[Lv + 1] : __ldcg(&lvl[Lv + 1]);
+      for (int i = l0 + t; i < l1; i += kCtaThreads) {
+        const uint32_t v = __ldcg(&acc[i]);
+        atomicAdd(&acc[__ldcg(&par[i])], v);
+        if (a.do_erode && v >= (uint32_t)d.tab_cap) {
+          if (atomicMax(&ctl->abort_k, (int)v) < (int)v) ctl->abort_r = r;
+        }
+      }
+      __syncthreads();  // this level's counts are final before the next reads them
+    }
+  }
+}
+
+template <int NMODE, int VAR>
+__global__ void __launch_bounds__(kCtaThreads) k_cta_erode(StepArgs a) {
+  constexpr bool ISUB = VAR == 1, GENERIC = VAR == 2;
+  Ctl *ctl = a.ctl;
+  if (stopped(ctl)) return;  // an error, or a count beyond a table: nothing changes
+  const int t = threadIdx.x;
+  for (int r = blockIdx.x; r < a.nreal; r += gridDim.x) {
+    const RealDesc d = a.desc[r];
+    const int nlev = __ldcg(&a.rctl[r].nlevels);
+    const int *lvl = a.lvl_off + d.lvl_base;
+    unsigned long long *hh = reinterpret_cast<unsigned long long *>(a.h + d.off);
+    const int32_t *ent = a.ent + d.off;
+    const uint8_t *pdir = a.pdir + d.off;
+    const uint32_t *acc = a.acc + d.off;
+    const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
+    // the pits (level 0 after the rings) are uplifted, not eroded
+    const int p1 = __ldcg(&lvl[1]);
+    for (int i = d.nring + t; i < p1; i += kCtaThreads) {
+      const int c = __ldcg(&ent[i]);
+      hh[c] = fadd_bits(__ldcg(&hh[c]), udt);
+    }
+    __syncthreads();
+    for (int Lv = 1; Lv < nlev; ++Lv) {
+      const int lo = __ldcg(&lvl[Lv]), hi = __ldcg(&lvl[Lv + 1]);
+      for (int i = lo + t; i < hi; i += kCtaThreads) {
+        const int c = __ldcg(&ent[i]);
+        const int dir = __ldcg(&pdir[i]);
+        const uint32_t k = __ldcg(&acc[i]);
+        const uint64_t h0 = uplift_bits(__ldcg(&hh[c]), udt);
+        const uint64_t hn = __ldcg(&hh[c + nbr_off(dir & 7, d.W)]);
+        const size_t rec_at = (size_t)k * kTabStride + 4 * (dir & 1);
+        uint64_t hnew;
+        if (NMODE == kNOne && !GENERIC) {
+          const unsigned long long *Tb = reinterpret_cast<const unsigned long long *>(d.tab) + rec_at;
+          hnew = erode_cell_n1<ISUB>(d, ctl, Tb, load_tab_n1(Tb), h0, hn);
+        } else if (NMODE == kNTwo && !GENERIC) {
+          hnew = erode_cell_n2<ISUB>(d, a.neq, ctl,
+                                     __ldg(reinterpret_cast<const unsigned long long *>(d.tab) + rec_at),
+                                     h0, hn);
+        } else {
+          hnew = (uint64_t)__double_as_longlong(erode_cell<NMODE>(
+              d, a.neq, ctl, d.tab + rec_at, __longlong_as_double(h0), __longlong_as_double(hn)));
+        }
+        if (((hnew >> 52) & 0x7FF) == 0x7FF)  // Inf or NaN
+          raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
+        hh[c] = hnew;
+      }
+      __syncthreads();  // this level's elevations are final before the next reads them
+    }
+  }
+  if (blockIdx.x == 0 && t == 0) atomicAdd(&ctl->steps_done, 1);
+}
+
 __global__ void k_check_finite(const double *__restrict__ h, long long n, Ctl *ctl) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
@@ -1973,6 +2131,38 @@ cudaError_t launch_accum(const StepArgs &a, int sms, int bps, cudaStream_t s) {
   void *params[] = {&args};
   return cudaLaunchCooperativeKernel(accum_kernel_ptr(a.nreal == 1), dim3(sms * bps),
                                      dim3(kWalkThreads), params, walk_smem_bytes(a.nreal), s);
+}
+
+const void *cta_erode_ptr(int nmode, int var) {
+  switch (nmode) {
+    case kNOne:
+      return var == 2 ? reinterpret_cast<const void *>(&k_cta_erode<kNOne, 2>)
+             : var == 1 ? reinterpret_cast<const void *>(&k_cta_erode<kNOne, 1>)
+                        : reinterpret_cast<const void *>(&k_cta_erode<kNOne, 0>);
+    case kNTwo:
+      return var == 2 ? reinterpret_cast<const void *>(&k_cta_erode<kNTwo, 2>)
+             : var == 1 ? reinterpret_cast<const void *>(&k_cta_erode<kNTwo, 1>)
+                        : reinterpret_cast<const void *>(&k_cta_erode<kNTwo, 0>);
+    default:
+      return reinterpret_cast<const void *>(&k_cta_erode<kNGeneral, 2>);
+  }
+}
+
+int cta_threads() { return kCtaThreads; }
+
+const void *cta_order_ptr() { return reinterpret_cast<const void *>(&k_cta_order_accum); }
+
+cudaError_t launch_cta_order(const StepArgs &a, int blocks, cudaStream_t s) {
+  k_cta_order_accum<<<blocks, kCtaThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cta_erode(const StepArgs &a, int blocks, cudaStream_t s) {
+  StepArgs args = a;
+  void *params[] = {&args};
+  const int var = a.erode_generic ? 2 : a.erode_isub ? 1 : 0;
+  return cudaLaunchKernel(cta_erode_ptr(a.nmode, var), dim3(blocks), dim3(kCtaThreads), params, 0,
+                          s);
 }
 
 cudaError_t launch_walk(const StepArgs &a, int sms, int order_bps, int accum_bps,

@@ -124,6 +124,11 @@ struct fs_batch {
   int order_max = 2, order_bps = 2;              // k_order blocks per SM: limit (2 or 3), in use
   int accum_bps = 1;                             // k_accum blocks per SM
   int erode_isub = 0;                            // k_erode's integer subtractions (n = 1)
+  // per-realization walk (one CTA per realization, block barriers only):
+  // used when cta_walk and the launch covers more than one realization;
+  // resident CTAs per SM of its ordering and erosion kernels (by variant)
+  bool cta_walk = false;
+  int cta_occ_order = 1, cta_occ_erode[3] = {1, 1, 1};
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
@@ -287,6 +292,19 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   return a;
 }
 
+// The per-realization walk runs when chosen and the launch covers more than
+// one realization (a single grid keeps the grid-wide walk).
+bool use_cta(const fs_batch *b, const fs::StepArgs &a) { return b->cta_walk && a.nreal > 1; }
+
+// CTAs of a per-realization walk kernel: every realization at once where
+// they fit, else as many as are resident (each loops over realizations).
+int cta_blocks(const fs_batch *b, const fs::StepArgs &a, bool erode) {
+  const int var = a.erode_generic ? 2 : a.erode_isub ? 1 : 0;
+  const int occ = erode ? b->cta_occ_erode[var] : b->cta_occ_order;
+  const int resident = b->walk_sms * std::max(occ, 1);
+  return std::max(1, std::min(a.nreal, resident));
+}
+
 // The launches of one timestep (no synchronization).
 cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
   cudaError_t e = cudaMemsetAsync(reinterpret_cast<char *>(b->d_ctl) + fs::kCtlResetOffset, 0,
@@ -298,11 +316,16 @@ cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
                            : fs::launch_receivers_fast(a, b->stream);
   if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
   if (e == cudaSuccess) {
-    if (b->act_n > 0)
+    if (use_cta(b, a)) {
+      e = fs::launch_cta_order(a, cta_blocks(b, a, false), b->stream);
+      if (e == cudaSuccess && a.do_erode)
+        e = fs::launch_cta_erode(a, cta_blocks(b, a, true), b->stream);
+    } else if (b->act_n > 0) {
       e = fs::launch_walk(a, b->walk_sms, b->act_order_bps, b->act_accum_bps, b->act_walk_bps,
                           b->stream);
-    else
+    } else {
       e = fs::launch_walk(a, b->walk_sms, b->order_bps, b->accum_bps, b->walk_bps, b->stream);
+    }
   }
   return e;
 }
@@ -334,6 +357,15 @@ int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
   FS_CUDA(cudaEventRecord(ev[2], b->stream));
   const bool act = b->act_n > 0;
+  if (use_cta(b, a)) {
+    // ordering + accumulation in one kernel (reported as the ordering's),
+    // then the erosion
+    FS_CUDA(fs::launch_cta_order(a, cta_blocks(b, a, false), b->stream));
+    FS_CUDA(cudaEventRecord(ev[3], b->stream));
+    FS_CUDA(cudaEventRecord(ev[4], b->stream));
+    FS_CUDA(fs::launch_cta_erode(a, cta_blocks(b, a, true), b->stream));
+    return FS_OK;
+  }
   FS_CUDA(fs::launch_order(a, b->walk_sms, act ? b->act_order_bps : b->order_bps, b->stream));
   FS_CUDA(cudaEventRecord(ev[3], b->stream));
   FS_CUDA(fs::launch_accum(a, b->walk_sms, act ? b->act_accum_bps : b->accum_bps, b->stream));
@@ -832,6 +864,15 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
   if (occ < 1) return fail(set_error(FS_ERR_CUDA, "walk kernel cannot be resident"));
   b->walk_occ = occ;
   b->walk_bps = std::min(occ, 2);
+  if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->cta_occ_order, fs::cta_order_ptr(),
+                                                        fs::cta_threads(), 0),
+          "occupancy"))
+    return fail(*status);
+  for (int v = 0; v < 3; v++)
+    if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &b->cta_occ_erode[v], fs::cta_erode_ptr(b->nmode, v), fs::cta_threads(), 0),
+            "occupancy"))
+      return fail(*status);
   // k_order: the variant with 3 blocks per SM where all three fit (a large
   // batch's shared memory may not allow it), else the 2-block one.
   for (int bps = 3; bps >= 2; bps--) {
@@ -1016,9 +1057,11 @@ int get_phase_times(const fs_batch *b, double *ms, int reset) {
 
 // Autotuner: times each candidate launch configuration -- ordering and
 // erosion blocks per SM with and without the captured graph, then for n = 1
-// the fastest of these with the erosion's integer subtractions -- on the
+// or 2 the fastest of these with the erosion's integer subtractions -- on the
 // batch's own state over `probe` timesteps, restoring the elevation after
-// every probe, and keeps the fastest.
+// every probe, and keeps the fastest; the level walk is chosen by size.
+constexpr int kCtaWalkCells = 1 << 19;
+
 int autotune(fs_batch *b, int probe, int *chosen) {
   DeviceGuard dg(b->device);
   double *save = nullptr;
@@ -1081,6 +1124,29 @@ int autotune(fs_batch *b, int probe, int *chosen) {
       best_isub = 1;
     }
   }
+  // The per-realization walk is chosen by size, not by the probes: its
+  // advantage (a block barrier per level instead of a grid barrier) grows with
+  // the number of levels, which the probes, run on the batch's current state,
+  // do not see when that state is young. With every realization at most
+  // kCtaWalkCells cells it wins at every depth measured (1024 x 512^2: 13.2 vs
+  // 19.0 ms per timestep over 2000 timesteps); a larger realization walked by
+  // one CTA serialises (a ragged batch up to 2048^2 ran 7x slower). Within the
+  // chosen walk the probes pick the graph.
+  const bool cta_before = b->cta_walk;
+  const bool want_cta = b->n > 1 && *std::max_element(b->size.begin(), b->size.end()) <= kCtaWalkCells;
+  if (want_cta && st == FS_OK) {
+    b->cta_walk = true;
+    best = 1e30f;
+    for (int gr = 0; gr < 2 && st == FS_OK; gr++) {
+      float ms = 0;
+      st = time_config(best_obps, best_bps, gr == 1, best_isub, &ms);
+      if (st == FS_OK && ms < best) {
+        best = ms;
+        best_graph = gr == 1 && b->use_graph;
+      }
+    }
+  }
+  b->cta_walk = st == FS_OK ? want_cta : cta_before;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaStreamSynchronize(b->stream);
@@ -1392,6 +1458,19 @@ int fs_launch_config(const fs_model *m, int *order_bps, int *erode_bps, int *gra
                      int *erode_int_sub) {
   FS_MODEL(m);
   return fs_batch_launch_config(m->b, order_bps, erode_bps, graph, erode_int_sub);
+}
+
+int fs_batch_use_cta_walk(fs_batch *b, int enable) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  b->cta_walk = enable != 0;
+  b->graph_dirty = true;
+  return FS_OK;
+}
+
+int fs_batch_walk_mode(const fs_batch *b, int *cta) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (cta) *cta = b->cta_walk ? 1 : 0;
+  return FS_OK;
 }
 
 int fs_batch_set_active(fs_batch *b, int n, const int *idx) {

@@ -368,7 +368,7 @@ def ensemble_spec(pkg, n: int, seed: int = 2019, side: int = 0):
     return [int(s) for s in sides], params
 
 
-def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local):
+def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local, walk="auto"):
     """Batched ensemble: realizations/s of nsteps-timestep runs from the
     initial fields (the launch shape the autotuner picks, CUDA events around
     the whole run on the batch's stream), then the same run once more from
@@ -380,6 +380,9 @@ def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local):
     # warm-up: the autotuner's probe timesteps (9 launch configurations x 3),
     # after which it restores the initial fields
     tune = b.autotune(probe_steps=2)
+    if walk != "auto":
+        b.use_cta_walk(walk == "cta")
+        tune = b.launch_config()
     b.set_timing(pkg.TIMING_CALL)
     b.phase_times(reset=True)
     b.synchronize()
@@ -391,6 +394,8 @@ def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local):
     levels = max(b.levels(r)[1] for r in range(len(sides)))
     b.close()
     b = pkg.FastScapeBatch(sides, sides, params, init=pkg.INIT_PHILOX, seeds=seeds)
+    b.use_cta_walk(tune.get("cta_walk", False))
+    b.use_int_sub(tune.get("erode_int_sub", False))
     b.set_timing(pkg.TIMING_KERNELS)
     b.phase_times(reset=True)
     b.step(nsteps)
@@ -439,7 +444,7 @@ def run_ensemble(args, dist, rank, ws, local):
     if ws > 1:
         torch.cuda.set_device(local)
     res = ensemble_result(pkg, args.realizations, args.ensemble_side, args.ensemble_steps,
-                          2019 + rank, rank, ws, dist, local)
+                          2019 + rank, rank, ws, dist, local, walk=args.walk)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if dist is not None:
@@ -875,6 +880,8 @@ def main():
                          "draw (1024 x 512 with 2000 timesteps is the plain batched method "
                          "at the surrogate ensemble's shape)")
     ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
+    ap.add_argument("--walk", default="auto", choices=["auto", "grid", "cta"],
+                    help="ensemble: level walk (auto: the library's choice)")
     ap.add_argument("--sg-traj", type=int, default=2000,
                     help="surrogate: realizations generating training data")
     ap.add_argument("--sg-per", type=int, default=10, help="surrogate: samples per realization")

@@ -236,8 +236,10 @@ int fs_batch_use_int_sub(fs_batch *b, int enable);
  * the erosion's elevation subtractions in integer arithmetic) over
  * probe_steps timesteps of the batch's own state, restores the state and
  * keeps the fastest; chosen[0] = erosion kernel blocks per SM, chosen[1] =
- * graph (fs_batch_launch_config reports every choice). Results do not depend
- * on the configuration. */
+ * graph (fs_batch_launch_config reports every choice). The level walk is set
+ * by size: per realization (fs_batch_use_cta_walk) when the batch has more
+ * than one realization and none has more than 2^19 cells, grid-wide
+ * otherwise. Results do not depend on the configuration. */
 int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen);
 /* The launch configuration in use: blocks per SM of the ordering kernel and
  * of the erosion kernel, graph replay (0/1), integer subtractions in the
@@ -245,6 +247,15 @@ int fs_batch_autotune(fs_batch *b, int probe_steps, int *chosen);
 int fs_batch_launch_config(const fs_batch *b, int *order_bps, int *erode_bps,
                            int *graph, int *erode_int_sub);
 int fs_batch_synchronize(const fs_batch *b);
+
+/* Level walk of a batch: 0 = grid-wide (every realization walks its levels
+ * in lock step, one grid barrier per level for the batch), 1 = one CTA per
+ * realization (block barriers only; for batches of many small realizations
+ * whose hundreds of levels each hold a few thousand cells). Identical
+ * results; fs_batch_autotune picks by realization size. A launch that covers a single
+ * realization always walks grid-wide. No reference counterpart. */
+int fs_batch_use_cta_walk(fs_batch *b, int enable);
+int fs_batch_walk_mode(const fs_batch *b, int *cta);
 
 /* Restricts the following fs_batch_step / fs_batch_run calls to the n
  * realizations listed in idx (distinct, in [0, number of realizations));

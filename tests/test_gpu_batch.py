@@ -38,13 +38,17 @@ def compare_with_singles(pkg, b, ws, hs, ps, singles, tag):
         assert np.array_equal(b.getH(r), m.getH()), f"{tag} h r={r}"
 
 
-@pytest.mark.parametrize("graph,int_sub", [(False, False), (True, False), (True, True)])
-def test_batch_equals_independent_models(pkg, graph, int_sub):
+@pytest.mark.parametrize("graph,int_sub,cta", [(False, False, False), (True, False, False),
+                                               (True, True, False), (False, False, True),
+                                               (True, True, True)])
+def test_batch_equals_independent_models(pkg, graph, int_sub, cta):
     ws, hs, ps = ensemble(9, 11)
     seeds = list(range(100, 109))
     with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=seeds) as b:
         b.use_graph(graph)
         b.use_int_sub(int_sub)
+        b.use_cta_walk(cta)
+        assert b.launch_config()["cta_walk"] == cta
         assert b.launch_config()["erode_int_sub"] == int_sub
         singles = [pkg.FastScape_RBP(w, h, params=p, init=pkg.INIT_PHILOX, seed=s)
                    for w, h, p, s in zip(ws, hs, ps, seeds)]
@@ -146,7 +150,8 @@ def test_large_and_small_mixed(pkg):
         compare_with_singles(pkg, b, ws, hs, ps, singles, "mixed")
 
 
-def test_batch_table_growth_in_one_realization(pkg):
+@pytest.mark.parametrize("cta", [False, True])
+def test_batch_table_growth_in_one_realization(pkg, cta):
     """A realization whose drainage counts outgrow its erosion table (a
     valley draining ~W*H cells to one outlet) stops the whole batch's
     timestep before any elevation changes; the host grows that table and
@@ -160,6 +165,7 @@ def test_batch_table_growth_in_one_realization(pkg):
     p = pkg.workload_params()
     ps = [ps0[0], p, ps0[1], ps0[2]]
     with pkg.FastScapeBatch(ws, hs, ps, init=pkg.INIT_PHILOX, seeds=[3, 0, 4, 5]) as b:
+        b.use_cta_walk(cta)
         b.setH(1, hv)
         singles = []
         for r in range(4):
@@ -210,3 +216,36 @@ def test_ragged_ensemble_at_its_own_scale(pkg, oracle):
         assert np.array_equal(b.getH(1), ref)
         for m in singles:
             m.close()
+
+
+@pytest.mark.parametrize("nmode", [1, 2])
+def test_cta_walk_equals_grid_walk_on_deep_levels(pkg, nmode):
+    """Long runs under strong uplift grow hundreds of levels (the regime the
+    per-realization walk is for): both walks give the same receivers, level
+    ids, accumulation and elevation bit for bit after 600 timesteps, with
+    and without the integer subtractions, also for a subset of the batch."""
+    n = 6
+    ws = [96, 128, 64, 128, 80, 112]
+    kw = dict(keq=1e-5, meq=0.6, ueq=5e-3, neq=float(nmode))
+    ps = [pkg.workload_params(**kw) for _ in range(n)]
+    seeds = list(range(30, 30 + n))
+    with pkg.FastScapeBatch(ws, ws, ps, init=pkg.INIT_PHILOX, seeds=seeds) as g, \
+            pkg.FastScapeBatch(ws, ws, ps, init=pkg.INIT_PHILOX, seeds=seeds) as c:
+        c.use_cta_walk(True)
+        c.use_int_sub(True)
+        g.step(600)
+        c.step(600)
+        assert max(g.levels(r)[1] for r in range(n)) > 60
+        for r in range(n):
+            assert np.array_equal(c.receivers(r), g.receivers(r)), r
+            lc, nc = c.levels(r)
+            lg, ng = g.levels(r)
+            assert nc == ng and np.array_equal(lc, lg), r
+            assert np.array_equal(c.accumulation(r), g.accumulation(r)), r
+            assert np.array_equal(c.getH(r), g.getH(r)), r
+        c.set_active([4, 1, 2])
+        g.set_active([4, 1, 2])
+        c.step(5)
+        g.step(5)
+        for r in range(n):
+            assert np.array_equal(c.getH(r), g.getH(r)), r
