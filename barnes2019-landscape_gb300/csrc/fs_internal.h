@@ -184,10 +184,10 @@ const void *accum_kernel_ptr(bool single);              // k_accum
 constexpr int kAccumMaxBps = 4;                         // k_accum's register budget
 cudaError_t prepare_walk_kernels();  // dynamic shared memory limit
 // The per-realization walk (batches of many small realizations): one CTA of
-// cta_threads() threads per realization (blocks CTAs in all, looping over
+// cta_threads(erode) threads per realization (blocks CTAs in all, looping over
 // the realizations); launch_cta_order orders and accumulates,
 // launch_cta_erode uplifts and erodes (skipped on an abort or error).
-int cta_threads();
+int cta_threads(bool erode);
 const void *cta_order_ptr();
 const void *cta_erode_ptr(int nmode, int var);
 cudaError_t launch_cta_order(const StepArgs &a, int blocks, cudaStream_t s);

@@ -1643,9 +1643,10 @@ __global__ void __launch_bounds__(kWalkThreads, 2) k_erode(StepArgs a) {
 //     (fastscape_RB.cpp:285-328 in the level order of fastscape_RB+P.cpp:
 //     319-350), exactly as k_accum's tail and k_erode do.
 // ---------------------------------------------------------------------------
-constexpr int kCtaThreads = 256;
+constexpr int kCtaThreads = 256;       // ordering CTAs (32 registers: 8 per SM)
+constexpr int kCtaErodeThreads = 128;  // erosion CTAs (at most 72 registers: 7 per SM)
 
-__global__ void __launch_bounds__(kCtaThreads) k_cta_order_accum(StepArgs a) {
+__global__ void __launch_bounds__(kCtaThreads, 8) k_cta_order_accum(StepArgs a) {
   Ctl *ctl = a.ctl;
   if (stopped(ctl)) return;
   const int t = threadIdx.x;
@@ -1717,11 +1718,19 @@ __global__ void __launch_bounds__(kCtaThreads) k_cta_order_accum(StepArgs a) {
     for (int Lv = nlev - 1; Lv >= 1; --Lv) {
       const int l0 = Lv <= kLevelCache ? s_lvl[Lv] : __ldcg(&lvl[Lv]);
       const int l1 = Lv + 1 <= kLevelCache ? s_lvl[Lv + 1] : __ldcg(&lvl[Lv + 1]);
-      for (int i = l0 + t; i < l1; i += kCtaThreads) {
+      // two entries per thread load before their pushes (which go one level
+      // down, so they cannot change the counts read here)
+      for (int i = l0 + t; i < l1; i += 2 * kCtaThreads) {
+        const int i2 = i + kCtaThreads;
         const uint32_t v = __ldcg(&acc[i]);
-        atomicAdd(&acc[__ldcg(&par[i])], v);
-        if (a.do_erode && v >= (uint32_t)d.tab_cap) {
-          if (atomicMax(&ctl->abort_k, (int)v) < (int)v) ctl->abort_r = r;
+        const int q = __ldcg(&par[i]);
+        const uint32_t v2 = i2 < l1 ? __ldcg(&acc[i2]) : 0u;
+        const int q2 = i2 < l1 ? __ldcg(&par[i2]) : 0;
+        atomicAdd(&acc[q], v);
+        if (i2 < l1) atomicAdd(&acc[q2], v2);
+        const uint32_t vm = v > v2 ? v : v2;
+        if (a.do_erode && vm >= (uint32_t)d.tab_cap) {
+          if (atomicMax(&ctl->abort_k, (int)vm) < (int)vm) ctl->abort_r = r;
         }
       }
       __syncthreads();  // this level's counts are final before the next reads them
@@ -1729,12 +1738,25 @@ __global__ void __launch_bounds__(kCtaThreads) k_cta_order_accum(StepArgs a) {
   }
 }
 
+// The erosion walk keeps two entries per thread in flight (as k_erode does):
+// the entry after next is loaded and the next one's own elevation gathered
+// while a cell erodes; only the receiver's elevation waits for the level
+// below, and the next level's first entries are loaded before the barrier
+// (a cell's own elevation is written only in its own level). Its CTAs are
+// small so that a batch's realizations walk at once (7 per SM, 1064 on 152
+// SMs): the walk is bound by the latency of each level, hidden across
+// realizations.
 template <int NMODE, int VAR>
-__global__ void __launch_bounds__(kCtaThreads) k_cta_erode(StepArgs a) {
+__global__ void __launch_bounds__(kCtaErodeThreads, 7) k_cta_erode(StepArgs a) {
   constexpr bool ISUB = VAR == 1, GENERIC = VAR == 2;
   Ctl *ctl = a.ctl;
   if (stopped(ctl)) return;  // an error, or a count beyond a table: nothing changes
   const int t = threadIdx.x;
+  struct Entry {
+    int c, dir;
+    uint32_t k;
+    bool ok;
+  };
   for (int r = blockIdx.x; r < a.nreal; r += gridDim.x) {
     const RealDesc d = a.desc[r];
     const int nlev = __ldcg(&a.rctl[r].nlevels);
@@ -1746,20 +1768,39 @@ __global__ void __launch_bounds__(kCtaThreads) k_cta_erode(StepArgs a) {
     const uint64_t udt = (uint64_t)__double_as_longlong(d.u_dt);
     // the pits (level 0 after the rings) are uplifted, not eroded
     const int p1 = __ldcg(&lvl[1]);
-    for (int i = d.nring + t; i < p1; i += kCtaThreads) {
+    for (int i = d.nring + t; i < p1; i += kCtaErodeThreads) {
       const int c = __ldcg(&ent[i]);
       hh[c] = fadd_bits(__ldcg(&hh[c]), udt);
     }
-    __syncthreads();
+    auto load_entry = [&](int i, int hi) -> Entry {
+      Entry e{0, 0, 0u, false};
+      if (i < hi) {
+        e.ok = true;
+        e.c = __ldcg(&ent[i]);
+        e.dir = __ldcg(&pdir[i]);
+        e.k = __ldcg(&acc[i]);
+      }
+      return e;
+    };
+    auto gather_hc = [&](const Entry &e) -> uint64_t { return e.ok ? __ldcg(&hh[e.c]) : 0ull; };
+    auto gather_hn = [&](const Entry &e) -> uint64_t {
+      return e.ok ? __ldcg(&hh[e.c + nbr_off(e.dir & 7, d.W)]) : 0ull;
+    };
+    int lo = p1, hi = nlev > 1 ? __ldcg(&lvl[2]) : p1;
+    Entry e1 = load_entry(lo + t, hi), e2 = load_entry(lo + t + kCtaErodeThreads, hi);
+    uint64_t hc1 = gather_hc(e1);
+    __syncthreads();  // the pits are uplifted
     for (int Lv = 1; Lv < nlev; ++Lv) {
-      const int lo = __ldcg(&lvl[Lv]), hi = __ldcg(&lvl[Lv + 1]);
-      for (int i = lo + t; i < hi; i += kCtaThreads) {
-        const int c = __ldcg(&ent[i]);
-        const int dir = __ldcg(&pdir[i]);
-        const uint32_t k = __ldcg(&acc[i]);
-        const uint64_t h0 = uplift_bits(__ldcg(&hh[c]), udt);
-        const uint64_t hn = __ldcg(&hh[c + nbr_off(dir & 7, d.W)]);
-        const size_t rec_at = (size_t)k * kTabStride + 4 * (dir & 1);
+      uint64_t hn1 = gather_hn(e1);
+      for (int i = lo + t; i < hi; i += kCtaErodeThreads) {
+        const Entry e = e1;
+        const uint64_t hc = hc1, hn = hn1;
+        e1 = e2;
+        e2 = load_entry(i + 2 * kCtaErodeThreads, hi);
+        hc1 = gather_hc(e1);
+        hn1 = gather_hn(e1);
+        const uint64_t h0 = uplift_bits(hc, udt);
+        const size_t rec_at = (size_t)e.k * kTabStride + 4 * (e.dir & 1);
         uint64_t hnew;
         if (NMODE == kNOne && !GENERIC) {
           const unsigned long long *Tb = reinterpret_cast<const unsigned long long *>(d.tab) + rec_at;
@@ -1774,7 +1815,14 @@ __global__ void __launch_bounds__(kCtaThreads) k_cta_erode(StepArgs a) {
         }
         if (((hnew >> 52) & 0x7FF) == 0x7FF)  // Inf or NaN
           raise_err(ctl, FS_ERR_NONFINITE, kPhaseErode);
-        hh[c] = hnew;
+        hh[e.c] = hnew;
+      }
+      if (Lv + 1 < nlev) {  // the next level's first entries
+        lo = hi;
+        hi = __ldcg(&lvl[Lv + 2]);
+        e1 = load_entry(lo + t, hi);
+        e2 = load_entry(lo + t + kCtaErodeThreads, hi);
+        hc1 = gather_hc(e1);
       }
       __syncthreads();  // this level's elevations are final before the next reads them
     }
@@ -2148,7 +2196,7 @@ const void *cta_erode_ptr(int nmode, int var) {
   }
 }
 
-int cta_threads() { return kCtaThreads; }
+int cta_threads(bool erode) { return erode ? kCtaErodeThreads : kCtaThreads; }
 
 const void *cta_order_ptr() { return reinterpret_cast<const void *>(&k_cta_order_accum); }
 
@@ -2161,7 +2209,7 @@ cudaError_t launch_cta_erode(const StepArgs &a, int blocks, cudaStream_t s) {
   StepArgs args = a;
   void *params[] = {&args};
   const int var = a.erode_generic ? 2 : a.erode_isub ? 1 : 0;
-  return cudaLaunchKernel(cta_erode_ptr(a.nmode, var), dim3(blocks), dim3(kCtaThreads), params, 0,
+  return cudaLaunchKernel(cta_erode_ptr(a.nmode, var), dim3(blocks), dim3(kCtaErodeThreads), params, 0,
                           s);
 }
 

@@ -865,12 +865,12 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
   b->walk_occ = occ;
   b->walk_bps = std::min(occ, 2);
   if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->cta_occ_order, fs::cta_order_ptr(),
-                                                        fs::cta_threads(), 0),
+                                                        fs::cta_threads(false), 0),
           "occupancy"))
     return fail(*status);
   for (int v = 0; v < 3; v++)
     if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &b->cta_occ_erode[v], fs::cta_erode_ptr(b->nmode, v), fs::cta_threads(), 0),
+                &b->cta_occ_erode[v], fs::cta_erode_ptr(b->nmode, v), fs::cta_threads(true), 0),
             "occupancy"))
       return fail(*status);
   // k_order: the variant with 3 blocks per SM where all three fit (a large

@@ -368,7 +368,8 @@ def ensemble_spec(pkg, n: int, seed: int = 2019, side: int = 0):
     return [int(s) for s in sides], params
 
 
-def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local, walk="auto"):
+def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local, walk="auto",
+                    int_sub="auto"):
     """Batched ensemble: realizations/s of nsteps-timestep runs from the
     initial fields (the launch shape the autotuner picks, CUDA events around
     the whole run on the batch's stream), then the same run once more from
@@ -382,7 +383,9 @@ def ensemble_result(pkg, n, side, nsteps, seed, rank, ws, dist, local, walk="aut
     tune = b.autotune(probe_steps=2)
     if walk != "auto":
         b.use_cta_walk(walk == "cta")
-        tune = b.launch_config()
+    if int_sub != "auto":
+        b.use_int_sub(int_sub == "1")
+    tune = b.launch_config()
     b.set_timing(pkg.TIMING_CALL)
     b.phase_times(reset=True)
     b.synchronize()
@@ -444,7 +447,8 @@ def run_ensemble(args, dist, rank, ws, local):
     if ws > 1:
         torch.cuda.set_device(local)
     res = ensemble_result(pkg, args.realizations, args.ensemble_side, args.ensemble_steps,
-                          2019 + rank, rank, ws, dist, local, walk=args.walk)
+                          2019 + rank, rank, ws, dist, local, walk=args.walk,
+                          int_sub=args.int_sub)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if dist is not None:
@@ -882,6 +886,8 @@ def main():
     ap.add_argument("--sizes", default="", help="sweep: comma-separated grid edges")
     ap.add_argument("--walk", default="auto", choices=["auto", "grid", "cta"],
                     help="ensemble: level walk (auto: the library's choice)")
+    ap.add_argument("--int-sub", default="auto", choices=["auto", "0", "1"],
+                    help="ensemble: erosion subtractions in integer arithmetic")
     ap.add_argument("--sg-traj", type=int, default=2000,
                     help="surrogate: realizations generating training data")
     ap.add_argument("--sg-per", type=int, default=10, help="surrogate: samples per realization")
