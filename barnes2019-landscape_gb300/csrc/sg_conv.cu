@@ -22,10 +22,12 @@
 //   range is split across CTAs; each adds its FP32 partial sums with
 //   reductions into dW.
 //
-// Warp roles (128 threads): warp 0 lane 0 issues the TMA loads into a ring
-// of stages (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees
-// each stage with tcgen05.commit, and all four warps run the epilogue, warp w
-// reading TMEM lanes 32w..32w+31 (its pixels, or its (tap, ci) rows). Every
+// Warp roles: warp 0 lane 0 issues the TMA loads into a ring of stages
+// (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees each stage
+// with tcgen05.commit, and the epilogue warps that follow (eight for the
+// forward / data-gradient kernels, four for the weight gradient) read the
+// accumulator back, warp w from TMEM lanes 32*(w%4)..+31 (its pixels, or its
+// (tap, ci) rows); two warps of one lane quarter split the columns. Every
 // mbarrier wait is bounded (1 s of the global timer): on expiry the CTA sets
 // the error word, stops issuing, waits (again bounded) for its own copies
 // and MMAs in flight, frees its TMEM and returns.

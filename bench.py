@@ -612,6 +612,64 @@ def run_surrogate(args, dist, rank, ws, local):
         dist.destroy_process_group()
 
 
+def training_speed(pkg, batch, steps, local, peak_b, peak_s, peak_kind, seed=1):
+    """The surrogate's training throughput at 512^2 and `batch` (Adam, on
+    2*batch samples the plain method generates on the device over 0..200
+    timesteps; three warm-up steps, then `steps` timed with CUDA events on the
+    network's stream) and one forward pass over a batch (five passes after a
+    warm-up). Returns (the network, the result dict)."""
+    net = pkg.Surrogate(512, 512, base_channels=32, batch=batch, jump=50, seed=seed)
+    net.reserve(2 * batch)
+    net.generate(batch, 2, 200, seed=7)
+    net.train(3, lr=1e-4)                      # warm-up steps
+    with Clocks(local) as clk:
+        net.train(steps, lr=1e-4)
+    ms, flops = net.train_stats()
+    tf = flops * steps / (ms * 1e-3) / 1e12
+    fwd_ms, fwd_flops = net.time_forward(reps=5)
+    fwd_tf = fwd_flops / (fwd_ms * 1e-3) / 1e12
+    res = {
+        "metric": f"surrogate training samples/s (512^2, batch {batch}, BF16 tcgen05, Adam)",
+        "value": batch * steps / (ms * 1e-3), "unit": "samples/s", "steps": steps, "warmup": 3,
+        "ms_per_step": ms / steps, "conv_tflops_per_step": flops / 1e12,
+        "roofline": {"bound": "tensor", "kernel": "training step (14 convolutions forward, "
+                                                   "data and weight gradients, and the rest)",
+                     "achieved": tf, "peak": peak_s, "unit": "TFLOP/s", "frac": tf / peak_s,
+                     "peak_source": f"{peak_kind} bf16_tflops_sustained"},
+        "forward_pass": {"ms": fwd_ms, "flops": fwd_flops, "achieved_tflops": fwd_tf,
+                         "peak": peak_b, "frac": fwd_tf / peak_b,
+                         "peak_source": f"{peak_kind} bf16_tflops (burst)"},
+        "data": f"{2 * batch} samples of 512^2 the plain method generated on the device "
+                "(0..200 timesteps); the full 20000-sample run is --workload surrogate",
+        "clocks": clk.summary()}
+    return net, res
+
+
+def run_conv(args, dist, rank, ws, local):
+    """The surrogate's tensor-core convolutions alone: training throughput and
+    one forward pass at 512^2, --sg-batch samples (no ensemble, no long
+    training; a case small enough for a profiler capture at --sg-batch 8)."""
+    import __graft_entry__ as ge
+    import torch  # noqa: F401
+    pkg = ge.load()
+    if ws > 1:
+        torch.cuda.set_device(local)
+    peak_b, peak_s, peak_kind = load_bf16_peak()
+    net, res = training_speed(pkg, args.sg_batch, args.sg_bench_steps, local, peak_b, peak_s,
+                              peak_kind, seed=1 + rank)
+    net.close()
+    line = dict(res)
+    line.update({"n_gpus": ws, "higher_is_better": True, "scaling": "weak",
+                 "vs_baseline": None, "dtype": "bf16",
+                 "config": {"workload": f"surrogate convolutions, 512^2, batch {args.sg_batch}, "
+                                        "c 32 (1.95M parameters)",
+                            "l2": "inputs larger than L2 (activations of one pass)"}})
+    line["ms_per_step"] = max_over_ranks(dist, line["ms_per_step"])
+    line["value"] = ws * args.sg_batch / (line["ms_per_step"] * 1e-3)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def surrogate_extras(pkg, args, local):
     """Configs 3 and 4 for the default run: the surrogate's training
     throughput (512^2, batch 32, Adam, on samples the plain method generates
@@ -620,31 +678,8 @@ def surrogate_extras(pkg, args, local):
     the committed trained parameters (SG_WEIGHTS)."""
     peak_b, peak_s, peak_kind = load_bf16_peak()
     out = {}
-    net = pkg.Surrogate(512, 512, base_channels=32, batch=32, jump=50, seed=1)
-    net.reserve(64)
-    net.generate(32, 2, 200, seed=7)
-    net.train(3, lr=1e-4)                      # warm-up steps
-    steps = args.sg_bench_steps
-    with Clocks(local) as clk:
-        net.train(steps, lr=1e-4)
-    ms, flops = net.train_stats()
-    tf = flops * steps / (ms * 1e-3) / 1e12
-    fwd_ms, fwd_flops = net.time_forward(reps=5)
-    fwd_tf = fwd_flops / (fwd_ms * 1e-3) / 1e12
-    out["training"] = {
-        "metric": "surrogate training samples/s (512^2, batch 32, BF16 tcgen05, Adam)",
-        "value": 32 * steps / (ms * 1e-3), "unit": "samples/s", "steps": steps, "warmup": 3,
-        "ms_per_step": ms / steps, "conv_tflops_per_step": flops / 1e12,
-        "roofline": {"bound": "tensor", "kernel": "training step (14 convolutions forward, "
-                                                   "data and weight gradients, and the rest)",
-                     "achieved": tf, "peak": peak_s, "unit": "TFLOP/s", "frac": tf / peak_s,
-                     "peak_source": f"{peak_kind} bf16_tflops_sustained"},
-        "forward_pass": {"ms": fwd_ms, "achieved_tflops": fwd_tf, "peak": peak_b,
-                         "frac": fwd_tf / peak_b,
-                         "peak_source": f"{peak_kind} bf16_tflops (burst)"},
-        "data": "64 samples of 512^2 the plain method generated on the device "
-                "(0..200 timesteps); the full 20000-sample run is --workload surrogate",
-        "clocks": clk.summary()}
+    net, out["training"] = training_speed(pkg, 32, args.sg_bench_steps, local, peak_b, peak_s,
+                                          peak_kind)
     if SG_WEIGHTS.exists():
         net.load(SG_WEIGHTS)
         ens = surrogate_ensemble(pkg, net, args.sg_realizations, 512, args.sg_ensemble_steps,
@@ -870,12 +905,14 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="grid",
-                    choices=["grid", "ensemble", "sweep", "deep", "refconst", "surrogate"],
+                    choices=["grid", "ensemble", "sweep", "deep", "refconst", "surrogate",
+                             "conv"],
                     help="grid: the 10000^2 timestep (default); ensemble: the ragged "
                          "256-realization batch; sweep: grid sizes 100..20000; deep: a "
                          "512^2 grid after 2000 timesteps of strong erosion (~290 levels); "
                          "refconst: the 10000^2 timestep with the reference's own "
-                         "constants (n 2)")
+                         "constants (n 2); surrogate: generation, training and the judged "
+                         "ensemble; conv: the surrogate's convolutions alone")
     ap.add_argument("--realizations", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=ENSEMBLE_STEPS,
                     help="ensemble: timesteps of the timed run (the metric's run length)")
@@ -898,7 +935,8 @@ def main():
     ap.add_argument("--sg-judge", type=float, default=0.05)
     ap.add_argument("--sg-save", default="", help="surrogate: write the trained parameters here")
     ap.add_argument("--sg-bench-steps", type=int, default=20,
-                    help="default run: timed surrogate training steps")
+                    help="default run and conv: timed surrogate training steps")
+    ap.add_argument("--sg-batch", type=int, default=32, help="conv: samples per batch")
     ap.add_argument("--sg-realizations", type=int, default=1024,
                     help="default run: realizations of the surrogate ensemble")
     ap.add_argument("--sg-ensemble-steps", type=int, default=2000,
@@ -930,6 +968,9 @@ def main():
         return
     if args.workload == "surrogate":
         run_surrogate(args, dist, rank, ws, local)
+        return
+    if args.workload == "conv":
+        run_conv(args, dist, rank, ws, local)
         return
 
     import __graft_entry__ as ge

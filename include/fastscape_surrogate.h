@@ -13,9 +13,13 @@
  * nearest-neighbour upsampling concatenated with the encoder's output of the
  * same level on the way up, and a 1x1 output head. Inputs are 16 planes: the
  * elevation divided by s = max(max h, u), log(s/u)/4, K, m and U mapped to
- * about [-1, 1], and the ring mask; u = jump*U*dt is the uplift of one jump.
- * It predicts y = (h_{t+jump} - h_t)/u on interior cells; rings never
- * change. Activations and weights are BF16, products accumulate in FP32 on
+ * about [-1, 1], the ring mask, log2 of the drainage count / 16 (from an
+ * erosion-free analysis of the field: receivers, ordering, accumulation),
+ * and on cells with a full neighbourhood the drop to the D8 receiver, the
+ * central differences along x and y (times 1/2) and h minus 1/8 of the sum
+ * of its 8 neighbours, each divided by u; the last five planes are zero.
+ * u = jump*U*dt is the uplift of one jump. It predicts
+ * y = (h_{t+jump} - h_t)/u on interior cells; rings never change. Activations and weights are BF16, products accumulate in FP32 on
  * the tensor cores (tcgen05), the master weights and Adam's moments are
  * FP32. Training minimises the mean over samples of
  *   (u / relief_{t+jump})^2 * mean over interior cells of (y_pred - y)^2,
