@@ -4,6 +4,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "fastscape_gb300.h"
 #include "fastscape_gb300_testing.h"
@@ -22,6 +23,25 @@ int cuda_fail(cudaError_t e, const char *what) {
   char buf[256];
   std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
   return fs::record_error(FS_ERR_CUDA, buf);
+}
+
+// NHWC host tensors <-> the device's plane-major layout [B][C/8][H][W][8].
+std::vector<uint16_t> to_planes(const uint16_t *x, long long pix_img, int B, int C) {
+  std::vector<uint16_t> o(static_cast<size_t>(pix_img) * B * C);
+  for (int b = 0; b < B; b++)
+    for (long long p = 0; p < pix_img; p++)
+      for (int c = 0; c < C; c++)
+        o[static_cast<size_t>(sg::plane_at(b, c / 8, p, C / 8, pix_img) + c % 8)] =
+            x[(static_cast<size_t>(b) * pix_img + p) * C + c];
+  return o;
+}
+
+void from_planes(const uint16_t *x, long long pix_img, int B, int C, uint16_t *o) {
+  for (int b = 0; b < B; b++)
+    for (long long p = 0; p < pix_img; p++)
+      for (int c = 0; c < C; c++)
+        o[(static_cast<size_t>(b) * pix_img + p) * C + c] =
+            x[static_cast<size_t>(sg::plane_at(b, c / 8, p, C / 8, pix_img) + c % 8)];
 }
 
 // Device buffers of one test call, released on every path.
@@ -50,7 +70,7 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
   if (B < 1 || H < 1 || W < 1 || cin < 16 || cout < 16 || cin % 16 || cout % 16 ||
       (taps != 1 && taps != 9) || !x || !w || !out)
     return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: bad shape or NULL buffer%s", "");
-  const long long pix = static_cast<long long>(B) * H * W;
+  const long long pix = static_cast<long long>(B) * H * W, hw = static_cast<long long>(H) * W;
   const size_t nw = static_cast<size_t>(cout) * taps * cin;
   Bufs bufs;
   sg::bf16 *dx = nullptr, *dw = nullptr, *dwd = nullptr, *dmask = nullptr, *dout = nullptr;
@@ -65,13 +85,14 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
     if (e == cudaSuccess) e = bufs.alloc(&dw, nw * 2);
     if (e == cudaSuccess) e = bufs.alloc(&dout, pix * cout * 2);
     if (e == cudaSuccess && bias) e = bufs.alloc(&dbias, cout * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dx, to_planes(x, hw, B, cin).data(), pix * cin * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dw, w, nw * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && bias) e = cudaMemcpy(dbias, bias, cout * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
     sg::Act src{dx, B, H, W, cin};
     sg::ConvPlan plan;
-    e = sg::plan_conv(plan, src, dw, taps, cout, dbias, relu, nullptr, 0, dout, cout, &why);
+    e = sg::plan_conv(plan, src, dw, taps, cout, dbias, relu, nullptr, dout, &why);
     if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
     e = sg::launch_conv(plan, derr, s);
   } else if (mode == 1) {
@@ -80,22 +101,27 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
     if (e == cudaSuccess) e = bufs.alloc(&dwd, nw * 2);
     if (e == cudaSuccess) e = bufs.alloc(&dout, pix * cin * 2);
     if (e == cudaSuccess && mask) e = bufs.alloc(&dmask, pix * cin * 2);
-    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cout * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dx, to_planes(x, hw, B, cout).data(), pix * cout * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dw, w, nw * 2, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && mask) e = cudaMemcpy(dmask, mask, pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && mask)
+      e = cudaMemcpy(dmask, to_planes(mask, hw, B, cin).data(), pix * cin * 2,
+                     cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = sg::launch_flip_weights(dw, dwd, cout, cin, taps, s);
     if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
     sg::Act src{dx, B, H, W, cout};
     sg::ConvPlan plan;
-    e = sg::plan_conv(plan, src, dwd, taps, cin, nullptr, 0, dmask, cin, dout, cin, &why);
+    e = sg::plan_conv(plan, src, dwd, taps, cin, nullptr, 0, dmask, dout, &why);
     if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
     e = sg::launch_conv(plan, derr, s);
   } else {
     if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cin * 2);
     if (e == cudaSuccess) e = bufs.alloc(&dw, pix * cout * 2);
     if (e == cudaSuccess) e = bufs.alloc(&dgw, nw * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemcpy(dx, x, pix * cin * 2, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dw, w, pix * cout * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dx, to_planes(x, hw, B, cin).data(), pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dw, to_planes(w, hw, B, cout).data(), pix * cout * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(dgw, 0, nw * sizeof(float));
     if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
     sg::Act xa{dx, B, H, W, cin}, ya{dw, B, H, W, cout};
@@ -112,9 +138,14 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
   e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: status");
   if (herr) return sg_fail(FS_ERR_TIMEOUT, "fs_test_sg_conv: a pipeline wait ran out%s", "");
-  if (mode == 0) e = cudaMemcpy(out, dout, pix * cout * 2, cudaMemcpyDeviceToHost);
-  else if (mode == 1) e = cudaMemcpy(out, dout, pix * cin * 2, cudaMemcpyDeviceToHost);
-  else e = cudaMemcpy(out, dgw, nw * sizeof(float), cudaMemcpyDeviceToHost);
+  if (mode == 2) {
+    e = cudaMemcpy(out, dgw, nw * sizeof(float), cudaMemcpyDeviceToHost);
+  } else {
+    const int co = mode == 0 ? cout : cin;
+    std::vector<uint16_t> t(static_cast<size_t>(pix) * co);
+    e = cudaMemcpy(t.data(), dout, pix * co * 2, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) from_planes(t.data(), hw, B, co, static_cast<uint16_t *>(out));
+  }
   if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: copy back");
   return FS_OK;
 }

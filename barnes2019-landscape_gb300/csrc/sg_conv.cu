@@ -1,5 +1,6 @@
 // sg_conv.cu -- the surrogate's dense contraction: 3x3 (and 1x1)
-// convolutions over NHWC BF16 tensors as implicit GEMMs on the 5th-generation
+// convolutions over plane-major BF16 tensors ([B][C/8][H][W][8], 16 bytes
+// per pixel per plane) as implicit GEMMs on the 5th-generation
 // tensor cores (tcgen05.mma kind::f16, BF16 x BF16 -> FP32), operands staged
 // in shared memory by TMA (cp.async.bulk.tensor), accumulators in tensor
 // memory (TMEM), read back with tcgen05.ld for a fused epilogue. No library
@@ -9,25 +10,32 @@
 // channels of A[p + off(tap)][ci] * Bw[n][tap*cin + ci].
 //   M = 128 pixels of one image (BW x BH, BW = min(W,128)), N = output
 //   channels of the tile (<= 256), K = taps * cin in blocks of cb channels.
-//   A block is one TMA load of a {cb, BW, BH, 1} box at the tap's offset:
-//   coordinates outside the image read zeros, which is the convolution's
-//   zero padding. Both operands are K-major with the box's swizzle (32-, 64-
-//   or 128-byte rows). The data gradient is the same kernel on the output
-//   gradient with flipped, transposed weights (launch_flip_weights).
+//   A block is one TMA load of cb/8 planes of the BW x BH pixels at the
+//   tap's offset: coordinates outside the image read zeros, which is the
+//   convolution's zero padding. The tensor maps view a plane row as 2*W
+//   64-bit elements, so one box row is a whole 128-pixel row of a plane
+//   (2048 bytes: the TMA engine issues requests per box row, and rows of a
+//   plane of 8 channels alone would be 16 bytes each). A is K-major without swizzle (8 pixels of a
+//   plane = one 128-byte core matrix, planes = K chunks), the weights
+//   K-major with the box's swizzle (32-, 64- or 128-byte rows). The data
+//   gradient is the same kernel on the output gradient with flipped,
+//   transposed weights (launch_flip_weights).
 // Weight gradient (k_wgrad): dW^T[(tap,ci)][co] = sum over pixels p of
 //   X[p + off(tap)][ci] * dY[p][co]. K = pixels (128 per step), both operands
-//   MN-major (channels contiguous in the NHWC boxes). The 128 M rows are
-//   chunks of (tap, channel block) stacked in shared memory at a fixed
-//   stride, so a 32-channel layer fills a tile with four taps. The pixel
+//   MN-major without swizzle (8 channels of 8 pixels = one core matrix,
+//   planes 2048 bytes apart). The 128 M rows are chunks of (tap, channel
+//   block) stacked in shared memory plane after plane, so a 32-channel layer
+//   fills a tile with four taps. The pixel
 //   range is split across CTAs; each adds its FP32 partial sums with
 //   reductions into dW.
 //
 // Warp roles: warp 0 lane 0 issues the TMA loads into a ring of stages
 // (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees each stage
 // with tcgen05.commit, and the epilogue warps that follow (eight for the
-// forward / data-gradient kernels, four for the weight gradient) read the
-// accumulator back, warp w from TMEM lanes 32*(w%4)..+31 (its pixels, or its
-// (tap, ci) rows); two warps of one lane quarter split the columns. Every
+// forward / data-gradient kernels, in two groups of four that take
+// alternate tiles; four for the weight gradient) read the accumulator back,
+// warp w from TMEM lanes 32*(w%4)..+31 (its pixels, or its (tap, ci) rows).
+// Every
 // mbarrier wait is bounded (1 s of the global timer): on expiry the CTA sets
 // the error word, stops issuing, waits (again bounded) for its own copies
 // and MMAs in flight, frees its TMEM and returns.
@@ -47,7 +55,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kM = 128;                             // rows of every MMA tile
 constexpr int kKPix = 128;                          // pixels per weight-gradient step
-constexpr int kMaxStages = 8;
+constexpr int kMaxStages = 16;
 constexpr int kMaxBias = 512;                       // biased outputs of a forward conv
 constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
 constexpr size_t kPlanarSmem = 222 * 1024;          // planar form: weights + ring + guard (+ static)
@@ -67,12 +75,6 @@ __device__ __forceinline__ unsigned long long gtimer() {
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
-               "r"(bytes)
-               : "memory");
 }
 
 __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
@@ -102,22 +104,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   }
 }
 
-__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar,
-                                            int c0, int c1, int c2, int c3) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(su32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
-      : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
-                                            int c0, int c1) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4}], [%2];" ::"r"(su32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1)
-      : "memory");
+// mbar_wait for a whole warp: true only if every lane saw the phase.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                               bool watch_abort) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity, abort, watch_abort));
 }
 
 __device__ __forceinline__ void tma_prefetch(const CUtensorMap *map) {
@@ -148,22 +138,55 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, BF16 inputs, FP32 accumulation.
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t idesc, uint32_t accumulate) {
+// The producer and MMA warps run their loops with every lane (the same,
+// warp-uniform coordinates and descriptors); one lane, chosen by elect.sync
+// inside the same statement, issues each TMA copy, MMA and commit.
+// umma_bf16_el: D[tmem] (+)= A[smem] * B[smem]^T, BF16 inputs, FP32
+// accumulation; umma_commit_el: the mbarrier receives one arrival once every
+// MMA issued before has completed.
+__device__ __forceinline__ void mbar_expect_tx_el(uint64_t *bar, uint32_t bytes) {
   asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\t"
+      "@p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n\t}" ::"r"(su32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d_el(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                               int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\t"
+      "@p cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];\n\t}" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d_el(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                               int c0, int c1) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\t"
+      "@p cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];\n\t}" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(su32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_bf16_el(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                             uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "elect.sync _|p, 0xffffffff;\n\t"
+      "setp.ne.b32 q, %4, 0;\n\t"
+      "@p tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n\t}" ::"r"(d_tmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 
-// The mbarrier receives one arrival once every MMA this thread issued before
-// has completed.
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+__device__ __forceinline__ void umma_commit_el(uint64_t *bar) {
   asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+      "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\t"
+      "@p tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(
           su32(bar))
       : "memory");
 }
@@ -229,10 +252,9 @@ struct ConvArgs {
   int mtiles, ntiles;  // tiles of 128 pixels, and of bn output channels
   const float *bias;
   int relu;
-  const bf16 *mask;
-  int ldm;
+  const bf16 *mask;   // ntot channels, plane-major like out
   bf16 *out;
-  int ldo;
+  int oplanes;        // planes per image of out and mask (ntot / 8)
   int *err;
 };
 
@@ -241,12 +263,24 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps
+constexpr int kMaxAccBufs = 4;      // accumulator buffers of a forward / data-gradient CTA
+
+// Accumulator columns of an N tile and the buffers TMEM's 512 columns hold:
+// the MMAs of the next tiles run while the epilogue drains earlier ones.
+__host__ __device__ constexpr uint32_t acc_cols(int bn) {
+  return bn <= 32 ? 32 : bn <= 64 ? 64 : bn <= 128 ? 128 : 256;
+}
+__host__ __device__ constexpr int acc_bufs(int bn) {
+  return static_cast<int>(512 / acc_cols(bn)) < kMaxAccBufs ? static_cast<int>(512 / acc_cols(bn))
+                                                            : kMaxAccBufs;
+}
 constexpr int kWgradThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
 
 // One 16-column chunk of a tile row: + bias (shared memory), ReLU, zeroed
-// where the mask is not positive, rounded to BF16, stored (32 bytes).
+// where the mask is not positive, rounded to BF16, stored as 16 bytes in
+// each of two planes (ps elements apart).
 __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, int relu,
-                                      const bf16 *msk, bf16 *out) {
+                                      const bf16 *msk, bf16 *out, long long ps) {
   float f[16];
 #pragma unroll
   for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
@@ -260,7 +294,7 @@ __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, 
   }
   if (msk) {
     const uint4 m0 = *reinterpret_cast<const uint4 *>(msk);
-    const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + 8);
+    const uint4 m1 = *reinterpret_cast<const uint4 *>(msk + ps);
     const bf16 *mb0 = reinterpret_cast<const bf16 *>(&m0);
     const bf16 *mb1 = reinterpret_cast<const bf16 *>(&m1);
 #pragma unroll
@@ -279,42 +313,48 @@ __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, 
   o1.z = pack_bf16(f[12], f[13]);
   o1.w = pack_bf16(f[14], f[15]);
   *reinterpret_cast<uint4 *>(out) = o0;
-  *reinterpret_cast<uint4 *>(out + 8) = o1;
+  *reinterpret_cast<uint4 *>(out + ps) = o1;
 }
 
 // Columns [c_lo, c_hi) of this warp's 32 TMEM lanes (d: lane quarter and
-// accumulator base), two 16-column loads in flight per wait.
+// accumulator base), two 16-column loads in flight per wait; out and msk
+// point at this lane's pixel in the plane of column 0, planes ps elements
+// apart.
 __device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, const float *sb,
-                                            int relu, const bf16 *msk, bf16 *out) {
+                                            int relu, const bf16 *msk, bf16 *out, long long ps) {
   int c = c_lo;
   for (; c + 32 <= c_hi; c += 32) {
     uint32_t v0[16], v1[16];
     tmem_ld16(d + c, v0);
     tmem_ld16(d + c + 16, v1);
     tmem_ld_wait();
-    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + c : nullptr, out + c);
-    epi16(v1, sb ? sb + c + 16 : nullptr, relu, msk ? msk + c + 16 : nullptr, out + c + 16);
+    const long long o0 = (c / 8) * ps, o1 = ((c + 16) / 8) * ps;
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps);
+    epi16(v1, sb ? sb + c + 16 : nullptr, relu, msk ? msk + o1 : nullptr, out + o1, ps);
   }
   if (c < c_hi) {
     uint32_t v0[16];
     tmem_ld16(d + c, v0);
     tmem_ld_wait();
-    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + c : nullptr, out + c);
+    const long long o0 = (c / 8) * ps;
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps);
   }
 }
 
 // ------------------------------------------------------ forward / dgrad ----
 // Persistent: CTA b takes tiles b, b + gridDim.x, ... (pixel tile major, N
-// tile minor). The stage ring runs on across tiles; the accumulator is
-// double-buffered in TMEM (acc_full: MMAs of a tile done; acc_empty: its
-// epilogue has read it), so the epilogue of one tile overlaps the MMAs of the
-// next.
+// tile minor). The stage ring runs on across tiles; the accumulator has up
+// to four buffers in TMEM (acc_full: MMAs of a tile done; acc_empty: its
+// epilogue has read it), and the epilogue warps form two groups of four
+// that drain alternate tiles, so the epilogues of two tiles overlap each
+// other and the MMAs of the next ones.
 template <int CB>
 __global__ void __launch_bounds__(kConvThreads, 1)
     k_conv(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
            const ConvArgs a) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[kMaxAccBufs],
+      acc_empty[kMaxAccBufs], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   __shared__ float s_bias[kMaxBias];
@@ -322,22 +362,24 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     for (int i = threadIdx.x; i < a.bn * a.ntiles; i += blockDim.x) s_bias[i] = a.bias[i];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  constexpr int kRow = CB * 2;  // bytes per operand row (the swizzle span)
+  constexpr int kRow = CB * 2;      // bytes per weight row (the swizzle span)
+  constexpr int kAPlane = kM * 16;  // one plane of the A tile: 128 pixels x 8 channels
   const int a_bytes = kM * kRow;
   const int b_bytes = a.bn * kRow;
   const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t cols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
+  const uint32_t cols = acc_cols(a.bn);
+  const int nbuf = acc_bufs(a.bn);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < nbuf; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], kConvThreads - 64);
+      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
     }
     mbar_init(&done, 1);
     abort_flag = 0;
@@ -347,7 +389,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     tma_prefetch(&tmb);
   }
   if (warp == 0) {
-    tmem_alloc(&tmem_slot, 2 * cols);
+    tmem_alloc(&tmem_slot, nbuf * cols);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -361,86 +403,82 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   const int ntot_tiles = a.mtiles * a.ntiles;
 
   if (warp == 0) {
-    if (lane == 0) {
-      // producer
-      int kbg = 0;
-      bool stop = false;
-      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
-        const int mt = t / a.ntiles, nt = t - mt * a.ntiles;
-        const int b = mt / tiles_img;
-        const int tt = mt - b * tiles_img;
-        const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
-        const int n0 = nt * a.bn;
-        for (int kb = 0; kb < nkb; kb++, kbg++) {
-          const int s = kbg % S;
-          if (!mbar_wait(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
-            sg_raise(a.err, &abort_flag, kSgTimeout);
-            stop = true;
-            break;
-          }
-          const int tap = kb / kch, cc = kb - tap * kch;
-          const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
-          unsigned char *sa = smem + s * stage_bytes;
-          mbar_expect_tx(&full[s], a_bytes + b_bytes);
-          tma_load_4d(sa, &tma, &full[s], cc * CB, x0 + dx, y0 + dy, b);
-          tma_load_2d(sa + a_bytes, &tmb, &full[s], tap * a.cin + cc * CB, n0);
-        }
-      }
-      // leave no copy in flight into this CTA's shared memory
-      for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
-        if (!mbar_wait(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+    // producer (the whole warp; one lane issues)
+    int kbg = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
+      const int mt = t / a.ntiles, nt = t - mt * a.ntiles;
+      const int b = mt / tiles_img;
+      const int tt = mt - b * tiles_img;
+      const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
+      const int n0 = nt * a.bn;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int s = kbg % S;
+        if (!mbar_wait_warp(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
           sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
           break;
         }
+        const int tap = kb / kch, cc = kb - tap * kch;
+        const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+        unsigned char *sa = smem + s * stage_bytes;
+        mbar_expect_tx_el(&full[s], a_bytes + b_bytes);
+        tma_load_4d_el(sa, &tma, &full[s], 2 * (x0 + dx), y0 + dy, cc * (CB / 8), b);
+        tma_load_2d_el(sa + a_bytes, &tmb, &full[s], tap * a.cin + cc * CB, n0);
+      }
     }
+    // leave no copy in flight into this CTA's shared memory
+    for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
+      if (!mbar_wait_warp(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
   } else if (warp == 1) {
-    if (lane == 0) {
-      // MMA issuer
-      const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
-      int kbg = 0, it = 0;
-      bool stop = false;
-      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
-        const int buf = it & 1;
-        if (!mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, &abort_flag, true)) {
+    // MMA issuer (the whole warp; one lane issues)
+    const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
+    int kbg = 0, it = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
+      const int buf = it % nbuf;
+      if (!mbar_wait_warp(&acc_empty[buf], ((it / nbuf) & 1) ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + buf * cols;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int s = kbg % S;
+        if (!mbar_wait_warp(&full[s], (kbg / S) & 1, &abort_flag, true)) {
           sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
           break;
         }
         tc_fence_after();
-        const uint32_t d = tmem + buf * cols;
-        for (int kb = 0; kb < nkb; kb++, kbg++) {
-          const int s = kbg % S;
-          if (!mbar_wait(&full[s], (kbg / S) & 1, &abort_flag, true)) {
-            sg_raise(a.err, &abort_flag, kSgTimeout);
-            stop = true;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t sa = su32(smem + s * stage_bytes);
-          const uint64_t da = smem_desc(sa, 16, 8 * kRow, swizzle_code(kRow));
-          const uint64_t db = smem_desc(sa + a_bytes, 16, 8 * kRow, swizzle_code(kRow));
+        const uint32_t sa = su32(smem + s * stage_bytes);
+        // A: K-major, no swizzle: K chunks (planes) kAPlane apart, 8-row
+        // groups 128 bytes apart; B: K-major, swizzled rows of kRow bytes
+        const uint64_t da = smem_desc(sa, kAPlane, 128, 0);
+        const uint64_t db = smem_desc(sa + a_bytes, 16, 8 * kRow, swizzle_code(kRow));
 #pragma unroll
-          for (int k = 0; k < CB / 16; k++)  // K = 16 per MMA: 32 bytes along the row
-            umma_bf16(d, da + 2 * k, db + 2 * k, idesc, (kb | k) != 0);
-          umma_commit(&empty[s]);
-        }
-        if (!stop) umma_commit(&acc_full[buf]);
+        for (int k = 0; k < CB / 16; k++)  // K = 16 per MMA: two planes of A, 32 bytes of B
+          umma_bf16_el(d, da + ((2 * k * kAPlane) >> 4), db + 2 * k, idesc, (kb | k) != 0);
+        umma_commit_el(&empty[s]);
       }
-      // every MMA this thread issued has completed before the teardown
-      umma_commit(&done);
-      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+      if (!stop) umma_commit_el(&acc_full[buf]);
     }
+    // every MMA this warp issued has completed before the teardown
+    umma_commit_el(&done);
+    if (!mbar_wait_warp(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (one pixel each);
-    // the two warps of a lane quarter split the columns
+    // group (w-2)/4 takes every other tile of this CTA
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
+    const int grp = (warp - 2) >> 2;
     const int r = q * 32 + lane;
-    const int csplit = a.bn % 32 == 0 ? a.bn / 2 : a.bn;
-    const int c_lo = half ? csplit : 0, c_hi = half ? a.bn : csplit;
-    int it = 0;
-    for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
-      const int buf = it & 1;
-      if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
+    for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
+         t += 2 * gridDim.x, it += 2) {
+      const int buf = it % nbuf;
+      if (!mbar_wait(&acc_full[buf], (it / nbuf) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
@@ -451,10 +489,11 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
       const int n0 = nt * a.bn;
       const int py = y0 + r / a.BW, px = x0 + r % a.BW;
-      const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
+      const long long hw = static_cast<long long>(a.H) * a.W;
+      const long long at = plane_at(b, n0 / 8, static_cast<long long>(py) * a.W + px, a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
-      epi_columns(d, c_lo, c_hi, a.bias ? s_bias + n0 : nullptr, a.relu,
-                  a.mask ? a.mask + pix * a.ldm + n0 : nullptr, a.out + pix * a.ldo + n0);
+      epi_columns(d, 0, a.bn, a.bias ? s_bias + n0 : nullptr, a.relu,
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -464,30 +503,34 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, 2 * cols);
+    tmem_dealloc(tmem, nbuf * cols);
   }
 }
 
 // ------------------------------------------- forward / dgrad, planar A ----
 // For images at least 128 pixels wide with 3x3 taps and weights that fit in
 // shared memory (the narrow layers): each K-block is one image row (dy) of
-// cb channels, staged once as cb/8 planes of 130 pixels x 8 channels (16
-// bytes per pixel, no swizzle: the K-major core-matrix layout with 8-row
-// groups 128 bytes apart and K chunks one plane apart), and the three taps
-// dx of that row are the same planes read from byte offset 16*dx -- a third
-// of the A traffic of one load per tap. The weights of every tap are loaded
-// into shared memory once per CTA and stay there.
-constexpr int kPlanePix = 130;                         // x0-1 .. x0+128
-constexpr int kPlaneBytes = kPlanePix * 16;            // one box: 2080 bytes
-constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;  // 128-byte aligned TMA targets
+// cb channels, staged once by one TMA box as cb/8 planes of 130 pixels x 8
+// channels (16 bytes per pixel, no swizzle: the K-major core-matrix layout
+// with 8-row groups 128 bytes apart and K chunks one plane apart), and the
+// three taps dx of that row are the same planes read from byte offset
+// 16*dx -- a third of the A traffic of one load per tap. The weights of
+// every tap are loaded into shared memory once per CTA and stay there.
+constexpr int kPlanePix = 130;                              // x0-1 .. x0+128
+constexpr int kPlaneBytes = kPlanePix * 16;                 // one staged plane row: 2080 bytes
+constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;    // 128-byte aligned TMA targets
+// A staged plane row is two TMA boxes: pixels x0-1 .. x0+126 (256 64-bit
+// elements, 2048 bytes) and the tail x0+127, x0+128 (4 elements).
 constexpr int kGuardBytes = 36 * 1024;  // slack after the ring: no descriptor reads past it
 
 template <int CB>
 __global__ void __launch_bounds__(kConvThreads, 1)
-    k_conv_planar(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmb,
+    k_conv_planar(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmt,
+                  const __grid_constant__ CUtensorMap tmb,
                   const ConvArgs a) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done, wfull;
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[kMaxAccBufs],
+      acc_empty[kMaxAccBufs], done, wfull;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   __shared__ float s_bias[kMaxBias];
@@ -504,16 +547,17 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   unsigned char *ring = smem + ((wbytes + 1023) & ~1023);
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t cols = a.bn <= 32 ? 32 : a.bn <= 64 ? 64 : a.bn <= 128 ? 128 : 256;
+  const uint32_t cols = acc_cols(a.bn);
+  const int nbuf = acc_bufs(a.bn);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < nbuf; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], kConvThreads - 64);
+      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
     }
     mbar_init(&done, 1);
     mbar_init(&wfull, 1);
@@ -521,10 +565,11 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tma_prefetch(&tmp);
+    tma_prefetch(&tmt);
     tma_prefetch(&tmb);
   }
   if (warp == 0) {
-    tmem_alloc(&tmem_slot, 2 * cols);
+    tmem_alloc(&tmem_slot, nbuf * cols);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -536,96 +581,95 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   const int ntot_tiles = a.mtiles;
 
   if (warp == 0) {
-    if (lane == 0) {
-      // weights once: box (tap, cc) at smem + (tap*kch + cc)*wbox
-      mbar_expect_tx(&wfull, wbytes);
-      for (int tap = 0; tap < 9; tap++)
-        for (int cc = 0; cc < kch; cc++)
-          tma_load_2d(smem + (tap * kch + cc) * wbox, &tmb, &wfull, tap * a.cin + cc * CB, 0);
-      int kbg = 0;
-      bool stop = false;
-      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
-        const int b = t / tiles_img;
-        const int tt = t - b * tiles_img;
-        const int y0 = tt / a.tiles_x, x0 = (tt % a.tiles_x) * 128;
-        for (int kb = 0; kb < nkb; kb++, kbg++) {
-          const int s = kbg % S;
-          if (!mbar_wait(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
-            sg_raise(a.err, &abort_flag, kSgTimeout);
-            stop = true;
-            break;
-          }
-          const int dy = kb / kch, cc = kb - dy * kch;
-          unsigned char *sa = ring + s * kStageA;
-          mbar_expect_tx(&full[s], kPlanes * kPlaneBytes);
-#pragma unroll
-          for (int pl = 0; pl < kPlanes; pl++)
-            tma_load_4d(sa + pl * kPlaneStride, &tmp, &full[s], cc * CB + 8 * pl, x0 - 1,
-                        y0 + dy - 1, b);
-        }
-      }
-      for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
-        if (!mbar_wait(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+    // producer (the whole warp; one lane issues)
+    // weights once: box (tap, cc) at smem + (tap*kch + cc)*wbox
+    mbar_expect_tx_el(&wfull, wbytes);
+    for (int tap = 0; tap < 9; tap++)
+      for (int cc = 0; cc < kch; cc++)
+        tma_load_2d_el(smem + (tap * kch + cc) * wbox, &tmb, &wfull, tap * a.cin + cc * CB, 0);
+    int kbg = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
+      const int b = t / tiles_img;
+      const int tt = t - b * tiles_img;
+      const int y0 = tt / a.tiles_x, x0 = (tt % a.tiles_x) * 128;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int s = kbg % S;
+        if (!mbar_wait_warp(&empty[s], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
           sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
           break;
         }
-      if (!mbar_wait(&wfull, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+        const int dy = kb / kch, cc = kb - dy * kch;
+        unsigned char *sa = ring + s * kStageA;
+        mbar_expect_tx_el(&full[s], kPlanes * kPlaneBytes);
+#pragma unroll
+        for (int pl = 0; pl < kPlanes; pl++) {
+          tma_load_4d_el(sa + pl * kPlaneStride, &tmp, &full[s], 2 * (x0 - 1), y0 + dy - 1,
+                         cc * kPlanes + pl, b);
+          tma_load_4d_el(sa + pl * kPlaneStride + 2048, &tmt, &full[s], 2 * (x0 + 127),
+                         y0 + dy - 1, cc * kPlanes + pl, b);
+        }
+      }
     }
+    for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
+      if (!mbar_wait_warp(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+    if (!mbar_wait_warp(&wfull, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
-      bool stop = !mbar_wait(&wfull, 0, &abort_flag, true);
-      if (stop) sg_raise(a.err, &abort_flag, kSgTimeout);
+    // MMA issuer (the whole warp; one lane issues)
+    const uint32_t idesc = idesc_bf16(a.bn, 0, 0);
+    bool stop = !mbar_wait_warp(&wfull, 0, &abort_flag, true);
+    if (stop) sg_raise(a.err, &abort_flag, kSgTimeout);
+    tc_fence_after();
+    const uint32_t wbase = su32(smem);
+    int kbg = 0, it = 0;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
+      const int buf = it % nbuf;
+      if (!mbar_wait_warp(&acc_empty[buf], ((it / nbuf) & 1) ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
       tc_fence_after();
-      const uint32_t wbase = su32(smem);
-      int kbg = 0, it = 0;
-      for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
-        const int buf = it & 1;
-        if (!mbar_wait(&acc_empty[buf], ((it >> 1) & 1) ^ 1, &abort_flag, true)) {
+      const uint32_t d = tmem + buf * cols;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int s = kbg % S;
+        if (!mbar_wait_warp(&full[s], (kbg / S) & 1, &abort_flag, true)) {
           sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
           break;
         }
         tc_fence_after();
-        const uint32_t d = tmem + buf * cols;
-        for (int kb = 0; kb < nkb; kb++, kbg++) {
-          const int s = kbg % S;
-          if (!mbar_wait(&full[s], (kbg / S) & 1, &abort_flag, true)) {
-            sg_raise(a.err, &abort_flag, kSgTimeout);
-            stop = true;
-            break;
-          }
-          tc_fence_after();
-          const int dy = kb / kch, cc = kb - dy * kch;
-          const uint32_t sa = su32(ring + s * kStageA);
+        const int dy = kb / kch, cc = kb - dy * kch;
+        const uint32_t sa = su32(ring + s * kStageA);
 #pragma unroll
-          for (int dx = 0; dx < 3; dx++) {
-            const uint32_t wb = wbase + ((3 * dy + dx) * kch + cc) * wbox;
-            const uint64_t db = smem_desc(wb, 16, 8 * kRow, swizzle_code(kRow));
+        for (int dx = 0; dx < 3; dx++) {
+          const uint32_t wb = wbase + ((3 * dy + dx) * kch + cc) * wbox;
+          const uint64_t db = smem_desc(wb, 16, 8 * kRow, swizzle_code(kRow));
 #pragma unroll
-            for (int k = 0; k < CB / 16; k++) {
-              // K-major, no swizzle: K chunks (planes) kPlaneStride apart, 8-row
-              // groups 128 bytes apart; 16 channels = two planes per MMA
-              const uint64_t da = smem_desc(sa + 16 * dx + 2 * k * kPlaneStride, kPlaneStride, 128, 0);
-              umma_bf16(d, da, db + 2 * k, idesc, (kb | dx | k) != 0);
-            }
+          for (int k = 0; k < CB / 16; k++) {
+            // K-major, no swizzle: K chunks (planes) kPlaneStride apart, 8-row
+            // groups 128 bytes apart; 16 channels = two planes per MMA
+            const uint64_t da = smem_desc(sa + 16 * dx + 2 * k * kPlaneStride, kPlaneStride, 128, 0);
+            umma_bf16_el(d, da, db + 2 * k, idesc, (kb | dx | k) != 0);
           }
-          umma_commit(&empty[s]);
         }
-        if (!stop) umma_commit(&acc_full[buf]);
+        umma_commit_el(&empty[s]);
       }
-      umma_commit(&done);
-      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+      if (!stop) umma_commit_el(&acc_full[buf]);
     }
+    umma_commit_el(&done);
+    if (!mbar_wait_warp(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
   } else {
     const int q = warp & 3;
-    const int half = (warp - 2) >> 2;
+    const int grp = (warp - 2) >> 2;
     const int r = q * 32 + lane;
-    const int csplit = a.bn % 32 == 0 ? a.bn / 2 : a.bn;
-    const int c_lo = half ? csplit : 0, c_hi = half ? a.bn : csplit;
-    int it = 0;
-    for (int t = blockIdx.x; t < ntot_tiles; t += gridDim.x, it++) {
-      const int buf = it & 1;
-      if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
+    for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
+         t += 2 * gridDim.x, it += 2) {
+      const int buf = it % nbuf;
+      if (!mbar_wait(&acc_full[buf], (it / nbuf) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
@@ -633,10 +677,11 @@ __global__ void __launch_bounds__(kConvThreads, 1)
       const int b = t / tiles_img;
       const int tt = t - b * tiles_img;
       const int py = tt / a.tiles_x, px = (tt % a.tiles_x) * 128 + r;
-      const long long pix = (static_cast<long long>(b) * a.H + py) * a.W + px;
+      const long long hw = static_cast<long long>(a.H) * a.W;
+      const long long at = plane_at(b, 0, static_cast<long long>(py) * a.W + px, a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
-      epi_columns(d, c_lo, c_hi, a.bias ? s_bias : nullptr, a.relu,
-                  a.mask ? a.mask + pix * a.ldm : nullptr, a.out + pix * a.ldo);
+      epi_columns(d, 0, a.bn, a.bias ? s_bias : nullptr, a.relu,
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -646,7 +691,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, 2 * cols);
+    tmem_dealloc(tmem, nbuf * cols);
   }
 }
 
@@ -670,8 +715,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   constexpr int kRowA = CWA * 2, kRowB = CWB * 2;
-  constexpr int kChunkA = kKPix * kRowA;  // one (tap, channel block) chunk: 128 pixel rows
+  constexpr int kChunkA = kKPix * kRowA;  // one (tap, channel block) chunk: CWA/8 planes
   constexpr int kChunkB = kKPix * kRowB;
+  constexpr int kPix16 = kKPix * 16;      // one plane of 128 pixels
   constexpr int kPerTile = kM / CWA;      // chunks stacked in one M tile
   const int a_bytes = kPerTile * kChunkA;  // = 128 * 256 bytes
   const int b_bytes = (a.cout / CWB) * kChunkB;
@@ -709,12 +755,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nk = k_hi - k_lo;
   const int tiles_img = a.tiles_x * a.tiles_y;
 
-  if (warp == 0 && lane == 0) {
+  if (warp == 0) {
+    // producer (the whole warp; one lane issues)
     int issued = 0;
     const uint32_t tx = nq * kChunkA + b_bytes;
     for (int i = 0; i < nk; i++) {
       const int s = i % S;
-      if (!mbar_wait(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
+      if (!mbar_wait_warp(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
@@ -723,42 +770,43 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int y0 = (t / a.tiles_x) * a.BH, x0 = (t % a.tiles_x) * a.BW;
       unsigned char *sa = smem + s * stage_bytes;
       unsigned char *sb = sa + a_bytes;
-      mbar_expect_tx(&full[s], tx);
+      mbar_expect_tx_el(&full[s], tx);
       for (int j = 0; j < nq; j++) {
         const int q = q0 + j;
         const int tap = q / kchx, cc = q - tap * kchx;
         const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
-        tma_load_4d(sa + j * kChunkA, &tmx, &full[s], cc * CWA, x0 + dx, y0 + dy, b);
+        tma_load_4d_el(sa + j * kChunkA, &tmx, &full[s], 2 * (x0 + dx), y0 + dy, cc * (CWA / 8),
+                       b);
       }
-      for (int j = 0; j < a.cout / CWB; j++)
-        tma_load_4d(sb + j * kChunkB, &tmy, &full[s], j * CWB, x0, y0, b);
+      tma_load_4d_el(sb, &tmy, &full[s], 2 * x0, y0, 0, b);  // every plane of dY
       issued = i + 1;
     }
     for (int i = issued > S ? issued - S : 0; i < issued; i++)
-      if (!mbar_wait(&full[i % S], (i / S) & 1, &abort_flag, false)) {
+      if (!mbar_wait_warp(&full[i % S], (i / S) & 1, &abort_flag, false)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
-  } else if (warp == 1 && lane == 0) {
+  } else if (warp == 1) {
+    // MMA issuer (the whole warp; one lane issues)
     const uint32_t idesc = idesc_bf16(a.cout, 1, 1);
     for (int i = 0; i < nk; i++) {
       const int s = i % S;
-      if (!mbar_wait(&full[s], (i / S) & 1, &abort_flag, true)) {
+      if (!mbar_wait_warp(&full[s], (i / S) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
       tc_fence_after();
       const uint32_t sa = su32(smem + s * stage_bytes);
-      // MN-major: LBO = stride between channel chunks, SBO = 8 pixel rows
-      const uint64_t da = smem_desc(sa, kChunkA, 8 * kRowA, swizzle_code(kRowA));
-      const uint64_t db = smem_desc(sa + a_bytes, kChunkB, 8 * kRowB, swizzle_code(kRowB));
+      // MN-major, no swizzle: MN chunks (planes) kPix16 apart, 8-pixel K
+      // groups 128 bytes apart; 16 pixels (256 bytes of every plane) per MMA
+      const uint64_t da = smem_desc(sa, 128, kPix16, 0);
+      const uint64_t db = smem_desc(sa + a_bytes, 128, kPix16, 0);
 #pragma unroll
-      for (int k = 0; k < kKPix / 16; k++)  // 16 pixel rows per MMA
-        umma_bf16(tmem, da + ((16 * kRowA * k) >> 4), db + ((16 * kRowB * k) >> 4), idesc,
-                  (i | k) != 0);
-      umma_commit(&empty[s]);
+      for (int k = 0; k < kKPix / 16; k++)
+        umma_bf16_el(tmem, da + 16 * k, db + 16 * k, idesc, (i | k) != 0);
+      umma_commit_el(&empty[s]);
     }
-    umma_commit(&accf);
+    umma_commit_el(&accf);
   }
   __syncwarp();
 
@@ -818,7 +866,8 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 }
 
 __global__ void __launch_bounds__(kWgradThreads, 1)
-    k_wgrad_planar(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmy,
+    k_wgrad_planar(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmt,
+                   const __grid_constant__ CUtensorMap tmy,
                    const WgradPlanarArgs a) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full, done;
@@ -829,6 +878,7 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int yp = a.cout / 8, xp = a.cin / 8;  // loaded planes of dY and of each X row
+  const int rowb = xp * kPlaneStride;          // bytes of one staged X row
   const uint32_t need = static_cast<uint32_t>(a.ntap * a.cpt);
   const uint32_t cols = need <= 32 ? 32 : need <= 64 ? 64 : need <= 128 ? 128 : need <= 256 ? 256 : 512;
 
@@ -849,6 +899,7 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     tma_prefetch(&tmx);
+    tma_prefetch(&tmt);
     tma_prefetch(&tmy);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -866,67 +917,65 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   const int nk = k_hi - k_lo;
 
   if (warp == 0) {
-    if (lane == 0) {
-      int issued = 0;
-      const uint32_t tx = yp * kYPlaneBytes + a.nrows * xp * kPlaneBytes;
-      for (int i = 0; i < nk; i++) {
-        const int s = i % S;
-        if (!mbar_wait(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
-          sg_raise(a.err, &abort_flag, kSgTimeout);
-          break;
-        }
-        const int kt = k_lo + i;
-        const int b = kt / tiles_img, t = kt - b * tiles_img;
-        const int y0 = t / a.tiles_x, x0 = (t % a.tiles_x) * 128;
-        unsigned char *sy = smem + s * a.stage_bytes;
-        unsigned char *sx = sy + 16 * kYPlaneBytes;
-        mbar_expect_tx(&full[s], tx);
-        for (int pl = 0; pl < yp; pl++)
-          tma_load_4d(sy + pl * kYPlaneBytes, &tmy, &full[s], 8 * pl, x0, y0, b);
-        for (int r = 0; r < a.nrows; r++)
-          for (int pl = 0; pl < xp; pl++)
-            tma_load_4d(sx + (r * xp + pl) * kPlaneStride, &tmx, &full[s], 8 * pl, x0 - 1,
-                        y0 + a.row0 + r - 1, b);
-        issued = i + 1;
+    // producer (the whole warp; one lane issues)
+    int issued = 0;
+    const uint32_t tx = yp * kYPlaneBytes + a.nrows * xp * kPlaneBytes;
+    for (int i = 0; i < nk; i++) {
+      const int s = i % S;
+      if (!mbar_wait_warp(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
       }
-      for (int i = issued > S ? issued - S : 0; i < issued; i++)
-        if (!mbar_wait(&full[i % S], (i / S) & 1, &abort_flag, false)) {
-          sg_raise(a.err, &abort_flag, kSgTimeout);
-          break;
+      const int kt = k_lo + i;
+      const int b = kt / tiles_img, t = kt - b * tiles_img;
+      const int y0 = t / a.tiles_x, x0 = (t % a.tiles_x) * 128;
+      unsigned char *sy = smem + s * a.stage_bytes;
+      unsigned char *sx = sy + 16 * kYPlaneBytes;
+      mbar_expect_tx_el(&full[s], tx);
+      tma_load_4d_el(sy, &tmy, &full[s], 2 * x0, y0, 0, b);
+      for (int r = 0; r < a.nrows; r++)
+        for (int pl = 0; pl < xp; pl++) {
+          unsigned char *d = sx + r * rowb + pl * kPlaneStride;
+          tma_load_4d_el(d, &tmx, &full[s], 2 * (x0 - 1), y0 + a.row0 + r - 1, pl, b);
+          tma_load_4d_el(d + 2048, &tmt, &full[s], 2 * (x0 + 127), y0 + a.row0 + r - 1, pl, b);
         }
+      issued = i + 1;
     }
+    for (int i = issued > S ? issued - S : 0; i < issued; i++)
+      if (!mbar_wait_warp(&full[i % S], (i / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(a.cin, 1, 1);
-      for (int i = 0; i < nk; i++) {
-        const int s = i % S;
-        if (!mbar_wait(&full[s], (i / S) & 1, &abort_flag, true)) {
-          sg_raise(a.err, &abort_flag, kSgTimeout);
-          break;
-        }
-        tc_fence_after();
-        const uint32_t sy = su32(smem + s * a.stage_bytes);
-        const uint32_t sx = sy + 16 * kYPlaneBytes;
+    // MMA issuer (the whole warp; one lane issues)
+    const uint32_t idesc = idesc_bf16(a.cin, 1, 1);
+    for (int i = 0; i < nk; i++) {
+      const int s = i % S;
+      if (!mbar_wait_warp(&full[s], (i / S) & 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sy = su32(smem + s * a.stage_bytes);
+      const uint32_t sx = sy + 16 * kYPlaneBytes;
+      // consecutive MMAs go to different taps' accumulators (independent)
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        // MN-major, no swizzle: MN chunks (planes) at the plane stride,
+        // 8-pixel K groups 128 bytes apart; 16 pixels per MMA
+        const uint64_t da = smem_desc(sy + 256 * k, 128, kYPlaneBytes, 0);
         for (int j = 0; j < a.ntap; j++) {
           const int tap = a.tap0 + j;
           const int r = tap / 3 - a.row0, dx = tap % 3;
-          const uint32_t d = tmem + j * a.cpt;
-#pragma unroll
-          for (int k = 0; k < 8; k++) {
-            // MN-major, no swizzle: MN chunks (planes) at the plane stride,
-            // 8-pixel K groups 128 bytes apart; 16 pixels per MMA
-            const uint64_t da = smem_desc(sy + 256 * k, 128, kYPlaneBytes, 0);
-            const uint64_t db = smem_desc(sx + r * xp * kPlaneStride + 16 * dx + 256 * k, 128,
-                                          kPlaneStride, 0);
-            umma_bf16(d, da, db, idesc, (i | k) != 0);
-          }
+          const uint64_t db = smem_desc(sx + r * rowb + 16 * dx + 256 * k, 128, kPlaneStride, 0);
+          umma_bf16_el(tmem + j * a.cpt, da, db, idesc, (i | k) != 0);
         }
-        umma_commit(&empty[s]);
       }
-      umma_commit(&acc_full);
-      umma_commit(&done);
-      if (!mbar_wait(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+      umma_commit_el(&empty[s]);
     }
+    umma_commit_el(&acc_full);
+    umma_commit_el(&done);
+    if (!mbar_wait_warp(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
   } else if (nk > 0) {
     const int q = warp & 3;
     const int co = q * 32 + lane;
@@ -998,37 +1047,23 @@ CUtensorMapSwizzle swizzle_of(int row_bytes) {
                            : CU_TENSOR_MAP_SWIZZLE_32B;
 }
 
-// {cb, BW, BH, 1} boxes of an NHWC tensor.
-cudaError_t map_act(CUtensorMap *m, const Act &t, int cb, const PixTile &pt) {
+// Boxes of a plane-major tensor viewed as 64-bit elements (2 per pixel of a
+// plane row), without swizzle: dims {2W, H, C/8, B}; box {e0, bh, np, 1} =
+// e0/2 pixels of bh rows of np planes, stored in shared memory plane after
+// plane (a box row of e0 elements is one run of e0*8 bytes).
+cudaError_t map_act(CUtensorMap *m, const Act &t, int e0, int bh, int np) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
-  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
-                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
-  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
-  const cuuint32_t box[4] = {static_cast<cuuint32_t>(cb), static_cast<cuuint32_t>(pt.BW),
-                             static_cast<cuuint32_t>(pt.BH), 1};
+  const cuuint64_t dims[4] = {2 * static_cast<cuuint64_t>(t.W), static_cast<cuuint64_t>(t.H),
+                              static_cast<cuuint64_t>(t.C / 8), static_cast<cuuint64_t>(t.B)};
+  const cuuint64_t hw16 = static_cast<cuuint64_t>(t.W) * t.H * 16;
+  // byte strides of dims 1..3: a row, a plane, an image
+  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.W) * 16, hw16,
+                                 hw16 * static_cast<cuuint64_t>(t.C / 8)};
+  const cuuint32_t box[4] = {static_cast<cuuint32_t>(e0), static_cast<cuuint32_t>(bh),
+                             static_cast<cuuint32_t>(np), 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_of(cb * 2),
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-
-// {8, 130, 1, 1} boxes of an NHWC tensor without swizzle: one plane of 8
-// channels over 130 pixels of one image row.
-cudaError_t map_planes(CUtensorMap *m, const Act &t) {
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return cudaErrorNotSupported;
-  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
-                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
-  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
-  const cuuint32_t box[4] = {8, static_cast<cuuint32_t>(kPlanePix), 1, 1};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, t.p, dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
@@ -1072,7 +1107,7 @@ PixTile pixel_tile(int H, int W) {
 }
 
 cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
-                      const float *bias, int relu, const bf16 *mask, int ldm, bf16 *out, int ldo,
+                      const float *bias, int relu, const bf16 *mask, bf16 *out,
                       const char **why) {
   const char *dummy;
   if (!why) why = &dummy;
@@ -1083,8 +1118,6 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   if (taps != 1 && taps != 9) return *why = "taps must be 1 or 9", cudaErrorInvalidValue;
   if (ntot % 16 || ntot <= 0) return *why = "output channels must be a multiple of 16", cudaErrorInvalidValue;
   if (bias && ntot > kMaxBias) return *why = "at most 512 biased output channels", cudaErrorInvalidValue;
-  if (ldo % 8 || ldo < ntot || (mask && (ldm % 8 || ldm < ntot)))
-    return *why = "output/mask row strides must be multiples of 8 covering the channels", cudaErrorInvalidValue;
   if (!aligned16(src.p) || !aligned16(w) || !aligned16(out) || (mask && !aligned16(mask)))
     return *why = "tensors must be 16-byte aligned", cudaErrorInvalidValue;
   // N tile: the whole output when it fits one accumulator, else the largest
@@ -1132,9 +1165,7 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   p.bias = bias;
   p.relu = relu;
   p.mask = mask;
-  p.ldm = ldm;
   p.out = out;
-  p.ldo = ldo;
   p.grid_x = static_cast<int>(src.pixels() / kM);
   p.grid_y = ntot / bn;
   int dev = 0;
@@ -1142,7 +1173,9 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   p.sms = 1;
   cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, dev);
   if (p.sms < 1) p.sms = 1;
-  cudaError_t e = p.planar ? map_planes(&p.tma, src) : map_act(&p.tma, src, p.cb, p.pt);
+  cudaError_t e = p.planar ? map_act(&p.tma, src, 256, 1, 1)
+                           : map_act(&p.tma, src, 2 * p.pt.BW, p.pt.BH, p.cb / 8);
+  if (e == cudaSuccess && p.planar) e = map_act(&p.tmt, src, 4, 1, 1);
   if (e != cudaSuccess) return *why = "tensor map (source)", e;
   e = map_mat(&p.tmb, w, ntot, taps * src.C, p.cb, bn);
   if (e != cudaSuccess) return *why = "tensor map (weights)", e;
@@ -1157,23 +1190,6 @@ void split_pixels(WgradPlan &p, int ksteps) {
   if (splits < 1) splits = 1;
   p.kper = (ksteps + splits - 1) / splits;
   p.splits = (ksteps + p.kper - 1) / p.kper;
-}
-
-// {8, 128, 1, 1} boxes: one plane of 8 channels over 128 pixels of a row.
-cudaError_t map_planes128(CUtensorMap *m, const Act &t) {
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return cudaErrorNotSupported;
-  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(t.C), static_cast<cuuint64_t>(t.W),
-                              static_cast<cuuint64_t>(t.H), static_cast<cuuint64_t>(t.B)};
-  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(t.C) * 2,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W,
-                                 static_cast<cuuint64_t>(t.C) * 2 * t.W * t.H};
-  const cuuint32_t box[4] = {8, 128, 1, 1};
-  const cuuint32_t estr[4] = {1, 1, 1, 1};
-  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, t.p, dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 // The planar weight gradient's tap groups: as many taps per CTA as their
@@ -1240,9 +1256,12 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
   split_pixels(p, p.ksteps);
   p.dw = dw;
   p.planar = plan_planar_groups(p) ? 1 : 0;
-  cudaError_t e = p.planar ? map_planes(&p.tmx, x) : map_act(&p.tmx, x, p.cwa, p.pt);
+  cudaError_t e = p.planar ? map_act(&p.tmx, x, 256, 1, 1)
+                           : map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, p.cwa / 8);
+  if (e == cudaSuccess && p.planar) e = map_act(&p.tmt, x, 4, 1, 1);
   if (e != cudaSuccess) return *why = "tensor map (X)", e;
-  e = p.planar ? map_planes128(&p.tmy, dy) : map_act(&p.tmy, dy, p.cwb, p.pt);
+  e = p.planar ? map_act(&p.tmy, dy, 2 * kM, 1, dy.C / 8)
+               : map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
   if (e != cudaSuccess) return *why = "tensor map (dY)", e;
   return cudaSuccess;
 }
@@ -1275,16 +1294,15 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   a.bias = p.bias;
   a.relu = p.relu;
   a.mask = p.mask;
-  a.ldm = p.ldm;
   a.out = p.out;
-  a.ldo = p.ldo;
+  a.oplanes = p.ntot / 8;
   a.err = err;
   a.mtiles = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
   a.ntiles = p.grid_y;
   const int tiles = a.mtiles * a.ntiles;
   const int grid = tiles < p.sms ? tiles : p.sms;
   if (p.planar)
-    k_conv_planar<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);
+    k_conv_planar<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
   else
     k_conv<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);
   return cudaGetLastError();
@@ -1376,7 +1394,7 @@ cudaError_t launch_wgrad_planar(const WgradPlan &p, int *err, cudaStream_t s, in
     a.dw = p.dw;
     a.err = err;
     const size_t smem = static_cast<size_t>(a.stages) * a.stage_bytes + 1024;
-    k_wgrad_planar<<<splits, kWgradThreads, smem, s>>>(p.tmx, p.tmy, a);
+    k_wgrad_planar<<<splits, kWgradThreads, smem, s>>>(p.tmx, p.tmt, p.tmy, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -2,10 +2,14 @@
 // the convolution kernels (sg_conv.cu), the network (sg_net.cu) and the
 // judged ensemble (sg_ensemble.cu). Not part of the public ABI.
 //
-// Activations are NHWC BF16 tensors (channels innermost, a multiple of 16);
-// weights of a 3x3 (or 1x1) convolution are BF16 [cout][tap][cin] with
-// tap = 3*dy + dx (the GEMM's K dimension tap*cin + ci contiguous), kept
-// with an FP32 master copy; weight gradients are FP32 in the same layout.
+// Activations are plane-major BF16 tensors [B][C/8][H][W][8]: a plane holds
+// 8 channels of one image, 16 bytes per pixel, so a row of a plane is one
+// contiguous run that a TMA box reads in full lines, and 8 consecutive
+// pixels of a plane are exactly one 128-byte core matrix of the tensor
+// cores' no-swizzle operand layouts (C a multiple of 16). Weights of a 3x3
+// (or 1x1) convolution are BF16 [cout][tap][cin] with tap = 3*dy + dx (the
+// GEMM's K dimension tap*cin + ci contiguous), kept with an FP32 master
+// copy; weight gradients are FP32 in the same layout.
 #pragma once
 
 #include <cuda.h>
@@ -25,7 +29,7 @@ enum SgErr : int {
   kSgTimeout = 1,  // an mbarrier wait ran out (producer, MMA or epilogue)
 };
 
-// An NHWC activation tensor on the device.
+// A plane-major activation tensor on the device.
 struct Act {
   bf16 *p = nullptr;
   int B = 0, H = 0, W = 0, C = 0;
@@ -33,9 +37,17 @@ struct Act {
   size_t bytes() const { return static_cast<size_t>(pixels()) * C * sizeof(bf16); }
 };
 
-// Channels one K-block (and one TMA box) of a tensor with C channels spans:
-// 64 when C is a multiple of 64, else 32, else 16 (128-, 64- or 32-byte rows,
-// the swizzle span of the box).
+// Element offset of channels [8*plane, 8*plane + 8) of pixel pix (y*W + x)
+// of image b in a plane-major tensor with `planes` planes per image of hw
+// pixels.
+__host__ __device__ inline long long plane_at(int b, int plane, long long pix, int planes,
+                                              long long hw) {
+  return ((static_cast<long long>(b) * planes + plane) * hw + pix) * 8;
+}
+
+// Channels one K-block (one TMA box of planes) of a tensor with C channels
+// spans: 64 when C is a multiple of 64, else 32, else 16; the weights' box
+// of the same K-block has 128-, 64- or 32-byte swizzled rows.
 inline int channel_block(int C) { return C % 64 == 0 ? 64 : C % 32 == 0 ? 32 : 16; }
 
 // Pixel tile of 128 pixels of one image: BW x BH with BW = min(W, 128).
@@ -48,16 +60,17 @@ PixTile pixel_tile(int H, int W);
 // A forward (or data-gradient) convolution prepared for launches: the tensor
 // maps of its source and weights, the tile shape and the epilogue.
 struct ConvPlan {
-  CUtensorMap tma;  // source activations, box {cb, BW, BH, 1} (planar: {8, 130, 1, 1})
+  // source planes viewed as 64-bit elements: box {2*BW, BH, cb/8, 1} (planar:
+  // {256, 1, 1, 1}, one plane row from x0-1, with tmt's {4, 1, 1, 1} tail)
+  CUtensorMap tma;
+  CUtensorMap tmt;
   CUtensorMap tmb;  // weights [ntot][taps*cin], box {cb, bn}
   int B = 0, H = 0, W = 0, cin = 0, taps = 9, ntot = 0, bn = 0, cb = 0, stages = 0;
   PixTile pt;
   const float *bias = nullptr;  // [ntot] or null
   int relu = 0;
-  const bf16 *mask = nullptr;   // output zeroed where mask <= 0 (or null)
-  int ldm = 0;
-  bf16 *out = nullptr;
-  int ldo = 0;
+  const bf16 *mask = nullptr;   // output zeroed where mask <= 0 (or null; ntot channels)
+  bf16 *out = nullptr;          // ntot channels
   size_t smem = 0;
   int grid_x = 0, grid_y = 0;  // pixel tiles and N tiles
   int sms = 1;                 // persistent CTAs launched (at most one per SM)
@@ -67,8 +80,12 @@ struct ConvPlan {
 // A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=
 // sum over pixels of dY[p][co] * X[p + off(tap)][ci].
 struct WgradPlan {
-  CUtensorMap tmx;  // X, box {cwa, BW, BH, 1} (planar: {8, 130, 1, 1})
-  CUtensorMap tmy;  // dY, box {cwb, BW, BH, 1} (planar: {8, 128, 1, 1})
+  // X and dY planes viewed as 64-bit elements: X box {2*BW, BH, cwa/8, 1}
+  // (planar: {256, 1, 1, 1} from x0-1 with tmt's {4, 1, 1, 1} tail), dY box
+  // {2*BW, BH, cout/8, 1}
+  CUtensorMap tmx;
+  CUtensorMap tmt;
+  CUtensorMap tmy;
   int B = 0, H = 0, W = 0, cin = 0, cout = 0, taps = 9, cwa = 0, cwb = 0, stages = 0;
   PixTile pt;
   int mtiles = 0, splits = 0, ksteps = 0, kper = 0, sms = 1;
@@ -84,8 +101,8 @@ struct WgradPlan {
 // shapes the kernels do not take. Source and output tensors must stay
 // allocated for the plan's lifetime.
 cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
-                      const float *bias, int relu, const bf16 *mask, int ldm, bf16 *out,
-                      int ldo, const char **why);
+                      const float *bias, int relu, const bf16 *mask, bf16 *out,
+                      const char **why);
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
                        const char **why);
 // nimg > 0 runs the plan over the first nimg images only (the tensor maps

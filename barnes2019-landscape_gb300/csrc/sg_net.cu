@@ -272,13 +272,13 @@ int build(fs_surrogate *s) {
     SG_CUDA(dalloc(s, &L.wd, nw));
     const char *why = nullptr;
     cudaError_t e = sg::plan_conv(L.fwd, *L.x, L.wf, L.taps, L.cout, s->p + L.b_off, 1, nullptr,
-                                  0, L.y->p, L.cout, &why);
+                                  L.y->p, &why);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d forward: %s", l, why);
     e = sg::plan_wgrad(L.wgr, *L.x, *L.gy, L.taps, s->g + L.w_off, s->sms, &why);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d weight gradient: %s", l, why);
     if (L.gx) {
       e = sg::plan_conv(L.dgr, *L.gy, L.wd, L.taps, L.cin, nullptr, 0,
-                        L.dmask ? L.dmask->p : nullptr, L.cin, L.gx->p, L.cin, &why);
+                        L.dmask ? L.dmask->p : nullptr, L.gx->p, &why);
       if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d data gradient: %s", l, why);
     }
   }

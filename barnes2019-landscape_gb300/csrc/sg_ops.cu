@@ -1,8 +1,10 @@
 // sg_ops.cu -- the surrogate network's memory-bound kernels: input planes,
 // 2x2 pooling and its adjoint, upsample-and-concatenate and its adjoint, the
 // 1x1 output head with the loss and its gradient, bias gradients, Adam, and
-// the jump that applies a prediction to an FP64 elevation field. All NHWC
-// BF16 tensors move 8 channels (16 bytes) per access.
+// the jump that applies a prediction to an FP64 elevation field. All
+// plane-major BF16 tensors ([B][C/8][H][W][8]) move one pixel of one plane
+// (8 channels, 16 bytes) per access, consecutive threads on consecutive
+// pixels of a plane.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -106,121 +108,108 @@ __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__rest
       lo[j] = f[j];
       hi[j] = f[8 + j];
     }
-    bf16 *o = in + i * kInputChannels;
-    store8(o, lo);
-    store8(o + 8, hi);
+    store8(in + plane_at(b, 0, pix, 2, hw), lo);
+    store8(in + plane_at(b, 1, pix, 2, hw), hi);
     if (yt) yt[i] = v.y ? v.y[static_cast<long long>(src) * hw + pix] : 0.0f;
   }
 }
 
+// out = 2x2 average of in; i runs over (image, plane) pairs and pixels of out
 __global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, int B, int Ho,
                            int Wo, int C) {
-  const int c8n = C / 8;
-  const long long n = static_cast<long long>(B) * Ho * Wo * c8n;
+  const long long hwo = static_cast<long long>(Ho) * Wo, Wi = 2ll * Wo;
+  const long long n = static_cast<long long>(B) * (C / 8) * hwo;
   for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * kBlock) {
-    const int c8 = static_cast<int>(i % c8n);
-    const long long pix = i / c8n;
-    const int x = static_cast<int>(pix % Wo);
-    const long long r = pix / Wo;
-    const int y = static_cast<int>(r % Ho);
-    const int b = static_cast<int>(r / Ho);
-    const long long Wi = 2ll * Wo;
-    const bf16 *p = in + ((static_cast<long long>(b) * 2 * Ho + 2 * y) * Wi + 2 * x) * C + c8 * 8;
+    const long long bp = i / hwo, po = i - bp * hwo;
+    const int x = static_cast<int>(po % Wo), y = static_cast<int>(po / Wo);
+    const bf16 *p = in + (bp * 4 * hwo + 2ll * y * Wi + 2 * x) * 8;
     float a[8], t[8];
     load8(p, a);
-    load8(p + C, t);
+    load8(p + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    load8(p + Wi * C, t);
+    load8(p + Wi * 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    load8(p + Wi * C + C, t);
+    load8(p + Wi * 8 + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] = 0.25f * (a[j] + t[j]);
-    store8(out + pix * C + c8 * 8, a);
+    store8(out + i * 8, a);
   }
 }
 
-// cat[b,y,x,0:Cd] = d[b,y/2,x/2,:], cat[b,y,x,Cd:Cd+Cs] = s[b,y,x,:]
+// cat[b, 0:Cd, y, x] = d[b, :, y/2, x/2], cat[b, Cd:Cd+Cs, y, x] = s[b, :, y, x]
 __global__ void k_upcat(const bf16 *__restrict__ d, const bf16 *__restrict__ s,
                         bf16 *__restrict__ cat, int B, int H, int W, int Cd, int Cs) {
-  const int C = Cd + Cs, c8n = C / 8;
-  const long long n = static_cast<long long>(B) * H * W * c8n;
+  const int pd = Cd / 8, ps = Cs / 8, pc = pd + ps;
+  const long long hw = static_cast<long long>(H) * W;
+  const long long n = static_cast<long long>(B) * pc * hw;
   for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * kBlock) {
-    const int c = static_cast<int>(i % c8n) * 8;
-    const long long pix = i / c8n;
+    const long long bp = i / hw, pix = i - bp * hw;
+    const int b = static_cast<int>(bp / pc), pl = static_cast<int>(bp - static_cast<long long>(b) * pc);
     uint4 v;
-    if (c < Cd) {
-      const int x = static_cast<int>(pix % W);
-      const long long r = pix / W;
-      const int y = static_cast<int>(r % H);
-      const int b = static_cast<int>(r / H);
-      const long long lp = (static_cast<long long>(b) * (H / 2) + y / 2) * (W / 2) + x / 2;
-      v = *reinterpret_cast<const uint4 *>(d + lp * Cd + c);
+    if (pl < pd) {
+      const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+      v = *reinterpret_cast<const uint4 *>(
+          d + plane_at(b, pl, static_cast<long long>(y / 2) * (W / 2) + x / 2, pd, hw / 4));
     } else {
-      v = *reinterpret_cast<const uint4 *>(s + pix * Cs + (c - Cd));
+      v = *reinterpret_cast<const uint4 *>(s + plane_at(b, pl - pd, pix, ps, hw));
     }
-    *reinterpret_cast<uint4 *>(cat + pix * C + c) = v;
+    *reinterpret_cast<uint4 *>(cat + i * 8) = v;
   }
 }
 
-// gd[b,y,x,:] = sum over the 2x2 block of g[b,2y+i,2x+j,0:Cd] (g has C
+// gd[b, :, y, x] = sum over the 2x2 block of g[b, 0:Cd, 2y+i, 2x+j] (g has C
 // channels at twice the resolution): the adjoint of nearest upsampling
 __global__ void k_sumpool2(const bf16 *__restrict__ g, int C, bf16 *__restrict__ gd, int B,
                            int Ho, int Wo, int Cd) {
-  const int c8n = Cd / 8;
-  const long long n = static_cast<long long>(B) * Ho * Wo * c8n;
+  const int pd = Cd / 8, pc = C / 8;
+  const long long hwo = static_cast<long long>(Ho) * Wo, Wi = 2ll * Wo;
+  const long long n = static_cast<long long>(B) * pd * hwo;
   for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * kBlock) {
-    const int c8 = static_cast<int>(i % c8n);
-    const long long pix = i / c8n;
-    const int x = static_cast<int>(pix % Wo);
-    const long long r = pix / Wo;
-    const int y = static_cast<int>(r % Ho);
-    const int b = static_cast<int>(r / Ho);
-    const long long Wi = 2ll * Wo;
-    const bf16 *p = g + ((static_cast<long long>(b) * 2 * Ho + 2 * y) * Wi + 2 * x) * C + c8 * 8;
+    const long long bp = i / hwo, po = i - bp * hwo;
+    const int b = static_cast<int>(bp / pd), pl = static_cast<int>(bp - static_cast<long long>(b) * pd);
+    const int x = static_cast<int>(po % Wo), y = static_cast<int>(po / Wo);
+    const bf16 *p = g + plane_at(b, pl, 2ll * y * Wi + 2 * x, pc, 4 * hwo);
     float a[8], t[8];
     load8(p, a);
-    load8(p + C, t);
+    load8(p + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    load8(p + Wi * C, t);
+    load8(p + Wi * 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    load8(p + Wi * C + C, t);
+    load8(p + Wi * 8 + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    store8(gd + pix * Cd + c8 * 8, a);
+    store8(gd + i * 8, a);
   }
 }
 
-// gs = gcat[..., Cd:Cd+Cs] + (s > 0) * gp(up) / 4: the skip tensor's gradient
+// gs = gcat[:, Cd:Cd+Cs] + (s > 0) * gp(up) / 4: the skip tensor's gradient
 // from the decoder (already masked) plus the pooling path's, masked by ReLU
 __global__ void k_skipgrad(const bf16 *__restrict__ gcat, int C, int Cd,
                            const bf16 *__restrict__ s, const bf16 *__restrict__ gp,
                            bf16 *__restrict__ gs, int B, int H, int W, int Cs) {
-  const int c8n = Cs / 8;
-  const long long n = static_cast<long long>(B) * H * W * c8n;
+  const int ps = Cs / 8, pc = C / 8, pd = Cd / 8;
+  const long long hw = static_cast<long long>(H) * W;
+  const long long n = static_cast<long long>(B) * ps * hw;
   for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * kBlock) {
-    const int c = static_cast<int>(i % c8n) * 8;
-    const long long pix = i / c8n;
-    const int x = static_cast<int>(pix % W);
-    const long long r = pix / W;
-    const int y = static_cast<int>(r % H);
-    const int b = static_cast<int>(r / H);
-    const long long lp = (static_cast<long long>(b) * (H / 2) + y / 2) * (W / 2) + x / 2;
+    const long long bp = i / hw, pix = i - bp * hw;
+    const int b = static_cast<int>(bp / ps), j = static_cast<int>(bp - static_cast<long long>(b) * ps);
+    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
     float a[8], sv[8], pv[8];
-    load8(gcat + pix * C + Cd + c, a);
-    load8(s + pix * Cs + c, sv);
-    load8(gp + lp * Cs + c, pv);
+    load8(gcat + plane_at(b, pd + j, pix, pc, hw), a);
+    load8(s + i * 8, sv);
+    load8(gp + plane_at(b, j, static_cast<long long>(y / 2) * (W / 2) + x / 2, ps, hw / 4), pv);
 #pragma unroll
-    for (int j = 0; j < 8; j++)
-      if (sv[j] > 0.0f) a[j] += 0.25f * pv[j];
-    store8(gs + pix * Cs + c, a);
+    for (int k = 0; k < 8; k++)
+      if (sv[k] > 0.0f) a[k] += 0.25f * pv[k];
+    store8(gs + i * 8, a);
   }
 }
 
@@ -256,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ 
 #pragma unroll
     for (int j = 0; j < C; j += 8) {
       float t[8];
-      load8(x + i * C + j, t);
+      load8(x + plane_at(b, j / 8, pix, C / 8, hwn), t);
 #pragma unroll
       for (int k = 0; k < 8; k++) xv[j + k] = t[k];
     }
@@ -276,7 +265,7 @@ __global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ 
       float t[8];
 #pragma unroll
       for (int k = 0; k < 8; k++) t[k] = xv[j + k] > 0.0f ? dz * s_w[j + k] : 0.0f;
-      store8(gx + i * C + j, t);
+      store8(gx + plane_at(b, j / 8, pix, C / 8, hwn), t);
     }
 #pragma unroll
     for (int j = 0; j < C; j++) acc[j] += dz * xv[j];
@@ -329,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) k_head_apply(const bf16 *__restrict__ 
 #pragma unroll
       for (int j = 0; j < C; j += 8) {
         float t[8];
-        load8(x + i * C + j, t);
+        load8(x + plane_at(b, j / 8, pix, C / 8, hwn), t);
 #pragma unroll
         for (int k = 0; k < 8; k++) z += s_w[j + k] * t[k];
       }
@@ -339,31 +328,34 @@ __global__ void __launch_bounds__(kBlock) k_head_apply(const bf16 *__restrict__ 
   }
 }
 
-// db[c] += sum over pixels of g[p][c]
-__global__ void __launch_bounds__(kBlock) k_bias_grad(const bf16 *__restrict__ g, long long pixels,
-                                                      int C, float *__restrict__ db) {
-  __shared__ float s_acc[kBlock][8];
-  const int c8n = C / 8;
-  const int per = kBlock / c8n;  // pixels per block row
-  const int c8 = threadIdx.x % c8n, row = threadIdx.x / c8n;
+// db[8*pl + j] += sum over pixels of plane pl (blockIdx.y) of g
+__global__ void __launch_bounds__(kBlock) k_bias_grad(const bf16 *__restrict__ g, int B,
+                                                      long long hw, int planes,
+                                                      float *__restrict__ db) {
+  __shared__ float s_acc[kBlock / 32][8];
+  const int pl = blockIdx.y;
+  const long long n = static_cast<long long>(B) * hw;
   float a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (row < per) {
-    for (long long p = blockIdx.x * static_cast<long long>(per) + row; p < pixels;
-         p += static_cast<long long>(gridDim.x) * per) {
-      float t[8];
-      load8(g + p * C + c8 * 8, t);
+  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kBlock) {
+    const int b = static_cast<int>(i / hw);
+    float t[8];
+    load8(g + plane_at(b, pl, i - b * hw, planes, hw), t);
 #pragma unroll
-      for (int j = 0; j < 8; j++) a[j] += t[j];
-    }
+    for (int j = 0; j < 8; j++) a[j] += t[j];
   }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int j = 0; j < 8; j++) s_acc[threadIdx.x][j] = a[j];
+  for (int j = 0; j < 8; j++) {
+    float t = a[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) s_acc[warp][j] = t;
+  }
   __syncthreads();
-  if (threadIdx.x < C) {
-    const int cg = threadIdx.x / 8, j = threadIdx.x % 8;
+  if (threadIdx.x < 8) {
     float t = 0.0f;
-    for (int r = 0; r < per; r++) t += s_acc[r * c8n + cg][j];
-    atomicAdd(db + threadIdx.x, t);
+    for (int w = 0; w < kBlock / 32; w++) t += s_acc[w][threadIdx.x];
+    atomicAdd(db + pl * 8 + threadIdx.x, t);
   }
 }
 
@@ -561,12 +553,18 @@ cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView 
 
 cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s) {
   if (g.C % 8 || g.C > 256) return cudaErrorInvalidValue;
-  // at least 64 pixel rows per block, at most four blocks per SM
-  const long long per = kBlock / (g.C / 8);
-  int blocks = static_cast<int>((g.pixels() + 64 * per - 1) / (64 * per));
-  if (blocks > 152 * 4) blocks = 152 * 4;
-  if (blocks < 1) blocks = 1;
-  k_bias_grad<<<blocks, kBlock, 0, s>>>(g.p, g.pixels(), g.C, db);
+  // per plane, at least 64 pixels per thread, about four blocks per SM in all
+  const int planes = g.C / 8;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) sms = 1;
+  long long bx = (g.pixels() + 64ll * kBlock - 1) / (64ll * kBlock);
+  const long long cap = (4ll * sms + planes - 1) / planes;
+  if (bx > cap) bx = cap;
+  if (bx < 1) bx = 1;
+  k_bias_grad<<<dim3(static_cast<unsigned>(bx), planes), kBlock, 0, s>>>(
+      g.p, g.B, static_cast<long long>(g.H) * g.W, planes, db);
   return cudaGetLastError();
 }
 
