@@ -15,19 +15,22 @@
 //   convolution's zero padding. The tensor maps view a plane row as 2*W
 //   64-bit elements, so one box row is a whole 128-pixel row of a plane
 //   (2048 bytes: the TMA engine issues requests per box row, and rows of a
-//   plane of 8 channels alone would be 16 bytes each). A is K-major without swizzle (8 pixels of a
-//   plane = one 128-byte core matrix, planes = K chunks), the weights
-//   K-major with the box's swizzle (32-, 64- or 128-byte rows). The data
-//   gradient is the same kernel on the output gradient with flipped,
-//   transposed weights (launch_flip_weights).
-// Weight gradient (k_wgrad): dW^T[(tap,ci)][co] = sum over pixels p of
-//   X[p + off(tap)][ci] * dY[p][co]. K = pixels (128 per step), both operands
-//   MN-major without swizzle (8 channels of 8 pixels = one core matrix,
-//   planes 2048 bytes apart). The 128 M rows are chunks of (tap, channel
-//   block) stacked in shared memory plane after plane, so a 32-channel layer
-//   fills a tile with four taps. The pixel
-//   range is split across CTAs; each adds its FP32 partial sums with
-//   reductions into dW.
+//   plane of 8 channels alone would be 16 bytes each). A is K-major without
+//   swizzle (8 pixels of a plane = one 128-byte core matrix, planes = K
+//   chunks), the weights K-major with the box's swizzle (32-, 64- or
+//   128-byte rows). The data gradient is the same kernel on the output
+//   gradient with flipped, transposed weights (launch_flip_weights).
+// Weight gradient, K = pixels (128 per step), both operands MN-major
+//   without swizzle (8 channels of 8 pixels = one core matrix, planes 2048
+//   bytes apart); the pixel range is split across CTAs, each adding its
+//   FP32 partial sums into dW with reductions.
+//   k_wgrad_taps (up to 128 output and 256 input channels):
+//     dW[co][tap][ci] = sum over q of dY[q - off(tap)][co] * X[q][ci], M =
+//     (tap, co) -- each tap's dY planes fetched at its shifted coordinates --
+//     and N = ci.
+//   k_wgrad (the rest): dW^T[(tap,ci)][co] = sum over p of X[p + off(tap)][ci]
+//     * dY[p][co], M = chunks of (tap, channel block) stacked plane after
+//     plane, N = co.
 //
 // Warp roles: warp 0 lane 0 issues the TMA loads into a ring of stages
 // (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees each stage
@@ -269,6 +272,9 @@ constexpr int kMaxAccBufs = 4;      // accumulator buffers of a forward / data-g
 // the MMAs of the next tiles run while the epilogue drains earlier ones.
 __host__ __device__ constexpr uint32_t acc_cols(int bn) {
   return bn <= 32 ? 32 : bn <= 64 ? 64 : bn <= 128 ? 128 : 256;
+}
+__host__ __device__ constexpr uint32_t pow2_cols(uint32_t n) {
+  return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
 }
 __host__ __device__ constexpr int acc_bufs(int bn) {
   return static_cast<int>(512 / acc_cols(bn)) < kMaxAccBufs ? static_cast<int>(512 / acc_cols(bn))
@@ -840,69 +846,59 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// ------------------------------------------------ weight grad, planar ----
-// For images at least 128 pixels wide, 3x3 taps and at most 128 output
-// channels: M = output channels (dY, zero planes up to 128 rows), N = input
-// channels (X), K = 128 pixels of one image row per step. Both operands are
-// MN-major without swizzle: planes of 8 channels x pixels, 16 bytes per
-// pixel, so 8-pixel K groups are 128 bytes apart and a tap's shift dx is a
-// 16*dx byte offset into X's planes. A step loads dY's row once and the X
-// rows its taps need once (the swizzled form loads X once per tap and
-// chunk); each tap of the CTA's tap group accumulates in its own TMEM
-// columns. The zero planes of dY are cleared once and never loaded.
-constexpr int kYPlaneBytes = 128 * 16;
-
-struct WgradPlanarArgs {
-  int H, W, tiles_x, cin, cout, tap0, ntap, row0, nrows, cpt, stages, ksteps, kper;
-  int stage_bytes;
-  float *dw;
-  int *err;
-};
-
 __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
                "f"(d)
                : "memory");
 }
 
+// -------------------------------------------- weight grad, taps on M ----
+// dW[co][tap][ci] = sum over pixels q of dY[q - off(tap)][co] * X[q][ci]:
+// M = (tap of the CTA's tap group, co) (ntap*cout <= 128 rows), N = ci,
+// K = 128 pixels per step. Each tap's dY operand is its own TMA box taken at
+// the shifted coordinates (outside the image it reads zeros, where the
+// forward convolution's padding was), so the taps' planes stack at one
+// stride; X's planes are loaded once per step for every tap of the group.
+// Both operands MN-major without swizzle. Rows of M beyond the group's taps
+// hold whatever the stage held and are never read back.
+struct WgradTapsArgs {
+  int H, W, BW, BH, tiles_x, tiles_y, cin, cout, taps, per, stages, ksteps, kper;
+  float *dw;
+  int *err;
+};
+
 __global__ void __launch_bounds__(kWgradThreads, 1)
-    k_wgrad_planar(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmt,
-                   const __grid_constant__ CUtensorMap tmy,
-                   const WgradPlanarArgs a) {
+    k_wgrad_taps(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmy,
+                 const WgradTapsArgs a) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full, done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kPlane = kKPix * 16;  // one plane of 128 pixels
+  const int yp = a.cout / 8, xp = a.cin / 8;
+  const int a_bytes = 16 * kPlane;    // the 128 rows of M
+  const int stage_bytes = a_bytes + xp * kPlane;
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int yp = a.cout / 8, xp = a.cin / 8;  // loaded planes of dY and of each X row
-  const int rowb = xp * kPlaneStride;          // bytes of one staged X row
-  const uint32_t need = static_cast<uint32_t>(a.ntap * a.cpt);
-  const uint32_t cols = need <= 32 ? 32 : need <= 64 ? 64 : need <= 128 ? 128 : need <= 256 ? 256 : 512;
+  const uint32_t cols = pow2_cols(static_cast<uint32_t>(a.cin));
+  const int tap0 = blockIdx.x * a.per;
+  const int ntap = min(a.per, a.taps - tap0);
 
-  // dY's planes yp..15 stay zero in every stage (generic-proxy stores made
-  // visible to the tensor cores by the proxy fence below)
-  for (int st = 0; st < S; st++) {
-    uint4 *z = reinterpret_cast<uint4 *>(smem + st * a.stage_bytes + yp * kYPlaneBytes);
-    const int n16 = (16 - yp) * kYPlaneBytes / 16;
-    for (int i = threadIdx.x; i < n16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
-  }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < S; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+    for (int st = 0; st < S; st++) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
     }
     mbar_init(&acc_full, 1);
     mbar_init(&done, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tma_prefetch(&tmx);
-    tma_prefetch(&tmt);
     tma_prefetch(&tmy);
   }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 0) {
     tmem_alloc(&tmem_slot, cols);
     tmem_relinquish();
@@ -911,34 +907,32 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const int tiles_img = a.tiles_x * a.H;
-  const int k_lo = blockIdx.x * a.kper;
+  const int tiles_img = a.tiles_x * a.tiles_y;
+  const int k_lo = blockIdx.y * a.kper;
   const int k_hi = min(a.ksteps, k_lo + a.kper);
   const int nk = k_hi - k_lo;
 
   if (warp == 0) {
     // producer (the whole warp; one lane issues)
     int issued = 0;
-    const uint32_t tx = yp * kYPlaneBytes + a.nrows * xp * kPlaneBytes;
+    const uint32_t tx = static_cast<uint32_t>((ntap * yp + xp) * kPlane);
     for (int i = 0; i < nk; i++) {
-      const int s = i % S;
-      if (!mbar_wait_warp(&empty[s], ((i / S) & 1) ^ 1, &abort_flag, true)) {
+      const int st = i % S;
+      if (!mbar_wait_warp(&empty[st], ((i / S) & 1) ^ 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
       const int kt = k_lo + i;
       const int b = kt / tiles_img, t = kt - b * tiles_img;
-      const int y0 = t / a.tiles_x, x0 = (t % a.tiles_x) * 128;
-      unsigned char *sy = smem + s * a.stage_bytes;
-      unsigned char *sx = sy + 16 * kYPlaneBytes;
-      mbar_expect_tx_el(&full[s], tx);
-      tma_load_4d_el(sy, &tmy, &full[s], 2 * x0, y0, 0, b);
-      for (int r = 0; r < a.nrows; r++)
-        for (int pl = 0; pl < xp; pl++) {
-          unsigned char *d = sx + r * rowb + pl * kPlaneStride;
-          tma_load_4d_el(d, &tmx, &full[s], 2 * (x0 - 1), y0 + a.row0 + r - 1, pl, b);
-          tma_load_4d_el(d + 2048, &tmt, &full[s], 2 * (x0 + 127), y0 + a.row0 + r - 1, pl, b);
-        }
+      const int y0 = (t / a.tiles_x) * a.BH, x0 = (t % a.tiles_x) * a.BW;
+      unsigned char *sa = smem + st * stage_bytes;
+      mbar_expect_tx_el(&full[st], tx);
+      for (int j = 0; j < ntap; j++) {
+        const int tap = tap0 + j;
+        const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+        tma_load_4d_el(sa + j * yp * kPlane, &tmy, &full[st], 2 * (x0 - dx), y0 - dy, 0, b);
+      }
+      tma_load_4d_el(sa + a_bytes, &tmx, &full[st], 2 * x0, y0, 0, b);
       issued = i + 1;
     }
     for (int i = issued > S ? issued - S : 0; i < issued; i++)
@@ -950,52 +944,43 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
     // MMA issuer (the whole warp; one lane issues)
     const uint32_t idesc = idesc_bf16(a.cin, 1, 1);
     for (int i = 0; i < nk; i++) {
-      const int s = i % S;
-      if (!mbar_wait_warp(&full[s], (i / S) & 1, &abort_flag, true)) {
+      const int st = i % S;
+      if (!mbar_wait_warp(&full[st], (i / S) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
       }
       tc_fence_after();
-      const uint32_t sy = su32(smem + s * a.stage_bytes);
-      const uint32_t sx = sy + 16 * kYPlaneBytes;
-      // consecutive MMAs go to different taps' accumulators (independent)
+      const uint32_t sa = su32(smem + st * stage_bytes);
+      // MN-major, no swizzle: MN chunks (planes) kPlane apart, 8-pixel K
+      // groups 128 bytes apart; 16 pixels per MMA
+      const uint64_t da = smem_desc(sa, 128, kPlane, 0);
+      const uint64_t db = smem_desc(sa + a_bytes, 128, kPlane, 0);
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        // MN-major, no swizzle: MN chunks (planes) at the plane stride,
-        // 8-pixel K groups 128 bytes apart; 16 pixels per MMA
-        const uint64_t da = smem_desc(sy + 256 * k, 128, kYPlaneBytes, 0);
-        for (int j = 0; j < a.ntap; j++) {
-          const int tap = a.tap0 + j;
-          const int r = tap / 3 - a.row0, dx = tap % 3;
-          const uint64_t db = smem_desc(sx + r * rowb + 16 * dx + 256 * k, 128, kPlaneStride, 0);
-          umma_bf16_el(tmem + j * a.cpt, da, db, idesc, (i | k) != 0);
-        }
-      }
-      umma_commit_el(&empty[s]);
+      for (int k = 0; k < kKPix / 16; k++)
+        umma_bf16_el(tmem, da + 16 * k, db + 16 * k, idesc, (i | k) != 0);
+      umma_commit_el(&empty[st]);
     }
     umma_commit_el(&acc_full);
     umma_commit_el(&done);
     if (!mbar_wait_warp(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
   } else if (nk > 0) {
     const int q = warp & 3;
-    const int co = q * 32 + lane;
+    const int m = q * 32 + lane;
+    const int j = m / a.cout, co = m - j * a.cout;
     const bool ok = mbar_wait(&acc_full, 0, &abort_flag, true);
     if (!ok) sg_raise(a.err, &abort_flag, kSgTimeout);
     tc_fence_after();
     if (ok && !abort_flag) {
-      const long long kdim = 9ll * a.cin;
-      for (int j = 0; j < a.ntap; j++) {
-        float *dst = a.dw + co * kdim + (a.tap0 + j) * a.cin;
-        for (int c = 0; c < a.cin; c += 16) {
-          uint32_t v[16];
-          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + j * a.cpt + c, v);
-          tmem_ld_wait();
-          if (co < a.cout) {
+      float *dst = a.dw + (static_cast<long long>(co) * a.taps + tap0 + j) * a.cin;
+      for (int c = 0; c < a.cin; c += 16) {
+        uint32_t v[16];
+        tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + c, v);
+        tmem_ld_wait();
+        if (j < ntap) {
 #pragma unroll
-            for (int u = 0; u < 16; u += 4)
-              red_add_v4(dst + c + u, __uint_as_float(v[u]), __uint_as_float(v[u + 1]),
-                         __uint_as_float(v[u + 2]), __uint_as_float(v[u + 3]));
-          }
+          for (int u = 0; u < 16; u += 4)
+            red_add_v4(dst + c + u, __uint_as_float(v[u]), __uint_as_float(v[u + 1]),
+                       __uint_as_float(v[u + 2]), __uint_as_float(v[u + 3]));
         }
       }
     }
@@ -1192,34 +1177,6 @@ void split_pixels(WgradPlan &p, int ksteps) {
   p.splits = (ksteps + p.kper - 1) / p.kper;
 }
 
-// The planar weight gradient's tap groups: as many taps per CTA as their
-// accumulators fit in 512 TMEM columns and their X rows plus dY's 16 planes
-// fit two stages of shared memory; false when no grouping fits (the MMA's N
-// is the input channel count, at most 256).
-bool plan_planar_groups(WgradPlan &p) {
-  if (p.taps != 9 || p.W < kM || p.cout > kM || p.W % kM || p.cin > 256) return false;
-  const int cpt = (p.cin + 31) / 32 * 32;
-  const int per = 512 / cpt < 9 ? 512 / cpt : 9;
-  if (per < 1) return false;
-  p.ngroups = 0;
-  for (int t0 = 0; t0 < 9; t0 += per) {
-    const int nt = 9 - t0 < per ? 9 - t0 : per;
-    const int r0 = t0 / 3, r1 = (t0 + nt - 1) / 3;
-    const size_t stage = (16 * static_cast<size_t>(kYPlaneBytes) +
-                          static_cast<size_t>(r1 - r0 + 1) * (p.cin / 8) * kPlaneStride + 1023) &
-                         ~static_cast<size_t>(1023);
-    if (2 * stage > kSmemBudget) return false;
-    p.grp_tap0[p.ngroups] = t0;
-    p.grp_ntap[p.ngroups] = nt;
-    p.grp_row0[p.ngroups] = r0;
-    p.grp_nrows[p.ngroups] = r1 - r0 + 1;
-    p.grp_stage[p.ngroups] = static_cast<int>(stage);
-    p.ngroups++;
-  }
-  p.cpt = cpt;
-  return true;
-}
-
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
                        const char **why) {
   const char *dummy;
@@ -1255,13 +1212,29 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
   p.sms = sms;
   split_pixels(p, p.ksteps);
   p.dw = dw;
-  p.planar = plan_planar_groups(p) ? 1 : 0;
-  cudaError_t e = p.planar ? map_act(&p.tmx, x, 256, 1, 1)
-                           : map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, p.cwa / 8);
-  if (e == cudaSuccess && p.planar) e = map_act(&p.tmt, x, 4, 1, 1);
+  // taps on M for up to 128 output and 256 input channels (any pixel tile)
+  if (dy.C <= kM && x.C <= 256) {
+    const int g = kM / dy.C;                 // taps one 128-row tile holds
+    const int ng = (taps + g - 1) / g;
+    p.tap_per = (taps + ng - 1) / ng;        // balanced groups
+    p.ngroups = (taps + p.tap_per - 1) / p.tap_per;
+    const size_t stage = static_cast<size_t>(16 + x.C / 8) * kKPix * 16;
+    int St = static_cast<int>(kSmemBudget / stage);
+    if (St > kMaxStages) St = kMaxStages;
+    if (St >= 2) {
+      p.form = 2;
+      p.stages = St;
+      p.smem = St * stage + 1024;
+      cudaError_t e = map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, x.C / 8);
+      if (e != cudaSuccess) return *why = "tensor map (X)", e;
+      e = map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
+      if (e != cudaSuccess) return *why = "tensor map (dY)", e;
+      return cudaSuccess;
+    }
+  }
+  cudaError_t e = map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, p.cwa / 8);
   if (e != cudaSuccess) return *why = "tensor map (X)", e;
-  e = p.planar ? map_act(&p.tmy, dy, 2 * kM, 1, dy.C / 8)
-               : map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
+  e = map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
   if (e != cudaSuccess) return *why = "tensor map (dY)", e;
   return cudaSuccess;
 }
@@ -1360,50 +1333,42 @@ cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s, int nimg) {
   }
 }
 
-cudaError_t launch_wgrad_planar(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
+cudaError_t launch_wgrad_taps(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_wgrad_planar, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_wgrad_taps, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kSmemBudget + 1024));
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  const int ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
-  for (int g = 0; g < p.ngroups; g++) {
-    WgradPlanarArgs a{};
-    a.H = p.H;
-    a.W = p.W;
-    a.tiles_x = p.pt.tiles_x;
-    a.cin = p.cin;
-    a.cout = p.cout;
-    a.tap0 = p.grp_tap0[g];
-    a.ntap = p.grp_ntap[g];
-    a.row0 = p.grp_row0[g];
-    a.nrows = p.grp_nrows[g];
-    a.cpt = p.cpt;
-    a.stage_bytes = p.grp_stage[g];
-    int S = static_cast<int>(kSmemBudget / a.stage_bytes);
-    a.stages = S > kMaxStages ? kMaxStages : S;
-    a.ksteps = ksteps;
-    // about three CTAs per SM over the groups, each over >= 8 steps
-    int splits = (3 * p.sms + p.ngroups - 1) / p.ngroups;
-    if (splits > ksteps / 8) splits = ksteps / 8;
-    if (splits < 1) splits = 1;
-    a.kper = (ksteps + splits - 1) / splits;
-    splits = (ksteps + a.kper - 1) / a.kper;
-    a.dw = p.dw;
-    a.err = err;
-    const size_t smem = static_cast<size_t>(a.stages) * a.stage_bytes + 1024;
-    k_wgrad_planar<<<splits, kWgradThreads, smem, s>>>(p.tmx, p.tmt, p.tmy, a);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  WgradTapsArgs a{};
+  a.H = p.H;
+  a.W = p.W;
+  a.BW = p.pt.BW;
+  a.BH = p.pt.BH;
+  a.tiles_x = p.pt.tiles_x;
+  a.tiles_y = p.pt.tiles_y;
+  a.cin = p.cin;
+  a.cout = p.cout;
+  a.taps = p.taps;
+  a.per = p.tap_per;
+  a.stages = p.stages;
+  a.ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
+  // about three CTAs per SM over the tap groups, each over >= 8 steps
+  int splits = (3 * p.sms + p.ngroups - 1) / p.ngroups;
+  if (splits > a.ksteps / 8) splits = a.ksteps / 8;
+  if (splits < 1) splits = 1;
+  a.kper = (a.ksteps + splits - 1) / splits;
+  splits = (a.ksteps + a.kper - 1) / a.kper;
+  a.dw = p.dw;
+  a.err = err;
+  k_wgrad_taps<<<dim3(p.ngroups, splits), kWgradThreads, p.smem, s>>>(p.tmx, p.tmy, a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_wgrad(const WgradPlan &p, int *err, cudaStream_t s, int nimg) {
   if (p.mtiles <= 0 || nimg < 0 || nimg > p.B) return cudaErrorInvalidValue;
-  if (p.planar) return launch_wgrad_planar(p, err, s, nimg);
+  if (p.form == 2) return launch_wgrad_taps(p, err, s, nimg);
   switch (p.cwa) {
     case 64: return launch_wgrad_a<64>(p, err, s, nimg);
     case 32: return launch_wgrad_a<32>(p, err, s, nimg);

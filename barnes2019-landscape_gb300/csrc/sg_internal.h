@@ -78,23 +78,21 @@ struct ConvPlan {
 };
 
 // A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=
-// sum over pixels of dY[p][co] * X[p + off(tap)][ci].
+// sum over pixels of dY[p][co] * X[p + off(tap)][ci]; the taps-on-M kernel
+// (k_wgrad_taps) where it fits, else the (tap, ci)-on-M kernel (k_wgrad).
 struct WgradPlan {
   // X and dY planes viewed as 64-bit elements: X box {2*BW, BH, cwa/8, 1}
-  // (planar: {256, 1, 1, 1} from x0-1 with tmt's {4, 1, 1, 1} tail), dY box
-  // {2*BW, BH, cout/8, 1}
+  // (taps form: {2*BW, BH, cin/8, 1}), dY box {2*BW, BH, cout/8, 1}
   CUtensorMap tmx;
-  CUtensorMap tmt;
   CUtensorMap tmy;
   int B = 0, H = 0, W = 0, cin = 0, cout = 0, taps = 9, cwa = 0, cwb = 0, stages = 0;
   PixTile pt;
   int mtiles = 0, splits = 0, ksteps = 0, kper = 0, sms = 1;
   float *dw = nullptr;
   size_t smem = 0;
-  // planar form (wide images, 3x3, <= 128 output channels): tap groups of
-  // one launch each, every group's taps accumulating in cpt TMEM columns
-  int planar = 0, ngroups = 0, cpt = 0;
-  int grp_tap0[9] = {}, grp_ntap[9] = {}, grp_row0[9] = {}, grp_nrows[9] = {}, grp_stage[9] = {};
+  // taps-on-M form (form 2: at most 128 output and 256 input channels):
+  // ngroups groups of tap_per taps, one CTA row of the grid each
+  int form = 0, ngroups = 0, tap_per = 0;
 };
 
 // Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for
