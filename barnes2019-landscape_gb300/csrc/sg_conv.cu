@@ -860,10 +860,14 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 // forward convolution's padding was), so the taps' planes stack at one
 // stride; X's planes are loaded once per step for every tap of the group.
 // Both operands MN-major without swizzle. Rows of M beyond the group's taps
-// hold whatever the stage held and are never read back.
+// hold whatever the stage held and are never read back. With db, N has 16
+// more columns whose X planes hold ones (written once, never loaded): for
+// the centre tap (offset 0) they are the bias gradient sum over q of
+// dY[q][co].
 struct WgradTapsArgs {
   int H, W, BW, BH, tiles_x, tiles_y, cin, cout, taps, per, stages, ksteps, kper;
   float *dw;
+  float *db;  // or null
   int *err;
 };
 
@@ -879,12 +883,23 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   constexpr int kPlane = kKPix * 16;  // one plane of 128 pixels
   const int yp = a.cout / 8, xp = a.cin / 8;
   const int a_bytes = 16 * kPlane;    // the 128 rows of M
-  const int stage_bytes = a_bytes + xp * kPlane;
+  const int stage_bytes = a_bytes + (xp + (a.db ? 2 : 0)) * kPlane;
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t cols = pow2_cols(static_cast<uint32_t>(a.cin));
+  const int nb = a.cin + (a.db ? 16 : 0);  // N: input channels (+ the ones)
+  const uint32_t cols = pow2_cols(static_cast<uint32_t>(nb));
   const int tap0 = blockIdx.x * a.per;
   const int ntap = min(a.per, a.taps - tap0);
+  const int centre = a.taps == 9 ? 4 : 0;
+  if (a.db) {
+    // the ones planes of X (bf16 1.0 = 0x3F80) in every stage, made visible
+    // to the tensor cores by the proxy fence below
+    for (int st = 0; st < S; st++) {
+      uint4 *o = reinterpret_cast<uint4 *>(smem + st * stage_bytes + a_bytes + xp * kPlane);
+      for (int i = threadIdx.x; i < 2 * kPlane / 16; i += blockDim.x)
+        o[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+    }
+  }
 
   if (threadIdx.x == 0) {
     for (int st = 0; st < S; st++) {
@@ -895,10 +910,10 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
     mbar_init(&done, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tma_prefetch(&tmx);
     tma_prefetch(&tmy);
   }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == 0) {
     tmem_alloc(&tmem_slot, cols);
     tmem_relinquish();
@@ -942,7 +957,7 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
       }
   } else if (warp == 1) {
     // MMA issuer (the whole warp; one lane issues)
-    const uint32_t idesc = idesc_bf16(a.cin, 1, 1);
+    const uint32_t idesc = idesc_bf16(nb, 1, 1);
     for (int i = 0; i < nk; i++) {
       const int st = i % S;
       if (!mbar_wait_warp(&full[st], (i / S) & 1, &abort_flag, true)) {
@@ -982,6 +997,12 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
             red_add_v4(dst + c + u, __uint_as_float(v[u]), __uint_as_float(v[u + 1]),
                        __uint_as_float(v[u + 2]), __uint_as_float(v[u + 3]));
         }
+      }
+      if (a.db && tap0 <= centre && centre < tap0 + ntap) {
+        uint32_t v[16];
+        tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + a.cin, v);
+        tmem_ld_wait();
+        if (j == centre - tap0) red_add_f32(a.db + co, __uint_as_float(v[0]));
       }
     }
   }
@@ -1178,7 +1199,7 @@ void split_pixels(WgradPlan &p, int ksteps) {
 }
 
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
-                       const char **why) {
+                       const char **why, float *db) {
   const char *dummy;
   if (!why) why = &dummy;
   p = WgradPlan{};
@@ -1218,11 +1239,13 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
     const int ng = (taps + g - 1) / g;
     p.tap_per = (taps + ng - 1) / ng;        // balanced groups
     p.ngroups = (taps + p.tap_per - 1) / p.tap_per;
-    const size_t stage = static_cast<size_t>(16 + x.C / 8) * kKPix * 16;
+    const bool ones = db && x.C + 16 <= 256;  // the bias gradient rides along
+    const size_t stage = static_cast<size_t>(16 + x.C / 8 + (ones ? 2 : 0)) * kKPix * 16;
     int St = static_cast<int>(kSmemBudget / stage);
     if (St > kMaxStages) St = kMaxStages;
     if (St >= 2) {
       p.form = 2;
+      p.db = ones ? db : nullptr;
       p.stages = St;
       p.smem = St * stage + 1024;
       cudaError_t e = map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, x.C / 8);
@@ -1361,6 +1384,7 @@ cudaError_t launch_wgrad_taps(const WgradPlan &p, int *err, cudaStream_t s, int 
   a.kper = (a.ksteps + splits - 1) / splits;
   splits = (a.ksteps + a.kper - 1) / a.kper;
   a.dw = p.dw;
+  a.db = p.db;
   a.err = err;
   k_wgrad_taps<<<dim3(p.ngroups, splits), kWgradThreads, p.smem, s>>>(p.tmx, p.tmy, a);
   return cudaGetLastError();

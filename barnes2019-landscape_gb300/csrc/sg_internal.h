@@ -93,6 +93,7 @@ struct WgradPlan {
   // taps-on-M form (form 2: at most 128 output and 256 input channels):
   // ngroups groups of tap_per taps, one CTA row of the grid each
   int form = 0, ngroups = 0, tap_per = 0;
+  float *db = nullptr;  // taps form: bias gradient accumulated too (else null)
 };
 
 // Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for
@@ -101,8 +102,10 @@ struct WgradPlan {
 cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
                       const float *bias, int relu, const bf16 *mask, bf16 *out,
                       const char **why);
+// db (optional): where the bias gradient goes; the plan's db is non-null
+// when its launches accumulate it (else the caller sums it separately).
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,
-                       const char **why);
+                       const char **why, float *db = nullptr);
 // nimg > 0 runs the plan over the first nimg images only (the tensor maps
 // cover the plan's full batch).
 cudaError_t launch_conv(const ConvPlan &p, int *err, cudaStream_t s, int nimg = 0);

@@ -274,7 +274,7 @@ int build(fs_surrogate *s) {
     cudaError_t e = sg::plan_conv(L.fwd, *L.x, L.wf, L.taps, L.cout, s->p + L.b_off, 1, nullptr,
                                   L.y->p, &why);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d forward: %s", l, why);
-    e = sg::plan_wgrad(L.wgr, *L.x, *L.gy, L.taps, s->g + L.w_off, s->sms, &why);
+    e = sg::plan_wgrad(L.wgr, *L.x, *L.gy, L.taps, s->g + L.w_off, s->sms, &why, s->g + L.b_off);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d weight gradient: %s", l, why);
     if (L.gx) {
       e = sg::plan_conv(L.dgr, *L.gy, L.wd, L.taps, L.cin, nullptr, 0,
@@ -352,7 +352,7 @@ int backward(fs_surrogate *s, const sg::SampleView &v) {
   auto layer = [&](int l) -> cudaError_t {
     SgLayer &L = s->L[l];
     cudaError_t e = sg::launch_wgrad(L.wgr, s->d_err, st, n);
-    if (e == cudaSuccess) e = sg::launch_bias_grad(view(*L.gy, n), s->g + L.b_off, st);
+    if (e == cudaSuccess && !L.wgr.db) e = sg::launch_bias_grad(view(*L.gy, n), s->g + L.b_off, st);
     if (e == cudaSuccess && L.gx) e = sg::launch_conv(L.dgr, s->d_err, st, n);
     return e;
   };
