@@ -708,6 +708,247 @@ struct WgradArgs {
   int *err;
 };
 
+// ---------------------------------- forward / dgrad, channels on M ----
+// For images whose rows are multiples of 256 pixels, 3x3 taps and at most
+// 128 output channels: D[co][p] = sum over (dy, dx, ci) of W[co][tap][ci] *
+// X[y + dy - 1][p + dx - 1][ci]. M = output channels: the resident weight
+// tiles are the K-major A operand (their rows beyond the output channels
+// read whatever follows them in shared memory and are discarded); N = 256
+// pixels of one row: each K-block stages a row (dy) of cb channels as cb/8
+// planes of 258 pixels, and the taps dx read them from byte offset 16*dx
+// (K-major, no swizzle). The MMAs then run at N = 256 whatever the channel
+// count (with N = the channel count they cost about the same per
+// instruction at a fraction of the work). One TMEM lane holds one channel,
+// so the epilogue transposes each warp's 32 channels x 16 pixels through
+// shared memory into 8-channel planes before the stores. No mask: the plan
+// sends data gradients to k_conv_planar.
+//
+// Used where it measured faster than k_conv_planar: forward convolutions
+// (no mask) with at least 64 input channels, whose MMAs per tile outweigh
+// the epilogue (96 -> 32 channels at 512^2: 1.63 -> 0.99 ms at batch 32).
+// With fewer input channels the two are even; with the data gradient's
+// mask it is about 2x slower (the epilogue's mask loads stall it; TMEM
+// reads of more lanes to spread the work slow the MMAs instead).
+constexpr int kTN = 256;                                     // pixels per tile
+constexpr int kTPix = kTN + 2;                               // x0-1 .. x0+256
+constexpr int kTSlot = (kTPix * 16 + 127) & ~127;            // 4224: a staged plane row
+constexpr size_t kTSmem = 208 * 1024;                        // dynamic shared memory
+
+template <int CB>
+__global__ void __launch_bounds__(kConvThreads, 1)
+    k_conv_t(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmt,
+             const __grid_constant__ CUtensorMap tmb, const ConvArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], done, wfull;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  __shared__ float s_bias[kM];
+  __shared__ uint32_t s_tr[8][32][8];  // per epilogue warp: 32 channels x 16 pixels (bf16 pairs)
+  if (a.bias)
+    for (int i = threadIdx.x; i < a.bn; i += blockDim.x) s_bias[i] = a.bias[i];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kRow = CB * 2;
+  constexpr int kPlanes = CB / 8;
+  constexpr int kStageB = (kPlanes * kTSlot + 1023) & ~1023;
+  const int kch = a.cin / CB;
+  const int wbox = a.bn * kRow;  // one (tap, channel block) box of weights
+  const int wbytes = 9 * kch * wbox;
+  unsigned char *ring = smem + ((wbytes + 1023) & ~1023);
+  const int S = a.stages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr uint32_t cols = kTN;
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < S; st++) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
+    }
+    mbar_init(&done, 1);
+    mbar_init(&wfull, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma_prefetch(&tmp);
+    tma_prefetch(&tmt);
+    tma_prefetch(&tmb);
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, 2 * cols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int tiles_row = a.W / kTN;
+  const int tiles_img = tiles_row * a.H;
+  const int nkb = 3 * kch;  // (dy, channel block)
+  const int ntot_tiles = a.mtiles;
+
+  if (warp == 0) {
+    // producer (the whole warp; one lane issues)
+    mbar_expect_tx_el(&wfull, wbytes);
+    for (int tap = 0; tap < 9; tap++)
+      for (int cc = 0; cc < kch; cc++)
+        tma_load_2d_el(smem + (tap * kch + cc) * wbox, &tmb, &wfull, tap * a.cin + cc * CB, 0);
+    int kbg = 0;
+    bool stop = false;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x) {
+      const int b = t / tiles_img;
+      const int tt = t - b * tiles_img;
+      const int y0 = tt / tiles_row, x0 = (tt % tiles_row) * kTN;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int st = kbg % S;
+        if (!mbar_wait_warp(&empty[st], ((kbg / S) & 1) ^ 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
+          break;
+        }
+        const int dy = kb / kch, cc = kb - dy * kch;
+        unsigned char *sb = ring + st * kStageB;
+        mbar_expect_tx_el(&full[st], kPlanes * kTPix * 16);
+#pragma unroll
+        for (int pl = 0; pl < kPlanes; pl++) {
+          unsigned char *d = sb + pl * kTSlot;
+          const int yy = y0 + dy - 1, pp = cc * kPlanes + pl;
+          tma_load_4d_el(d, &tmp, &full[st], 2 * (x0 - 1), yy, pp, b);
+          tma_load_4d_el(d + 2048, &tmp, &full[st], 2 * (x0 + 127), yy, pp, b);
+          tma_load_4d_el(d + 4096, &tmt, &full[st], 2 * (x0 + 255), yy, pp, b);
+        }
+      }
+    }
+    for (int k = kbg > S ? kbg - S : 0; k < kbg; k++)
+      if (!mbar_wait_warp(&full[k % S], (k / S) & 1, &abort_flag, false)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+    if (!mbar_wait_warp(&wfull, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+  } else if (warp == 1) {
+    // MMA issuer (the whole warp; one lane issues)
+    const uint32_t idesc = idesc_bf16(kTN, 0, 0);
+    bool stop = !mbar_wait_warp(&wfull, 0, &abort_flag, true);
+    if (stop) sg_raise(a.err, &abort_flag, kSgTimeout);
+    tc_fence_after();
+    const uint32_t wbase = su32(smem);
+    int kbg = 0, it = 0;
+    for (int t = blockIdx.x; t < ntot_tiles && !stop; t += gridDim.x, it++) {
+      const int buf = it & 1;
+      if (!mbar_wait_warp(&acc_empty[buf], ((it >> 1) & 1) ^ 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + buf * cols;
+      for (int kb = 0; kb < nkb; kb++, kbg++) {
+        const int st = kbg % S;
+        if (!mbar_wait_warp(&full[st], (kbg / S) & 1, &abort_flag, true)) {
+          sg_raise(a.err, &abort_flag, kSgTimeout);
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const int dy = kb / kch, cc = kb - dy * kch;
+        const uint32_t sb = su32(ring + st * kStageB);
+#pragma unroll
+        for (int dx = 0; dx < 3; dx++) {
+          // A: the weight tile (K-major, swizzled rows of kRow bytes)
+          const uint32_t wa = wbase + ((3 * dy + dx) * kch + cc) * wbox;
+          const uint64_t da = smem_desc(wa, 16, 8 * kRow, swizzle_code(kRow));
+#pragma unroll
+          for (int k = 0; k < CB / 16; k++) {
+            // B: K-major, no swizzle: K chunks (planes) kTSlot apart, 8-pixel
+            // groups 128 bytes apart; 16 channels = two planes per MMA
+            const uint64_t db = smem_desc(sb + 16 * dx + 2 * k * kTSlot, kTSlot, 128, 0);
+            umma_bf16_el(d, da + 2 * k, db, idesc, (kb | dx | k) != 0);
+          }
+        }
+        umma_commit_el(&empty[st]);
+      }
+      if (!stop) umma_commit_el(&acc_full[buf]);
+    }
+    umma_commit_el(&done);
+    if (!mbar_wait_warp(&done, 0, &abort_flag, false)) sg_raise(a.err, &abort_flag, kSgTimeout);
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4)..+31 = channels; group
+    // (w-2)/4 takes every other tile of this CTA
+    const int q = warp & 3;
+    const int grp = (warp - 2) >> 2;
+    const int co = q * 32 + lane;
+    const int g = lane >> 3, kk = lane & 7;  // after the transpose: plane 4q+g, pixels 2kk, 2kk+1
+    const int cg = 4 * q + g;
+    const bool active = q * 32 < a.bn;
+    const bool writer = 8 * cg < a.bn;
+    uint32_t(*tr)[8] = s_tr[warp - 2];
+    const float bias = a.bias && co < a.bn ? s_bias[co] : 0.0f;
+    const long long hw = static_cast<long long>(a.H) * a.W;
+    for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
+         t += 2 * gridDim.x, it += 2) {
+      const int buf = it & 1;
+      const int b = t / tiles_img;
+      const int tt = t - b * tiles_img;
+      const int y0 = tt / tiles_row, x0 = (tt % tiles_row) * kTN;
+      const long long at = plane_at(b, writer ? cg : 0,
+                                    static_cast<long long>(y0) * a.W + x0 + 2 * kk, a.oplanes, hw);
+      if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
+        sg_raise(a.err, &abort_flag, kSgTimeout);
+        break;
+      }
+      tc_fence_after();
+      if (active) {
+        const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
+        for (int c = 0; c < kTN; c += 16) {
+          uint32_t v[16];
+          tmem_ld16(d + c, v);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 16; j += 2) {
+            float f0 = __uint_as_float(v[j]) + bias, f1 = __uint_as_float(v[j + 1]) + bias;
+            if (a.relu) {
+              f0 = fmaxf(f0, 0.0f);
+              f1 = fmaxf(f1, 0.0f);
+            }
+            tr[lane][j / 2] = pack_bf16(f0, f1);  // pixels c+j, c+j+1 of channel co
+          }
+          __syncwarp();
+          // pixels c+2kk and c+2kk+1, channels 8g .. 8g+7 of this quarter
+          uint32_t w[8];
+#pragma unroll
+          for (int ch = 0; ch < 8; ch++) w[ch] = tr[8 * g + ch][kk];
+          __syncwarp();
+          uint4 o0, o1;
+          o0.x = __byte_perm(w[0], w[1], 0x5410);
+          o0.y = __byte_perm(w[2], w[3], 0x5410);
+          o0.z = __byte_perm(w[4], w[5], 0x5410);
+          o0.w = __byte_perm(w[6], w[7], 0x5410);
+          o1.x = __byte_perm(w[0], w[1], 0x7632);
+          o1.y = __byte_perm(w[2], w[3], 0x7632);
+          o1.z = __byte_perm(w[4], w[5], 0x7632);
+          o1.w = __byte_perm(w[6], w[7], 0x7632);
+          if (writer) {
+            const long long o = at + 8ll * c;
+            *reinterpret_cast<uint4 *>(a.out + o) = o0;
+            *reinterpret_cast<uint4 *>(a.out + o + 8) = o1;
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * cols);
+  }
+}
+
 // --------------------------------------------------------- weight grad ----
 // CWA: channels per chunk of X (M side), CWB: per chunk of dY (N side).
 template <int CWA, int CWB>
@@ -1160,7 +1401,16 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
     const size_t wbytes = (static_cast<size_t>(9) * src.C * bn * 2 + 1023) & ~static_cast<size_t>(1023);
     const size_t stage_a = (static_cast<size_t>(p.cb / 8) * kPlaneStride + 1023) & ~static_cast<size_t>(1023);
     const size_t room = kPlanarSmem - 1024 - kGuardBytes;
-    if (taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room) {
+    const size_t stage_t = (static_cast<size_t>(p.cb / 8) * kTSlot + 1023) & ~static_cast<size_t>(1023);
+    const size_t room_t = kTSmem - 1024 - 16 * 1024;  // slack: the weight tiles' extra rows read into it
+    if (taps == 9 && src.W % kTN == 0 && bn == ntot && ntot <= kM && !mask && src.C >= 64 &&
+        wbytes + 2 * stage_t <= room_t) {
+      int St = static_cast<int>((room_t - wbytes) / stage_t);
+      if (St > kMaxStages) St = kMaxStages;
+      p.planar = 2;
+      p.stages = St;
+      p.smem = kTSmem;
+    } else if (taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room) {
       int Sp = static_cast<int>((room - wbytes) / stage_a);
       if (Sp > kMaxStages) Sp = kMaxStages;
       p.planar = 1;
@@ -1273,6 +1523,9 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_conv_planar<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(kPlanarSmem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_conv_t<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kTSmem));
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -1295,9 +1548,12 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   a.err = err;
   a.mtiles = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
   a.ntiles = p.grid_y;
+  if (p.planar == 2) a.mtiles = (nimg > 0 ? nimg : p.B) * p.H * (p.W / kTN);
   const int tiles = a.mtiles * a.ntiles;
   const int grid = tiles < p.sms ? tiles : p.sms;
-  if (p.planar)
+  if (p.planar == 2)
+    k_conv_t<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
+  else if (p.planar)
     k_conv_planar<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
   else
     k_conv<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);

@@ -74,7 +74,8 @@ struct ConvPlan {
   size_t smem = 0;
   int grid_x = 0, grid_y = 0;  // pixel tiles and N tiles
   int sms = 1;                 // persistent CTAs launched (at most one per SM)
-  int planar = 0;              // planar source staging with resident weights
+  int planar = 0;              // resident weights with row staging: 1 pixels on M (k_conv_planar),
+                               // 2 channels on M and 256 pixels on N (k_conv_t)
 };
 
 // A weight-gradient convolution prepared for launches: dW[co][tap][ci] +=

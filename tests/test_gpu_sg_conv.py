@@ -6,8 +6,10 @@ data-gradient outputs are rounded to BF16 (relative 2^-8 of the value) on
 top of FP32 accumulation (at most ~1e-6 of the sum of |terms|); the weight
 gradient stays FP32, compared at 2e-5 of the sum of |terms| per entry.
 Shapes cover every channel-block width (16, 32, 64), N tiles above 256, the
-narrow-image pixel tile (W < 128), 1x1 and 3x3 taps, zero padding at every
-border, bias, ReLU and the data gradient's mask."""
+narrow-image pixel tile (W < 128), rows of 256 and 512 pixels (forward
+convolutions of at least 64 input channels there put the output channels
+on M and 256 pixels on N), 1x1 and 3x3 taps, zero padding at every border,
+bias, ReLU and the data gradient's mask."""
 import numpy as np
 import pytest
 
@@ -34,6 +36,9 @@ SHAPES = [
     (2, 4, 128, 32, 32, 9),
     (1, 8, 64, 64, 64, 9),
     (2, 2, 256, 96, 32, 9),
+    (1, 3, 512, 32, 32, 9),
+    (1, 2, 256, 16, 48, 9),
+    (1, 2, 256, 64, 128, 9),
     (1, 4, 128, 128, 256, 9),
     (1, 2, 128, 64, 384, 9),
     (2, 16, 32, 32, 16, 1),
