@@ -53,6 +53,7 @@ ABI_SYMBOLS = [
     "fs_batch_autotune", "fs_batch_launch_config", "fs_batch_synchronize",
     "fs_autotune", "fs_launch_config",
     "fs_batch_use_cta_walk", "fs_batch_walk_mode",
+    "fs_batch_use_tma_staging", "fs_batch_tma_staging", "fs_use_tma_staging", "fs_tma_staging",
     "fs_batch_set_active", "fs_batch_analyze", "fs_batch_drainage_counts",
     "fs_batch_device_elevation", "fs_batch_stream",
     "fs_batch_get_params", "fs_batch_get_shape",
@@ -191,6 +192,10 @@ def library() -> C.CDLL:
     L.fs_batch_synchronize.argtypes = [vp]
     L.fs_batch_use_cta_walk.argtypes = [vp, C.c_int]
     L.fs_batch_walk_mode.argtypes = [vp, ip]
+    L.fs_batch_use_tma_staging.argtypes = [vp, C.c_int]
+    L.fs_batch_tma_staging.argtypes = [vp, ip]
+    L.fs_use_tma_staging.argtypes = [vp, C.c_int]
+    L.fs_tma_staging.argtypes = [vp, ip]
     L.fs_batch_set_active.argtypes = [vp, C.c_int, ip]
     L.fs_batch_analyze.argtypes = [vp]
     L.fs_batch_drainage_counts.argtypes = [vp, C.c_int, vp]
@@ -391,11 +396,18 @@ class FastScape_RBP:
         check(library().fs_use_int_sub(self._m, int(bool(on))))
 
     def launch_config(self):
-        o, e, g, i = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        o, e, g, i, t = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(library().fs_launch_config(self._m, C.byref(o), C.byref(e), C.byref(g),
                                          C.byref(i)))
+        check(library().fs_tma_staging(self._m, C.byref(t)))
         return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
-                "graph": bool(g.value), "erode_int_sub": bool(i.value)}
+                "graph": bool(g.value), "erode_int_sub": bool(i.value),
+                "receivers_tma": bool(t.value)}
+
+    def use_tma_staging(self, on: bool = True) -> None:
+        """The receiver filter stages its tiles by TMA instead of loads
+        (even widths); identical results."""
+        check(library().fs_use_tma_staging(self._m, int(bool(on))))
 
     def set_barrier_timeout(self, ms: float) -> None:
         check(library().fs_set_barrier_timeout(self._m, float(ms)))
@@ -524,9 +536,16 @@ class FastScapeBatch:
         check(library().fs_batch_launch_config(self._b, C.byref(o), C.byref(e), C.byref(g),
                                                C.byref(i)))
         check(library().fs_batch_walk_mode(self._b, C.byref(w)))
+        t = C.c_int()
+        check(library().fs_batch_tma_staging(self._b, C.byref(t)))
         return {"order_blocks_per_sm": o.value, "erode_blocks_per_sm": e.value,
                 "graph": bool(g.value), "erode_int_sub": bool(i.value),
-                "cta_walk": bool(w.value)}
+                "cta_walk": bool(w.value), "receivers_tma": bool(t.value)}
+
+    def use_tma_staging(self, on: bool = True) -> None:
+        """A single grid's receiver filter stages its tiles by TMA instead of
+        loads (even widths); identical results."""
+        check(library().fs_batch_use_tma_staging(self._b, int(bool(on))))
 
     def use_cta_walk(self, on: bool = True) -> None:
         """One CTA per realization walks its levels (block barriers only)

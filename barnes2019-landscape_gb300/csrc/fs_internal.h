@@ -10,6 +10,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace fs {
@@ -165,7 +166,11 @@ size_t walk_smem_bytes(int nreal);
 
 // Kernel launchers (fs_kernels.cu). All are asynchronous on `s`.
 cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s);
-cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s);
+// hmap: a single grid's elevation as a {W, H} map of 64-bit elements with
+// {36, 98} boxes (make_receiver_map): the filter stages its tiles by TMA.
+cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s,
+                                  const CUtensorMap *hmap = nullptr);
+bool make_receiver_map(CUtensorMap *m, const double *h, int W, int H);
 cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s);
 // The level walk: k_order with order_bps blocks per SM (2 or 3; each has
 // its own register budget), k_accum with accum_bps, then (when a.do_erode)

@@ -23,10 +23,12 @@
 // file is compiled with -fmad=false so no multiply-add is contracted, every
 // FP64 division is correctly rounded, and the additions and subtractions
 // done in integer arithmetic (fs_bits.h) give the bits of the FP64 ones.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <type_traits>
 
 #include "fastscape_gb300.h"
@@ -426,9 +428,54 @@ __global__ void __launch_bounds__(256) k_receivers_exact(StepArgs a) {
 constexpr int kRelEmin = 1030;  // |h| >= 128
 constexpr int kRelEmax = 1123;  // |h| < 2^101
 
-__global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
+// TMA staging of a single grid's tile (TMA variant): one box of FP64 values,
+// columns x0-2 .. x0+33 (the box's x must be even: 16-byte aligned) and rows
+// y0-1 .. y0+96, into shared memory; the staging then reads the values from
+// there (column offset 1) instead of loading them from global memory.
+constexpr int kRtW = kRxTile + 4, kRtH = kRyTile + 2;
+
+__device__ __forceinline__ uint32_t rf_smem(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Loads the box into dst with the transaction counted on bar (thread 0).
+__device__ __forceinline__ void rf_tma_tile(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                            int x, int y) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(rf_smem(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rf_smem(bar)),
+               "r"(static_cast<uint32_t>(kRtW * kRtH * 8))
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(rf_smem(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(rf_smem(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Waits for the box (phase 0 of bar); false after limit_ns.
+__device__ __forceinline__ bool rf_wait(uint64_t *bar, unsigned long long limit_ns) {
+  const unsigned long long t0 = globaltimer_ns();
+  for (int it = 0;; it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(rf_smem(bar))
+        : "memory");
+    if (ok) return true;
+    if ((it & 15) == 15 && globaltimer_ns() - t0 > limit_ns) return false;
+  }
+}
+
+template <bool TMA>
+__global__ void __launch_bounds__(256)
+    k_receivers_filter(const __grid_constant__ CUtensorMap hmap, StepArgs a) {
   if (stopped(a.ctl)) return;
   __shared__ float s[kRyTile + 2][kRxTile + 3];
+  __shared__ alignas(128) unsigned long long s64[TMA ? kRtH : 1][TMA ? kRtW : 1];
+  __shared__ uint64_t s_bar;
   __shared__ unsigned s_wmax[8];
   const Tile t = a.rtiles[blockIdx.x];
   const RealDesc &d = a.desc[t.r];
@@ -444,9 +491,18 @@ __global__ void __launch_bounds__(256) k_receivers_filter(StepArgs a) {
   constexpr int kSPer = (kSn + 255) / 256;  // staged values per thread
   // all of a thread's loads in flight before the first is used
   const int t0 = threadIdx.y * 32 + threadIdx.x;
+  if (TMA) {
+    if (t0 == 0) rf_tma_tile(&s64[0][0], &hmap, &s_bar, x0 - 1, y0);
+    __syncthreads();  // the barrier is initialised
+    if (!rf_wait(&s_bar, a.timeout_ns)) {
+      raise_err(a.ctl, FS_ERR_TIMEOUT, kPhaseNone);
+      return;
+    }
+  }
   auto load_value = [&](int tb, int k) -> unsigned long long {  // staged value tb + 256k
     const int i = tb + 256 * k;
     const int ly = i / kSw, lx = i - ly * kSw;
+    if (TMA) return i < kSn ? s64[ly][lx + 1] : 0ull;  // zero-filled outside the grid
     const int gx = x0 + lx, gy = y0 + ly;
     if (i < kSn && gx < W && gy < H)
       return __ldg(reinterpret_cast<const unsigned long long *>(h) + (gy * W + gx));
@@ -2143,13 +2199,45 @@ cudaError_t launch_receivers_exact(const StepArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s) {
+cudaError_t launch_receivers_fast(const StepArgs &a, cudaStream_t s, const CUtensorMap *hmap) {
   if (a.nrtiles == 0) return cudaSuccess;
-  k_receivers_filter<<<a.nrtiles, dim3(32, 8), 0, s>>>(a);
+  if (hmap) {
+    k_receivers_filter<true><<<a.nrtiles, dim3(32, 8), 0, s>>>(*hmap, a);
+  } else {
+    CUtensorMap none;
+    std::memset(&none, 0, sizeof(none));
+    k_receivers_filter<false><<<a.nrtiles, dim3(32, 8), 0, s>>>(none, a);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_receivers_fixup<<<8 * sm_count(), 256, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+bool make_receiver_map(CUtensorMap *m, const double *h, int W, int H) {
+  typedef CUresult (*Encode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                             const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                             const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                             CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode enc = nullptr;
+  if (!enc) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return false;
+    enc = reinterpret_cast<Encode>(fn);
+  }
+  // row stride a multiple of 16 bytes; the tiles' boxes start at even x
+  if (W % 2 || W < kRxTile + 4 || H < 5) return false;
+  const cuuint64_t dims[2] = {static_cast<cuuint64_t>(W), static_cast<cuuint64_t>(H)};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(W) * 8};
+  const cuuint32_t box[2] = {static_cast<cuuint32_t>(kRtW), static_cast<cuuint32_t>(kRtH)};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<double *>(h), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 cudaError_t launch_donors_level0(const StepArgs &a, cudaStream_t s) {

@@ -129,6 +129,10 @@ struct fs_batch {
   // resident CTAs per SM of its ordering and erosion kernels (by variant)
   bool cta_walk = false;
   int cta_occ_order = 1, cta_occ_erode[3] = {1, 1, 1};
+  // a single grid's receiver filter may stage its tiles by TMA (rmap_ok:
+  // the map exists; rtma: in use; the autotuner decides)
+  CUtensorMap rmap;
+  bool rmap_ok = false, rtma = false;
   unsigned long long timeout_ns = 2000000000ull;
   long long steps = 0;
   bool have_step = false;
@@ -292,6 +296,10 @@ fs::StepArgs step_args(const fs_batch *b, int do_erode) {
   return a;
 }
 
+const CUtensorMap *receiver_map(const fs_batch *b) {
+  return b->rtma && b->rmap_ok && b->n == 1 ? &b->rmap : nullptr;
+}
+
 // The per-realization walk runs when chosen and the launch covers more than
 // one realization (a single grid keeps the grid-wide walk).
 bool use_cta(const fs_batch *b, const fs::StepArgs &a) { return b->cta_walk && a.nreal > 1; }
@@ -313,7 +321,7 @@ cudaError_t launch_step(fs_batch *b, const fs::StepArgs &a) {
     e = cudaMemsetAsync(a.rctl, 0, sizeof(fs::RealCtl) * a.nreal, b->stream);
   if (e == cudaSuccess)
     e = b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
-                           : fs::launch_receivers_fast(a, b->stream);
+                           : fs::launch_receivers_fast(a, b->stream, receiver_map(b));
   if (e == cudaSuccess) e = fs::launch_donors_level0(a, b->stream);
   if (e == cudaSuccess) {
     if (use_cta(b, a)) {
@@ -352,7 +360,7 @@ int timed_step(fs_batch *b, const fs::StepArgs &a, int i) {
                           fs::kCtlResetBytes, b->stream));
   FS_CUDA(cudaMemsetAsync(a.rctl, 0, sizeof(fs::RealCtl) * a.nreal, b->stream));
   FS_CUDA(b->exact_receivers ? fs::launch_receivers_exact(a, b->stream)
-                             : fs::launch_receivers_fast(a, b->stream));
+                             : fs::launch_receivers_fast(a, b->stream, receiver_map(b)));
   FS_CUDA(cudaEventRecord(ev[1], b->stream));
   FS_CUDA(fs::launch_donors_level0(a, b->stream));
   FS_CUDA(cudaEventRecord(ev[2], b->stream));
@@ -862,6 +870,7 @@ fs_batch *batch_create(int n, const int *widths, const int *heights, const fs_pa
           "occupancy"))
     return fail(*status);
   if (occ < 1) return fail(set_error(FS_ERR_CUDA, "walk kernel cannot be resident"));
+  b->rmap_ok = n == 1 && fs::make_receiver_map(&b->rmap, b->h, b->W[0], b->H[0]);
   b->walk_occ = occ;
   b->walk_bps = std::min(occ, 2);
   if (!cu(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->cta_occ_order, fs::cta_order_ptr(),
@@ -1124,6 +1133,18 @@ int autotune(fs_batch *b, int probe, int *chosen) {
       best_isub = 1;
     }
   }
+  // a single grid: the receiver filter's tiles staged by TMA or by loads
+  bool best_rtma = false;
+  if (st == FS_OK && b->rmap_ok) {
+    float ms = 0;
+    b->rtma = true;
+    st = time_config(best_obps, best_bps, best_graph, best_isub, &ms);
+    if (st == FS_OK && ms < best) {
+      best = ms;
+      best_rtma = true;
+    }
+  }
+  b->rtma = best_rtma;
   // The per-realization walk is chosen by size, not by the probes: its
   // advantage (a block barrier per level instead of a grid barrier) grows with
   // the number of levels, which the probes, run on the batch's current state,
@@ -1471,6 +1492,32 @@ int fs_batch_walk_mode(const fs_batch *b, int *cta) {
   if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
   if (cta) *cta = b->cta_walk ? 1 : 0;
   return FS_OK;
+}
+
+int fs_batch_use_tma_staging(fs_batch *b, int enable) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (enable && !b->rmap_ok)
+    return set_error(FS_ERR_ARG, "TMA staging of the receiver filter needs a single grid of "
+                                 "even width");
+  b->rtma = enable != 0;
+  b->graph_dirty = true;
+  return FS_OK;
+}
+
+int fs_batch_tma_staging(const fs_batch *b, int *on) {
+  if (!b) return set_error(FS_ERR_ARG, "batch is NULL");
+  if (on) *on = b->rtma ? 1 : 0;
+  return FS_OK;
+}
+
+int fs_use_tma_staging(fs_model *m, int enable) {
+  FS_MODEL(m);
+  return fs_batch_use_tma_staging(m->b, enable);
+}
+
+int fs_tma_staging(const fs_model *m, int *on) {
+  FS_MODEL(m);
+  return fs_batch_tma_staging(m->b, on);
 }
 
 int fs_batch_set_active(fs_batch *b, int n, const int *idx) {

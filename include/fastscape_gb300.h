@@ -257,6 +257,16 @@ int fs_batch_synchronize(const fs_batch *b);
 int fs_batch_use_cta_walk(fs_batch *b, int enable);
 int fs_batch_walk_mode(const fs_batch *b, int *cta);
 
+/* Receiver filter staging of a single grid of even width: 1 = each tile's
+ * FP64 values arrive in shared memory by one TMA box (cp.async.bulk.tensor),
+ * 0 = by loads (default). Identical results; fs_batch_autotune picks by
+ * speed. FS_ERR_ARG when enabling it for a batch of more than one
+ * realization or an odd width. No reference counterpart. */
+int fs_batch_use_tma_staging(fs_batch *b, int enable);
+int fs_batch_tma_staging(const fs_batch *b, int *on);
+int fs_use_tma_staging(fs_model *m, int enable);
+int fs_tma_staging(const fs_model *m, int *on);
+
 /* Restricts the following fs_batch_step / fs_batch_run calls to the n
  * realizations listed in idx (distinct, in [0, number of realizations));
  * n = 0 (idx may be NULL) makes every realization active again. Inactive

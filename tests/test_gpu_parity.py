@@ -481,6 +481,51 @@ def test_receiver_filter_high_ground(pkg):
             assert np.array_equal(a.getH(), b.getH()), f"step {s}"
 
 
+@pytest.mark.parametrize("W,H", [(1000, 900), (902, 641)])
+def test_receiver_filter_tma_staging(pkg, W, H):
+    """The receiver filter's tiles staged by one TMA box (even widths)
+    give the same receivers, levels and elevations as staged by loads, bit
+    for bit, on the reference field and on high ground with negative
+    ground, subnormals and flats (the relative restaging reads the same
+    shared tile), with the grid's right and bottom edges cutting tiles."""
+    p = pkg.workload_params()
+    rng = np.random.default_rng(7)
+    h = relief(W, H, 4000.0, 1.0)
+    yy, xx = np.divmod(np.arange(W * H), W)
+    interior = (xx > 1) & (yy > 1) & (xx < W - 2) & (yy < H - 2)
+    a_neg = interior & (xx < 150) & (yy < 200)
+    h[a_neg] = -3000.0 + rng.uniform(0, 50, a_neg.sum())
+    a_tiny = interior & (xx >= 200) & (xx < 300) & (yy < 300) & (np.arange(W * H) % 7 == 0)
+    h[a_tiny] = rng.choice([0.0, -0.0, 1e-300, 5e-324], a_tiny.sum())
+    a_flat = interior & (xx >= 500) & (xx < 700) & (yy >= 300) & (yy < 400)
+    h[a_flat] = 5000.0
+    for init in (None, h):
+        with pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_REFERENCE, seed=3) as a, \
+                pkg.FastScape_RBP(W, H, params=p, init=pkg.INIT_REFERENCE, seed=3) as b:
+            b.use_tma_staging(True)
+            assert b.launch_config()["receivers_tma"]
+            if init is not None:
+                a.setH(init)
+                b.setH(init)
+            for s in range(4):
+                a.step(1)
+                b.step(1)
+                assert np.array_equal(a.receivers(), b.receivers()), f"step {s}"
+                assert np.array_equal(a.levels()[0], b.levels()[0]), f"step {s}"
+                assert np.array_equal(a.getH(), b.getH()), f"step {s}"
+
+
+def test_tma_staging_refused_where_it_does_not_apply(pkg):
+    """Odd widths and batches of several realizations keep the loads."""
+    p = pkg.workload_params()
+    with pkg.FastScape_RBP(301, 200, params=p, init=pkg.INIT_REFERENCE, seed=1) as m:
+        with pytest.raises(pkg.FastScapeError):
+            m.use_tma_staging(True)
+    with pkg.FastScapeBatch([64, 64], [64, 64], [p, p], init=pkg.INIT_PHILOX, seeds=[1, 2]) as b:
+        with pytest.raises(pkg.FastScapeError):
+            b.use_tma_staging(True)
+
+
 def valley(W, H):
     """V-shaped valley whose axis runs down to the base-level ring at y = 1:
     nearly every cell drains into the axis, so the axis cell next to base
