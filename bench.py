@@ -24,6 +24,15 @@ ordering, accumulation, uplift, erosion.
 the reference's own FastScape_RBP compiled from its sources (oracle/_ref)
 where that build exists, else the oracle's restatement of it.
 
+The default run's line also carries `ensemble_ragged` (the 256-member
+ragged ensemble, 200 timesteps) and `surrogate` (the learned surrogate's
+training throughput at 512^2, batch 32, and the judged surrogate ensemble
+against the plain batched method, 1024 x 512^2, 2000 timesteps, with the
+committed parameters), each with its own clocks; --no-extras drops them.
+Other workloads (--workload): ensemble, sweep, deep, refconst, surrogate
+(generation, training and the judged ensemble), conv (the surrogate's
+convolutions alone).
+
 Multi-GPU (torchrun): one independent replica per rank ("replicas only": a
 single grid does not shard); value = all ranks' cell-steps / max time.
 """
