@@ -62,6 +62,7 @@ constexpr int kMaxStages = 16;
 constexpr int kMaxBias = 512;                       // biased outputs of a forward conv
 constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
 constexpr size_t kPlanarSmem = 222 * 1024;          // planar form: weights + ring + guard (+ static)
+constexpr size_t kPairSmem = 104 * 1024;            // one of two CTAs per SM
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
 // ---------------------------------------------------------------- PTX ----
@@ -258,6 +259,7 @@ struct ConvArgs {
   const bf16 *mask;   // ntot channels, plane-major like out
   bf16 *out;
   int oplanes;        // planes per image of out and mask (ntot / 8)
+  int nbuf;           // TMEM accumulator buffers (k_conv, k_conv_planar)
   int *err;
 };
 
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t cols = acc_cols(a.bn);
-  const int nbuf = acc_bufs(a.bn);
+  const int nbuf = a.nbuf;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
@@ -527,7 +529,7 @@ constexpr int kPlaneBytes = kPlanePix * 16;                 // one staged plane 
 constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;    // 128-byte aligned TMA targets
 // A staged plane row is two TMA boxes: pixels x0-1 .. x0+126 (256 64-bit
 // elements, 2048 bytes) and the tail x0+127, x0+128 (4 elements).
-constexpr int kGuardBytes = 36 * 1024;  // slack after the ring: no descriptor reads past it
+constexpr int kGuardBytes = 4 * 1024;  // slack after the ring (the MMAs read inside each stage)
 
 template <int CB>
 __global__ void __launch_bounds__(kConvThreads, 1)
@@ -554,7 +556,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t cols = acc_cols(a.bn);
-  const int nbuf = acc_bufs(a.bn);
+  const int nbuf = a.nbuf;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; s++) {
@@ -1395,6 +1397,24 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
   if (S < 2) return *why = "stage does not fit shared memory", cudaErrorInvalidValue;
   p.stages = S;
   p.smem = S * stage + 1024;
+  p.cps = 1;
+  p.nbuf = acc_bufs(bn);
+  // Two CTAs per SM (two pipelines interleaving their waits) where each fits
+  // half the shared memory with a ring of at least three stages and half the
+  // TMEM with at least two accumulator buffers.
+  {
+    const int nb2 = static_cast<int>(256 / acc_cols(bn)) < kMaxAccBufs
+                        ? static_cast<int>(256 / acc_cols(bn)) : kMaxAccBufs;
+    int S2 = static_cast<int>((kPairSmem - 1024) / stage);
+    if (S2 > kMaxStages) S2 = kMaxStages;
+    if (S2 > nkb) S2 = nkb;
+    if (nb2 >= 2 && S2 >= 3) {
+      p.cps = 2;
+      p.nbuf = nb2;
+      p.stages = S2;
+      p.smem = S2 * stage + 1024;
+    }
+  }
   // the planar form: wide images, 3x3 taps, one N tile whose weights fit
   // beside a ring of at least two stages and the guard
   {
@@ -1410,12 +1430,26 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
       p.planar = 2;
       p.stages = St;
       p.smem = kTSmem;
+      p.cps = 1;
     } else if (taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room) {
       int Sp = static_cast<int>((room - wbytes) / stage_a);
       if (Sp > kMaxStages) Sp = kMaxStages;
       p.planar = 1;
       p.stages = Sp;
       p.smem = wbytes + Sp * stage_a + kGuardBytes + 1024;
+      p.cps = 1;
+      p.nbuf = acc_bufs(bn);
+      const int nb2 = static_cast<int>(256 / acc_cols(bn)) < kMaxAccBufs
+                          ? static_cast<int>(256 / acc_cols(bn)) : kMaxAccBufs;
+      const size_t room2 = kPairSmem - 1024 - kGuardBytes;
+      if (nb2 >= 2 && wbytes + 3 * stage_a <= room2) {
+        int S2 = static_cast<int>((room2 - wbytes) / stage_a);
+        if (S2 > kMaxStages) S2 = kMaxStages;
+        p.cps = 2;
+        p.nbuf = nb2;
+        p.stages = S2;
+        p.smem = wbytes + S2 * stage_a + kGuardBytes + 1024;
+      }
     }
   }
   p.bias = bias;
@@ -1498,6 +1532,10 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
       p.db = ones ? db : nullptr;
       p.stages = St;
       p.smem = St * stage + 1024;
+      if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {  // two CTAs per SM
+        p.stages = 2;
+        p.smem = 2 * stage + 1024;
+      }
       cudaError_t e = map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, x.C / 8);
       if (e != cudaSuccess) return *why = "tensor map (X)", e;
       e = map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
@@ -1545,12 +1583,13 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   a.mask = p.mask;
   a.out = p.out;
   a.oplanes = p.ntot / 8;
+  a.nbuf = p.nbuf;
   a.err = err;
   a.mtiles = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;
   a.ntiles = p.grid_y;
   if (p.planar == 2) a.mtiles = (nimg > 0 ? nimg : p.B) * p.H * (p.W / kTN);
   const int tiles = a.mtiles * a.ntiles;
-  const int grid = tiles < p.sms ? tiles : p.sms;
+  const int grid = tiles < p.cps * p.sms ? tiles : p.cps * p.sms;
   if (p.planar == 2)
     k_conv_t<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
   else if (p.planar)
