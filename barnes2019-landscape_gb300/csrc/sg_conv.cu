@@ -725,12 +725,13 @@ struct WgradArgs {
 // shared memory into 8-channel planes before the stores. No mask: the plan
 // sends data gradients to k_conv_planar.
 //
-// Used where it measured faster than k_conv_planar: forward convolutions
-// (no mask) with at least 64 input channels, whose MMAs per tile outweigh
-// the epilogue (96 -> 32 channels at 512^2: 1.63 -> 0.99 ms at batch 32).
-// With fewer input channels the two are even; with the data gradient's
-// mask it is about 2x slower (the epilogue's mask loads stall it; TMEM
-// reads of more lanes to spread the work slow the MMAs instead).
+// Used for forward convolutions (no mask) of at least 64 input channels
+// whose weights leave no room for two planar CTAs per SM (64 -> 64 channels
+// at 256^2: 0.20 against 0.24 ms at batch 32); where two planar CTAs fit,
+// they are as fast (96 -> 32 at 512^2: both ~0.97 ms, against 1.63 ms for
+// one planar CTA). With fewer input channels one CTA of each is even; with
+// the data gradient's mask it is about 2x slower (the epilogue's mask loads
+// stall it; TMEM reads of more lanes to spread the work slow the MMAs).
 constexpr int kTN = 256;                                     // pixels per tile
 constexpr int kTPix = kTN + 2;                               // x0-1 .. x0+256
 constexpr int kTSlot = (kTPix * 16 + 127) & ~127;            // 4224: a staged plane row
@@ -1423,15 +1424,22 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
     const size_t room = kPlanarSmem - 1024 - kGuardBytes;
     const size_t stage_t = (static_cast<size_t>(p.cb / 8) * kTSlot + 1023) & ~static_cast<size_t>(1023);
     const size_t room_t = kTSmem - 1024 - 16 * 1024;  // slack: the weight tiles' extra rows read into it
-    if (taps == 9 && src.W % kTN == 0 && bn == ntot && ntot <= kM && !mask && src.C >= 64 &&
-        wbytes + 2 * stage_t <= room_t) {
+    // the planar form with two CTAs per SM where it fits, else channels on M
+    // (k_conv_t) where it applies, else the planar form with one CTA per SM
+    const int nb2 = static_cast<int>(256 / acc_cols(bn)) < kMaxAccBufs
+                        ? static_cast<int>(256 / acc_cols(bn)) : kMaxAccBufs;
+    const size_t room2 = kPairSmem - 1024 - kGuardBytes;
+    const bool planar_ok = taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room;
+    const bool planar_pair = planar_ok && nb2 >= 2 && wbytes + 3 * stage_a <= room2;
+    if (!planar_pair && taps == 9 && src.W % kTN == 0 && bn == ntot && ntot <= kM && !mask &&
+        src.C >= 64 && wbytes + 2 * stage_t <= room_t) {
       int St = static_cast<int>((room_t - wbytes) / stage_t);
       if (St > kMaxStages) St = kMaxStages;
       p.planar = 2;
       p.stages = St;
       p.smem = kTSmem;
       p.cps = 1;
-    } else if (taps == 9 && src.W >= kM && bn == ntot && wbytes + 2 * stage_a <= room) {
+    } else if (planar_ok) {
       int Sp = static_cast<int>((room - wbytes) / stage_a);
       if (Sp > kMaxStages) Sp = kMaxStages;
       p.planar = 1;
@@ -1439,10 +1447,7 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
       p.smem = wbytes + Sp * stage_a + kGuardBytes + 1024;
       p.cps = 1;
       p.nbuf = acc_bufs(bn);
-      const int nb2 = static_cast<int>(256 / acc_cols(bn)) < kMaxAccBufs
-                          ? static_cast<int>(256 / acc_cols(bn)) : kMaxAccBufs;
-      const size_t room2 = kPairSmem - 1024 - kGuardBytes;
-      if (nb2 >= 2 && wbytes + 3 * stage_a <= room2) {
+      if (planar_pair) {
         int S2 = static_cast<int>((room2 - wbytes) / stage_a);
         if (S2 > kMaxStages) S2 = kMaxStages;
         p.cps = 2;

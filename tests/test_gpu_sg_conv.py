@@ -6,10 +6,11 @@ data-gradient outputs are rounded to BF16 (relative 2^-8 of the value) on
 top of FP32 accumulation (at most ~1e-6 of the sum of |terms|); the weight
 gradient stays FP32, compared at 2e-5 of the sum of |terms| per entry.
 Shapes cover every channel-block width (16, 32, 64), N tiles above 256, the
-narrow-image pixel tile (W < 128), rows of 256 and 512 pixels (forward
-convolutions of at least 64 input channels there put the output channels
-on M and 256 pixels on N), 1x1 and 3x3 taps, zero padding at every border,
-bias, ReLU and the data gradient's mask."""
+narrow-image pixel tile (W < 128), rows of 256 and 512 pixels (two planar
+CTAs per SM where their weights leave room, else -- forward, at least 64
+input channels -- the output channels on M and 256 pixels on N), 1x1 and
+3x3 taps, zero padding at every border, bias, ReLU and the data gradient's
+mask."""
 import numpy as np
 import pytest
 
