@@ -63,6 +63,7 @@ constexpr int kMaxBias = 512;                       // biased outputs of a forwa
 constexpr size_t kSmemBudget = 200 * 1024;          // stage ring (plus 1 KB alignment slack)
 constexpr size_t kPlanarSmem = 222 * 1024;          // planar form: weights + ring + guard (+ static)
 constexpr size_t kPairSmem = 104 * 1024;            // one of two CTAs per SM
+constexpr size_t kTripleSmem = 70 * 1024;           // one of three CTAs per SM (one epilogue group)
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
 // ---------------------------------------------------------------- PTX ----
@@ -267,7 +268,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps
+constexpr int kConvThreads = 320;   // producer warp, MMA warp, 8 epilogue warps (k_conv_t)
 constexpr int kMaxAccBufs = 4;      // accumulator buffers of a forward / data-gradient CTA
 
 // Accumulator columns of an N tile and the buffers TMEM's 512 columns hold:
@@ -356,8 +357,8 @@ __device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, cons
 // epilogue has read it), and the epilogue warps form two groups of four
 // that drain alternate tiles, so the epilogues of two tiles overlap each
 // other and the MMAs of the next ones.
-template <int CB>
-__global__ void __launch_bounds__(kConvThreads, 1)
+template <int CB, int NG>
+__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
     k_conv(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
            const ConvArgs a) {
   extern __shared__ unsigned char smem_raw[];
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
     for (int i = 0; i < nbuf; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
+      mbar_init(&acc_empty[i], 128);  // one epilogue group of four warps
     }
     mbar_init(&done, 1);
     abort_flag = 0;
@@ -484,7 +485,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     const int grp = (warp - 2) >> 2;
     const int r = q * 32 + lane;
     for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
-         t += 2 * gridDim.x, it += 2) {
+         t += NG * gridDim.x, it += NG) {
       const int buf = it % nbuf;
       if (!mbar_wait(&acc_full[buf], (it / nbuf) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
@@ -531,8 +532,8 @@ constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;    // 128-byte aligned 
 // elements, 2048 bytes) and the tail x0+127, x0+128 (4 elements).
 constexpr int kGuardBytes = 4 * 1024;  // slack after the ring (the MMAs read inside each stage)
 
-template <int CB>
-__global__ void __launch_bounds__(kConvThreads, 1)
+template <int CB, int NG>
+__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
     k_conv_planar(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmt,
                   const __grid_constant__ CUtensorMap tmb,
                   const ConvArgs a) {
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
     for (int i = 0; i < nbuf; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
+      mbar_init(&acc_empty[i], 128);  // one epilogue group of four warps
     }
     mbar_init(&done, 1);
     mbar_init(&wfull, 1);
@@ -675,7 +676,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     const int grp = (warp - 2) >> 2;
     const int r = q * 32 + lane;
     for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
-         t += 2 * gridDim.x, it += 2) {
+         t += NG * gridDim.x, it += NG) {
       const int buf = it % nbuf;
       if (!mbar_wait(&acc_full[buf], (it / nbuf) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
@@ -769,7 +770,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     }
     for (int i = 0; i < 2; i++) {
       mbar_init(&acc_full[i], 1);
-      mbar_init(&acc_empty[i], (kConvThreads - 64) / 2);  // one epilogue group
+      mbar_init(&acc_empty[i], 128);  // one epilogue group of four warps
     }
     mbar_init(&done, 1);
     mbar_init(&wfull, 1);
@@ -1415,6 +1416,17 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
       p.stages = S2;
       p.smem = S2 * stage + 1024;
     }
+    const int nb3 = static_cast<int>(128 / acc_cols(bn)) < kMaxAccBufs
+                        ? static_cast<int>(128 / acc_cols(bn)) : kMaxAccBufs;
+    int S3 = static_cast<int>((kTripleSmem - 1024) / stage);
+    if (S3 > kMaxStages) S3 = kMaxStages;
+    if (S3 > nkb) S3 = nkb;
+    if (nb3 >= 2 && S3 >= 3) {
+      p.cps = 3;
+      p.nbuf = nb3;
+      p.stages = S3;
+      p.smem = S3 * stage + 1024;
+    }
   }
   // the planar form: wide images, 3x3 taps, one N tile whose weights fit
   // beside a ring of at least two stages and the guard
@@ -1447,7 +1459,17 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
       p.smem = wbytes + Sp * stage_a + kGuardBytes + 1024;
       p.cps = 1;
       p.nbuf = acc_bufs(bn);
-      if (planar_pair) {
+      const int nb3 = static_cast<int>(128 / acc_cols(bn)) < kMaxAccBufs
+                          ? static_cast<int>(128 / acc_cols(bn)) : kMaxAccBufs;
+      const size_t room3 = kTripleSmem - 1024 - kGuardBytes;
+      if (nb3 >= 2 && wbytes + 3 * stage_a <= room3) {
+        int S3 = static_cast<int>((room3 - wbytes) / stage_a);
+        if (S3 > kMaxStages) S3 = kMaxStages;
+        p.cps = 3;
+        p.nbuf = nb3;
+        p.stages = S3;
+        p.smem = wbytes + S3 * stage_a + kGuardBytes + 1024;
+      } else if (planar_pair) {
         int S2 = static_cast<int>((room2 - wbytes) / stage_a);
         if (S2 > kMaxStages) S2 = kMaxStages;
         p.cps = 2;
@@ -1561,11 +1583,17 @@ template <int CB>
 cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_conv<CB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kSmemBudget + 1024));
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_conv_planar<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(k_conv<CB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kTripleSmem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_conv_planar<CB, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(kPlanarSmem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_conv_planar<CB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kTripleSmem));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_conv_t<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(kTSmem));
@@ -1597,10 +1625,14 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   const int grid = tiles < p.cps * p.sms ? tiles : p.cps * p.sms;
   if (p.planar == 2)
     k_conv_t<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
+  else if (p.planar && p.cps == 3)
+    k_conv_planar<CB, 1><<<grid, 64 + 128, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
   else if (p.planar)
-    k_conv_planar<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
+    k_conv_planar<CB, 2><<<grid, 64 + 256, p.smem, s>>>(p.tma, p.tmt, p.tmb, a);
+  else if (p.cps == 3)
+    k_conv<CB, 1><<<grid, 64 + 128, p.smem, s>>>(p.tma, p.tmb, a);
   else
-    k_conv<CB><<<grid, kConvThreads, p.smem, s>>>(p.tma, p.tmb, a);
+    k_conv<CB, 2><<<grid, 64 + 256, p.smem, s>>>(p.tma, p.tmb, a);
   return cudaGetLastError();
 }
 

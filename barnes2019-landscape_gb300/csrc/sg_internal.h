@@ -74,7 +74,7 @@ struct ConvPlan {
   size_t smem = 0;
   int grid_x = 0, grid_y = 0;  // pixel tiles and N tiles
   int sms = 1;                 // SMs of the device
-  int cps = 1;                 // persistent CTAs per SM (1 or 2)
+  int cps = 1;                 // persistent CTAs per SM (1, 2, or 3 with one epilogue group)
   int nbuf = 2;                // TMEM accumulator buffers per CTA
   int planar = 0;              // resident weights with row staging: 1 pixels on M (k_conv_planar),
                                // 2 channels on M and 256 pixels on N (k_conv_t)
