@@ -1111,6 +1111,7 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 // dY[q][co].
 struct WgradTapsArgs {
   int H, W, BW, BH, tiles_x, tiles_y, cin, cout, taps, per, stages, ksteps, kper;
+  int kpix;   // pixels per K step (128, or 64 where that lets two CTAs share an SM)
   float *dw;
   float *db;  // or null
   int *err;
@@ -1125,7 +1126,7 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
   __shared__ int abort_flag;
   unsigned char *smem = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  constexpr int kPlane = kKPix * 16;  // one plane of 128 pixels
+  const int kPlane = a.kpix * 16;     // one plane of a K step's pixels
   const int yp = a.cout / 8, xp = a.cin / 8;
   const int a_bytes = 16 * kPlane;    // the 128 rows of M
   const int stage_bytes = a_bytes + (xp + (a.db ? 2 : 0)) * kPlane;
@@ -1215,8 +1216,7 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
       // groups 128 bytes apart; 16 pixels per MMA
       const uint64_t da = smem_desc(sa, 128, kPlane, 0);
       const uint64_t db = smem_desc(sa + a_bytes, 128, kPlane, 0);
-#pragma unroll
-      for (int k = 0; k < kKPix / 16; k++)
+      for (int k = 0; k < a.kpix / 16; k++)
         umma_bf16_el(tmem, da + 16 * k, db + 16 * k, idesc, (i | k) != 0);
       umma_commit_el(&empty[st]);
     }
@@ -1554,21 +1554,41 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
     p.tap_per = (taps + ng - 1) / ng;        // balanced groups
     p.ngroups = (taps + p.tap_per - 1) / p.tap_per;
     const bool ones = db && x.C + 16 <= 256;  // the bias gradient rides along
-    const size_t stage = static_cast<size_t>(16 + x.C / 8 + (ones ? 2 : 0)) * kKPix * 16;
+    const size_t planes = 16 + x.C / 8 + (ones ? 2 : 0);  // per stage
+    const size_t stage = planes * kKPix * 16;
     int St = static_cast<int>(kSmemBudget / stage);
     if (St > kMaxStages) St = kMaxStages;
     if (St >= 2) {
       p.form = 2;
       p.db = ones ? db : nullptr;
+      p.kpix = kKPix;
       p.stages = St;
       p.smem = St * stage + 1024;
-      if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {  // two CTAs per SM
+      // two CTAs per SM: two stages of 128-pixel steps where they fit, else
+      // for one-tap groups 64-pixel steps (planes of half the bytes) with at
+      // least three stages (128 -> 128 channels: 0.22 -> 0.17 ms; with three
+      // taps a step of four MMAs waits on four copies, 0.77 -> 1.00 ms)
+      const size_t half = planes * 64 * 16;
+      if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {
         p.stages = 2;
         p.smem = 2 * stage + 1024;
+      } else if (p.tap_per == 1 && 3 * half + 1024 <= kPairSmem && x.W >= 64 && x.W % 64 == 0) {
+        int S2 = static_cast<int>((kPairSmem - 1024) / half);
+        if (S2 > kMaxStages) S2 = kMaxStages;
+        p.kpix = 64;
+        p.stages = S2;
+        p.smem = S2 * half + 1024;
       }
-      cudaError_t e = map_act(&p.tmx, x, 2 * p.pt.BW, p.pt.BH, x.C / 8);
+      p.tpt = p.pt;
+      if (p.kpix == 64) {
+        p.tpt.BW = 64;
+        p.tpt.BH = 1;
+        p.tpt.tiles_x = x.W / 64;
+        p.tpt.tiles_y = x.H;
+      }
+      cudaError_t e = map_act(&p.tmx, x, 2 * p.tpt.BW, p.tpt.BH, x.C / 8);
       if (e != cudaSuccess) return *why = "tensor map (X)", e;
-      e = map_act(&p.tmy, dy, 2 * p.pt.BW, p.pt.BH, dy.C / 8);
+      e = map_act(&p.tmy, dy, 2 * p.tpt.BW, p.tpt.BH, dy.C / 8);
       if (e != cudaSuccess) return *why = "tensor map (dY)", e;
       return cudaSuccess;
     }
@@ -1702,16 +1722,17 @@ cudaError_t launch_wgrad_taps(const WgradPlan &p, int *err, cudaStream_t s, int 
   WgradTapsArgs a{};
   a.H = p.H;
   a.W = p.W;
-  a.BW = p.pt.BW;
-  a.BH = p.pt.BH;
-  a.tiles_x = p.pt.tiles_x;
-  a.tiles_y = p.pt.tiles_y;
+  a.BW = p.tpt.BW;
+  a.BH = p.tpt.BH;
+  a.tiles_x = p.tpt.tiles_x;
+  a.tiles_y = p.tpt.tiles_y;
   a.cin = p.cin;
   a.cout = p.cout;
   a.taps = p.taps;
   a.per = p.tap_per;
   a.stages = p.stages;
-  a.ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
+  a.kpix = p.kpix;
+  a.ksteps = (nimg > 0 ? nimg : p.B) * p.tpt.tiles_x * p.tpt.tiles_y;
   // about three CTAs per SM over the tap groups, each over >= 8 steps
   int splits = (3 * p.sms + p.ngroups - 1) / p.ngroups;
   if (splits > a.ksteps / 8) splits = a.ksteps / 8;

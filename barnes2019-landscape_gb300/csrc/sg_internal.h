@@ -96,6 +96,8 @@ struct WgradPlan {
   // taps-on-M form (form 2: at most 128 output and 256 input channels):
   // ngroups groups of tap_per taps, one CTA row of the grid each
   int form = 0, ngroups = 0, tap_per = 0;
+  int kpix = 128;  // taps form: pixels per K step, and their tile
+  PixTile tpt;
   float *db = nullptr;  // taps form: bias gradient accumulated too (else null)
 };
 
