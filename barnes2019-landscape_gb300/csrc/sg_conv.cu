@@ -20,10 +20,11 @@
 //   chunks), the weights K-major with the box's swizzle (32-, 64- or
 //   128-byte rows). The data gradient is the same kernel on the output
 //   gradient with flipped, transposed weights (launch_flip_weights).
-// Weight gradient, K = pixels (128 per step), both operands MN-major
-//   without swizzle (8 channels of 8 pixels = one core matrix, planes 2048
-//   bytes apart); the pixel range is split across CTAs, each adding its
-//   FP32 partial sums into dW with reductions.
+// Forward, channels on M (k_conv_t): see there.
+// Weight gradient, K = pixels (128 per step, or 64), both operands MN-major
+//   without swizzle (8 channels of 8 pixels = one core matrix, planes one
+//   step's pixels apart); the pixel range is split across CTAs, each adding
+//   its FP32 partial sums into dW with reductions.
 //   k_wgrad_taps (up to 128 output and 256 input channels):
 //     dW[co][tap][ci] = sum over q of dY[q - off(tap)][co] * X[q][ci], M =
 //     (tap, co) -- each tap's dY planes fetched at its shifted coordinates --
@@ -32,16 +33,18 @@
 //     * dY[p][co], M = chunks of (tap, channel block) stacked plane after
 //     plane, N = co.
 //
-// Warp roles: warp 0 lane 0 issues the TMA loads into a ring of stages
-// (full/empty mbarriers), warp 1 lane 0 issues the MMAs and frees each stage
-// with tcgen05.commit, and the epilogue warps that follow (eight for the
-// forward / data-gradient kernels, in two groups of four that take
-// alternate tiles; four for the weight gradient) read the accumulator back,
-// warp w from TMEM lanes 32*(w%4)..+31 (its pixels, or its (tap, ci) rows).
-// Every
-// mbarrier wait is bounded (1 s of the global timer): on expiry the CTA sets
-// the error word, stops issuing, waits (again bounded) for its own copies
-// and MMAs in flight, frees its TMEM and returns.
+// Warp roles: warp 0 issues the TMA loads into a ring of stages
+// (full/empty mbarriers), warp 1 issues the MMAs and frees each stage with
+// tcgen05.commit -- both run their loops with every lane and issue through
+// elect.sync -- and the epilogue warps that follow read the accumulator
+// back, warp w from TMEM lanes 32*(w%4)..+31 (its pixels, or its rows):
+// for the forward / data-gradient kernels NG groups of four warps that take
+// every NG-th tile (NG = 2, or 1 when three CTAs share an SM), four for the
+// weight gradient. CTAs are persistent; one, two or three share an SM
+// (ConvPlan::cps), their pipelines hiding each other's waits.
+// Every mbarrier wait is bounded (1 s of the global timer): on expiry the
+// CTA sets the error word, stops issuing, waits (again bounded) for its own
+// copies and MMAs in flight, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
