@@ -49,6 +49,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -1131,7 +1132,12 @@ __global__ void __launch_bounds__(kWgradThreads, 1)
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   const int kPlane = a.kpix * 16;     // one plane of a K step's pixels
   const int yp = a.cout / 8, xp = a.cin / 8;
-  const int a_bytes = 16 * kPlane;    // the 128 rows of M
+  // M's planes: the group's taps' dY planes; the MMA reads 16 planes (128
+  // rows) from the stage's start, the rows beyond the taps reading the X
+  // planes that follow (discarded), so the region is at least 16 planes
+  // less X's
+  const int a_planes = max(a.per * yp, 16 - xp - (a.db ? 2 : 0));
+  const int a_bytes = a_planes * kPlane;
   const int stage_bytes = a_bytes + (xp + (a.db ? 2 : 0)) * kPlane;
   const int S = a.stages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1557,7 +1563,8 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
     p.tap_per = (taps + ng - 1) / ng;        // balanced groups
     p.ngroups = (taps + p.tap_per - 1) / p.tap_per;
     const bool ones = db && x.C + 16 <= 256;  // the bias gradient rides along
-    const size_t planes = 16 + x.C / 8 + (ones ? 2 : 0);  // per stage
+    const int a_planes = std::max(p.tap_per * dy.C / 8, 16 - x.C / 8 - (ones ? 2 : 0));
+    const size_t planes = a_planes + x.C / 8 + (ones ? 2 : 0);  // per stage (>= 16)
     const size_t stage = planes * kKPix * 16;
     int St = static_cast<int>(kSmemBudget / stage);
     if (St > kMaxStages) St = kMaxStages;
@@ -1572,7 +1579,12 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
       // least three stages (128 -> 128 channels: 0.22 -> 0.17 ms; with three
       // taps a step of four MMAs waits on four copies, 0.77 -> 1.00 ms)
       const size_t half = planes * 64 * 16;
-      if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {
+      const uint32_t cols = pow2_cols(static_cast<uint32_t>(x.C + (ones ? 16 : 0)));
+      // three CTAs per SM (static shared memory 288 bytes: 74 KB each fit)
+      if (2 * stage + 1024 <= 74 * 1024 && cols <= 128) {
+        p.stages = 2;
+        p.smem = 2 * stage + 1024;
+      } else if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {
         p.stages = 2;
         p.smem = 2 * stage + 1024;
       } else if (p.tap_per == 1 && 3 * half + 1024 <= kPairSmem && x.W >= 64 && x.W % 64 == 0) {
