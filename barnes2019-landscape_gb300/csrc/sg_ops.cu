@@ -36,6 +36,13 @@ __device__ __forceinline__ void store8(bf16 *p, const float (&f)[8]) {
   *reinterpret_cast<uint4 *>(p) = v;
 }
 
+// Index arithmetic of the network kernels is 32-bit: their launchers refuse
+// tensors of 2^31 or more 16-byte groups (a batch of 32 planes of 512^2 has
+// 2^23 pixels).
+constexpr long long kMaxGroups = 1ll << 31;
+
+bool fits32(long long n) { return n >= 0 && n < kMaxGroups; }
+
 int blocks_for(long long n) {
   long long b = (n + kBlock - 1) / kBlock;
   if (b > 152 * 16) b = 152 * 16;
@@ -60,13 +67,13 @@ __device__ __forceinline__ float count_plane(uint32_t c) {
 // pipe; -fmad=false keeps every operation separately rounded).
 __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__restrict__ yt, int W,
                         int H) {
-  const long long hw = static_cast<long long>(W) * H;
-  const long long n = hw * v.n;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
+  const unsigned hw = static_cast<unsigned>(W) * static_cast<unsigned>(H);
+  const unsigned n = hw * static_cast<unsigned>(v.n);
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
     const int b = static_cast<int>(i / hw);
-    const long long pix = i - b * hw;
-    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+    const unsigned pix = i - static_cast<unsigned>(b) * hw;
+    const int y = static_cast<int>(pix / static_cast<unsigned>(W));
+    const int x = static_cast<int>(pix - static_cast<unsigned>(y) * static_cast<unsigned>(W));
     const int src = v.idx ? v.idx[b] : b;
     const SampleMeta m = v.meta[src];
     const float h = field_at(v, src, hw, pix);
@@ -117,13 +124,14 @@ __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__rest
 // out = 2x2 average of in; i runs over (image, plane) pairs and pixels of out
 __global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, int B, int Ho,
                            int Wo, int C) {
-  const long long hwo = static_cast<long long>(Ho) * Wo, Wi = 2ll * Wo;
-  const long long n = static_cast<long long>(B) * (C / 8) * hwo;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
-    const long long bp = i / hwo, po = i - bp * hwo;
-    const int x = static_cast<int>(po % Wo), y = static_cast<int>(po / Wo);
-    const bf16 *p = in + (bp * 4 * hwo + 2ll * y * Wi + 2 * x) * 8;
+  const unsigned hwo = static_cast<unsigned>(Ho) * static_cast<unsigned>(Wo);
+  const long long Wi = 2ll * Wo;
+  const unsigned n = static_cast<unsigned>(B) * (C / 8) * hwo;
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+    const unsigned bp = i / hwo, po = i - bp * hwo;
+    const int y = static_cast<int>(po / static_cast<unsigned>(Wo));
+    const int x = static_cast<int>(po - static_cast<unsigned>(y) * static_cast<unsigned>(Wo));
+    const bf16 *p = in + (static_cast<long long>(bp) * 4 * hwo + 2ll * y * Wi + 2 * x) * 8;
     float a[8], t[8];
     load8(p, a);
     load8(p + 8, t);
@@ -135,7 +143,7 @@ __global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, 
     load8(p + Wi * 8 + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] = 0.25f * (a[j] + t[j]);
-    store8(out + i * 8, a);
+    store8(out + static_cast<long long>(i) * 8, a);
   }
 }
 
@@ -143,21 +151,22 @@ __global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, 
 __global__ void k_upcat(const bf16 *__restrict__ d, const bf16 *__restrict__ s,
                         bf16 *__restrict__ cat, int B, int H, int W, int Cd, int Cs) {
   const int pd = Cd / 8, ps = Cs / 8, pc = pd + ps;
-  const long long hw = static_cast<long long>(H) * W;
-  const long long n = static_cast<long long>(B) * pc * hw;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
-    const long long bp = i / hw, pix = i - bp * hw;
-    const int b = static_cast<int>(bp / pc), pl = static_cast<int>(bp - static_cast<long long>(b) * pc);
+  const unsigned hw = static_cast<unsigned>(H) * static_cast<unsigned>(W);
+  const unsigned n = static_cast<unsigned>(B) * pc * hw;
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+    const unsigned bp = i / hw, pix = i - bp * hw;
+    const int b = static_cast<int>(bp / static_cast<unsigned>(pc));
+    const int pl = static_cast<int>(bp - static_cast<unsigned>(b) * pc);
     uint4 v;
     if (pl < pd) {
-      const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+      const int y = static_cast<int>(pix / static_cast<unsigned>(W));
+      const int x = static_cast<int>(pix - static_cast<unsigned>(y) * static_cast<unsigned>(W));
       v = *reinterpret_cast<const uint4 *>(
           d + plane_at(b, pl, static_cast<long long>(y / 2) * (W / 2) + x / 2, pd, hw / 4));
     } else {
       v = *reinterpret_cast<const uint4 *>(s + plane_at(b, pl - pd, pix, ps, hw));
     }
-    *reinterpret_cast<uint4 *>(cat + i * 8) = v;
+    *reinterpret_cast<uint4 *>(cat + static_cast<long long>(i) * 8) = v;
   }
 }
 
@@ -166,13 +175,15 @@ __global__ void k_upcat(const bf16 *__restrict__ d, const bf16 *__restrict__ s,
 __global__ void k_sumpool2(const bf16 *__restrict__ g, int C, bf16 *__restrict__ gd, int B,
                            int Ho, int Wo, int Cd) {
   const int pd = Cd / 8, pc = C / 8;
-  const long long hwo = static_cast<long long>(Ho) * Wo, Wi = 2ll * Wo;
-  const long long n = static_cast<long long>(B) * pd * hwo;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
-    const long long bp = i / hwo, po = i - bp * hwo;
-    const int b = static_cast<int>(bp / pd), pl = static_cast<int>(bp - static_cast<long long>(b) * pd);
-    const int x = static_cast<int>(po % Wo), y = static_cast<int>(po / Wo);
+  const unsigned hwo = static_cast<unsigned>(Ho) * static_cast<unsigned>(Wo);
+  const long long Wi = 2ll * Wo;
+  const unsigned n = static_cast<unsigned>(B) * pd * hwo;
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+    const unsigned bp = i / hwo, po = i - bp * hwo;
+    const int b = static_cast<int>(bp / static_cast<unsigned>(pd));
+    const int pl = static_cast<int>(bp - static_cast<unsigned>(b) * pd);
+    const int y = static_cast<int>(po / static_cast<unsigned>(Wo));
+    const int x = static_cast<int>(po - static_cast<unsigned>(y) * static_cast<unsigned>(Wo));
     const bf16 *p = g + plane_at(b, pl, 2ll * y * Wi + 2 * x, pc, 4 * hwo);
     float a[8], t[8];
     load8(p, a);
@@ -185,7 +196,7 @@ __global__ void k_sumpool2(const bf16 *__restrict__ g, int C, bf16 *__restrict__
     load8(p + Wi * 8 + 8, t);
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] += t[j];
-    store8(gd + i * 8, a);
+    store8(gd + static_cast<long long>(i) * 8, a);
   }
 }
 
@@ -195,21 +206,22 @@ __global__ void k_skipgrad(const bf16 *__restrict__ gcat, int C, int Cd,
                            const bf16 *__restrict__ s, const bf16 *__restrict__ gp,
                            bf16 *__restrict__ gs, int B, int H, int W, int Cs) {
   const int ps = Cs / 8, pc = C / 8, pd = Cd / 8;
-  const long long hw = static_cast<long long>(H) * W;
-  const long long n = static_cast<long long>(B) * ps * hw;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
-    const long long bp = i / hw, pix = i - bp * hw;
-    const int b = static_cast<int>(bp / ps), j = static_cast<int>(bp - static_cast<long long>(b) * ps);
-    const int x = static_cast<int>(pix % W), y = static_cast<int>(pix / W);
+  const unsigned hw = static_cast<unsigned>(H) * static_cast<unsigned>(W);
+  const unsigned n = static_cast<unsigned>(B) * ps * hw;
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
+    const unsigned bp = i / hw, pix = i - bp * hw;
+    const int b = static_cast<int>(bp / static_cast<unsigned>(ps));
+    const int j = static_cast<int>(bp - static_cast<unsigned>(b) * ps);
+    const int y = static_cast<int>(pix / static_cast<unsigned>(W));
+    const int x = static_cast<int>(pix - static_cast<unsigned>(y) * static_cast<unsigned>(W));
     float a[8], sv[8], pv[8];
     load8(gcat + plane_at(b, pd + j, pix, pc, hw), a);
-    load8(s + i * 8, sv);
+    load8(s + static_cast<long long>(i) * 8, sv);
     load8(gp + plane_at(b, j, static_cast<long long>(y / 2) * (W / 2) + x / 2, ps, hw / 4), pv);
 #pragma unroll
     for (int k = 0; k < 8; k++)
       if (sv[k] > 0.0f) a[k] += 0.25f * pv[k];
-    store8(gs + i * 8, a);
+    store8(gs + static_cast<long long>(i) * 8, a);
   }
 }
 
@@ -229,18 +241,20 @@ __global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ 
   __shared__ float s_red[kBlock / 32][C + 2];
   if (threadIdx.x <= C) s_w[threadIdx.x] = hw_[threadIdx.x];
   __syncthreads();
-  const long long hwn = static_cast<long long>(W) * H;
-  const long long n = hwn * v.n;
-  const double inv_int = 1.0 / (static_cast<double>(W - 4) * (H - 4) * v.n);
+  // 32-bit index arithmetic (a batch's pixels stay below 2^31) and FP32 per
+  // pixel: the FP64 pipe is narrow on this part, the loss only a diagnostic
+  const unsigned hwn = static_cast<unsigned>(W) * static_cast<unsigned>(H);
+  const unsigned n = hwn * static_cast<unsigned>(v.n);
+  const float inv_int = static_cast<float>(1.0 / (static_cast<double>(W - 4) * (H - 4) * v.n));
   float acc[C + 1];
 #pragma unroll
   for (int j = 0; j <= C; j++) acc[j] = 0.0f;
-  double lsum = 0.0;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
+  float lsum = 0.0f;
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
     const int b = static_cast<int>(i / hwn);
-    const long long pix = i - b * hwn;
-    const int px = static_cast<int>(pix % W), py = static_cast<int>(pix / W);
+    const unsigned pix = i - static_cast<unsigned>(b) * hwn;
+    const int py = static_cast<int>(pix / static_cast<unsigned>(W));
+    const int px = static_cast<int>(pix - static_cast<unsigned>(py) * static_cast<unsigned>(W));
     float xv[C];
 #pragma unroll
     for (int j = 0; j < C; j += 8) {
@@ -257,8 +271,9 @@ __global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ 
       const int src = v.idx ? v.idx[b] : b;
       const float wgt = v.meta[src].weight;
       const float err = z - yt[i];
-      lsum += static_cast<double>(wgt) * err * err * inv_int;
-      dz = static_cast<float>(2.0 * wgt * err * inv_int);
+      const float we = wgt * err * inv_int;
+      lsum += we * err;
+      dz = 2.0f * we;
     }
 #pragma unroll
     for (int j = 0; j < C; j += 8) {
@@ -280,7 +295,7 @@ __global__ void __launch_bounds__(kBlock) k_head_train(const bf16 *__restrict__ 
     if (lane == 0) s_red[warp][j] = t;
   }
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-  if (lane == 0) s_red[warp][C + 1] = static_cast<float>(lsum);
+  if (lane == 0) s_red[warp][C + 1] = lsum;
   __syncthreads();
   if (threadIdx.x <= C) {
     float t = 0.0f;
@@ -303,13 +318,13 @@ __global__ void __launch_bounds__(kBlock) k_head_apply(const bf16 *__restrict__ 
   __shared__ float s_w[C + 1];
   if (threadIdx.x <= C) s_w[threadIdx.x] = hw_[threadIdx.x];
   __syncthreads();
-  const long long hwn = static_cast<long long>(W) * H;
-  const long long n = hwn * v.n;
-  for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kBlock) {
+  const unsigned hwn = static_cast<unsigned>(W) * static_cast<unsigned>(H);
+  const unsigned n = hwn * static_cast<unsigned>(v.n);
+  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
     const int b = static_cast<int>(i / hwn);
-    const long long pix = i - b * hwn;
-    const int px = static_cast<int>(pix % W), py = static_cast<int>(pix / W);
+    const unsigned pix = i - static_cast<unsigned>(b) * hwn;
+    const int py = static_cast<int>(pix / static_cast<unsigned>(W));
+    const int px = static_cast<int>(pix - static_cast<unsigned>(py) * static_cast<unsigned>(W));
     const int src = v.idx ? v.idx[b] : b;
     const double h = v.h64[src][pix];
     double out = h;
@@ -495,23 +510,28 @@ __global__ void k_copy_fields(double *const *__restrict__ src, double *const *__
 }  // namespace
 
 cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H, cudaStream_t s) {
+  // 16 planes per pixel: the input tensor's groups are the pixels times two
+  if (!fits32(2ll * W * H * v.n)) return cudaErrorInvalidValue;
   k_input<<<blocks_for(static_cast<long long>(W) * H * v.n), kBlock, 0, s>>>(v, in, yt, W, H);
   return cudaGetLastError();
 }
 
 cudaError_t launch_avgpool2(const Act &in, const Act &out, cudaStream_t s) {
+  if (!fits32(out.pixels() * out.C / 8)) return cudaErrorInvalidValue;
   k_avgpool2<<<blocks_for(out.pixels() * out.C / 8), kBlock, 0, s>>>(in.p, out.p, out.B, out.H,
                                                                       out.W, out.C);
   return cudaGetLastError();
 }
 
 cudaError_t launch_upcat(const Act &d, const Act &skip, const Act &cat, cudaStream_t s) {
+  if (!fits32(cat.pixels() * cat.C / 8)) return cudaErrorInvalidValue;
   k_upcat<<<blocks_for(cat.pixels() * cat.C / 8), kBlock, 0, s>>>(d.p, skip.p, cat.p, cat.B,
                                                                    cat.H, cat.W, d.C, skip.C);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s) {
+  if (!fits32(gcat.pixels() * gcat.C / 8)) return cudaErrorInvalidValue;
   k_sumpool2<<<blocks_for(gd.pixels() * gd.C / 8), kBlock, 0, s>>>(gcat.p, gcat.C, gd.p, gd.B,
                                                                    gd.H, gd.W, gd.C);
   return cudaGetLastError();
@@ -519,6 +539,7 @@ cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s) {
 
 cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act &gp,
                             const Act &gs, cudaStream_t s) {
+  if (!fits32(gcat.pixels() * gcat.C / 8)) return cudaErrorInvalidValue;
   k_skipgrad<<<blocks_for(gs.pixels() * gs.C / 8), kBlock, 0, s>>>(
       gcat.p, gcat.C, cd, skip.p, gp.p, gs.p, gs.B, gs.H, gs.W, gs.C);
   return cudaGetLastError();
@@ -527,6 +548,7 @@ cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act 
 cudaError_t launch_head_train(const Act &x, const float *head, const float *yt,
                               const SampleView &v, const Act &gx, float *dhead, double *loss,
                               cudaStream_t s) {
+  if (!fits32(x.pixels() * x.C / 8)) return cudaErrorInvalidValue;
   const int blocks = blocks_for(x.pixels());
   switch (x.C) {
     case 16:
@@ -542,6 +564,7 @@ cudaError_t launch_head_train(const Act &x, const float *head, const float *yt,
 
 cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView &v,
                               double *const *hout, cudaStream_t s) {
+  if (!fits32(x.pixels() * x.C / 8)) return cudaErrorInvalidValue;
   const int blocks = blocks_for(x.pixels());
   switch (x.C) {
     case 16: k_head_apply<16><<<blocks, kBlock, 0, s>>>(x.p, head, v, x.W, x.H, hout); break;
