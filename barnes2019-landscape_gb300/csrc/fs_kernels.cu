@@ -268,45 +268,48 @@ __device__ __forceinline__ uint64_t sub_sterbenz(uint64_t x, uint64_t y) {
   return fadd_bits_volatile(x, y ^ kSignBit);
 }
 
-// -RN(num/D) on bit patterns, given Rn = -R, R = RN(1/D), in three FP64
-// operations. q0 = RN(num*R) and r0 = num - q0*D by a fused multiply-add;
-// when q0 is not a power of two, its exponent is far from the range limits,
-// D is positive and normal with D*ulp(q0) normal too (the threshold below
-// is built by adding exponents) and |r0| < D*ulp(q0), q0 lies within one
-// ulp of num/D, r0 is
-// exact, and by Markstein's theorem (P. Markstein, IBM J. Res. Dev. 34(1),
-// 1990) q1 = RN(q0 + r0*R) is the correctly rounded quotient
-// (tests/native/division_check.cpp replays this on the host against the
-// IEEE division, near rounding midpoints included). (A q0 more
-// than an ulp away makes |num - q0*D| >= D*ulp(q0), which its rounding
-// keeps, so the test is never passed wrongly.) Every quotient is carried
-// negated -- RN is symmetric; q0n = RN(num*Rn) = -q0 -- which puts the
-// negations into the operands; the caller adds the result to h0. Anything
-// else takes the IEEE division, volatile PTX in a branch; the numerator and
-// result stay in integer registers.
+// -RN(num/D) on bit patterns, given Rn = -R, R = RN(1/D), in one FP64
+// operation. q0n = RN(num*Rn) = -RN(num*R) (RN is symmetric), within
+// 2^-52 (1 + 2^-52) of num/D relatively when num, q0, D and 1/D are normal.
+// The residual |num| - |q0|*|D| is then exact in integer arithmetic, in
+// units of ulp(q0)*ulp(D): r = mn*2^k - mq*mD with mn, mq, mD the
+// significands (implicit bit set) and k = en - eq - eD + 1075 from the
+// biased exponents; |r| < 2.01 mD < 2^55, so the difference taken modulo
+// 2^64 (the low halves of the 106-bit products) is r itself. In magnitude
+// num/D = q0 + (r/mD) ulp(q0), so the correctly rounded quotient is q0 when
+// 2|r| < mD and q0 one ulp further from or nearer to 0 when mD < 2|r| < 3mD
+// (q0 not a power of two, so the spacing is ulp(q0) on both sides; a
+// quotient is never a rounding midpoint, and the equalities fall back).
+// tests/native/division_check.cpp replays this on the host against the
+// IEEE division, near rounding midpoints included. It replaces Markstein's
+// correction q1 = RN(q0 + r0*R) with r0 = num - q0*D by a fused
+// multiply-add (P. Markstein, IBM J. Res. Dev. 34(1), 1990), which cost two
+// more FP64 operations on the erosion's FP64 pipe. Anything else takes the
+// IEEE division, volatile PTX in a branch; the numerator and result stay in
+// integer registers.
 __device__ __forceinline__ uint64_t neg_div_rn_bits(uint64_t numb, double D, double Rn) {
-  const double num = __longlong_as_double(numb);
-  const double q0n = num * Rn;
-  const double r0 = fma(q0n, D, num);
-  // Magnitudes are compared with the sign shifted out (x << 1) rather than
-  // masked: the compiler turns a sign mask of a double into an FP64
-  // absolute value.
-  const uint64_t q0b = (uint64_t)__double_as_longlong(q0n);
-  const int e = (int)((q0b << 1) >> 53);
-  const int ed = (int)((uint64_t)__double_as_longlong(D) >> 52);  // sign and exponent of D
-  const int et = ed + e - 1075;                                    // exponent of D*ulp(q0)
-  if (e >= 64 && e <= 1980 && ed >= 1 && ed <= 2046 && et >= 1 && et <= 2046 &&
-      (q0b << 12) != 0) {
-    const uint64_t thr = (uint64_t)(__double_as_longlong(D) + ((long long)(e - 1075) << 52));
-    if (((uint64_t)__double_as_longlong(r0) << 1) < (thr << 1))
-      return (uint64_t)__double_as_longlong(fma(r0, Rn, q0n));
+  constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
+  const uint64_t q0b = (uint64_t)__double_as_longlong(__longlong_as_double(numb) * Rn);
+  const uint64_t Db = (uint64_t)__double_as_longlong(D);
+  const int eq = (int)((q0b << 1) >> 53);
+  const int en = (int)((numb << 1) >> 53);
+  const int ed = (int)((Db << 1) >> 53);
+  const int k = en - eq - ed + 1075;
+  if ((unsigned)(eq - 64) <= 1980u - 64u && (unsigned)(en - 1) <= 2045u &&
+      (unsigned)(ed - 1) <= 2043u && (unsigned)(k - 48) <= 12u && (q0b << 12) != 0) {
+    const uint64_t mq = (q0b & kMant) | kHidden, mn = (numb & kMant) | kHidden,
+                   md = (Db & kMant) | kHidden;
+    const long long r = (long long)((mn << k) - mq * md);
+    const uint64_t a2 = (uint64_t)(r < 0 ? -r : r) << 1;
+    if (a2 < md) return q0b;
+    if (a2 > md && a2 < 3 * md) return r > 0 ? q0b + 1 : q0b - 1;
   }
   uint64_t r;
   asm volatile(
       "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
       "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
       : "=l"(r)
-      : "l"(numb), "l"((uint64_t)__double_as_longlong(D)));
+      : "l"(numb), "l"(Db));
   return r ^ kSignBit;
 }
 

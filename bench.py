@@ -72,13 +72,14 @@ ALG_BYTES = {
     "erode": 4 + 1 + 4 + 8 + 8,
     # k_erode: entry, direction, count, h read, h write
 }
-# k_erode leans on the FP64 pipe: per eroded cell fact*dh and the three
-# operations of the division, plus h0 - hn and h0 - q unless those run in
-# integer arithmetic (the autotuner's erode_int_sub); the uplift always runs
-# in integer arithmetic. Peak measured here with a probe kernel: 1.59 FP64
+# k_erode leans on the FP64 pipe: per eroded cell fact*dh and the
+# division's one multiplication (its residual and rounding run in integer
+# arithmetic), plus h0 - hn and h0 - q unless those run in integer
+# arithmetic too (the autotuner's erode_int_sub); the uplift always runs in
+# integer arithmetic. Peak measured here with a probe kernel: 1.59 FP64
 # lanes/clock/SM x 152 SMs x 2.07 GHz.
 def erode_fp64_per_cell(int_sub: bool) -> int:
-    return 4 if int_sub else 6
+    return 2 if int_sub else 4
 
 
 FP64_PEAK_TFLOPS = 1.59 * 152 * 2.07e9 / 1e12

@@ -9,6 +9,14 @@
 // on operands built next to rounding midpoints (num = RN(D * midpoint)),
 // D of all significand shapes and exponents (below 1, huge, negative, the
 // receiver slopes' divisors), and reports the acceptance rate.
+// It checks the integer form the kernel uses the same way: q0 = RN(num * R)
+// and the residual num - q0*D exactly in integer arithmetic, in units of
+// ulp(q0)*ulp(D): R' = mn*2^k - mq*mD from the significands (implicit bit
+// set) and k = en - eq - eD + 1075 from the biased exponents. Because
+// |q0 - num/D| <= 2^-52 |num/D| (1 + 2^-52), |R'| < 2.01 mD < 2^55 and the
+// difference taken modulo 2^64 is exact; num/D = q0 + (R'/mD) ulp(q0) in
+// magnitude, so RN(num/D) is q0 when 2|R'| < mD and q0 one ulp up or down
+// when mD < 2|R'| < 3 mD (a quotient is never a rounding midpoint).
 // Usage: division_check <cases> <seed>; exit 1 on the first mismatch.
 #include <cinttypes>
 #include <cmath>
@@ -40,10 +48,35 @@ static bool fast_quotient(double num, double D, double R, double *q) {
   return false;
 }
 
+// Returns true and *q = RN(num/D) when the integer form accepts.
+static bool int_quotient(double num, double D, double R, double *q) {
+  const uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
+  const uint64_t numb = bits(num), Db = bits(D);
+  const uint64_t q0b = bits(num * -R);
+  const int eq = (int)((q0b << 1) >> 53);
+  const int en = (int)((numb << 1) >> 53);
+  const int ed = (int)((Db << 1) >> 53);
+  const int k = en - eq - ed + 1075;
+  if ((unsigned)(eq - 64) <= 1980u - 64u && (unsigned)(en - 1) <= 2045u &&
+      (unsigned)(ed - 1) <= 2043u && (unsigned)(k - 48) <= 12u && (q0b << 12) != 0) {
+    const uint64_t mq = (q0b & kMant) | kHidden, mn = (numb & kMant) | kHidden,
+                   md = (Db & kMant) | kHidden;
+    const int64_t r = (int64_t)((mn << k) - mq * md);
+    const uint64_t a2 = (uint64_t)(r < 0 ? -r : r) << 1;
+    uint64_t qb;
+    if (a2 < md) qb = q0b;
+    else if (a2 > md && a2 < 3 * md) qb = r > 0 ? q0b + 1 : q0b - 1;
+    else return false;
+    *q = -dbl(qb);
+    return true;
+  }
+  return false;
+}
+
 int main(int argc, char **argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 10000000;
   std::mt19937_64 g(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
-  long accepted = 0;
+  long accepted = 0, accepted_int = 0;
   for (long i = 0; i < n; i++) {
     // D = 1 + F, F from tiny to huge; significands of every shape; also the
     // receiver slopes' divisors (dx, dx*sqrt(2)), D below 1, huge D (where
@@ -74,6 +107,14 @@ int main(int argc, char **argv) {
     }
     if (g() & 1) num = -num;
     double q;
+    if (int_quotient(num, D, R, &q)) {
+      accepted_int++;
+      const double ex = num / D;
+      if (bits(q) != bits(ex)) {
+        std::printf("MISMATCH (integer form) num=%a D=%a int=%a ieee=%a\n", num, D, q, ex);
+        return 1;
+      }
+    }
     if (fast_quotient(num, D, R, &q)) {
       accepted++;
       const double ex = num / D;
@@ -83,7 +124,8 @@ int main(int argc, char **argv) {
       }
     }
   }
-  std::printf("%ld cases, %ld accepted by the fast path, all equal to the IEEE quotient\n", n,
-              accepted);
+  std::printf("%ld cases, %ld accepted by the fast path, %ld by the integer form, all equal to the "
+              "IEEE quotient\n",
+              n, accepted, accepted_int);
   return 0;
 }
