@@ -589,7 +589,10 @@ def sg_conv(mode: int, x_bits: np.ndarray, w_bits: np.ndarray, taps: int = 9, bi
     (fs_test_sg_conv). mode 0: forward, x [B,H,W,cin], w [cout,taps,cin] ->
     BF16 bits [B,H,W,cout]; mode 1: data gradient, x = dy [B,H,W,cout], w as
     above, mask [B,H,W,cin] or None -> BF16 bits [B,H,W,cin]; mode 2: weight
-    gradient, x [B,H,W,cin], w = dy [B,H,W,cout] -> FP32 [cout,taps,cin]."""
+    gradient, x [B,H,W,cin], w = dy [B,H,W,cout] -> FP32 [cout,taps,cin];
+    mode 3: mode 0 written into the middle planes of a wider tensor (the
+    library checks the others stay untouched); mode 4: mode 3 stored
+    upsampled 2x (nearest) -> [B,2H,2W,cout]."""
     x_bits = np.ascontiguousarray(x_bits, np.uint16)
     w_bits = np.ascontiguousarray(w_bits, np.uint16)
     B, H, W = x_bits.shape[:3]
@@ -600,7 +603,8 @@ def sg_conv(mode: int, x_bits: np.ndarray, w_bits: np.ndarray, taps: int = 9, bi
         cout, t, cin = w_bits.shape
         if t != taps:
             raise ValueError("weights do not match taps")
-        out = np.empty((B, H, W, cout if mode == 0 else cin), np.uint16)
+        f = 2 if mode == 4 else 1
+        out = np.empty((B, f * H, f * W, cin if mode == 1 else cout), np.uint16)
     u16 = C.POINTER(C.c_uint16)
     bp = None
     if bias is not None:

@@ -66,7 +66,8 @@ struct Bufs {
 extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout, int taps,
                                const uint16_t *x, const uint16_t *w, const float *bias, int relu,
                                const uint16_t *mask, void *out) {
-  if (mode < 0 || mode > 2) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: mode must be 0, 1 or 2%s", "");
+  if (mode < 0 || mode > 4)
+    return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: mode must be 0 to 4%s", "");
   if (B < 1 || H < 1 || W < 1 || cin < 16 || cout < 16 || cin % 16 || cout % 16 ||
       (taps != 1 && taps != 9) || !x || !w || !out)
     return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: bad shape or NULL buffer%s", "");
@@ -80,6 +81,14 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
   cudaError_t e = bufs.alloc(&derr, sizeof(int));
   const char *why = nullptr;
   if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  // modes 3 and 4: the output's cout channels are planes [kGuard, kGuard +
+  // cout/8) of a tensor with kGuard sentinel planes before and after them
+  // (at 2H x 2W in mode 4)
+  constexpr int kGuard = 2;
+  constexpr uint16_t kSentinel = 0x7FC5;
+  const int up = mode == 4 ? 1 : 0;
+  const long long opix = pix << (2 * up), ohw = hw << (2 * up);
+  const int oplanes = cout / 8 + 2 * kGuard;
   if (mode == 0) {
     if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cin * 2);
     if (e == cudaSuccess) e = bufs.alloc(&dw, nw * 2);
@@ -93,6 +102,27 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
     sg::Act src{dx, B, H, W, cin};
     sg::ConvPlan plan;
     e = sg::plan_conv(plan, src, dw, taps, cout, dbias, relu, nullptr, dout, &why);
+    if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
+    e = sg::launch_conv(plan, derr, s);
+  } else if (mode >= 3) {
+    const size_t on = static_cast<size_t>(opix) * oplanes * 8;
+    if (e == cudaSuccess) e = bufs.alloc(&dx, pix * cin * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dw, nw * 2);
+    if (e == cudaSuccess) e = bufs.alloc(&dout, on * 2);
+    if (e == cudaSuccess && bias) e = bufs.alloc(&dbias, cout * sizeof(float));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(dx, to_planes(x, hw, B, cin).data(), pix * cin * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dw, w, nw * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bias) e = cudaMemcpy(dbias, bias, cout * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      const std::vector<uint16_t> fill(on, kSentinel);
+      e = cudaMemcpy(dout, fill.data(), on * 2, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: buffers");
+    sg::Act src{dx, B, H, W, cin};
+    sg::ConvPlan plan;
+    e = sg::plan_conv(plan, src, dw, taps, cout, dbias, relu, nullptr,
+                      dout + static_cast<size_t>(kGuard) * ohw * 8, &why, oplanes, up);
     if (e != cudaSuccess) return sg_fail(FS_ERR_ARG, "fs_test_sg_conv: %s", why);
     e = sg::launch_conv(plan, derr, s);
   } else if (mode == 1) {
@@ -140,6 +170,32 @@ extern "C" int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout,
   if (herr) return sg_fail(FS_ERR_TIMEOUT, "fs_test_sg_conv: a pipeline wait ran out%s", "");
   if (mode == 2) {
     e = cudaMemcpy(out, dgw, nw * sizeof(float), cudaMemcpyDeviceToHost);
+  } else if (mode >= 3) {
+    // every guard plane must still hold the sentinel; the output's planes
+    // come back as [B, H, W, cout] (2H x 2W in mode 4)
+    std::vector<uint16_t> t(static_cast<size_t>(opix) * oplanes * 8);
+    e = cudaMemcpy(t.data(), dout, t.size() * 2, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "fs_test_sg_conv: copy back");
+    std::vector<uint16_t> o(static_cast<size_t>(opix) * cout);
+    for (int b = 0; b < B; b++)
+      for (int pl = 0; pl < oplanes; pl++) {
+        const uint16_t *src = t.data() + static_cast<size_t>(b * oplanes + pl) * ohw * 8;
+        const bool guard = pl < kGuard || pl >= kGuard + cout / 8;
+        if (guard) {
+          for (long long k = 0; k < ohw * 8; k++)
+            if (src[k] != kSentinel) {
+              char where[64];
+              std::snprintf(where, sizeof(where), "image %d plane %d", b, pl);
+              return sg_fail(FS_ERR_CUDA, "fs_test_sg_conv: %s outside the output was written",
+                             where);
+            }
+          continue;
+        }
+        for (long long q = 0; q < ohw; q++)
+          std::memcpy(o.data() + (static_cast<size_t>(b) * ohw + q) * cout + 8 * (pl - kGuard),
+                      src + q * 8, 16);
+      }
+    std::memcpy(out, o.data(), o.size() * 2);
   } else {
     const int co = mode == 0 ? cout : cin;
     std::vector<uint16_t> t(static_cast<size_t>(pix) * co);

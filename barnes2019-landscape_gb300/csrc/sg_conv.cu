@@ -263,7 +263,8 @@ struct ConvArgs {
   int relu;
   const bf16 *mask;   // ntot channels, plane-major like out
   bf16 *out;
-  int oplanes;        // planes per image of out and mask (ntot / 8)
+  int oplanes;        // planes per image of out and mask (ntot / 8, or more)
+  int up;             // 1: out is 2H x 2W, each pixel stored into its 2x2 block
   int nbuf;           // TMEM accumulator buffers (k_conv, k_conv_planar)
   int *err;
 };
@@ -291,9 +292,11 @@ constexpr int kWgradThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
 
 // One 16-column chunk of a tile row: + bias (shared memory), ReLU, zeroed
 // where the mask is not positive, rounded to BF16, stored as 16 bytes in
-// each of two planes (ps elements apart).
+// each of two planes (ps elements apart); with rowd > 0 (an output upsampled
+// 2x, rows rowd elements apart) into the pixel's 2x2 block of each plane.
 __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, int relu,
-                                      const bf16 *msk, bf16 *out, long long ps) {
+                                      const bf16 *msk, bf16 *out, long long ps,
+                                      long long rowd) {
   float f[16];
 #pragma unroll
   for (int j = 0; j < 16; j++) f[j] = __uint_as_float(v[j]);
@@ -327,14 +330,23 @@ __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, 
   o1.w = pack_bf16(f[14], f[15]);
   *reinterpret_cast<uint4 *>(out) = o0;
   *reinterpret_cast<uint4 *>(out + ps) = o1;
+  if (rowd) {
+    *reinterpret_cast<uint4 *>(out + 8) = o0;
+    *reinterpret_cast<uint4 *>(out + ps + 8) = o1;
+    *reinterpret_cast<uint4 *>(out + rowd) = o0;
+    *reinterpret_cast<uint4 *>(out + rowd + 8) = o0;
+    *reinterpret_cast<uint4 *>(out + ps + rowd) = o1;
+    *reinterpret_cast<uint4 *>(out + ps + rowd + 8) = o1;
+  }
 }
 
 // Columns [c_lo, c_hi) of this warp's 32 TMEM lanes (d: lane quarter and
 // accumulator base), two 16-column loads in flight per wait; out and msk
 // point at this lane's pixel in the plane of column 0, planes ps elements
-// apart.
+// apart (rowd: as in epi16).
 __device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, const float *sb,
-                                            int relu, const bf16 *msk, bf16 *out, long long ps) {
+                                            int relu, const bf16 *msk, bf16 *out, long long ps,
+                                            long long rowd) {
   int c = c_lo;
   for (; c + 32 <= c_hi; c += 32) {
     uint32_t v0[16], v1[16];
@@ -342,15 +354,15 @@ __device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, cons
     tmem_ld16(d + c + 16, v1);
     tmem_ld_wait();
     const long long o0 = (c / 8) * ps, o1 = ((c + 16) / 8) * ps;
-    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps);
-    epi16(v1, sb ? sb + c + 16 : nullptr, relu, msk ? msk + o1 : nullptr, out + o1, ps);
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps, rowd);
+    epi16(v1, sb ? sb + c + 16 : nullptr, relu, msk ? msk + o1 : nullptr, out + o1, ps, rowd);
   }
   if (c < c_hi) {
     uint32_t v0[16];
     tmem_ld16(d + c, v0);
     tmem_ld_wait();
     const long long o0 = (c / 8) * ps;
-    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps);
+    epi16(v0, sb ? sb + c : nullptr, relu, msk ? msk + o0 : nullptr, out + o0, ps, rowd);
   }
 }
 
@@ -362,7 +374,7 @@ __device__ __forceinline__ void epi_columns(uint32_t d, int c_lo, int c_hi, cons
 // that drain alternate tiles, so the epilogues of two tiles overlap each
 // other and the MMAs of the next ones.
 template <int CB, int NG>
-__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
+__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 2)
     k_conv(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb,
            const ConvArgs a) {
   extern __shared__ unsigned char smem_raw[];
@@ -502,11 +514,13 @@ __global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
       const int y0 = (tt / a.tiles_x) * a.BH, x0 = (tt % a.tiles_x) * a.BW;
       const int n0 = nt * a.bn;
       const int py = y0 + r / a.BW, px = x0 + r % a.BW;
-      const long long hw = static_cast<long long>(a.H) * a.W;
-      const long long at = plane_at(b, n0 / 8, static_cast<long long>(py) * a.W + px, a.oplanes, hw);
+      const long long hw = static_cast<long long>(a.H) * a.W << (2 * a.up);
+      const long long at =
+          plane_at(b, n0 / 8, (static_cast<long long>(py) * a.W << (2 * a.up)) + (px << a.up),
+                   a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
       epi_columns(d, 0, a.bn, a.bias ? s_bias + n0 : nullptr, a.relu,
-                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8);
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, a.up ? 16ll * a.W : 0);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -537,7 +551,7 @@ constexpr int kPlaneStride = (kPlaneBytes + 127) & ~127;    // 128-byte aligned 
 constexpr int kGuardBytes = 4 * 1024;  // slack after the ring (the MMAs read inside each stage)
 
 template <int CB, int NG>
-__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
+__global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 2)
     k_conv_planar(const __grid_constant__ CUtensorMap tmp, const __grid_constant__ CUtensorMap tmt,
                   const __grid_constant__ CUtensorMap tmb,
                   const ConvArgs a) {
@@ -690,11 +704,13 @@ __global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 1)
       const int b = t / tiles_img;
       const int tt = t - b * tiles_img;
       const int py = tt / a.tiles_x, px = (tt % a.tiles_x) * 128 + r;
-      const long long hw = static_cast<long long>(a.H) * a.W;
-      const long long at = plane_at(b, 0, static_cast<long long>(py) * a.W + px, a.oplanes, hw);
+      const long long hw = static_cast<long long>(a.H) * a.W << (2 * a.up);
+      const long long at =
+          plane_at(b, 0, (static_cast<long long>(py) * a.W << (2 * a.up)) + (px << a.up),
+                   a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
       epi_columns(d, 0, a.bn, a.bias ? s_bias : nullptr, a.relu,
-                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8);
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, a.up ? 16ll * a.W : 0);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -893,15 +909,17 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     const bool writer = 8 * cg < a.bn;
     uint32_t(*tr)[8] = s_tr[warp - 2];
     const float bias = a.bias && co < a.bn ? s_bias[co] : 0.0f;
-    const long long hw = static_cast<long long>(a.H) * a.W;
+    const long long hw = static_cast<long long>(a.H) * a.W << (2 * a.up);
     for (int t = blockIdx.x + grp * gridDim.x, it = grp; t < ntot_tiles;
          t += 2 * gridDim.x, it += 2) {
       const int buf = it & 1;
       const int b = t / tiles_img;
       const int tt = t - b * tiles_img;
       const int y0 = tt / tiles_row, x0 = (tt % tiles_row) * kTN;
-      const long long at = plane_at(b, writer ? cg : 0,
-                                    static_cast<long long>(y0) * a.W + x0 + 2 * kk, a.oplanes, hw);
+      const long long at =
+          plane_at(b, writer ? cg : 0,
+                   (static_cast<long long>(y0) * a.W << (2 * a.up)) + ((x0 + 2 * kk) << a.up),
+                   a.oplanes, hw);
       if (!mbar_wait(&acc_full[buf], (it >> 1) & 1, &abort_flag, true)) {
         sg_raise(a.err, &abort_flag, kSgTimeout);
         break;
@@ -937,10 +955,22 @@ __global__ void __launch_bounds__(kConvThreads, 1)
           o1.y = __byte_perm(w[2], w[3], 0x7632);
           o1.z = __byte_perm(w[4], w[5], 0x7632);
           o1.w = __byte_perm(w[6], w[7], 0x7632);
-          if (writer) {
+          if (writer && !a.up) {
             const long long o = at + 8ll * c;
             *reinterpret_cast<uint4 *>(a.out + o) = o0;
             *reinterpret_cast<uint4 *>(a.out + o + 8) = o1;
+          } else if (writer) {
+            // pixels 2p .. 2p+3 of rows 2y0 and 2y0+1 of the 2x output
+            uint4 *o = reinterpret_cast<uint4 *>(a.out + at + 16ll * c);
+            uint4 *o2 = o + 2 * a.W;
+            o[0] = o0;
+            o[1] = o0;
+            o[2] = o1;
+            o[3] = o1;
+            o2[0] = o0;
+            o2[1] = o0;
+            o2[2] = o1;
+            o2[3] = o1;
           }
         }
       }
@@ -1368,10 +1398,15 @@ PixTile pixel_tile(int H, int W) {
 
 cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
                       const float *bias, int relu, const bf16 *mask, bf16 *out,
-                      const char **why) {
+                      const char **why, int out_planes, int out_up) {
   const char *dummy;
   if (!why) why = &dummy;
   p = ConvPlan{};
+  if (out_planes && (out_planes < ntot / 8 || mask))
+    return *why = "an output inside a wider tensor needs room for ntot channels and no mask",
+           cudaErrorInvalidValue;
+  if (out_up && mask) return *why = "an upsampled output takes no mask", cudaErrorInvalidValue;
+  p.up = out_up ? 1 : 0;
   p.pt = pixel_tile(src.H, src.W);
   if (!p.pt.ok) return *why = "image width must divide or be a multiple of 128", cudaErrorInvalidValue;
   if (src.C % 16 || src.C <= 0) return *why = "source channels must be a multiple of 16", cudaErrorInvalidValue;
@@ -1394,6 +1429,7 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
         break;
       }
   }
+  p.oplanes = out_planes ? out_planes : ntot / 8;
   p.B = src.B;
   p.H = src.H;
   p.W = src.W;
@@ -1653,7 +1689,8 @@ cudaError_t launch_conv_cb(const ConvPlan &p, int *err, cudaStream_t s, int nimg
   a.relu = p.relu;
   a.mask = p.mask;
   a.out = p.out;
-  a.oplanes = p.ntot / 8;
+  a.oplanes = p.oplanes;
+  a.up = p.up;
   a.nbuf = p.nbuf;
   a.err = err;
   a.mtiles = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.grid_x;

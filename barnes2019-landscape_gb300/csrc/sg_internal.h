@@ -71,6 +71,10 @@ struct ConvPlan {
   int relu = 0;
   const bf16 *mask = nullptr;   // output zeroed where mask <= 0 (or null; ntot channels)
   bf16 *out = nullptr;          // ntot channels
+  int oplanes = 0;              // planes per image of out: ntot / 8, or more when out is
+                                // a run of planes inside a wider tensor
+  int up = 0;                   // 1: out is 2H x 2W, each output pixel stored into its
+                                // 2x2 block (nearest-neighbour upsampling)
   size_t smem = 0;
   int grid_x = 0, grid_y = 0;  // pixel tiles and N tiles
   int sms = 1;                 // SMs of the device
@@ -103,10 +107,14 @@ struct WgradPlan {
 
 // Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for
 // shapes the kernels do not take. Source and output tensors must stay
-// allocated for the plan's lifetime.
+// allocated for the plan's lifetime. out_planes > 0 writes the output into
+// ntot/8 planes of a tensor with out_planes planes per image, from `out`
+// (which then points at the first of them in image 0); out_up != 0 writes
+// it upsampled 2x (nearest) into an output of 2H x 2W pixels. No mask with
+// either.
 cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int ntot,
                       const float *bias, int relu, const bf16 *mask, bf16 *out,
-                      const char **why);
+                      const char **why, int out_planes = 0, int out_up = 0);
 // db (optional): where the bias gradient goes; the plan's db is non-null
 // when its launches accumulate it (else the caller sums it separately).
 cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, float *dw, int sms,

@@ -78,6 +78,8 @@ struct SgLayer {
   bf16 *wf = nullptr, *wd = nullptr;
   Act *x = nullptr, *y = nullptr, *gy = nullptr, *gx = nullptr;
   Act *dmask = nullptr;  // ReLU output whose mask the data gradient applies
+  int y_planes = 0;      // planes per image of the buffer y lies in (0: y's own)
+  int y_up = 0;          // 1: y is stored upsampled 2x into that buffer
   sg::ConvPlan fwd, dgr;
   sg::WgradPlan wgr;
 };
@@ -193,12 +195,12 @@ int build(fs_surrogate *s) {
     Act *a;
     int h, w, ch;
   } acts[] = {
-      {&s->in0, H, W, sg::kInputChannels}, {&s->e0a, H, W, c}, {&s->s0, H, W, c},
-      {&s->p0, H1, W1, c}, {&s->e1a, H1, W1, 2 * c}, {&s->s1, H1, W1, 2 * c},
-      {&s->p1, H2, W2, 2 * c}, {&s->e2a, H2, W2, 4 * c}, {&s->s2, H2, W2, 4 * c},
-      {&s->p2, H3, W3, 4 * c}, {&s->b1, H3, W3, 8 * c}, {&s->b2, H3, W3, 8 * c},
-      {&s->cat2, H2, W2, 12 * c}, {&s->d2a, H2, W2, 4 * c}, {&s->d2b, H2, W2, 4 * c},
-      {&s->cat1, H1, W1, 6 * c}, {&s->d1a, H1, W1, 2 * c}, {&s->d1b, H1, W1, 2 * c},
+      {&s->in0, H, W, sg::kInputChannels}, {&s->e0a, H, W, c},
+      {&s->p0, H1, W1, c}, {&s->e1a, H1, W1, 2 * c},
+      {&s->p1, H2, W2, 2 * c}, {&s->e2a, H2, W2, 4 * c},
+      {&s->p2, H3, W3, 4 * c}, {&s->b1, H3, W3, 8 * c},
+      {&s->cat2, H2, W2, 12 * c}, {&s->d2a, H2, W2, 4 * c},
+      {&s->cat1, H1, W1, 6 * c}, {&s->d1a, H1, W1, 2 * c},
       {&s->cat0, H, W, 3 * c}, {&s->d0a, H, W, c}, {&s->d0b, H, W, c},
       {&s->g_d0b, H, W, c}, {&s->g_d0a, H, W, c}, {&s->g_cat0, H, W, 3 * c},
       {&s->g_d1b, H1, W1, 2 * c}, {&s->g_d1a, H1, W1, 2 * c}, {&s->g_cat1, H1, W1, 6 * c},
@@ -209,6 +211,28 @@ int build(fs_surrogate *s) {
       {&s->g_s0, H, W, c}, {&s->g_e0a, H, W, c},
   };
   for (auto &a : acts) SG_CUDA(act_alloc(s, *a.a, a.h, a.w, a.ch));
+  // The concatenations are written by the convolutions of both their
+  // halves: the decoder output one level down stored upsampled 2x into the
+  // first planes, the encoder's skip tensor into the planes after them.
+  // Neither exists on its own (the backward takes the ReLU masks from the
+  // concatenations).
+  auto skip_in = [&](Act &sk, const Act &cat, int cd) {
+    sk = cat;
+    sk.C = cat.C - cd;
+    sk.p = cat.p + static_cast<size_t>(cd / 8) * cat.H * cat.W * 8;
+  };
+  auto up_in = [&](Act &d, const Act &cat, int cd) {
+    d = cat;
+    d.C = cd;
+    d.H = cat.H / 2;
+    d.W = cat.W / 2;
+  };
+  skip_in(s->s0, s->cat0, 2 * c);
+  skip_in(s->s1, s->cat1, 4 * c);
+  skip_in(s->s2, s->cat2, 8 * c);
+  up_in(s->d1b, s->cat0, 2 * c);
+  up_in(s->d2b, s->cat1, 4 * c);
+  up_in(s->b2, s->cat2, 8 * c);
   // layers: input, output, output gradient, input gradient, mask
   struct Wire {
     Act *x, *y, *gy, *gx, *mask;
@@ -236,6 +260,10 @@ int build(fs_surrogate *s) {
     L.gy = wire[l].gy;
     L.gx = wire[l].gx;
     L.dmask = wire[l].mask;
+    if (L.y == &s->s0 || L.y == &s->d1b) L.y_planes = s->cat0.C / 8;
+    if (L.y == &s->s1 || L.y == &s->d2b) L.y_planes = s->cat1.C / 8;
+    if (L.y == &s->s2 || L.y == &s->b2) L.y_planes = s->cat2.C / 8;
+    L.y_up = L.y == &s->d1b || L.y == &s->d2b || L.y == &s->b2;
     L.cin = L.x->C;
     L.cout = L.y->C;
     L.taps = 9;
@@ -272,7 +300,7 @@ int build(fs_surrogate *s) {
     SG_CUDA(dalloc(s, &L.wd, nw));
     const char *why = nullptr;
     cudaError_t e = sg::plan_conv(L.fwd, *L.x, L.wf, L.taps, L.cout, s->p + L.b_off, 1, nullptr,
-                                  L.y->p, &why);
+                                  L.y->p, &why, L.y_planes, L.y_up);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d forward: %s", l, why);
     e = sg::plan_wgrad(L.wgr, *L.x, *L.gy, L.taps, s->g + L.w_off, s->sms, &why, s->g + L.b_off);
     if (e != cudaSuccess) return fail(FS_ERR_ARG, "surrogate layer %d weight gradient: %s", l, why);
@@ -322,22 +350,19 @@ int forward(fs_surrogate *s, const sg::SampleView &v, bool train) {
   auto conv = [&](int l) -> cudaError_t { return sg::launch_conv(s->L[l].fwd, s->d_err, st, n); };
   SG_CUDA(conv(0));
   SG_CUDA(conv(1));
-  SG_CUDA(sg::launch_avgpool2(view(s->s0, n), view(s->p0, n), st));
+  SG_CUDA(sg::launch_avgpool2(view(s->cat0, n), 2 * s->c0 / 8, view(s->p0, n), st));
   SG_CUDA(conv(2));
   SG_CUDA(conv(3));
-  SG_CUDA(sg::launch_avgpool2(view(s->s1, n), view(s->p1, n), st));
+  SG_CUDA(sg::launch_avgpool2(view(s->cat1, n), 4 * s->c0 / 8, view(s->p1, n), st));
   SG_CUDA(conv(4));
   SG_CUDA(conv(5));
-  SG_CUDA(sg::launch_avgpool2(view(s->s2, n), view(s->p2, n), st));
+  SG_CUDA(sg::launch_avgpool2(view(s->cat2, n), 8 * s->c0 / 8, view(s->p2, n), st));
   SG_CUDA(conv(6));
   SG_CUDA(conv(7));
-  SG_CUDA(sg::launch_upcat(view(s->b2, n), view(s->s2, n), view(s->cat2, n), st));
   SG_CUDA(conv(8));
   SG_CUDA(conv(9));
-  SG_CUDA(sg::launch_upcat(view(s->d2b, n), view(s->s1, n), view(s->cat1, n), st));
   SG_CUDA(conv(10));
   SG_CUDA(conv(11));
-  SG_CUDA(sg::launch_upcat(view(s->d1b, n), view(s->s0, n), view(s->cat0, n), st));
   SG_CUDA(conv(12));
   SG_CUDA(conv(13));
   return FS_OK;
@@ -368,15 +393,15 @@ int backward(fs_surrogate *s, const sg::SampleView &v) {
   SG_CUDA(sg::launch_sumpool2(view(s->g_cat2, n), view(s->g_b2, n), st));
   SG_CUDA(layer(7));
   SG_CUDA(layer(6));
-  SG_CUDA(sg::launch_skipgrad(view(s->g_cat2, n), 8 * c, view(s->s2, n), view(s->g_p2, n),
+  SG_CUDA(sg::launch_skipgrad(view(s->g_cat2, n), 8 * c, view(s->cat2, n), view(s->g_p2, n),
                               view(s->g_s2, n), st));
   SG_CUDA(layer(5));
   SG_CUDA(layer(4));
-  SG_CUDA(sg::launch_skipgrad(view(s->g_cat1, n), 4 * c, view(s->s1, n), view(s->g_p1, n),
+  SG_CUDA(sg::launch_skipgrad(view(s->g_cat1, n), 4 * c, view(s->cat1, n), view(s->g_p1, n),
                               view(s->g_s1, n), st));
   SG_CUDA(layer(3));
   SG_CUDA(layer(2));
-  SG_CUDA(sg::launch_skipgrad(view(s->g_cat0, n), 2 * c, view(s->s0, n), view(s->g_p0, n),
+  SG_CUDA(sg::launch_skipgrad(view(s->g_cat0, n), 2 * c, view(s->cat0, n), view(s->g_p0, n),
                               view(s->g_s0, n), st));
   SG_CUDA(layer(1));
   SG_CUDA(layer(0));

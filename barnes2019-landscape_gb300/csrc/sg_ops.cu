@@ -121,17 +121,21 @@ __global__ void k_input(const SampleView v, bf16 *__restrict__ in, float *__rest
   }
 }
 
-// out = 2x2 average of in; i runs over (image, plane) pairs and pixels of out
-__global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, int B, int Ho,
-                           int Wo, int C) {
+// out = 2x2 average of planes [ioff, ioff + C/8) of in (ip planes per image
+// at twice the resolution); i runs over (image, plane) pairs and pixels of out
+__global__ void k_avgpool2(const bf16 *__restrict__ in, int ip, int ioff, bf16 *__restrict__ out,
+                           int B, int Ho, int Wo, int C) {
+  const int po_ = C / 8;
   const unsigned hwo = static_cast<unsigned>(Ho) * static_cast<unsigned>(Wo);
   const long long Wi = 2ll * Wo;
-  const unsigned n = static_cast<unsigned>(B) * (C / 8) * hwo;
+  const unsigned n = static_cast<unsigned>(B) * po_ * hwo;
   for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
     const unsigned bp = i / hwo, po = i - bp * hwo;
+    const int b = static_cast<int>(bp / static_cast<unsigned>(po_));
+    const int pl = static_cast<int>(bp - static_cast<unsigned>(b) * po_);
     const int y = static_cast<int>(po / static_cast<unsigned>(Wo));
     const int x = static_cast<int>(po - static_cast<unsigned>(y) * static_cast<unsigned>(Wo));
-    const bf16 *p = in + (static_cast<long long>(bp) * 4 * hwo + 2ll * y * Wi + 2 * x) * 8;
+    const bf16 *p = in + plane_at(b, ioff + pl, 2ll * y * Wi + 2 * x, ip, 4ll * hwo);
     float a[8], t[8];
     load8(p, a);
     load8(p + 8, t);
@@ -144,29 +148,6 @@ __global__ void k_avgpool2(const bf16 *__restrict__ in, bf16 *__restrict__ out, 
 #pragma unroll
     for (int j = 0; j < 8; j++) a[j] = 0.25f * (a[j] + t[j]);
     store8(out + static_cast<long long>(i) * 8, a);
-  }
-}
-
-// cat[b, 0:Cd, y, x] = d[b, :, y/2, x/2], cat[b, Cd:Cd+Cs, y, x] = s[b, :, y, x]
-__global__ void k_upcat(const bf16 *__restrict__ d, const bf16 *__restrict__ s,
-                        bf16 *__restrict__ cat, int B, int H, int W, int Cd, int Cs) {
-  const int pd = Cd / 8, ps = Cs / 8, pc = pd + ps;
-  const unsigned hw = static_cast<unsigned>(H) * static_cast<unsigned>(W);
-  const unsigned n = static_cast<unsigned>(B) * pc * hw;
-  for (unsigned i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
-    const unsigned bp = i / hw, pix = i - bp * hw;
-    const int b = static_cast<int>(bp / static_cast<unsigned>(pc));
-    const int pl = static_cast<int>(bp - static_cast<unsigned>(b) * pc);
-    uint4 v;
-    if (pl < pd) {
-      const int y = static_cast<int>(pix / static_cast<unsigned>(W));
-      const int x = static_cast<int>(pix - static_cast<unsigned>(y) * static_cast<unsigned>(W));
-      v = *reinterpret_cast<const uint4 *>(
-          d + plane_at(b, pl, static_cast<long long>(y / 2) * (W / 2) + x / 2, pd, hw / 4));
-    } else {
-      v = *reinterpret_cast<const uint4 *>(s + plane_at(b, pl - pd, pix, ps, hw));
-    }
-    *reinterpret_cast<uint4 *>(cat + static_cast<long long>(i) * 8) = v;
   }
 }
 
@@ -201,9 +182,10 @@ __global__ void k_sumpool2(const bf16 *__restrict__ g, int C, bf16 *__restrict__
 }
 
 // gs = gcat[:, Cd:Cd+Cs] + (s > 0) * gp(up) / 4: the skip tensor's gradient
-// from the decoder (already masked) plus the pooling path's, masked by ReLU
+// from the decoder (already masked) plus the pooling path's, masked by ReLU;
+// s is read from the concatenation cat (same layout as gcat)
 __global__ void k_skipgrad(const bf16 *__restrict__ gcat, int C, int Cd,
-                           const bf16 *__restrict__ s, const bf16 *__restrict__ gp,
+                           const bf16 *__restrict__ cat, const bf16 *__restrict__ gp,
                            bf16 *__restrict__ gs, int B, int H, int W, int Cs) {
   const int ps = Cs / 8, pc = C / 8, pd = Cd / 8;
   const unsigned hw = static_cast<unsigned>(H) * static_cast<unsigned>(W);
@@ -215,8 +197,9 @@ __global__ void k_skipgrad(const bf16 *__restrict__ gcat, int C, int Cd,
     const int y = static_cast<int>(pix / static_cast<unsigned>(W));
     const int x = static_cast<int>(pix - static_cast<unsigned>(y) * static_cast<unsigned>(W));
     float a[8], sv[8], pv[8];
-    load8(gcat + plane_at(b, pd + j, pix, pc, hw), a);
-    load8(s + static_cast<long long>(i) * 8, sv);
+    const long long at = plane_at(b, pd + j, pix, pc, hw);
+    load8(gcat + at, a);
+    load8(cat + at, sv);
     load8(gp + plane_at(b, j, static_cast<long long>(y / 2) * (W / 2) + x / 2, ps, hw / 4), pv);
 #pragma unroll
     for (int k = 0; k < 8; k++)
@@ -516,17 +499,12 @@ cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H,
   return cudaGetLastError();
 }
 
-cudaError_t launch_avgpool2(const Act &in, const Act &out, cudaStream_t s) {
-  if (!fits32(out.pixels() * out.C / 8)) return cudaErrorInvalidValue;
-  k_avgpool2<<<blocks_for(out.pixels() * out.C / 8), kBlock, 0, s>>>(in.p, out.p, out.B, out.H,
-                                                                      out.W, out.C);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_upcat(const Act &d, const Act &skip, const Act &cat, cudaStream_t s) {
-  if (!fits32(cat.pixels() * cat.C / 8)) return cudaErrorInvalidValue;
-  k_upcat<<<blocks_for(cat.pixels() * cat.C / 8), kBlock, 0, s>>>(d.p, skip.p, cat.p, cat.B,
-                                                                   cat.H, cat.W, d.C, skip.C);
+cudaError_t launch_avgpool2(const Act &in, int in_off, const Act &out, cudaStream_t s) {
+  if (!fits32(in.pixels() * in.C / 8) || in_off < 0 || (in_off + out.C / 8) * 8 > in.C ||
+      in.B != out.B || in.H != 2 * out.H || in.W != 2 * out.W)
+    return cudaErrorInvalidValue;
+  k_avgpool2<<<blocks_for(out.pixels() * out.C / 8), kBlock, 0, s>>>(
+      in.p, in.C / 8, in_off, out.p, out.B, out.H, out.W, out.C);
   return cudaGetLastError();
 }
 
@@ -537,11 +515,13 @@ cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act &gp,
+cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &cat, const Act &gp,
                             const Act &gs, cudaStream_t s) {
-  if (!fits32(gcat.pixels() * gcat.C / 8)) return cudaErrorInvalidValue;
+  if (!fits32(gcat.pixels() * gcat.C / 8) || cat.C != gcat.C || cat.H != gcat.H ||
+      cat.W != gcat.W || cd + gs.C > gcat.C)
+    return cudaErrorInvalidValue;
   k_skipgrad<<<blocks_for(gs.pixels() * gs.C / 8), kBlock, 0, s>>>(
-      gcat.p, gcat.C, cd, skip.p, gp.p, gs.p, gs.B, gs.H, gs.W, gs.C);
+      gcat.p, gcat.C, cd, cat.p, gp.p, gs.p, gs.B, gs.H, gs.W, gs.C);
   return cudaGetLastError();
 }
 

@@ -39,10 +39,12 @@ struct SampleView {
 };
 
 cudaError_t launch_input(const SampleView &v, bf16 *in, float *yt, int W, int H, cudaStream_t s);
-cudaError_t launch_avgpool2(const Act &in, const Act &out, cudaStream_t s);
-cudaError_t launch_upcat(const Act &d, const Act &skip, const Act &cat, cudaStream_t s);
+// out = 2x2 average of out.C channels of in from plane in_off on
+cudaError_t launch_avgpool2(const Act &in, int in_off, const Act &out, cudaStream_t s);
 cudaError_t launch_sumpool2(const Act &gcat, const Act &gd, cudaStream_t s);
-cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &skip, const Act &gp,
+// gs = gcat's channels [cd, cd + gs.C) + the pooling path's gp, masked where
+// the skip tensor (those channels of cat) is not positive
+cudaError_t launch_skipgrad(const Act &gcat, int cd, const Act &cat, const Act &gp,
                             const Act &gs, cudaStream_t s);
 // head = [w_0 .. w_{C-1}, b] (FP32); dhead accumulates the same layout
 cudaError_t launch_head_train(const Act &x, const float *head, const float *yt,

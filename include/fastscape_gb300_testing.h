@@ -56,6 +56,11 @@ int fs_test_table_capacity(const fs_model *m, int32_t *cap);
  *                      x holds dy [B,H,W,cout], out: [B,H,W,cin] BF16.
  *   mode 2 (weight gradient): out[co][tap][ci] = sum_p dy[p][co] x[p+off][ci]
  *                      (FP32); x: [B,H,W,cin], w holds dy [B,H,W,cout].
+ *   mode 3: mode 0 with the output written as planes of a wider tensor (two
+ *                      sentinel planes on each side, which must stay
+ *                      untouched: FS_ERR_CUDA otherwise); out as in mode 0.
+ *   mode 4: mode 3 with the output upsampled 2x (nearest) as it is stored:
+ *                      out [B,2H,2W,cout].
  * No counterpart in the reference (it has no learned part). */
 int fs_test_sg_conv(int mode, int B, int H, int W, int cin, int cout, int taps,
                     const uint16_t *x, const uint16_t *w, const float *bias, int relu,

@@ -63,6 +63,23 @@ def test_forward(pkg, shape):
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_forward_into_wider_and_upsampled_outputs(pkg, shape):
+    # The network writes its skip tensors into the concatenations they join
+    # (planes inside a wider tensor) and its decoder outputs upsampled 2x
+    # into them: same values as the plain forward, bit for bit, and nothing
+    # written outside the output's planes (the library checks the sentinels).
+    B, H, W, cin, cout, taps = shape
+    rng = np.random.default_rng(sum(shape) + 1)
+    x = _bits(rng, (B, H, W, cin))
+    w = _bits(rng, (cout, taps, cin), 1 / np.sqrt(taps * cin))
+    bias = rng.normal(0, 0.1, cout).astype(np.float32)
+    plain = pkg.sg_conv(0, x, w, taps, bias=bias, relu=True)
+    assert np.array_equal(pkg.sg_conv(3, x, w, taps, bias=bias, relu=True), plain)
+    up = pkg.sg_conv(4, x, w, taps, bias=bias, relu=True)
+    assert np.array_equal(up, np.repeat(np.repeat(plain, 2, axis=1), 2, axis=2))
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
 def test_data_gradient(pkg, shape):
     B, H, W, cin, cout, taps = shape
     rng = np.random.default_rng(7 + sum(shape))
