@@ -415,17 +415,21 @@ int adam(fs_surrogate *s, float lr) {
   const double c1 = 1.0 - std::pow(0.9, t), c2 = 1.0 - std::pow(0.999, t);
   const float lr_t = static_cast<float>(lr * std::sqrt(c2) / c1);
   const float eps_t = static_cast<float>(eps * std::sqrt(c2));
+  // every parameter (weights, biases, head) in one launch; the weight runs
+  // also refresh their BF16 copies
+  sg::AdamRuns runs;
   for (int l = 0; l < 14; l++) {
     const SgLayer &L = s->L[l];
-    const long long nw = static_cast<long long>(L.cout) * L.taps * L.cin;
-    SG_CUDA(sg::launch_adam(s->p + L.w_off, s->g + L.w_off, s->m + L.w_off, s->v + L.w_off, nw,
-                            lr_t, b1, b2, eps_t, L.wf, L.wd, L.cout, L.cin, L.taps, s->stream));
-    SG_CUDA(sg::launch_adam(s->p + L.b_off, s->g + L.b_off, s->m + L.b_off, s->v + L.b_off,
-                            L.cout, lr_t, b1, b2, eps_t, nullptr, nullptr, 0, 1, 1, s->stream));
+    runs.off[runs.n] = L.w_off;
+    runs.wf[runs.n] = L.wf;
+    runs.wd[runs.n] = L.wd;
+    runs.cout[runs.n] = L.cout;
+    runs.cin[runs.n] = L.cin;
+    runs.taps[runs.n] = L.taps;
+    runs.n++;
   }
-  SG_CUDA(sg::launch_adam(s->p + s->head_off, s->g + s->head_off, s->m + s->head_off,
-                          s->v + s->head_off, s->c0 + 1, lr_t, b1, b2, eps_t, nullptr, nullptr, 0,
-                          1, 1, s->stream));
+  SG_CUDA(sg::launch_adam(s->p, s->g, s->m, s->v, s->head_off + s->c0 + 1, lr_t, b1, b2, eps_t,
+                          runs, s->stream));
   return FS_OK;
 }
 

@@ -360,10 +360,11 @@ __global__ void __launch_bounds__(kBlock) k_bias_grad(const bf16 *__restrict__ g
 // Adam (bias-corrected) on FP32 masters; conv weights also refresh their BF16
 // copies: forward layout [cout][tap][cin] and the data-gradient layout
 // [cin][taps-1-tap][cout]
+// Adam over the whole parameter vector; an element inside a weight run
+// also writes its BF16 forward and flipped copies
 __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m,
                        float *__restrict__ v, long long n, float lr_t, float b1, float b2,
-                       float eps_t, bf16 *__restrict__ wf, bf16 *__restrict__ wd, int cout,
-                       int cin, int taps) {
+                       float eps_t, const AdamRuns runs) {
   for (long long i = blockIdx.x * static_cast<long long>(kBlock) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * kBlock) {
     const float gi = g[i];
@@ -373,13 +374,17 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
     v[i] = vi;
     const float pi = p[i] - lr_t * mi / (sqrtf(vi) + eps_t);
     p[i] = pi;
-    if (wf) {
+    for (int k = 0; k < runs.n; k++) {
+      const int cin = runs.cin[k], taps = runs.taps[k], cout = runs.cout[k];
+      const long long j = i - runs.off[k];
+      if (j < 0 || j >= static_cast<long long>(cout) * taps * cin) continue;
       const bf16 q = __float2bfloat16_rn(pi);
-      wf[i] = q;
-      const int ci = static_cast<int>(i % cin);
-      const int tap = static_cast<int>((i / cin) % taps);
-      const int co = static_cast<int>(i / (static_cast<long long>(cin) * taps));
-      wd[(static_cast<long long>(ci) * taps + (taps - 1 - tap)) * cout + co] = q;
+      runs.wf[k][j] = q;
+      const int ci = static_cast<int>(j % cin);
+      const int tap = static_cast<int>((j / cin) % taps);
+      const int co = static_cast<int>(j / (static_cast<long long>(cin) * taps));
+      runs.wd[k][(static_cast<long long>(ci) * taps + (taps - 1 - tap)) * cout + co] = q;
+      break;
     }
   }
 }
@@ -572,10 +577,9 @@ cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s) {
 }
 
 cudaError_t launch_adam(float *p, const float *g, float *m, float *v, long long n, float lr_t,
-                        float b1, float b2, float eps_t, bf16 *wf, bf16 *wd, int cout, int cin,
-                        int taps, cudaStream_t s) {
-  k_adam<<<blocks_for(n), kBlock, 0, s>>>(p, g, m, v, n, lr_t, b1, b2, eps_t, wf, wd, cout, cin,
-                                          taps);
+                        float b1, float b2, float eps_t, const AdamRuns &runs, cudaStream_t s) {
+  if (runs.n < 0 || runs.n > AdamRuns::kMax) return cudaErrorInvalidValue;
+  k_adam<<<blocks_for(n), kBlock, 0, s>>>(p, g, m, v, n, lr_t, b1, b2, eps_t, runs);
   return cudaGetLastError();
 }
 

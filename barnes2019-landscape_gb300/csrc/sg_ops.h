@@ -55,9 +55,20 @@ cudaError_t launch_head_apply(const Act &x, const float *head, const SampleView 
 cudaError_t launch_bias_grad(const Act &g, float *db, cudaStream_t s);
 // lr_t, eps_t: Adam's bias-corrected step size and epsilon; wf/wd (may be
 // null): BF16 copies in the forward and data-gradient layouts
+// The weight runs of a parameter vector with BF16 copies: run k is
+// elements [off[k], off[k] + cout*taps*cin), weights [cout][tap][cin], whose
+// forward copy goes to wf[k] and flipped copy ([cin][8 - tap][cout]) to wd[k].
+struct AdamRuns {
+  static constexpr int kMax = 16;
+  int n = 0;
+  long long off[kMax];
+  bf16 *wf[kMax], *wd[kMax];
+  int cout[kMax], cin[kMax], taps[kMax];
+};
+// One Adam step over the n elements of p (bias-corrected lr_t, eps_t), and
+// the BF16 copies of the weight runs in one launch.
 cudaError_t launch_adam(float *p, const float *g, float *m, float *v, long long n, float lr_t,
-                        float b1, float b2, float eps_t, bf16 *wf, bf16 *wd, int cout, int cin,
-                        int taps, cudaStream_t s);
+                        float b1, float b2, float eps_t, const AdamRuns &runs, cudaStream_t s);
 cudaError_t launch_to_bf16(const float *p, long long n, bf16 *wf, bf16 *wd, int cout, int cin,
                            int taps, cudaStream_t s);
 cudaError_t launch_field_max(double *const *h64, const float *h32, int nfields, long long hw,
