@@ -290,10 +290,33 @@ __host__ __device__ constexpr int acc_bufs(int bn) {
 }
 constexpr int kWgradThreads = 192;  // producer warp, MMA warp, 4 epilogue warps
 
+// Stores of an output upsampled 2x when the warp's 32 lanes hold 32
+// consecutive pixels of one row: the row's 64 slots from the warp's first
+// pixel (lane 0's out minus 16 lane elements) as two fully used 512-byte
+// stores, slot s holding pixel s/2 (values moved by shuffles), in both rows.
+__device__ __forceinline__ void store_up_rows(uint4 o, bf16 *out, long long rowd) {
+  const int lane = threadIdx.x & 31;
+  uint4 a, b;
+  a.x = __shfl_sync(0xffffffffu, o.x, lane >> 1);
+  a.y = __shfl_sync(0xffffffffu, o.y, lane >> 1);
+  a.z = __shfl_sync(0xffffffffu, o.z, lane >> 1);
+  a.w = __shfl_sync(0xffffffffu, o.w, lane >> 1);
+  b.x = __shfl_sync(0xffffffffu, o.x, 16 + (lane >> 1));
+  b.y = __shfl_sync(0xffffffffu, o.y, 16 + (lane >> 1));
+  b.z = __shfl_sync(0xffffffffu, o.z, 16 + (lane >> 1));
+  b.w = __shfl_sync(0xffffffffu, o.w, 16 + (lane >> 1));
+  bf16 *base = out - 8 * lane;  // slot `lane` of the warp's row run
+  *reinterpret_cast<uint4 *>(base) = a;
+  *reinterpret_cast<uint4 *>(base + 256) = b;
+  *reinterpret_cast<uint4 *>(base + rowd) = a;
+  *reinterpret_cast<uint4 *>(base + rowd + 256) = b;
+}
+
 // One 16-column chunk of a tile row: + bias (shared memory), ReLU, zeroed
 // where the mask is not positive, rounded to BF16, stored as 16 bytes in
 // each of two planes (ps elements apart); with rowd > 0 (an output upsampled
-// 2x, rows rowd elements apart) into the pixel's 2x2 block of each plane.
+// 2x, rows rowd elements apart) into the pixel's 2x2 block of each plane
+// (rowd < 0: the same, the warp holding 32 consecutive pixels of one row).
 __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, int relu,
                                       const bf16 *msk, bf16 *out, long long ps,
                                       long long rowd) {
@@ -328,6 +351,11 @@ __device__ __forceinline__ void epi16(const uint32_t (&v)[16], const float *sb, 
   o1.y = pack_bf16(f[10], f[11]);
   o1.z = pack_bf16(f[12], f[13]);
   o1.w = pack_bf16(f[14], f[15]);
+  if (rowd < 0) {
+    store_up_rows(o0, out, -rowd);
+    store_up_rows(o1, out + ps, -rowd);
+    return;
+  }
   *reinterpret_cast<uint4 *>(out) = o0;
   *reinterpret_cast<uint4 *>(out + ps) = o1;
   if (rowd) {
@@ -519,8 +547,10 @@ __global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 2)
           plane_at(b, n0 / 8, (static_cast<long long>(py) * a.W << (2 * a.up)) + (px << a.up),
                    a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
+      // a warp's 32 pixels lie in one row when the tile is a multiple of 32 wide
+      const long long rowd = !a.up ? 0 : a.BW % 32 == 0 ? -16ll * a.W : 16ll * a.W;
       epi_columns(d, 0, a.bn, a.bias ? s_bias + n0 : nullptr, a.relu,
-                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, a.up ? 16ll * a.W : 0);
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, rowd);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
@@ -710,7 +740,7 @@ __global__ void __launch_bounds__(64 + 128 * NG, NG == 1 ? 3 : 2)
                    a.oplanes, hw);
       const uint32_t d = tmem + buf * cols + (static_cast<uint32_t>(q * 32) << 16);
       epi_columns(d, 0, a.bn, a.bias ? s_bias : nullptr, a.relu,
-                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, a.up ? 16ll * a.W : 0);
+                  a.mask ? a.mask + at : nullptr, a.out + at, hw * 8, a.up ? -16ll * a.W : 0);
       tc_fence_before();
       mbar_arrive(&acc_empty[buf]);
     }
