@@ -1579,10 +1579,30 @@ cudaError_t plan_conv(ConvPlan &p, const Act &src, const bf16 *w, int taps, int 
 
 // Splits `ksteps` pixel steps so that about three CTAs per SM run, each
 // over at least 8 steps.
-void split_pixels(WgradPlan &p, int ksteps) {
-  int splits = (3 * p.sms + p.mtiles - 1) / p.mtiles;
-  if (splits > ksteps / 8) splits = ksteps / 8;
-  if (splits < 1) splits = 1;
+// Pixel splits of a weight gradient over `groups` row tiles with
+// `resident` CTAs on the whole GPU at once: the count whose groups x splits
+// CTAs fill whole rounds best (at most three rounds; a smaller count unless
+// a larger one fills 2% better), each split at least 8 steps. (Three CTAs
+// per SM regardless of what fits left 1.5 rounds for the two-per-SM forms
+// and a few CTAs in a fourth round for the one-per-SM forms.)
+int best_splits(int groups, int ksteps, int resident) {
+  const int most = std::max(1, ksteps / 8);
+  int best = 1;
+  double beff = -1.0;
+  for (int sp = 1; sp <= most && groups * sp <= 3 * resident; sp++) {
+    const int tot = groups * sp;
+    const int rounds = (tot + resident - 1) / resident;
+    const double eff = static_cast<double>(tot) / (static_cast<double>(rounds) * resident);
+    if (eff > beff + 0.02) {
+      beff = eff;
+      best = sp;
+    }
+  }
+  return best;
+}
+
+void split_pixels(WgradPlan &p, int ksteps, int resident) {
+  const int splits = best_splits(p.mtiles, ksteps, resident);
   p.kper = (ksteps + splits - 1) / splits;
   p.splits = (ksteps + p.kper - 1) / p.kper;
 }
@@ -1620,7 +1640,7 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
   p.mtiles = (nchunk + (kM / p.cwa) - 1) / (kM / p.cwa);
   p.ksteps = static_cast<int>(x.pixels() / kKPix);
   p.sms = sms;
-  split_pixels(p, p.ksteps);
+  split_pixels(p, p.ksteps, sms);  // one CTA per SM (its shared memory holds no second)
   p.dw = dw;
   // taps on M for up to 128 output and 256 input channels (any pixel tile)
   if (dy.C <= kM && x.C <= 256) {
@@ -1650,15 +1670,18 @@ cudaError_t plan_wgrad(WgradPlan &p, const Act &x, const Act &dy, int taps, floa
       if (2 * stage + 1024 <= 74 * 1024 && cols <= 128) {
         p.stages = 2;
         p.smem = 2 * stage + 1024;
+        p.cps = 3;
       } else if (2 * stage + 1024 <= kPairSmem + 6 * 1024) {
         p.stages = 2;
         p.smem = 2 * stage + 1024;
+        p.cps = 2;
       } else if (p.tap_per == 1 && 3 * half + 1024 <= kPairSmem && x.W >= 64 && x.W % 64 == 0) {
         int S2 = static_cast<int>((kPairSmem - 1024) / half);
         if (S2 > kMaxStages) S2 = kMaxStages;
         p.kpix = 64;
         p.stages = S2;
         p.smem = S2 * half + 1024;
+        p.cps = 2;
       }
       p.tpt = p.pt;
       if (p.kpix == 64) {
@@ -1748,6 +1771,11 @@ cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s, int ni
     cudaError_t e = cudaFuncSetAttribute(k_wgrad<CWA, CWB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kSmemBudget + 1024));
+    // the largest shared-memory carveout, which the occupancy calculator
+    // then assumes as the launches get it
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_wgrad<CWA, CWB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               static_cast<int>(cudaSharedmemCarveoutMaxShared));
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -1764,7 +1792,7 @@ cudaError_t launch_wgrad_cw(const WgradPlan &p, int *err, cudaStream_t s, int ni
   a.nchunk = p.taps * (p.cin / p.cwa);
   a.stages = p.stages;
   WgradPlan q = p;
-  if (nimg > 0) split_pixels(q, nimg * p.pt.tiles_x * p.pt.tiles_y);
+  split_pixels(q, nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps, p.cps * p.sms);
   a.ksteps = nimg > 0 ? nimg * p.pt.tiles_x * p.pt.tiles_y : p.ksteps;
   a.kper = q.kper;
   a.dw = p.dw;
@@ -1798,6 +1826,9 @@ cudaError_t launch_wgrad_taps(const WgradPlan &p, int *err, cudaStream_t s, int 
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_wgrad_taps, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kSmemBudget + 1024));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_wgrad_taps, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               static_cast<int>(cudaSharedmemCarveoutMaxShared));
     if (e != cudaSuccess) return e;
     attr = true;
   }
@@ -1815,10 +1846,9 @@ cudaError_t launch_wgrad_taps(const WgradPlan &p, int *err, cudaStream_t s, int 
   a.stages = p.stages;
   a.kpix = p.kpix;
   a.ksteps = (nimg > 0 ? nimg : p.B) * p.tpt.tiles_x * p.tpt.tiles_y;
-  // about three CTAs per SM over the tap groups, each over >= 8 steps
-  int splits = (3 * p.sms + p.ngroups - 1) / p.ngroups;
-  if (splits > a.ksteps / 8) splits = a.ksteps / 8;
-  if (splits < 1) splits = 1;
+  // whole rounds of the CTAs the plan sized to share an SM (shared memory,
+  // TMEM) over the tap groups, each split over >= 8 steps
+  int splits = best_splits(p.ngroups, a.ksteps, p.cps * p.sms);
   a.kper = (a.ksteps + splits - 1) / splits;
   splits = (a.ksteps + a.kper - 1) / a.kper;
   a.dw = p.dw;

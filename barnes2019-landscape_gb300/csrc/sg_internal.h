@@ -103,6 +103,7 @@ struct WgradPlan {
   int kpix = 128;  // taps form: pixels per K step, and their tile
   PixTile tpt;
   float *db = nullptr;  // taps form: bias gradient accumulated too (else null)
+  int cps = 1;          // CTAs per SM its shared memory and TMEM are sized for
 };
 
 // Builds a plan; returns cudaErrorInvalidValue (with a message in *why) for
