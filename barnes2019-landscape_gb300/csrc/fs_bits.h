@@ -25,6 +25,52 @@ FS_BITS_FN float float_from_bits(uint32_t u) {
 #endif
 }
 
+// Correctly rounded quotient from an approximate one: an = |num|, ad = |den|
+// (bits of positive normal doubles) and q0 = bits of an approximation of
+// an/ad within 2^9 ulp. The residual an - q0*ad is exact in integer
+// arithmetic in units of ulp(q0)*ulp(ad): r = mn*2^k - mq*md from the
+// significands (implicit bit set) and k = en - eq - ed + 1075; |r| < 2^62,
+// so the difference of the products' low 64 bits is r itself. With
+// an/ad = (mq + r/md) ulp(q0), n = the nearest integer to r/md (from the top
+// bits of r and md, within one of it) and r' = r - n*md, the correctly
+// rounded quotient's significand is mq + n when 2|r'| < md, one more or
+// one less when md < 2|r'| < 3md (a quotient is never a rounding midpoint),
+// as long as it stays in q0's binade (a result at the binade's lower edge
+// with the quotient below it may round into the binade beneath). Returns
+// the quotient's bits, or 0 where this does not decide (the caller then
+// divides).
+FS_BITS_FN uint64_t round_quotient_bits(uint64_t an, uint64_t ad, uint64_t q0) {
+  constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
+  const int en = (int)(an >> 52), ed = (int)(ad >> 52), eq = (int)(q0 >> 52);
+  const int k = en - eq - ed + 1075;
+  if ((unsigned)(k - 48) > 12u || (unsigned)(eq - 64) > 1916u) return 0;
+  const uint64_t mq = (q0 & kMant) | kHidden, mn = (an & kMant) | kHidden,
+                 md = (ad & kMant) | kHidden;
+  long long r = (long long)((mn << k) - mq * md);
+  // any integer n keeps the result exact (the checks below decide); the
+  // estimate's accuracy only sets how often they do
+#if defined(__CUDA_ARCH__)
+  const float t = __fdividef((float)(int)(r >> 32), (float)(int)(md >> 32));
+#else
+  const float t = (float)(int)(r >> 32) / (float)(int)(md >> 32);
+#endif
+  const long long n = (long long)(t < 0.0f ? -(int)(0.5f - t) : (int)(t + 0.5f));
+  if (n > 1024 || n < -1024) return 0;
+  r -= n * (long long)md;
+  long long m = (long long)mq + n;
+  const uint64_t a2 = (uint64_t)(r < 0 ? -r : r) << 1;
+  if (a2 > md) {
+    if (a2 >= 3 * md) return 0;
+    m += r > 0 ? 1 : -1;
+    r -= r > 0 ? (long long)md : -(long long)md;
+  } else if (a2 == md) {
+    return 0;
+  }
+  if (m < (long long)kHidden || m >= 2 * (long long)kHidden) return 0;
+  if (m == (long long)kHidden && r < 0) return 0;
+  return ((uint64_t)eq << 52) | ((uint64_t)m & kMant);
+}
+
 // Truncation of a double (as bits) to FP32 with integer operations only:
 // rebias the exponent, keep the top 23 fraction bits. Values below 2^-126
 // flush to signed zero; |x| >= 2^128, Inf and NaN give NaN.

@@ -882,13 +882,50 @@ __device__ __forceinline__ uint64_t add_correction(uint64_t x, uint64_t y) {
 }
 
 // RN(x / y) of bit patterns on the FP64 pipe.
-__device__ __forceinline__ uint64_t fdiv_bits(uint64_t a, uint64_t b) {
+// IEEE division in a branch taken by few cells (volatile: not executed
+// speculatively for the others).
+__device__ __forceinline__ uint64_t fdiv_bits_volatile(uint64_t a, uint64_t b) {
   uint64_t r;
-  asm("{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
+  asm volatile(
+      "{\n\t.reg .f64 x, y;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\t"
       "div.rn.f64 x, x, y;\n\tmov.b64 %0, x;\n\t}"
       : "=l"(r)
       : "l"(a), "l"(b));
   return r;
+}
+
+__device__ __forceinline__ uint64_t ffma_bits(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("{\n\t.reg .f64 x, y, z;\n\tmov.b64 x, %1;\n\tmov.b64 y, %2;\n\tmov.b64 z, %3;\n\t"
+      "fma.rn.f64 x, x, y, z;\n\tmov.b64 %0, x;\n\t}"
+      : "=l"(r)
+      : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// RN(num/den) on bit patterns for a denominator with no tabled reciprocal
+// (the n = 2 erosion's), in three FP64 operations: the IEEE FP32 reciprocal
+// of |den| truncated to FP32 (within 1.5*2^-23 of 1/|den|), one Newton step
+// r1 = r0 + r0*(1 - |den|*r0) by fused multiply-adds (within ~2^-44.8),
+// q0 = RN(|num|*r1) (within ~2^8.2 ulp of the quotient), and the rounding
+// from the exact integer residual (round_quotient_bits, fs_bits.h). Newton's
+// iteration for the reciprocal and the residual check are the published
+// methods (e.g. P. Markstein, IBM J. Res. Dev. 34(1), 1990);
+// tests/native/division_check.cpp replays the sequence on the host against
+// the IEEE division. Operands outside [2^-99, 2^102) and the rare cases the
+// rounding leaves open take the IEEE division.
+__device__ __forceinline__ uint64_t fdiv_rn_bits(uint64_t nb, uint64_t db) {
+  const uint64_t an = nb & ~kSignBit, ad = db & ~kSignBit;
+  if ((unsigned)((int)(an >> 52) - 924) <= 200u && (unsigned)((int)(ad >> 52) - 924) <= 200u) {
+    const uint32_t rb = __float_as_uint(__frcp_rn(trunc_bits_to_float(ad)));
+    // widen the positive normal FP32 reciprocal to FP64 bits
+    const uint64_t r0 = ((uint64_t)((rb >> 23) + 896) << 52) | ((uint64_t)(rb & 0x7FFFFFu) << 29);
+    const uint64_t e = ffma_bits(ad ^ kSignBit, r0, 0x3FF0000000000000ull);  // 1 - |den| r0
+    const uint64_t r1 = ffma_bits(r0, e, r0);
+    const uint64_t q = round_quotient_bits(an, ad, fmul_bits(an, r1));
+    if (q) return q | ((nb ^ db) & kSignBit);
+  }
+  return fdiv_bits_volatile(nb, db);
 }
 
 // RN(x - y) for any operands: in integer arithmetic when both are positive
@@ -938,7 +975,7 @@ __device__ __forceinline__ uint64_t erode_cell_n2(const RealDesc &d, double neq,
       num = ISUB ? sub_gen(fpn, a ^ kSignBit) : fadd_bits(a, fpn);
     }
     const uint64_t den = fadd_bits(kOne, fmul_bits(fact2, dx));
-    const uint64_t q = fdiv_bits(num, den);
+    const uint64_t q = fdiv_rn_bits(num, den);
     const uint64_t xn = sub(x, q);
     if (step_below_tol(q ^ kSignBit, x, d)) return xn;
     const uint64_t df = sub(xn, x);

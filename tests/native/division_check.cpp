@@ -17,6 +17,12 @@
 // difference taken modulo 2^64 is exact; num/D = q0 + (R'/mD) ulp(q0) in
 // magnitude, so RN(num/D) is q0 when 2|R'| < mD and q0 one ulp up or down
 // when mD < 2|R'| < 3 mD (a quotient is never a rounding midpoint).
+// A third form divides by any denominator (the n = 2 erosion's, which has no
+// tabled reciprocal): the FP32 reciprocal of |den| truncated to FP32 as the
+// seed (IEEE round to nearest, as __frcp_rn), one FP64 Newton step
+// r1 = r0 + r0*(1 - |den|*r0) by fused multiply-adds, q0 = RN(|num|*r1)
+// within ~2^8.2 ulp, then round_quotient_bits (fs_bits.h), the integer
+// rounding the kernel uses.
 // Usage: division_check <cases> <seed>; exit 1 on the first mismatch.
 #include <cinttypes>
 #include <cmath>
@@ -24,6 +30,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
+
+#include "../../barnes2019-landscape_gb300/csrc/fs_bits.h"
 
 static double dbl(uint64_t u) { double d; std::memcpy(&d, &u, 8); return d; }
 static uint64_t bits(double d) { uint64_t u; std::memcpy(&u, &d, 8); return u; }
@@ -73,10 +81,26 @@ static bool int_quotient(double num, double D, double R, double *q) {
   return false;
 }
 
+// Returns true and *q = RN(num/den) when the general form accepts.
+static bool gen_quotient(double num, double den, double *q) {
+  const uint64_t kSign = 1ull << 63;
+  const uint64_t an = bits(num) & ~kSign, ad = bits(den) & ~kSign;
+  const int en = (int)(an >> 52), ed = (int)(ad >> 52);
+  if ((unsigned)(en - 924) > 200u || (unsigned)(ed - 924) > 200u) return false;
+  const float rf = 1.0f / fs::trunc_bits_to_float(ad);
+  const double r0 = (double)rf;
+  const double e = std::fma(-dbl(ad), r0, 1.0);
+  const double r1 = std::fma(r0, e, r0);
+  const uint64_t qb = fs::round_quotient_bits(an, ad, bits(dbl(an) * r1));
+  if (!qb) return false;
+  *q = dbl(qb | ((bits(num) ^ bits(den)) & kSign));
+  return true;
+}
+
 int main(int argc, char **argv) {
   const long n = argc > 1 ? std::atol(argv[1]) : 10000000;
   std::mt19937_64 g(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 1);
-  long accepted = 0, accepted_int = 0;
+  long accepted = 0, accepted_int = 0, accepted_gen = 0;
   for (long i = 0; i < n; i++) {
     // D = 1 + F, F from tiny to huge; significands of every shape; also the
     // receiver slopes' divisors (dx, dx*sqrt(2)), D below 1, huge D (where
@@ -107,6 +131,14 @@ int main(int argc, char **argv) {
     }
     if (g() & 1) num = -num;
     double q;
+    if (gen_quotient(num, D, &q)) {
+      accepted_gen++;
+      const double ex = num / D;
+      if (bits(q) != bits(ex)) {
+        std::printf("MISMATCH (general form) num=%a D=%a gen=%a ieee=%a\n", num, D, q, ex);
+        return 1;
+      }
+    }
     if (int_quotient(num, D, R, &q)) {
       accepted_int++;
       const double ex = num / D;
@@ -124,8 +156,8 @@ int main(int argc, char **argv) {
       }
     }
   }
-  std::printf("%ld cases, %ld accepted by the fast path, %ld by the integer form, all equal to the "
-              "IEEE quotient\n",
-              n, accepted, accepted_int);
+  std::printf("%ld cases, %ld accepted by the fast path, %ld by the integer form, %ld by the "
+              "general form, all equal to the IEEE quotient\n",
+              n, accepted, accepted_int, accepted_gen);
   return 0;
 }
