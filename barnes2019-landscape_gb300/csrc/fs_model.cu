@@ -139,7 +139,7 @@ struct fs_batch {
   int timing = 0;          // 0 off, 1 per kernel (direct launches), 2 whole calls
   bool exact_receivers = false;
   bool erode_generic = false;                    // test: the reference's Newton loop literally
-  bool use_graph = false;
+  bool use_graph = true;  // the autotuner's choice at every size measured
   cudaGraphExec_t graph = nullptr;
   bool graph_dirty = true;
   std::vector<cudaEvent_t> ev;

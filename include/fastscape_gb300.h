@@ -224,8 +224,9 @@ int fs_batch_get_stack_dfs(const fs_batch *b, int r, int32_t *stack,
 int fs_batch_info(const fs_batch *b, int *n, int64_t *cells);
 int fs_batch_set_timing(fs_batch *b, int enable);
 int fs_batch_get_phase_times(const fs_batch *b, double *ms, int reset);
-/* Replays each timestep from a captured CUDA graph (1) or launches it
- * directly (0, default). */
+/* Replays each timestep from a captured CUDA graph (1, default: the
+ * autotuner's choice at every grid size and ensemble measured) or launches
+ * it directly (0). A capture that fails falls back to direct launches. */
 int fs_batch_use_graph(fs_batch *b, int enable);
 /* With n = 1 or 2, the erosion subtracts elevations in integer arithmetic
  * (1) or on the FP64 pipe (0, default); identical results, different speed
