@@ -1,8 +1,11 @@
-"""The erosion kernel's three-operation quotient (neg_div_rn_bits) replayed
-on the host: every quotient its fast path accepts must equal the IEEE
-division, on random operands and on operands next to rounding midpoints.
-The GPU parity tests check the device code itself bit for bit against the
-oracle."""
+"""The erosion kernels' quotients replayed on the host: the n = 1 form with a
+tabled reciprocal (neg_div_rn_bits: one FP64 multiplication, rounding from
+the exact integer residual), its earlier fused multiply-add form, and the
+n = 2 form for any denominator (fdiv_rn_bits: FP32 seed, one Newton step,
+round_quotient_bits from fs_bits.h, the function the kernels compile). Every
+quotient a form accepts must equal the IEEE division, on random operands and
+on operands next to rounding midpoints. The GPU parity tests check the
+device code itself bit for bit against the oracle."""
 import shutil
 import subprocess
 from pathlib import Path
